@@ -1,0 +1,89 @@
+"""ctypes binding of the C ABI in include/eqfield.h (``eq_gb300/libeqfield.so``).
+
+The CUDA library is the only implementation: if it is missing this module raises,
+and there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libeqfield.so")
+
+EQF_OK = 0
+EQF_ERR_INVALID = -1
+EQF_ERR_CUDA = -2
+EQF_ERR_NOT_CONVERGED = -3
+EQF_ERR_NO_DEVICE = -4
+EQF_ERR_NOMEM = -5
+
+EQF_WALL_BOTTOM, EQF_WALL_TOP, EQF_WALL_LEFT, EQF_WALL_RIGHT = 1, 2, 4, 8
+EQF_PREC_FP64, EQF_PREC_FP32_IR = 0, 1
+
+# every entry point declared in include/eqfield.h
+EXPORTS = (
+    "eqf_default_opts", "eqf_create", "eqf_destroy", "eqf_last_error", "eqf_num_nodes",
+    "eqf_set_cells", "eqf_set_cell_rates", "eqf_set_nodal", "eqf_add_nodal", "eqf_step",
+    "eqf_read_nodal", "eqf_read_cells", "eqf_boundary_flux", "eqf_total_mass", "eqf_stats",
+    "eqf_sync",
+)
+
+
+class TrapParams(C.Structure):
+    _fields_ = [("width", C.c_double), ("height", C.c_double), ("nx", C.c_int32),
+                ("ny", C.c_int32), ("D", C.c_double), ("dt", C.c_double), ("decay", C.c_double),
+                ("adv_u", C.c_double), ("adv_len", C.c_double), ("walls", C.c_uint32)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_sweeps", C.c_int32),
+                ("max_iters", C.c_int32), ("inner_tol", C.c_double), ("cheb_pre", C.c_int32),
+                ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
+                ("use_graph", C.c_int32), ("adaptive", C.c_int32)]
+
+
+class EqfError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"eqfield error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the in-tree CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m eq_gb300.build` "
+                           "(there is no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    dp, i64p = P(C.c_double), P(C.c_int64)
+    sig = {
+        "eqf_default_opts": (C.c_int, [C.c_int32, P(SolverOpts)]),
+        "eqf_create": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), P(C.c_void_p)]),
+        "eqf_destroy": (C.c_int, [C.c_void_p]),
+        "eqf_last_error": (C.c_char_p, [C.c_void_p]),
+        "eqf_num_nodes": (C.c_int, [C.c_void_p, C.c_int32, i64p]),
+        "eqf_set_cells": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp]),
+        "eqf_set_cell_rates": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp]),
+        "eqf_set_nodal": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+        "eqf_add_nodal": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, i64p, dp]),
+        "eqf_step": (C.c_int, [C.c_void_p, C.c_int32]),
+        "eqf_read_nodal": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+        "eqf_read_cells": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp]),
+        "eqf_boundary_flux": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+        "eqf_total_mass": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+        "eqf_stats": (C.c_int, [C.c_void_p, C.c_int32, i64p, i64p, i64p, dp]),
+        "eqf_sync": (C.c_int, [C.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib

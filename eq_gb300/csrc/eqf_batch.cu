@@ -1,0 +1,993 @@
+// Batch runtime and C ABI of the GB300 trap field solver.
+//
+// A batch holds every trap's multigrid hierarchy in flat per-level arrays, the
+// tile work lists that let one launch cover all traps, the FP64 field and load,
+// and the device-resident per-trap solver state.  One backward-Euler step is a
+// fixed launch sequence (refinement sweeps x preconditioned CG iterations x
+// V-cycles); converged traps drop out through per-trap skip flags, so the same
+// sequence can be captured once as a CUDA graph and replayed every step.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/eqfield.h"
+#include "eqf_cells.cuh"
+#include "eqf_common.cuh"
+#include "eqf_kernels.cuh"
+
+namespace eqf {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define EQF_CK(call)                                                                       \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      throw ::eqf::Error(e_ == cudaErrorMemoryAllocation ? EQF_ERR_NOMEM : EQF_ERR_CUDA,   \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+#define EQF_LAUNCH_CHECK() EQF_CK(cudaGetLastError())
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    EQF_CK(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    EQF_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+constexpr int kTileNodes = 2048;
+constexpr int kMaxLevels = 16;
+
+static inline long long align_up(long long v, long long a) { return (v + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// Spectrum bounds of D^-1 A on a level (host).
+static void spectrum_bounds(LevelGeom& g) {
+  // Fourier symbol of the uniform-interior stencil
+  double smax = 0.0, smin = 1e300;
+  const int NS = 48;
+  for (int a = 0; a <= NS; ++a) {
+    const double tx = M_PI * a / NS;
+    for (int b = -NS; b <= NS; ++b) {
+      const double ty = M_PI * b / NS;
+      const double v =
+          (g.cC + 2 * g.cE * cos(tx) + 2 * g.cN * cos(ty) + 2 * g.cD * cos(tx + ty)) / g.cC;
+      smax = std::max(smax, v);
+      smin = std::min(smin, v);
+    }
+  }
+  // Gershgorin over every distinct row type (edges, corners, near-edge rows)
+  double gmax = 0.0;
+  const int is[] = {0, 1, 2, g.ny / 2, g.ny - 2, g.ny - 1, g.ny};
+  const int js[] = {0, 1, 2, g.nx / 2, g.nx - 2, g.nx - 1, g.nx};
+  for (int i : is) {
+    if (i < 0 || i > g.ny) continue;
+    for (int j : js) {
+      if (j < 0 || j > g.nx) continue;
+      if (g.walls && is_dirichlet(g, i, j)) continue;
+      const Sten<double> s = stencil_general<double>(g, i, j);
+      const double r = (std::fabs(s.c) + std::fabs(s.e) + std::fabs(s.w) + std::fabs(s.n) +
+                        std::fabs(s.s) + std::fabs(s.ne) + std::fabs(s.sw)) /
+                       s.c;
+      gmax = std::max(gmax, r);
+    }
+  }
+  g.lam_max = (float)std::min(gmax, 1.15 * smax);
+  g.lam_min = (float)std::max(0.9 * smin, 1e-3 * smax);
+}
+
+static void interior_constants(LevelGeom& g) {
+  LevelGeom q = g;
+  q.nx = q.ny = 1000;
+  q.walls = 0;
+  q.adv = 0.0;
+  const Sten<double> s = stencil_general<double>(q, 500, 500);
+  g.cC = s.c;
+  g.cE = s.e;
+  g.cN = s.n;
+  g.cD = s.ne;
+  g.fC = (float)s.c;
+  g.fE = (float)s.e;
+  g.fN = (float)s.n;
+  g.fD = (float)s.ne;
+}
+
+struct Level {
+  std::vector<LevelGeom> geom;  // per trap
+  std::vector<Tile> tiles;
+  long long nodes = 0;
+  DevBuf<LevelGeom> dgeom;
+  DevBuf<Tile> dtiles;
+  int ntiles() const { return (int)tiles.size(); }
+};
+
+// ---------------------------------------------------------------------------
+struct WorkBase {
+  virtual ~WorkBase() = default;
+  virtual void enqueue_sweep(cudaStream_t s, bool first) = 0;
+  virtual void enqueue_check(cudaStream_t s) = 0;
+};
+
+class Batch;
+
+template <class T>
+struct Work : WorkBase {
+  Batch& B;
+  struct Lv {
+    DevBuf<T> b, x, y, d, t;
+  };
+  std::vector<Lv> lv;
+  DevBuf<T> xs, p0, p1, q;  // fine CG: correction, directions, A p
+  explicit Work(Batch& b);
+  void enqueue_sweep(cudaStream_t s, bool first) override;
+  void enqueue_check(cudaStream_t s) override;
+  T* vcycle(cudaStream_t s, int lev, bool dot);
+};
+
+class Batch {
+ public:
+  int ntraps = 0;
+  int nlev = 0;
+  eqf_solver_opts opts{};
+  std::vector<eqf_trap_params> params;
+  std::vector<Level> L;
+  std::vector<TileRange> range;  // fine tiles per trap
+  DevBuf<TileRange> drange;
+  DevBuf<CgState> dstate;
+  DevBuf<int> d_ir_done, d_cg_skip, d_fail;
+  DevBuf<double> dpart;
+  DevBuf<double> u, b64, F;  // fine FP64 field, refinement rhs, load
+  std::unique_ptr<WorkBase> work;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  std::string err;
+  long long steps_done = 0;
+
+  // cells
+  std::vector<std::vector<double>> cell_xy, cell_s;  // per trap (host copies)
+  bool cells_dirty = false;
+  int ncells = 0, nseg = 0;
+  DevBuf<CellGeom> dcg;
+  DevBuf<int> d_cell_trap, d_ent_node, d_perm, d_seg_start;
+  DevBuf<double> d_cell_xy, d_cell_s, d_ent_w, d_ent_val, d_scale;
+  std::vector<int> cell_first;  // first cell index of each trap in the batch arrays
+
+  explicit Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o);
+  ~Batch();
+  void build_levels();
+  void step(int n);
+  void run_step();
+  void rebuild_cells();
+  void refresh_load();
+  void build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
+                      DevBuf<int>& seg_start, int& nseg_out);
+  long long fine_nodes(int t) const {
+    return (long long)(L[0].geom[t].nx + 1) * (L[0].geom[t].ny + 1);
+  }
+  void sync() { EQF_CK(cudaStreamSynchronize(stream)); }
+  void check_fail();
+  void scan(int n, const int* in, int* out);
+};
+
+// ---------------------------------------------------------------------------
+Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
+    : ntraps(n), opts(o), params(p, p + n) {
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    throw Error(EQF_ERR_NO_DEVICE, "no CUDA device visible");
+  EQF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  build_levels();
+  const long long N0 = L[0].nodes;
+  u.alloc(N0);
+  b64.alloc(N0);
+  F.alloc(N0);
+  EQF_CK(cudaMemsetAsync(u.p, 0, N0 * sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(F.p, 0, N0 * sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(b64.p, 0, N0 * sizeof(double), stream));
+  dstate.alloc(ntraps);
+  EQF_CK(cudaMemsetAsync(dstate.p, 0, ntraps * sizeof(CgState), stream));
+  d_ir_done.alloc(ntraps);
+  d_cg_skip.alloc(ntraps);
+  d_fail.alloc(1);
+  EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+  dpart.alloc(2 * (size_t)L[0].ntiles());
+  if (opts.precision == EQF_PREC_FP32_IR)
+    work.reset(new Work<float>(*this));
+  else
+    work.reset(new Work<double>(*this));
+  cell_xy.resize(ntraps);
+  cell_s.resize(ntraps);
+  sync();
+}
+
+Batch::~Batch() {
+  if (graph) cudaGraphExecDestroy(graph);
+  work.reset();
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void Batch::build_levels() {
+  // level count: coarsen until the Fourier number beta/h^2 drops below ~1
+  int nl = 1;
+  for (const auto& p : params) {
+    const double hmin = std::min(p.width / p.nx, p.height / p.ny);
+    const double beta = p.dt * p.D;
+    int k = 0;
+    double h = hmin;
+    while (beta / (h * h) > 1.0 && k < kMaxLevels - 1) {
+      h *= 2;
+      ++k;
+    }
+    nl = std::max(nl, k + 1);
+  }
+  nlev = nl;
+  L.resize(nlev);
+  for (int l = 0; l < nlev; ++l) L[l].geom.resize(ntraps);
+  for (int t = 0; t < ntraps; ++t) {
+    const auto& p = params[t];
+    LevelGeom g{};
+    g.nx = p.nx;
+    g.ny = p.ny;
+    g.trap = t;
+    g.walls = p.walls;
+    g.hx = g.hxl = p.width / p.nx;
+    g.hy = g.hyl = p.height / p.ny;
+    g.alpha = 1.0 + p.dt * p.decay;
+    g.beta = p.dt * p.D;
+    g.adv = (p.adv_u != 0.0 && p.adv_len > 0.0) ? p.dt * p.adv_u / p.adv_len : 0.0;
+    for (int l = 0; l < nlev; ++l) {
+      if (l > 0) {
+        LevelGeom c = g;
+        c.fine_nx = g.nx;
+        c.fine_ny = g.ny;
+        c.cx = g.nx >= 4;
+        c.cy = g.ny >= 4;
+        if (c.cx) {
+          c.nx = (g.nx + 1) / 2;
+          c.hxl = (g.nx % 2 == 0) ? g.hx + g.hxl : g.hxl;
+          c.hx = 2 * g.hx;
+        }
+        if (c.cy) {
+          c.ny = (g.ny + 1) / 2;
+          c.hyl = (g.ny % 2 == 0) ? g.hy + g.hyl : g.hyl;
+          c.hy = 2 * g.hy;
+        }
+        g = c;
+      }
+      interior_constants(g);
+      spectrum_bounds(g);
+      L[l].geom[t] = g;
+    }
+  }
+  // offsets, fine offsets and tiles
+  for (int l = 0; l < nlev; ++l) {
+    long long off = 0;
+    for (int t = 0; t < ntraps; ++t) {
+      LevelGeom& g = L[l].geom[t];
+      g.off = off;
+      const long long n = (long long)(g.nx + 1) * (g.ny + 1);
+      if (l > 0) g.fine_off = L[l - 1].geom[t].off;
+      for (long long k0 = 0; k0 < n; k0 += kTileNodes)
+        L[l].tiles.push_back(Tile{t, (int)k0, (int)std::min<long long>(n, k0 + kTileNodes)});
+      off = align_up(off + n, 32);
+    }
+    L[l].nodes = off;
+    if (off >= (1ll << 31)) throw Error(EQF_ERR_INVALID, "batch too large for 32-bit node indices");
+    L[l].dgeom.alloc(ntraps);
+    L[l].dgeom.upload(L[l].geom.data(), ntraps, stream);
+    L[l].dtiles.alloc(L[l].tiles.size());
+    L[l].dtiles.upload(L[l].tiles.data(), L[l].tiles.size(), stream);
+  }
+  range.assign(ntraps, TileRange{0, 0});
+  for (int i = 0; i < L[0].ntiles(); ++i) {
+    const int t = L[0].tiles[i].geom;
+    if (range[t].count == 0) range[t].first = i;
+    range[t].count++;
+  }
+  drange.alloc(ntraps);
+  drange.upload(range.data(), ntraps, stream);
+  sync();
+}
+
+// ---------------------------------------------------------------------------
+template <class T>
+Work<T>::Work(Batch& b) : B(b) {
+  lv.resize(B.nlev);
+  for (int l = 0; l < B.nlev; ++l) {
+    const size_t n = B.L[l].nodes;
+    lv[l].b.alloc(n);
+    lv[l].x.alloc(n);
+    lv[l].y.alloc(n);
+    lv[l].d.alloc(n);
+    lv[l].t.alloc(n);
+    // zero once so padding between traps never holds garbage
+    for (DevBuf<T>* v : {&lv[l].b, &lv[l].x, &lv[l].y, &lv[l].d, &lv[l].t})
+      EQF_CK(cudaMemsetAsync(v->p, 0, n * sizeof(T), B.stream));
+  }
+  const size_t n0 = B.L[0].nodes;
+  for (DevBuf<T>* v : {&xs, &p0, &p1, &q}) {
+    v->alloc(n0);
+    EQF_CK(cudaMemsetAsync(v->p, 0, n0 * sizeof(T), B.stream));
+  }
+}
+
+// V-cycle on level `lev` with rhs lv[lev].b; returns the buffer holding x.
+template <class T>
+T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
+  const Level& Lv_ = B.L[lev];
+  Lv& v = lv[lev];
+  const int nt = Lv_.ntiles();
+  const int* skip = B.d_cg_skip.p;
+  const LevelGeom* G = Lv_.dgeom.p;
+  const Tile* tl = Lv_.dtiles.p;
+  double* part = B.dpart.p;
+  T* cur = v.x.p;
+  T* oth = v.y.p;
+  const bool coarsest = lev == B.nlev - 1;
+  const float ratio = coarsest ? 0.f : (float)B.opts.cheb_ratio;
+  const int deg_pre = coarsest ? B.opts.cheb_coarse : B.opts.cheb_pre;
+  // pre-smoothing (or coarsest solve) from zero
+  {
+    const bool last_dot = dot && coarsest && deg_pre == 1;
+    if (last_dot)
+      k_cheb<T, true, true, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur, cur,
+                                                          v.d.p, part);
+    else
+      k_cheb<T, true, true, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
+                                                           cur, v.d.p, part);
+    EQF_LAUNCH_CHECK();
+    for (int st = 1; st < deg_pre; ++st) {
+      const bool ld = dot && coarsest && st == deg_pre - 1;
+      if (ld)
+        k_cheb<T, false, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p, cur,
+                                                              oth, v.d.p, part);
+      else
+        k_cheb<T, false, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
+                                                               cur, oth, v.d.p, part);
+      EQF_LAUNCH_CHECK();
+      std::swap(cur, oth);
+    }
+  }
+  if (coarsest) return cur;
+  // residual, restriction, coarse correction, prolongation
+  k_resid<T><<<nt, kThreads, 0, s>>>(G, tl, skip, v.b.p, cur, v.t.p);
+  EQF_LAUNCH_CHECK();
+  const Level& Lc = B.L[lev + 1];
+  k_restrict<T><<<Lc.ntiles(), kThreads, 0, s>>>(Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p,
+                                                  lv[lev + 1].b.p);
+  EQF_LAUNCH_CHECK();
+  T* xc = vcycle(s, lev + 1, false);
+  k_prolong<T><<<nt, kThreads, 0, s>>>(G, Lc.dgeom.p, tl, skip, xc, cur);
+  EQF_LAUNCH_CHECK();
+  // post-smoothing from the corrected iterate
+  const int deg_post = B.opts.cheb_post;
+  for (int st = 0; st < deg_post; ++st) {
+    const bool ld = dot && st == deg_post - 1;
+    if (st == 0) {
+      if (ld)
+        k_cheb<T, true, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
+                                                             oth, v.d.p, part);
+      else
+        k_cheb<T, true, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
+                                                              oth, v.d.p, part);
+    } else {
+      if (ld)
+        k_cheb<T, false, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
+                                                              cur, oth, v.d.p, part);
+      else
+        k_cheb<T, false, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
+                                                               cur, oth, v.d.p, part);
+    }
+    EQF_LAUNCH_CHECK();
+    std::swap(cur, oth);
+  }
+  return cur;
+}
+
+// One refinement sweep: FP64 residual, preconditioned CG on the correction, update.
+template <class T>
+void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
+  const Level& L0 = B.L[0];
+  const int nt = L0.ntiles();
+  const int nb = (B.ntraps + 127) / 128;
+  const LevelGeom* G = L0.dgeom.p;
+  const Tile* tl = L0.dtiles.p;
+  double* part = B.dpart.p;
+  T* r = lv[0].b.p;  // CG residual = V-cycle rhs on level 0
+  const bool fp32 = std::is_same<T, float>::value;
+  const double tol_rel = fp32 ? B.opts.inner_tol : 0.0;
+  const double tol_abs = fp32 ? 0.0 : B.opts.rtol;
+  if (first)
+    k_ir_residual<T, true><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, B.F.p, B.u.p, B.b64.p,
+                                                    r, part, nt);
+  else
+    k_ir_residual<T, false><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, B.F.p, B.u.p, B.b64.p,
+                                                     r, part, nt);
+  EQF_LAUNCH_CHECK();
+  k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
+                            B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p);
+  EQF_LAUNCH_CHECK();
+  EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
+  T* pin = p0.p;
+  T* pout = p1.p;
+  for (int it = 0; it < B.opts.max_iters; ++it) {
+    T* z = vcycle(s, 0, true);
+    k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p);
+    EQF_LAUNCH_CHECK();
+    if (it == 0)
+      k_cg_dir<T, true><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, z, pin, pout,
+                                                 q.p, part);
+    else
+      k_cg_dir<T, false><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, z, pin, pout,
+                                                  q.p, part);
+    EQF_LAUNCH_CHECK();
+    k_s_pq<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p);
+    EQF_LAUNCH_CHECK();
+    k_cg_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p, xs.p, r,
+                                           part);
+    EQF_LAUNCH_CHECK();
+    k_s_rr<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
+                              B.d_cg_skip.p);
+    EQF_LAUNCH_CHECK();
+    std::swap(pin, pout);
+  }
+  k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, B.u.p);
+  EQF_LAUNCH_CHECK();
+}
+
+__global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
+                          const double* __restrict__ part, int ntiles, double rtol,
+                          CgState* __restrict__ st, int* __restrict__ ir_done,
+                          int* __restrict__ fail) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntraps || ir_done[t]) return;
+  CgState s = st[t];
+  s.r64 = trap_sum(part + ntiles, range[t]);
+  if (s.r64 <= rtol * rtol * s.bb || s.bb == 0.0)
+    ir_done[t] = 1;
+  else
+    atomicAdd(fail, 1);
+  st[t] = s;
+}
+
+// Final FP64 residual check after the last sweep: marks converged traps and
+// counts the others in d_fail.
+template <class T>
+void Work<T>::enqueue_check(cudaStream_t s) {
+  const Level& L0 = B.L[0];
+  const int nt = L0.ntiles();
+  k_ir_residual<T, false><<<nt, kThreads, 0, s>>>(L0.dgeom.p, L0.dtiles.p, B.d_ir_done.p, B.F.p,
+                                                   B.u.p, B.b64.p, lv[0].b.p, B.dpart.p, nt);
+  EQF_LAUNCH_CHECK();
+  k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
+                                                    B.opts.rtol, B.dstate.p, B.d_ir_done.p,
+                                                    B.d_fail.p);
+  EQF_LAUNCH_CHECK();
+}
+
+void Batch::run_step() {
+  EQF_CK(cudaMemsetAsync(d_ir_done.p, 0, ntraps * sizeof(int), stream));
+  for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
+  work->enqueue_check(stream);
+}
+
+void Batch::check_fail() {
+  int f = 0;
+  EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  sync();
+  if (f > 0) {
+    EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+    throw Error(EQF_ERR_NOT_CONVERGED,
+                std::to_string(f) + " trap-step(s) missed rtol within the solver schedule");
+  }
+}
+
+void Batch::step(int n) {
+  if (cells_dirty) rebuild_cells();
+  for (int k = 0; k < n; ++k) {
+    if (opts.use_graph) {
+      if (!graph) {
+        cudaGraph_t gr;
+        EQF_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        run_step();
+        EQF_CK(cudaStreamEndCapture(stream, &gr));
+        EQF_CK(cudaGraphInstantiate(&graph, gr, 0));
+        cudaGraphDestroy(gr);
+      }
+      EQF_CK(cudaGraphLaunch(graph, stream));
+    } else {
+      run_step();
+    }
+    if (opts.adaptive) {
+      // add sweeps for traps that missed rtol (others are skipped by ir_done)
+      int f = 0;
+      for (int extra = 0; extra < 8; ++extra) {
+        EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (f == 0) break;
+        EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        work->enqueue_sweep(stream, false);
+        work->enqueue_check(stream);
+      }
+      if (f != 0) {
+        EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        throw Error(EQF_ERR_NOT_CONVERGED, "trap(s) missed rtol after extra refinement sweeps");
+      }
+    }
+    ++steps_done;
+  }
+}
+
+// ---------------------------------------------------------------------------
+void Batch::scan(int n, const int* in, int* out) {
+  if (n <= 0) return;
+  const int nb = (n + kScanTile - 1) / kScanTile;
+  DevBuf<int> sums;
+  sums.alloc(nb);
+  k_scan_sums<<<nb, kScanBlock, 0, stream>>>(n, in, sums.p);
+  EQF_LAUNCH_CHECK();
+  k_scan_top<<<1, kScanBlock, 0, stream>>>(nb, sums.p);
+  EQF_LAUNCH_CHECK();
+  k_scan_apply<<<nb, kScanBlock, 0, stream>>>(n, in, sums.p, out);
+  EQF_LAUNCH_CHECK();
+  sync();
+}
+
+// Deterministic sort of entries by node: counting sort, then each bucket ordered
+// by entry index; segments = buckets.  d_counts holds per-node counts on entry.
+void Batch::build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
+                           DevBuf<int>& seg_start, int& nseg_out) {
+  const long long N = L[0].nodes;
+  DevBuf<int> start, cursor, head, head_scan;
+  start.alloc(N + 1);
+  cursor.alloc(N);
+  scan((int)N, d_counts, start.p);
+  EQF_CK(cudaMemsetAsync(cursor.p, 0, N * sizeof(int), stream));
+  perm.alloc(std::max(nent, 1));
+  head.alloc(std::max(nent, 1));
+  head_scan.alloc(nent + 1);
+  const int bs = 256, gb = (nent + bs - 1) / bs;
+  k_cells_place<<<gb, bs, 0, stream>>>(nent, d_node, start.p, cursor.p, perm.p);
+  EQF_LAUNCH_CHECK();
+  k_cells_heads<<<gb, bs, 0, stream>>>(nent, d_node, start.p, perm.p, head.p);
+  EQF_LAUNCH_CHECK();
+  k_cells_bucket_sort<<<gb, bs, 0, stream>>>(nent, d_node, start.p, head.p, perm.p);
+  EQF_LAUNCH_CHECK();
+  scan(nent, head.p, head_scan.p);
+  int ns = 0;
+  EQF_CK(cudaMemcpyAsync(&ns, head_scan.p + nent, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  sync();
+  seg_start.alloc(ns + 1);
+  k_cells_segments<<<gb, bs, 0, stream>>>(nent, head.p, head_scan.p, seg_start.p, ns);
+  EQF_LAUNCH_CHECK();
+  sync();
+  nseg_out = ns;
+}
+
+void Batch::rebuild_cells() {
+  cells_dirty = false;
+  cell_first.assign(ntraps + 1, 0);
+  for (int t = 0; t < ntraps; ++t) cell_first[t + 1] = cell_first[t] + (int)cell_s[t].size();
+  ncells = cell_first[ntraps];
+  EQF_CK(cudaMemsetAsync(F.p, 0, L[0].nodes * sizeof(double), stream));
+  if (ncells == 0) {
+    nseg = 0;
+    sync();
+    return;
+  }
+  std::vector<double> xy(2 * (size_t)ncells), sv(ncells);
+  std::vector<int> trap(ncells);
+  std::vector<CellGeom> cg(ntraps);
+  std::vector<double> scale(ntraps);
+  for (int t = 0; t < ntraps; ++t) {
+    const LevelGeom& g = L[0].geom[t];
+    cg[t] = CellGeom{g.off, g.nx, g.ny, g.hx, g.hy};
+    scale[t] = params[t].dt;
+    std::copy(cell_xy[t].begin(), cell_xy[t].end(), xy.begin() + 2 * (size_t)cell_first[t]);
+    std::copy(cell_s[t].begin(), cell_s[t].end(), sv.begin() + cell_first[t]);
+    std::fill(trap.begin() + cell_first[t], trap.begin() + cell_first[t + 1], t);
+  }
+  d_cell_xy.alloc(xy.size());
+  d_cell_xy.upload(xy.data(), xy.size(), stream);
+  d_cell_s.alloc(ncells);
+  d_cell_s.upload(sv.data(), ncells, stream);
+  d_cell_trap.alloc(ncells);
+  d_cell_trap.upload(trap.data(), ncells, stream);
+  dcg.alloc(ntraps);
+  dcg.upload(cg.data(), ntraps, stream);
+  d_scale.alloc(ntraps);
+  d_scale.upload(scale.data(), ntraps, stream);
+  const int nent = 3 * ncells;
+  d_ent_node.alloc(nent);
+  d_ent_w.alloc(nent);
+  d_ent_val.alloc(nent);
+  DevBuf<int> counts;
+  counts.alloc(L[0].nodes);
+  EQF_CK(cudaMemsetAsync(counts.p, 0, L[0].nodes * sizeof(int), stream));
+  k_cells_locate<<<(ncells + 255) / 256, 256, 0, stream>>>(ncells, dcg.p, d_cell_trap.p,
+                                                           d_cell_xy.p, d_ent_node.p, d_ent_w.p,
+                                                           counts.p);
+  EQF_LAUNCH_CHECK();
+  build_segments(nent, d_ent_node.p, counts.p, d_perm, d_seg_start, nseg);
+  refresh_load();
+}
+
+// F = dt * sum_i s_i phi(x_i) from the current rates (segments fixed)
+void Batch::refresh_load() {
+  if (ncells == 0) return;
+  k_cells_values<<<(ncells + 255) / 256, 256, 0, stream>>>(ncells, d_ent_w.p, d_cell_s.p,
+                                                           d_scale.p, d_cell_trap.p, d_ent_val.p);
+  EQF_LAUNCH_CHECK();
+  k_seg_sum<false><<<(nseg + 255) / 256, 256, 0, stream>>>(nseg, d_seg_start.p, d_perm.p,
+                                                           d_ent_node.p, d_ent_val.p, F.p);
+  EQF_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Readouts: boundary flux and total mass of one trap (FP64, tile partials).
+__global__ void k_trap_reduce(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+                              int first_tile, const double* __restrict__ u, int what,
+                              double* __restrict__ part) {
+  const Tile tile = tiles[first_tile + blockIdx.x];
+  const LevelGeom g = G[tile.geom];
+  const double* us = u + g.off;
+  const int P = g.nx + 1;
+  double acc = 0.0;
+  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+    const int k = w.k, i = w.i, j = w.j;
+    if (what == 0) {  // 1^T M u
+      const Sten<double> m = mass_stencil<double>(g, i, j);
+      acc += (m.c + m.e + m.w + m.n + m.s + m.ne + m.sw) * us[k];
+    } else {  // -int grad u . n ds, each boundary edge owned by one node
+      if (i == 0 && j < g.nx) acc += (us[k + P + 1] - us[k + 1]) / g.hy * g.hx;
+      if (i == g.ny && j < g.nx) acc += -(us[k] - us[k - P]) / g.hy * g.hx;
+      if (j == 0 && i < g.ny) acc += (us[k + P + 1] - us[k + P]) / g.hx * g.hy;
+      if (j == g.nx && i < g.ny) acc += -(us[k] - us[k - 1]) / g.hx * g.hy;
+    }
+  }
+  const double t = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+}  // namespace eqf
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using eqf::Batch;
+using eqf::Error;
+
+struct eqf_batch {
+  std::unique_ptr<Batch> impl;
+  std::string err;
+};
+
+static thread_local std::string g_create_err;
+
+template <class F>
+static int guarded(eqf_batch* b, F&& f) {
+  try {
+    f();
+    return EQF_OK;
+  } catch (const Error& e) {
+    if (b) b->err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (b) b->err = "host allocation failed";
+    return EQF_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    if (b) b->err = e.what();
+    return EQF_ERR_INVALID;
+  }
+}
+
+#define EQF_REQUIRE(cond, msg) \
+  do {                         \
+    if (!(cond)) throw Error(EQF_ERR_INVALID, msg); \
+  } while (0)
+
+extern "C" {
+
+int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
+  if (!o) return EQF_ERR_INVALID;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = precision;
+  o->cheb_pre = 2;
+  o->cheb_post = 2;
+  o->cheb_coarse = 12;
+  o->cheb_ratio = 5.0;
+  o->use_graph = 0;
+  o->adaptive = 1;
+  if (precision == EQF_PREC_FP32_IR) {
+    o->rtol = 1e-9;
+    o->max_sweeps = 3;
+    o->max_iters = 8;
+    o->inner_tol = 1e-5;
+  } else if (precision == EQF_PREC_FP64) {
+    o->rtol = 1e-10;
+    o->max_sweeps = 1;
+    o->max_iters = 30;
+    o->inner_tol = 0.0;
+  } else {
+    return EQF_ERR_INVALID;
+  }
+  return EQF_OK;
+}
+
+int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+               eqf_batch** out) {
+  if (!out) return EQF_ERR_INVALID;
+  *out = nullptr;
+  auto* h = new (std::nothrow) eqf_batch();
+  if (!h) return EQF_ERR_NOMEM;
+  const int rc = guarded(h, [&] {
+    EQF_REQUIRE(n_traps > 0 && traps, "need at least one trap");
+    eqf_solver_opts o;
+    if (opts)
+      o = *opts;
+    else
+      eqf_default_opts(EQF_PREC_FP64, &o);
+    EQF_REQUIRE(o.precision == EQF_PREC_FP64 || o.precision == EQF_PREC_FP32_IR,
+                "unknown precision");
+    EQF_REQUIRE(o.max_sweeps >= 1 && o.max_iters >= 1 && o.cheb_post >= 1 && o.cheb_pre >= 1 &&
+                    o.cheb_coarse >= 1 && o.cheb_ratio > 1.0 && o.rtol > 0.0,
+                "invalid solver options");
+    for (int t = 0; t < n_traps; ++t) {
+      const auto& p = traps[t];
+      EQF_REQUIRE(p.nx >= 1 && p.ny >= 1 && p.width > 0 && p.height > 0 && p.dt > 0 &&
+                      p.D >= 0 && p.decay >= 0 && (p.walls & ~15u) == 0,
+                  "invalid trap parameters (trap " + std::to_string(t) + ")");
+    }
+    h->impl.reset(new Batch(n_traps, traps, o));
+  });
+  if (rc != EQF_OK) {
+    g_create_err = h->err;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return EQF_OK;
+}
+
+int eqf_destroy(eqf_batch* b) {
+  if (!b) return EQF_ERR_INVALID;
+  delete b;
+  return EQF_OK;
+}
+
+const char* eqf_last_error(const eqf_batch* b) {
+  return b ? b->err.c_str() : g_create_err.c_str();
+}
+
+#define EQF_TRAP_CHECK(b, trap)                                                     \
+  EQF_REQUIRE((trap) >= 0 && (trap) < (b)->impl->ntraps, "trap index out of range")
+
+int eqf_num_nodes(const eqf_batch* b, int32_t trap, int64_t* n) {
+  if (!b || !n || trap < 0 || trap >= b->impl->ntraps) return EQF_ERR_INVALID;
+  *n = b->impl->fine_nodes(trap);
+  return EQF_OK;
+}
+
+int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const double* s) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(n >= 0 && (n == 0 || (xy && s)), "bad cell arrays");
+    const auto& p = b->impl->params[trap];
+    for (int64_t i = 0; i < n; ++i) {
+      EQF_REQUIRE(std::isfinite(xy[2 * i]) && std::isfinite(xy[2 * i + 1]) && std::isfinite(s[i]),
+                  "non-finite cell position or rate");
+      EQF_REQUIRE(xy[2 * i] >= 0 && xy[2 * i] <= p.width && xy[2 * i + 1] >= 0 &&
+                      xy[2 * i + 1] <= p.height,
+                  "cell outside the trap");
+    }
+    b->impl->cell_xy[trap].assign(xy, xy + 2 * n);
+    b->impl->cell_s[trap].assign(s, s + n);
+    b->impl->cells_dirty = true;
+  });
+}
+
+int eqf_set_cell_rates(eqf_batch* b, int32_t trap, int64_t n, const double* s) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    EQF_REQUIRE(n == (int64_t)B.cell_s[trap].size() && (n == 0 || s), "rate count mismatch");
+    for (int64_t i = 0; i < n; ++i) EQF_REQUIRE(std::isfinite(s[i]), "non-finite cell rate");
+    B.cell_s[trap].assign(s, s + n);
+    if (B.cells_dirty) return;  // the rebuild will pick the rates up
+    if (n == 0) return;
+    EQF_CK(cudaMemcpyAsync(B.d_cell_s.p + B.cell_first[trap], s, n * sizeof(double),
+                           cudaMemcpyHostToDevice, B.stream));
+    B.refresh_load();
+    B.sync();
+  });
+}
+
+int eqf_set_nodal(eqf_batch* b, int32_t trap, const double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(c != nullptr, "null field");
+    Batch& B = *b->impl;
+    EQF_CK(cudaMemcpyAsync(B.u.p + B.L[0].geom[trap].off, c, B.fine_nodes(trap) * sizeof(double),
+                           cudaMemcpyHostToDevice, B.stream));
+    B.sync();
+  });
+}
+
+int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
+                  const double* delta) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(n >= 0 && (n == 0 || (node && delta)), "bad nodal arrays");
+    if (n == 0) return;
+    Batch& B = *b->impl;
+    const int64_t nn = B.fine_nodes(trap);
+    for (int64_t i = 0; i < n; ++i)
+      EQF_REQUIRE(node[i] >= 0 && node[i] < nn && std::isfinite(delta[i]),
+                  "node index out of range or non-finite increment");
+    eqf::DevBuf<long long> dn;
+    eqf::DevBuf<double> dv;
+    eqf::DevBuf<int> ent, counts, perm, seg;
+    dn.alloc(n);
+    dn.upload(reinterpret_cast<const long long*>(node), n, B.stream);
+    dv.alloc(n);
+    dv.upload(delta, n, B.stream);
+    ent.alloc(n);
+    counts.alloc(B.L[0].nodes);
+    EQF_CK(cudaMemsetAsync(counts.p, 0, B.L[0].nodes * sizeof(int), B.stream));
+    eqf::k_nodal_entries<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
+        (int)n, B.L[0].geom[trap].off, dn.p, ent.p, counts.p);
+    EQF_LAUNCH_CHECK();
+    int ns = 0;
+    B.build_segments((int)n, ent.p, counts.p, perm, seg, ns);
+    eqf::k_seg_sum<true><<<(ns + 255) / 256, 256, 0, B.stream>>>(ns, seg.p, perm.p, ent.p, dv.p,
+                                                                  B.u.p);
+    EQF_LAUNCH_CHECK();
+    B.sync();
+  });
+}
+
+int eqf_step(eqf_batch* b, int32_t n_steps) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_REQUIRE(n_steps >= 0, "negative step count");
+    b->impl->step(n_steps);
+  });
+}
+
+int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(c != nullptr, "null output");
+    Batch& B = *b->impl;
+    EQF_CK(cudaMemcpyAsync(c, B.u.p + B.L[0].geom[trap].off, B.fine_nodes(trap) * sizeof(double),
+                           cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    B.check_fail();
+  });
+}
+
+int eqf_read_cells(eqf_batch* b, int32_t trap, int64_t n, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    if (B.cells_dirty) B.rebuild_cells();
+    EQF_REQUIRE(n == (int64_t)B.cell_s[trap].size() && (n == 0 || c), "cell count mismatch");
+    if (n == 0) return;
+    eqf::DevBuf<double> out;
+    out.alloc(n);
+    const int c0 = B.cell_first[trap];
+    eqf::k_cells_gather<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
+        (int)n, B.d_ent_node.p + 3 * (size_t)c0, B.d_ent_w.p + 3 * (size_t)c0, B.u.p, out.p);
+    EQF_LAUNCH_CHECK();
+    EQF_CK(cudaMemcpyAsync(c, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    B.check_fail();
+  });
+}
+
+static double trap_reduce(Batch& B, int trap, int what) {
+  const eqf::TileRange tr = B.range[trap];
+  eqf::DevBuf<double> part;
+  part.alloc(tr.count);
+  eqf::k_trap_reduce<<<tr.count, eqf::kThreads, 0, B.stream>>>(
+      B.L[0].dgeom.p, B.L[0].dtiles.p, tr.first, B.u.p, what, part.p);
+  EQF_LAUNCH_CHECK();
+  std::vector<double> h(tr.count);
+  EQF_CK(cudaMemcpyAsync(h.data(), part.p, tr.count * sizeof(double), cudaMemcpyDeviceToHost,
+                         B.stream));
+  B.sync();
+  double s = 0.0;
+  for (double v : h) s += v;
+  return s;
+}
+
+int eqf_boundary_flux(eqf_batch* b, int32_t trap, double* flux) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(flux != nullptr, "null output");
+    Batch& B = *b->impl;
+    *flux = B.params[trap].D * B.params[trap].dt * trap_reduce(B, trap, 1);
+  });
+}
+
+int eqf_total_mass(eqf_batch* b, int32_t trap, double* mass) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(mass != nullptr, "null output");
+    *mass = trap_reduce(*b->impl, trap, 0);
+  });
+}
+
+int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64_t* iters,
+              double* last_rel_residual) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    eqf::CgState st;
+    EQF_CK(cudaMemcpyAsync(&st, B.dstate.p + trap, sizeof(st), cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    if (steps) *steps = B.steps_done;
+    if (sweeps) *sweeps = st.sweeps;
+    if (iters) *iters = st.iters;
+    if (last_rel_residual) *last_rel_residual = st.bb > 0 ? std::sqrt(st.r64 / st.bb) : 0.0;
+  });
+}
+
+int eqf_sync(eqf_batch* b) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    b->impl->sync();
+    b->impl->check_fail();
+  });
+}
+
+}  // extern "C"

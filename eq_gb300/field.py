@@ -1,0 +1,234 @@
+"""Host-side mirror of eQ's diffusion-solver plugin over the CUDA C ABI.
+
+``TrapBatch`` is a thin object wrapper of include/eqfield.h (one handle = many
+independent traps).  ``FieldSolver`` mirrors the reference's plugin interface
+``eQ::diffusionSolver`` (src/eQ.h:302-330) as implemented by ``fenicsInterface``
+(src/fHSL.h:333-449): ``initDiffusion(params)``, ``stepDiffusion()``,
+``getBoundaryFlux()``, ``writeDiffusionFiles(t)``, ``finalize()`` and the
+``solution_vector`` / ``totalBoundaryFlux`` data plane that
+``Simulation::stepSimulation`` reads and writes (src/simulation.cpp:455-505).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import math
+import os
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import EqfError, SolverOpts, TrapParams
+
+WALL_BOTTOM, WALL_TOP, WALL_LEFT, WALL_RIGHT = 1, 2, 4, 8
+FP64, FP32_IR = _lib.EQF_PREC_FP64, _lib.EQF_PREC_FP32_IR
+
+# trapType -> Dirichlet walls under boundaryType DIRICHLET_0 (src/fHSL.cpp:557-569)
+TRAP_TYPES = {"NOWALLED": 15, "THREEWALLED": WALL_BOTTOM, "TWOWALLED": WALL_BOTTOM | WALL_TOP,
+              "ONEWALLED": WALL_BOTTOM | WALL_LEFT | WALL_RIGHT}
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _check(lib, h, rc):
+    if rc != _lib.EQF_OK:
+        msg = lib.eqf_last_error(h)
+        raise EqfError(rc, msg.decode() if msg else "")
+
+
+def default_opts(precision: int = FP64, **over) -> SolverOpts:
+    lib = _lib.load()
+    o = SolverOpts()
+    _check(lib, None, lib.eqf_default_opts(precision, C.byref(o)))
+    for k, v in over.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+def trap_params(W, H, nx, ny, D, dt, decay=0.0, walls=WALL_BOTTOM, adv_u=0.0,
+                adv_len=1.0) -> TrapParams:
+    return TrapParams(float(W), float(H), int(nx), int(ny), float(D), float(dt), float(decay),
+                      float(adv_u), float(adv_len), int(walls))
+
+
+class TrapBatch:
+    """A batch of independent traps on the GPU (C ABI handle)."""
+
+    def __init__(self, traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None):
+        self._lib = _lib.load()
+        arr = (TrapParams * len(traps))(*traps)
+        self._h = C.c_void_p()
+        o = opts if opts is not None else default_opts()
+        rc = self._lib.eqf_create(len(traps), arr, C.byref(o), C.byref(self._h))
+        _check(self._lib, None, rc)
+        self.n_traps = len(traps)
+        self.params = list(traps)
+        self.opts = o
+        self._ncells = [0] * self.n_traps
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.eqf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        _check(self._lib, self._h, rc)
+
+    def num_nodes(self, trap: int) -> int:
+        n = C.c_int64()
+        self._ck(self._lib.eqf_num_nodes(self._h, trap, C.byref(n)))
+        return n.value
+
+    def set_cells(self, trap: int, xy: np.ndarray, s: np.ndarray):
+        xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        s = np.ascontiguousarray(s, dtype=np.float64).ravel()
+        if len(s) != len(xy):
+            raise ValueError("xy and s lengths differ")
+        self._ck(self._lib.eqf_set_cells(self._h, trap, len(s), _dp(xy), _dp(s)))
+        self._ncells[trap] = len(s)
+
+    def set_cell_rates(self, trap: int, s: np.ndarray):
+        s = np.ascontiguousarray(s, dtype=np.float64).ravel()
+        self._ck(self._lib.eqf_set_cell_rates(self._h, trap, len(s), _dp(s)))
+
+    def set_nodal(self, trap: int, c: np.ndarray):
+        c = np.ascontiguousarray(c, dtype=np.float64).ravel()
+        if len(c) != self.num_nodes(trap):
+            raise ValueError("nodal vector length mismatch")
+        self._ck(self._lib.eqf_set_nodal(self._h, trap, _dp(c)))
+
+    def add_nodal(self, trap: int, nodes: np.ndarray, delta: np.ndarray):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int64).ravel()
+        delta = np.ascontiguousarray(delta, dtype=np.float64).ravel()
+        if len(nodes) != len(delta):
+            raise ValueError("nodes and delta lengths differ")
+        self._ck(self._lib.eqf_add_nodal(self._h, trap, len(nodes),
+                                         nodes.ctypes.data_as(C.POINTER(C.c_int64)), _dp(delta)))
+
+    def step(self, n: int = 1):
+        self._ck(self._lib.eqf_step(self._h, int(n)))
+
+    def read_nodal(self, trap: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.num_nodes(trap))
+        self._ck(self._lib.eqf_read_nodal(self._h, trap, _dp(out)))
+        return out
+
+    def read_cells(self, trap: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        n = self._ncells[trap]
+        if out is None:
+            out = np.empty(n)
+        self._ck(self._lib.eqf_read_cells(self._h, trap, n, _dp(out)))
+        return out
+
+    def boundary_flux(self, trap: int) -> float:
+        v = C.c_double()
+        self._ck(self._lib.eqf_boundary_flux(self._h, trap, C.byref(v)))
+        return v.value
+
+    def total_mass(self, trap: int) -> float:
+        v = C.c_double()
+        self._ck(self._lib.eqf_total_mass(self._h, trap, C.byref(v)))
+        return v.value
+
+    def stats(self, trap: int) -> Dict[str, float]:
+        st, sw, it = C.c_int64(), C.c_int64(), C.c_int64()
+        rr = C.c_double()
+        self._ck(self._lib.eqf_stats(self._h, trap, C.byref(st), C.byref(sw), C.byref(it),
+                                     C.byref(rr)))
+        return {"steps": st.value, "sweeps": sw.value, "iters": it.value,
+                "last_rel_residual": rr.value}
+
+    def sync(self):
+        self._ck(self._lib.eqf_sync(self._h))
+
+
+@dataclass
+class DiffusionParams:
+    """The fields of eQ::diffusionSolver::params (src/eQ.h:305-321) the field step uses."""
+    dt: float
+    D_HSL: float
+    trapWidthMicrons: float
+    trapHeightMicrons: float
+    nodesPerMicron: float
+    uniqueID: int = 0
+    filePath: str = ""
+    trapChannelVelocity: float = 0.0
+
+
+class FieldSolver:
+    """One HSL layer behind the reference's plugin interface.
+
+    Mesh sizes follow fenicsClassInit: nodesW = ceil(W*npm), nodesH = ceil(H*npm)
+    squares (src/fHSL.cpp:242-243).  The default walls are the THREEWALLED
+    DIRICHLET_0 trap.  ``solution_vector`` is a grid-order numpy array; as in the
+    reference the caller may modify it between steps (deposits), and
+    ``stepDiffusion`` pushes it to the device, steps and pulls it back.
+    """
+
+    def __init__(self, trapType: str = "THREEWALLED", decay: float = 0.0,
+                 precision: int = FP64, opts: Optional[SolverOpts] = None):
+        self.walls = TRAP_TYPES[trapType]
+        self.decay = decay
+        self.precision = precision
+        self.opts = opts
+        self.batch: Optional[TrapBatch] = None
+        self.solution_vector = np.zeros(0)
+        self.totalBoundaryFlux = 0.0
+        self.myParams: Optional[DiffusionParams] = None
+        self._pushed = None
+
+    def initDiffusion(self, params: DiffusionParams):
+        self.myParams = params
+        nx = int(math.ceil(params.trapWidthMicrons * params.nodesPerMicron))
+        ny = int(math.ceil(params.trapHeightMicrons * params.nodesPerMicron))
+        tp = trap_params(params.trapWidthMicrons, params.trapHeightMicrons, nx, ny,
+                         params.D_HSL, params.dt, self.decay, self.walls)
+        o = self.opts if self.opts is not None else default_opts(self.precision)
+        self.batch = TrapBatch([tp], o)
+        self.nodesW, self.nodesH = nx + 1, ny + 1
+        self.solution_vector = np.zeros(self.nodesW * self.nodesH)
+        self._pushed = self.solution_vector.copy()
+
+    def stepDiffusion(self):
+        if not np.array_equal(self.solution_vector, self._pushed):
+            self.batch.set_nodal(0, self.solution_vector)
+        self.batch.step(1)
+        self.solution_vector = self.batch.read_nodal(0)
+        self._pushed = self.solution_vector.copy()
+        self.totalBoundaryFlux = self.batch.boundary_flux(0)
+
+    def getBoundaryFlux(self) -> Dict[str, float]:
+        return {"totalFlux": self.totalBoundaryFlux}
+
+    def writeDiffusionFiles(self, timestamp: float):
+        """Nodal snapshot in grid order (the reference writes DOLFIN .pvd files)."""
+        if not self.myParams or not self.myParams.filePath:
+            return
+        base = os.path.splitext(self.myParams.filePath)[0]
+        with open(f"{base}_{timestamp:.6g}.json", "w") as f:
+            json.dump({"time": timestamp, "nodesW": self.nodesW, "nodesH": self.nodesH,
+                       "externalHSL": self.solution_vector.tolist()}, f)
+
+    def finalize(self):
+        if self.batch is not None:
+            self.batch.close()
+            self.batch = None

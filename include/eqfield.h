@@ -1,0 +1,155 @@
+/*
+ * eqfield — GB300-native quorum-sensing field step (C ABI).
+ *
+ * One handle = one batch of independent traps (HSL layers); a single trap is a
+ * batch of one.  Each trap carries one species on a structured "right"
+ * triangulation of [0, W] x [0, H] and is stepped by backward Euler:
+ *
+ *   ((1 + dt*g) M + dt*D*K + dt*C(v)) c^{n+1} = M c^n + F,  c = 0 on Dirichlet walls
+ *
+ * with F = dt * sum_i s_i phi(x_i) from point cells (sources) and/or values added
+ * to the nodal field before a step (the reference's deposit into u0).
+ *
+ * This replaces the reference's FEniCS/PETSc layer solver, the plugin
+ * eQ::diffusionSolver (src/eQ.h:302-330) as implemented by fenicsInterface
+ * (src/fHSL.h:333-449, src/fHSL.cpp), together with the controller-side
+ * deposit/gather lambdas writeHSL/readHSL (src/abm/eQabm.cpp:326-359).  Each
+ * entry point names the reference interface it replaces.
+ *
+ * Conventions: every call returns EQF_OK (0) or a negative EQF_ERR_* code and
+ * records a message readable with eqf_last_error().  Nodal vectors are in grid
+ * order k = j + i*(nx+1) (eQ::data::index_from_ij, src/eQ.h:131-134); the DOLFIN
+ * DOF map of the reference is the identity here.  The library owns all device
+ * memory; host buffers are read or written only during the call.  A handle is
+ * not thread-safe: use one handle per host thread or lock externally.
+ */
+#ifndef EQFIELD_H
+#define EQFIELD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EQF_OK 0
+#define EQF_ERR_INVALID (-1)        /* bad argument or size */
+#define EQF_ERR_CUDA (-2)           /* CUDA runtime error (message has the detail) */
+#define EQF_ERR_NOT_CONVERGED (-3)  /* a trap missed its tolerance within the schedule */
+#define EQF_ERR_NO_DEVICE (-4)      /* no CUDA device visible */
+#define EQF_ERR_NOMEM (-5)          /* device allocation failed */
+
+/* Dirichlet walls (c = 0); unset walls are zero-flux.  The reference's trap types
+ * (src/fHSL.h:456-504, decoded at src/fHSL.cpp:557-569) map to:
+ * THREEWALLED = BOTTOM, TWOWALLED = BOTTOM|TOP, ONEWALLED = BOTTOM|LEFT|RIGHT,
+ * NOWALLED = all four. */
+#define EQF_WALL_BOTTOM 1u
+#define EQF_WALL_TOP 2u
+#define EQF_WALL_LEFT 4u
+#define EQF_WALL_RIGHT 8u
+
+/* Arithmetic of the solve. */
+#define EQF_PREC_FP64 0    /* plain form: FP64 operator, multigrid and Krylov */
+#define EQF_PREC_FP32_IR 1 /* FP32 operator/multigrid/Krylov inside FP64 refinement */
+
+/* Per-trap parameters.  Replaces eQ::diffusionSolver::params (src/eQ.h:305-321):
+ * trapWidthMicrons/trapHeightMicrons -> width/height, nodesPerMicron -> nx, ny
+ * (the reference uses nx = ceil(W*npm), ny = ceil(H*npm), src/fHSL.cpp:242-243),
+ * D_HSL -> D, dt -> dt.  decay and the advection velocity are extensions. */
+typedef struct eqf_trap_params {
+  double width, height; /* trap size W, H */
+  int32_t nx, ny;       /* squares along x, y (nodes: (nx+1)*(ny+1)) */
+  double D;             /* diffusion constant */
+  double dt;            /* time step */
+  double decay;         /* first-order decay g (0 in the reference form) */
+  double adv_u;         /* advection v = (0, -adv_u * y / adv_len); 0 = none */
+  double adv_len;
+  uint32_t walls;       /* EQF_WALL_* bits */
+} eqf_trap_params;
+
+/* Solver options shared by a batch. */
+typedef struct eqf_solver_opts {
+  int32_t precision;  /* EQF_PREC_* */
+  double rtol;        /* |b - A c| <= rtol |b| per trap and step (FP64 residual) */
+  int32_t max_sweeps; /* refinement sweeps per step (FP64 form: Krylov restarts) */
+  int32_t max_iters;  /* preconditioned Krylov iterations per sweep */
+  double inner_tol;   /* FP32 inner solve: relative residual reduction per sweep */
+  int32_t cheb_pre, cheb_post, cheb_coarse; /* Chebyshev degrees */
+  double cheb_ratio;  /* smoothing interval [lmax/ratio, lmax] */
+  int32_t use_graph;  /* capture steps as CUDA graphs */
+  int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
+} eqf_solver_opts;
+
+typedef struct eqf_batch eqf_batch;
+
+/* Fills opts with the defaults for a precision. */
+int eqf_default_opts(int32_t precision, eqf_solver_opts* opts);
+
+/* Creates a batch of n_traps traps on the current CUDA device.
+ * Replaces fenicsInterface::initDiffusion (src/fHSL.cpp:37-53) -> fenicsClassInit
+ * (src/fHSL.cpp:195-328: mesh, forms, boundary conditions, solver). */
+int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+               eqf_batch** out);
+
+/* Releases all device memory.  Replaces fenicsInterface::finalize / destructor
+ * (src/fHSL.cpp:655-661). */
+int eqf_destroy(eqf_batch* b);
+
+/* Message of the last failed call on this handle (or of the last eqf_create). */
+const char* eqf_last_error(const eqf_batch* b);
+
+/* Node count of a trap. */
+int eqf_num_nodes(const eqf_batch* b, int32_t trap, int64_t* n_nodes);
+
+/* Point cells of trap `trap`: positions xy[2*n] (x, y interleaved) and source
+ * rates s[n].  The load dt * sum s_i phi(x_i) is deposited deterministically
+ * onto the containing triangles and applied every step until replaced.
+ * Replaces the deposit writeHSL (src/abm/eQabm.cpp:338-359) for point cells. */
+int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const double* s);
+
+/* Replaces the source rates of the cells set by eqf_set_cells (same order),
+ * keeping their positions and sort order. */
+int eqf_set_cell_rates(eqf_batch* b, int32_t trap, int64_t n, const double* s);
+
+/* Sets the nodal field (grid order).  Replaces the controller's write of
+ * solution_vector before stepDiffusion (src/simulation.cpp:455-463, 500-505;
+ * src/fHSL.cpp:104). */
+int eqf_set_nodal(eqf_batch* b, int32_t trap, const double* c);
+
+/* Adds increments to nodes (grid-order indices): the reference deposit that
+ * adds dHSL into u0 (src/abm/eQabm.cpp:347-358). */
+int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
+                  const double* delta);
+
+/* Advances every trap of the batch by n_steps backward-Euler steps.
+ * Replaces fenicsInterface::stepDiffusion (src/fHSL.cpp:98-161). */
+int eqf_step(eqf_batch* b, int32_t n_steps);
+
+/* Reads the nodal field (grid order).  Replaces reading solution_vector after
+ * stepDiffusion (src/fHSL.cpp:108; src/simulation.cpp:491-492). */
+int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c);
+
+/* Concentration at the cells set by eqf_set_cells, sampled on their triangles.
+ * Replaces the gather readHSL (src/abm/eQabm.cpp:326-337) for point cells. */
+int eqf_read_cells(eqf_batch* b, int32_t trap, int64_t n, double* c);
+
+/* D * dt * (-int grad c . n ds): the reference's totalBoundaryFlux
+ * (fenics/boundary.ufl:9-12, src/fHSL.cpp:156-160, read by getBoundaryFlux). */
+int eqf_boundary_flux(eqf_batch* b, int32_t trap, double* flux);
+
+/* Total amount 1^T M c (FP64), for the mass-balance check. */
+int eqf_total_mass(eqf_batch* b, int32_t trap, double* mass);
+
+/* Solver statistics of a trap since creation: steps, refinement sweeps and
+ * Krylov iterations, and the last step's relative FP64 residual. */
+int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64_t* iters,
+              double* last_rel_residual);
+
+/* Waits for queued device work and reports deferred errors (convergence). */
+int eqf_sync(eqf_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EQFIELD_H */
