@@ -1,0 +1,403 @@
+"""Benchmark of the quorum-sensing field step on GB300.
+
+Metric: DOF-steps/s (mesh nodes x species x steps) of the batched FP32+FP64-
+refinement form at relL2 <= 1e-6 against the plain FP64 form, with p50/p99 step
+latency.  Workload (default): 512 uneven traps, nx ~ U{64..1024}, ny ~ U{32..512},
+h = 0.25 um, round(0.02*nx*ny) point cells each, D=490, g=0.01, dt=0.1 (seeded
+synthetic inputs; the reference publishes no benchmark data).  One bench step =
+one backward-Euler step of every trap.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Ours: the batch is one C-ABI handle stepped with CUDA graphs; the timed region
+is bracketed by CUDA events on the batch's stream.  The working set (several GB)
+is far larger than L2, so no flush is needed between steps.  A second, profiled
+pass (no graphs, CUDA events around every launch) gives the per-kernel-class
+split used for the roofline.  `e2e` repeats the timed loop through the batch-wide
+host API with pinned host buffers: per-cell rates in, per-cell concentrations out.
+
+Reference arm (--impl reference): the reference's algorithm for this path on the
+host cores (re-assemble the hslD system and LU-factor it every step, as DOLFIN's
+LinearVariationalSolver does), run by the oracle restatement over a sample of the
+workload's traps in a spawn process pool using every host core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-steps/s at relL2<=1e-6: batched FP32+IR vs plain FP64; p50/p99 step ms"
+UNIT = "DOF-steps/s"
+
+
+# --------------------------------------------------------------------------- util
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- workloads
+def make_workload(name: str, seed: int, n_traps: int):
+    from eq_gb300 import workloads as wl
+    if name == "batched_uneven":
+        return wl.batched_uneven(seed=seed, n_traps=n_traps)
+    if name == "single_large":
+        return [wl.single_large(seed)]
+    if name == "single_small":
+        return [wl.single_small(seed)]
+    raise ValueError(name)
+
+
+def trap_params_of(traps):
+    from eq_gb300 import field as F
+    return [F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls) for t in traps]
+
+
+def sample_indices(traps, k: int, seed: int = 11):
+    """k traps stratified by node count (deterministic)."""
+    order = np.argsort([t.n_nodes for t in traps], kind="stable")
+    if k >= len(traps):
+        return list(order)
+    pos = np.linspace(0, len(traps) - 1, k).round().astype(int)
+    return [int(order[p]) for p in pos]
+
+
+# ------------------------------------------------------------- CPU baselines
+def cpu_reference_rate(traps, idx, steps_per_trap: int, budget_s: float):
+    from oracle import cpu_baseline
+    return cpu_baseline.reference_rate(traps, idx, steps_per_trap, budget_s)
+
+
+# -------------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from eq_gb300 import field as F
+
+    torch.cuda.set_device(local_rank)
+    traps = make_workload(args.workload, args.seed + rank, args.traps)
+    tps = trap_params_of(traps)
+    nodes = sum(t.n_nodes for t in traps)
+    ncells = sum(t.n_cells for t in traps)
+
+    opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1)
+    b = F.TrapBatch(tps, opts)
+    for i, t in enumerate(traps):
+        b.set_cells(i, t.cell_xy, t.cell_s)
+    stream = torch.cuda.ExternalStream(b.stream_handle())
+
+    # warm-up (graph capture happens on the first steps)
+    b.step(args.warmup)
+    b.sync()
+    probe = sample_indices(traps, 8)
+    st0 = [b.stats(i) for i in probe]
+
+    # ---- timed region: K graph-replayed steps, CUDA events per step
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks = ClockSampler(local_rank)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        b.step(1)
+        ev[k + 1].record(stream)
+    b.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    st1 = [b.stats(i) for i in probe]
+    sweeps_ps = sum(a["sweeps"] - z["sweeps"] for a, z in zip(st1, st0)) / len(probe) / args.steps
+    iters_ps = sum(a["iters"] - z["iters"] for a, z in zip(st1, st0)) / len(probe) / args.steps
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    dof_steps = nodes * args.steps
+    value = dof_steps * world / (total_ms / 1e3)
+
+    # ---- relL2 of the chosen form against the plain FP64 form (sampled traps),
+    #      and the plain FP64 single-trap throughput (traps one by one)
+    total_steps = args.warmup + args.steps
+    idx = sample_indices(traps, args.fp64_sample)
+    u32 = {i: b.read_nodal(i) for i in idx}
+    c32 = {i: b.read_cells(i) for i in idx}
+    rels, relc = [], []
+    fp64_ms, fp64_dofs = 0.0, 0
+    o64 = F.default_opts(F.FP64, use_graph=1, adaptive=1)
+    for i in idx:
+        with F.TrapBatch([tps[i]], o64) as b1:
+            b1.set_cells(0, traps[i].cell_xy, traps[i].cell_s)
+            s1 = torch.cuda.ExternalStream(b1.stream_handle())
+            b1.step(1)
+            b1.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s1)
+            b1.step(total_steps - 1)
+            e1.record(s1)
+            b1.sync()
+            fp64_ms += e0.elapsed_time(e1)
+            fp64_dofs += traps[i].n_nodes * (total_steps - 1)
+            u64 = b1.read_nodal(0)
+            cc = b1.read_cells(0)
+        rels.append(float(np.linalg.norm(u32[i] - u64) / max(np.linalg.norm(u64), 1e-300)))
+        relc.append(float(np.linalg.norm(c32[i] - cc) / max(np.linalg.norm(cc), 1e-300)))
+    fp64_rate = fp64_dofs / (fp64_ms / 1e3)
+
+    # ---- profiled pass (no graphs): per kernel class time / nodes / bytes
+    prof_steps = max(2, min(args.steps, 5))
+    b.profile(True)
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0.record(stream)
+    b.step(prof_steps)
+    pe1.record(stream)
+    b.sync()
+    prof = b.profile_read()
+    b.profile(False)
+    prof_total = pe0.elapsed_time(pe1)
+    launches_per_step = sum(v["launches"] for v in prof.values()) / prof_steps
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        if tj.get("class") == dom and tj.get("workload") == args.workload:
+            traffic = tj.get("bytes_per_launch")
+    roofline = {"bound": "hbm", "kernel_class": dom, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "peak_source": peak_kind,
+                "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
+                "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
+
+    # ---- e2e through the host API: pinned rates in, pinned concentrations out
+    rates = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
+    rates.numpy()[:] = np.concatenate([t.cell_s for t in traps])
+    cout = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
+    e2e_steps = max(1, min(args.steps, 10))
+    b.sync()
+    t0 = time.perf_counter()
+    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ee0.record(stream)
+    for _ in range(e2e_steps):
+        b.set_cell_rates_all(rates.numpy())
+        b.step(1)
+        b.read_cells_all(cout.numpy())
+    ee1.record(stream)
+    b.sync()
+    e2e_ms = ee0.elapsed_time(ee1)
+    e2e_wall = time.perf_counter() - t0
+    e2e = {"value": nodes * e2e_steps / (max(e2e_ms, e2e_wall * 1e3) / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": ncells * 8, "d2h_bytes_per_step": ncells * 8,
+           "steps": e2e_steps}
+
+    b.close()
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            cidx = sample_indices(traps, args.cpu_sample)
+            cpu = cpu_reference_rate(traps, cidx, args.cpu_steps, args.cpu_budget)
+        sm = sorted(step_ms)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "p50_step_ms": float(np.percentile(sm, 50)), "p99_step_ms": float(np.percentile(sm, 99)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-ir",
+            "data": "synthetic (seeded PCG64; the reference publishes no dataset)",
+            "config": {"workload": args.workload, "traps": len(traps), "nodes": nodes,
+                       "cells": ncells, "seed": args.seed, "precision": "FP32 inner + FP64 refinement",
+                       "rtol": opts.rtol, "graphs": True,
+                       "l2": "working set (several GB) >> L2, no flush needed",
+                       "parallelism": f"independent traps, {world} replica(s)"},
+            "relL2_vs_fp64": {"nodal_max": max(rels), "cells_max": max(relc),
+                              "traps_checked": len(idx), "steps": total_steps},
+            "plain_fp64_single_trap": {"value": fp64_rate, "unit": UNIT,
+                                       "sample": f"{len(idx)} traps one by one, graphs, "
+                                                 f"{total_steps - 1} timed steps each",
+                                       "speedup_of_batched_fp32ir": value / world / fp64_rate},
+            "solver": {"sweeps_per_step": sweeps_ps, "iters_per_step": iters_ps,
+                       "sample": f"{len(probe)} traps stratified by size, timed steps"},
+            "roofline": roofline,
+            "profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                            "GBps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else 0}
+                        for k, v in prof.items()},
+            "profiled_pass_ms": prof_total, "profiled_steps": prof_steps,
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "e2e": e2e,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+    return out
+
+
+# --------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    traps = make_workload(args.workload, args.seed, args.traps)
+    cores = os.cpu_count() or 1
+    idx = sample_indices(traps, max(cores, 4))
+    # warm-up steps
+    for _ in range(args.warmup):
+        cpu_reference_rate(traps, idx[:min(len(idx), cores)], 1, args.cpu_budget)
+    vals = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_reference_rate(traps, idx, 1, args.cpu_budget)
+        vals.append(last["value"])
+    value = float(np.median(vals))
+    nodes = sum(traps[i].n_nodes for i in idx)
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": nodes / value * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": args.workload, "traps": len(traps), "seed": args.seed,
+                       "sampled_traps": len(idx)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference FEniCS/PETSc stack is not installable here (no DOLFIN/PETSc/MPI); "
+                    "its algorithm (assemble + LU per step) runs through the FP64 restatement"}
+
+
+def run_ncu_target(args):
+    """Minimal run for ncu captures: build the batch, step without graphs, exit."""
+    from eq_gb300 import field as F
+    traps = make_workload(args.workload, args.seed, args.traps)
+    prec = F.FP64 if args.fp64 else F.FP32_IR
+    b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1))
+    for i, t in enumerate(traps):
+        b.set_cells(i, t.cell_xy, t.cell_s)
+    b.step(args.warmup + args.steps)
+    b.sync()
+    b.close()
+    print(json.dumps({"ncu_target": args.workload, "traps": len(traps),
+                      "nodes": sum(t.n_nodes for t in traps),
+                      "steps": args.warmup + args.steps}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched_uneven")
+    ap.add_argument("--traps", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--fp64-sample", type=int, default=8)
+    ap.add_argument("--cpu-sample", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu", action="store_true",
+                    help="minimal run (no graphs, no timing) as an ncu capture target")
+    ap.add_argument("--fp64", action="store_true", help="with --ncu: plain FP64 form")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local_rank = env_rank()
+    if args.ncu:
+        run_ncu_target(args)
+        return
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

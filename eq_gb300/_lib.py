@@ -26,8 +26,11 @@ EXPORTS = (
     "eqf_default_opts", "eqf_create", "eqf_destroy", "eqf_last_error", "eqf_num_nodes",
     "eqf_set_cells", "eqf_set_cell_rates", "eqf_set_nodal", "eqf_add_nodal", "eqf_step",
     "eqf_read_nodal", "eqf_read_cells", "eqf_boundary_flux", "eqf_total_mass", "eqf_stats",
-    "eqf_sync",
+    "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
+    "eqf_profile_read", "eqf_stream",
 )
+PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
+                "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
 
 
 class TrapParams(C.Structure):
@@ -80,6 +83,11 @@ def load() -> C.CDLL:
         "eqf_total_mass": (C.c_int, [C.c_void_p, C.c_int32, dp]),
         "eqf_stats": (C.c_int, [C.c_void_p, C.c_int32, i64p, i64p, i64p, dp]),
         "eqf_sync": (C.c_int, [C.c_void_p]),
+        "eqf_set_cell_rates_all": (C.c_int, [C.c_void_p, C.c_int64, dp]),
+        "eqf_read_cells_all": (C.c_int, [C.c_void_p, C.c_int64, dp]),
+        "eqf_profile": (C.c_int, [C.c_void_p, C.c_int32]),
+        "eqf_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
+        "eqf_profile_read": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p, i64p, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -7,6 +7,7 @@
 // V-cycles); converged traps drop out through per-trap skip flags, so the same
 // sequence can be captured once as a CUDA graph and replayed every step.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -116,20 +117,92 @@ static void spectrum_bounds(LevelGeom& g) {
   g.lam_min = (float)std::max(0.9 * smin, 1e-3 * smax);
 }
 
+template <class T>
+static Lens<T> make_lens(const LevelGeom& g) {
+  Lens<T> L;
+  L.hx = (T)g.hx;
+  L.hy = (T)g.hy;
+  L.hxl = (T)g.hxl;
+  L.hyl = (T)g.hyl;
+  L.ihx = (T)(1.0 / g.hx);
+  L.ihy = (T)(1.0 / g.hy);
+  L.ihxl = (T)(1.0 / g.hxl);
+  L.ihyl = (T)(1.0 / g.hyl);
+  L.alpha = (T)g.alpha;
+  L.beta = (T)g.beta;
+  L.adv = (T)g.adv;
+  return L;
+}
+
 static void interior_constants(LevelGeom& g) {
+  g.adv_on = g.adv != 0.0 ? 1 : 0;
+  g.ld = make_lens<double>(g);
+  g.lf = make_lens<float>(g);
   LevelGeom q = g;
   q.nx = q.ny = 1000;
   q.walls = 0;
   q.adv = 0.0;
+  q.adv_on = 0;
   const Sten<double> s = stencil_general<double>(q, 500, 500);
   g.cC = s.c;
   g.cE = s.e;
   g.cN = s.n;
   g.cD = s.ne;
+  g.cCinv = 1.0 / s.c;
   g.fC = (float)s.c;
   g.fE = (float)s.e;
   g.fN = (float)s.n;
   g.fD = (float)s.ne;
+  g.fCinv = (float)(1.0 / s.c);
+  const Sten<double> m = mass_stencil<double>(q, 500, 500);
+  g.mC = m.c;
+  g.mE = m.e;
+  g.mN = m.n;
+  g.mD = m.ne;
+}
+
+// Shared-memory bytes of one staged range [ka, kb) (same widening as Stager::add).
+static size_t staged_bytes(long long ka, long long kb, int tsize, long long nalloc) {
+  const long long V = 16 / tsize;
+  const long long a = (ka / V) * V;
+  long long b = ((kb + V - 1) / V) * V;
+  b = std::min(b, nalloc);
+  const long long nb = b > a ? (b - a) * tsize : 0;
+  return (size_t)((nb + 15) & ~15ll);
+}
+
+// Class tables: the stencil of every (row class, column class) pair of a trap on
+// one level, classes {0, 1, interior, n-1, n} (as node_class), evaluated at a
+// representative node of each class.  MASS selects the unscaled mass stencil.
+template <class T, bool MASS>
+static void build_table(const LevelGeom& g, T* out) {
+  auto rep = [](int c, int n) { return c < 2 ? c : (c == 2 ? 2 : (c == 3 ? n - 1 : n)); };
+  auto cls = [](int i, int n) { return i < 2 ? i : (i > n - 2 ? 4 - (n - i) : 2); };
+  for (int ci = 0; ci < 5; ++ci)
+    for (int cj = 0; cj < 5; ++cj) {
+      T* e = out + (ci * 5 + cj) * kTabStride;
+      for (int q = 0; q < kTabStride; ++q) e[q] = T(0);
+      const int i = rep(ci, g.ny), j = rep(cj, g.nx);
+      if (i < 0 || i > g.ny || j < 0 || j > g.nx || cls(i, g.ny) != ci || cls(j, g.nx) != cj)
+        continue;  // class absent on this grid
+      const Sten<T> s = MASS ? mass_stencil<T>(g, i, j) : stencil_general<T>(g, i, j);
+      e[0] = s.c;
+      e[1] = s.e;
+      e[2] = s.w;
+      e[3] = s.n;
+      e[4] = s.s;
+      e[5] = s.ne;
+      e[6] = s.sw;
+      e[7] = MASS ? T(0) : T(1) / s.c;
+    }
+}
+
+// Shared-memory bytes of a guarded window (same widening as Stager::add_guarded).
+static size_t guarded_bytes(long long ka, long long kb, int tsize) {
+  const long long V = 16 / tsize;
+  const long long wa = ka >= 0 ? (ka / V) * V : -(((-ka) + V - 1) / V) * V;
+  const long long wb = ((kb + V - 1) / V) * V;
+  return (size_t)(((wb - wa) * tsize + 15) & ~15ll);
 }
 
 struct Level {
@@ -138,10 +211,65 @@ struct Level {
   long long nodes = 0;
   DevBuf<LevelGeom> dgeom;
   DevBuf<Tile> dtiles;
+  DevBuf<float> tabf;   // per-trap class tables (kTabPerTrap entries), FP32
+  DevBuf<double> tabd;  // same in FP64
+  // dynamic shared memory per staged kernel (max over this level's tiles)
+  size_t sm_cheb = 0, sm_resid = 0, sm_cgdir = 0, sm_ir = 0;
+  size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
+  size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
+  size_t sm_coarse = 0;    // single-CTA coarsest solve (0 = not possible)
   int ntiles() const { return (int)tiles.size(); }
 };
 
+constexpr size_t kSmemHeader = 16;              // mbarrier
+constexpr size_t kMaxDynSmem = 200 * 1024;      // per CTA budget for staged kernels
+
 // ---------------------------------------------------------------------------
+// Kernel classes for the built-in profiler (CUDA events around each launch and a
+// device counter of the nodes each launch actually processed).
+enum KClass : int {
+  KC_SMOOTH0 = 0,     // finest-level Chebyshev steps that apply the operator
+  KC_SMOOTH0_FIRST,   // finest-level first pre-smoothing step (zero start, no operator)
+  KC_RESID0,          // finest-level multigrid residual
+  KC_RESTRICT0,       // restriction from the finest level (counts coarse nodes)
+  KC_PROLONG0,        // prolongation to the finest level
+  KC_COARSE,          // every kernel on coarser levels
+  KC_CG_DIR,          // p = z + beta p, q = A p
+  KC_CG_UPDATE,       // x += alpha p, r -= alpha q
+  KC_IR_RESID_FIRST,  // FP64 b = F + M u, r = b - A u
+  KC_IR_RESID,        // FP64 r = b - A u
+  KC_IR_UPDATE,       // FP64 u += x
+  KC_SCALAR,          // per-trap scalar phases
+  KC_COUNT
+};
+static_assert(KC_COUNT == EQF_PROF_CLASSES, "profiler class count");
+
+// algorithmic bytes per processed node: (words of the inner type, FP64 bytes)
+static void class_bytes(int cls, int tsize, double& per_node) {
+  switch (cls) {
+    case KC_SMOOTH0: per_node = 5.0 * tsize; break;        // x, d, b in; x', d out
+    case KC_SMOOTH0_FIRST: per_node = 3.0 * tsize; break;  // b in; x, d out
+    case KC_RESID0: per_node = 3.0 * tsize; break;         // b, x in; t out
+    case KC_RESTRICT0: per_node = 5.0 * tsize; break;      // ~4 fine in; 1 coarse out
+    case KC_PROLONG0: per_node = 2.25 * tsize; break;      // x in/out; 1/4 coarse in
+    case KC_CG_DIR: per_node = 4.0 * tsize; break;         // z, p in; p', q out
+    case KC_CG_UPDATE: per_node = 6.0 * tsize; break;      // x, p, r, q in; x, r out
+    case KC_IR_RESID_FIRST: per_node = 24.0 + tsize; break;  // F, u in; b out; r out
+    case KC_IR_RESID: per_node = 16.0 + tsize; break;      // b, u in; r out
+    case KC_IR_UPDATE: per_node = 16.0 + tsize; break;     // x, u in; u out
+    default: per_node = 0.0;
+  }
+}
+
+struct Prof {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;  // pairs
+  std::vector<int> cls;
+  size_t used = 0;
+  bool overflow = false;
+  DevBuf<unsigned long long> work;  // one counter per record
+};
+
 struct WorkBase {
   virtual ~WorkBase() = default;
   virtual void enqueue_sweep(cudaStream_t s, bool first) = 0;
@@ -176,12 +304,38 @@ class Batch {
   DevBuf<CgState> dstate;
   DevBuf<int> d_ir_done, d_cg_skip, d_fail;
   DevBuf<double> dpart;
-  DevBuf<double> u, b64, F;  // fine FP64 field, refinement rhs, load
+  DevBuf<double> U[2];  // fine FP64 field; a step reads U[cur] and writes U[1 - cur]
+  DevBuf<float> Dd[2];  // step increments (previous / current), for the initial guess
+  int cur = 0;
+  DevBuf<double> b64, F;  // refinement rhs, load
+  DevBuf<double> tabA0, tabM0;  // finest-level FP64 operator and mass tables
+  double* u_cur() { return U[cur].p; }
   std::unique_ptr<WorkBase> work;
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per step parity
   std::string err;
   long long steps_done = 0;
+  Prof prof;
+  int cur_cls = -1;
+  // profiling hooks: begin() returns the node counter of this launch (or null)
+  unsigned long long* prof_begin(int c) {
+    if (!prof.on) return nullptr;
+    if (prof.used >= prof.cls.size()) {
+      prof.overflow = true;
+      cur_cls = -1;
+      return nullptr;
+    }
+    cur_cls = c;
+    EQF_CK(cudaEventRecord(prof.ev[2 * prof.used], stream));
+    return prof.work.p + prof.used;
+  }
+  void prof_end() {
+    if (!prof.on || cur_cls < 0) return;
+    EQF_CK(cudaEventRecord(prof.ev[2 * prof.used + 1], stream));
+    prof.cls[prof.used] = cur_cls;
+    ++prof.used;
+    cur_cls = -1;
+  }
 
   // cells
   std::vector<std::vector<double>> cell_xy, cell_s;  // per trap (host copies)
@@ -189,7 +343,7 @@ class Batch {
   int ncells = 0, nseg = 0;
   DevBuf<CellGeom> dcg;
   DevBuf<int> d_cell_trap, d_ent_node, d_perm, d_seg_start;
-  DevBuf<double> d_cell_xy, d_cell_s, d_ent_w, d_ent_val, d_scale;
+  DevBuf<double> d_cell_xy, d_cell_s, d_ent_w, d_ent_val, d_scale, d_cells_out;
   std::vector<int> cell_first;  // first cell index of each trap in the batch arrays
 
   explicit Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o);
@@ -218,10 +372,14 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
   EQF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   build_levels();
   const long long N0 = L[0].nodes;
-  u.alloc(N0);
+  for (int q = 0; q < 2; ++q) {
+    U[q].alloc(N0);
+    Dd[q].alloc(N0);
+    EQF_CK(cudaMemsetAsync(U[q].p, 0, N0 * sizeof(double), stream));
+    EQF_CK(cudaMemsetAsync(Dd[q].p, 0, N0 * sizeof(float), stream));
+  }
   b64.alloc(N0);
   F.alloc(N0);
-  EQF_CK(cudaMemsetAsync(u.p, 0, N0 * sizeof(double), stream));
   EQF_CK(cudaMemsetAsync(F.p, 0, N0 * sizeof(double), stream));
   EQF_CK(cudaMemsetAsync(b64.p, 0, N0 * sizeof(double), stream));
   dstate.alloc(ntraps);
@@ -230,7 +388,7 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
   d_cg_skip.alloc(ntraps);
   d_fail.alloc(1);
   EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
-  dpart.alloc(2 * (size_t)L[0].ntiles());
+  dpart.alloc(3 * (size_t)L[0].ntiles());
   if (opts.precision == EQF_PREC_FP32_IR)
     work.reset(new Work<float>(*this));
   else
@@ -241,7 +399,9 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
 }
 
 Batch::~Batch() {
-  if (graph) cudaGraphExecDestroy(graph);
+  for (auto& gx : graph)
+    if (gx) cudaGraphExecDestroy(gx);
+  for (auto& e : prof.ev) cudaEventDestroy(e);
   work.reset();
   if (stream) cudaStreamDestroy(stream);
 }
@@ -299,16 +459,22 @@ void Batch::build_levels() {
       L[l].geom[t] = g;
     }
   }
-  // offsets, fine offsets and tiles
+  // offsets, fine offsets and row tiles (about kTileNodes nodes each, whole rows)
+  const int tsz = opts.precision == EQF_PREC_FP32_IR ? 4 : 8;
+  const long long target = tsz == 4 ? kTileNodes : kTileNodes / 2;
   for (int l = 0; l < nlev; ++l) {
     long long off = 0;
     for (int t = 0; t < ntraps; ++t) {
       LevelGeom& g = L[l].geom[t];
       g.off = off;
-      const long long n = (long long)(g.nx + 1) * (g.ny + 1);
+      const long long P = g.nx + 1;
+      const long long n = P * (g.ny + 1);
       if (l > 0) g.fine_off = L[l - 1].geom[t].off;
-      for (long long k0 = 0; k0 < n; k0 += kTileNodes)
-        L[l].tiles.push_back(Tile{t, (int)k0, (int)std::min<long long>(n, k0 + kTileNodes)});
+      const int R = (int)std::max<long long>(1, target / P);
+      for (int r0 = 0; r0 <= g.ny; r0 += R) {
+        const int r1 = std::min(g.ny + 1, r0 + R);
+        L[l].tiles.push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
+      }
       off = align_up(off + n, 32);
     }
     L[l].nodes = off;
@@ -317,6 +483,85 @@ void Batch::build_levels() {
     L[l].dgeom.upload(L[l].geom.data(), ntraps, stream);
     L[l].dtiles.alloc(L[l].tiles.size());
     L[l].dtiles.upload(L[l].tiles.data(), L[l].tiles.size(), stream);
+    std::vector<float> tf((size_t)ntraps * kTabPerTrap);
+    std::vector<double> td((size_t)ntraps * kTabPerTrap);
+    for (int t = 0; t < ntraps; ++t) {
+      build_table<float, false>(L[l].geom[t], tf.data() + (size_t)t * kTabPerTrap);
+      build_table<double, false>(L[l].geom[t], td.data() + (size_t)t * kTabPerTrap);
+    }
+    L[l].tabf.alloc(tf.size());
+    L[l].tabf.upload(tf.data(), tf.size(), stream);
+    L[l].tabd.alloc(td.size());
+    L[l].tabd.upload(td.data(), td.size(), stream);
+    if (l == 0) {
+      std::vector<double> tm((size_t)ntraps * kTabPerTrap);
+      for (int t = 0; t < ntraps; ++t)
+        build_table<double, true>(L[0].geom[t], tm.data() + (size_t)t * kTabPerTrap);
+      tabM0.alloc(tm.size());
+      tabM0.upload(tm.data(), tm.size(), stream);
+    }
+    sync();  // host vectors go out of scope
+  }
+  // dynamic shared memory of the staged kernels
+  for (int l = 0; l < nlev; ++l) {
+    Level& Lv = L[l];
+    for (const Tile& tl : Lv.tiles) {
+      const LevelGeom& g = Lv.geom[tl.geom];
+      const long long P = g.nx + 1, n = P * (g.ny + 1), na = align_up(n, 32);
+      (void)n;
+      const long long ka = (long long)tl.k0 - P - 1;  // guarded halo window
+      const long long kb = (long long)tl.k1 + P + 1;
+      const size_t halo = guarded_bytes(ka, kb, tsz);
+      const size_t own = staged_bytes(tl.k0, tl.k1, tsz, na);
+      Lv.sm_cheb = std::max(Lv.sm_cheb, kSmemHeader + halo + 2 * own);
+      Lv.sm_resid = std::max(Lv.sm_resid, kSmemHeader + halo + own);
+      Lv.sm_cgdir = std::max(Lv.sm_cgdir, kSmemHeader + 2 * halo);
+      // first refinement residual: u (FP64, halo), F (FP64), d (FP32, halo)
+      Lv.sm_ir = std::max(Lv.sm_ir, kSmemHeader + guarded_bytes(ka, kb, 8) +
+                                        staged_bytes(tl.k0, tl.k1, 8, na) +
+                                        guarded_bytes(ka, kb, 4) +
+                                        (size_t)((kb - ka) * 8 + 15) / 16 * 16);
+      if (l > 0) {  // restriction into level l stages fine rows f(r0)-1 .. f(r1-1)+1
+        const LevelGeom& f = L[l - 1].geom[tl.geom];
+        auto c2f = [](int K, int nf, int h) { return h ? std::min(2 * K, nf) : K; };
+        const long long PF = f.nx + 1;
+        long long fr0 = std::max(0, c2f(tl.r0, f.ny, g.cy) - 1);
+        long long fr1 = std::min(f.ny + 1, c2f(tl.r1 - 1, f.ny, g.cy) + 2);
+        Lv.sm_restrict = std::max(Lv.sm_restrict,
+                                  kSmemHeader + staged_bytes(fr0 * PF, fr1 * PF, tsz,
+                                                             align_up(PF * (f.ny + 1), 32)));
+      }
+      if (l + 1 < nlev) {  // prolongation into level l stages coarse rows lo(r0) .. hi(r1-1)
+        const LevelGeom& c = L[l + 1].geom[tl.geom];
+        auto f2c_lo = [](int f, int nf, int h) {
+          return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2));
+        };
+        auto f2c_hi = [](int f, int nf, int h) {
+          return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2 + 1));
+        };
+        const long long PC = c.nx + 1;
+        const long long lo = f2c_lo(tl.r0, g.ny, c.cy), hi = f2c_hi(tl.r1 - 1, g.ny, c.cy);
+        Lv.sm_prolong = std::max(Lv.sm_prolong,
+                                 kSmemHeader + staged_bytes(lo * PC, (hi + 1) * PC, tsz,
+                                                            align_up(PC * (c.ny + 1), 32)));
+      }
+    }
+    for (size_t v : {Lv.sm_cheb, Lv.sm_resid, Lv.sm_cgdir, Lv.sm_restrict, Lv.sm_prolong})
+      if (v > kMaxDynSmem)
+        throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
+    if (l == 0 && Lv.sm_ir > kMaxDynSmem)
+      throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
+  }
+  {  // single-CTA coarsest solve when every trap's coarsest grid fits
+    Level& Lc = L[nlev - 1];
+    size_t need = 0;
+    for (const LevelGeom& g : Lc.geom) {
+      const long long n = (long long)(g.nx + 1) * (g.ny + 1), na = align_up(n, 32);
+      const long long gpad = ((g.nx + 2 + 7) / 8) * 8;
+      need = std::max(need, kSmemHeader + staged_bytes(0, n, tsz, na) +
+                                (size_t)(3 * na + 5 * gpad) * tsz);
+    }
+    Lc.sm_coarse = (nlev > 1 && need <= kMaxDynSmem) ? need : 0;
   }
   range.assign(ntraps, TileRange{0, 0});
   for (int i = 0; i < L[0].ntiles(); ++i) {
@@ -331,7 +576,35 @@ void Batch::build_levels() {
 
 // ---------------------------------------------------------------------------
 template <class T>
+static void allow_dyn_smem() {
+  const int mx = (int)kMaxDynSmem;
+  EQF_CK(cudaFuncSetAttribute(k_cheb<T, true, false, true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_cheb<T, true, false, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_cheb<T, false, false, true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_cheb<T, false, false, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_resid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_restrict<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_prolong<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_coarse_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              mx));
+  EQF_CK(cudaFuncSetAttribute(k_cg_dir<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              mx));
+  EQF_CK(cudaFuncSetAttribute(k_cg_dir<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              mx));
+  EQF_CK(cudaFuncSetAttribute(k_ir_first<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_ir_residual<T, true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(k_ir_residual<T, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+}
+
+template <class T>
 Work<T>::Work(Batch& b) : B(b) {
+  allow_dyn_smem<T>();
   lv.resize(B.nlev);
   for (int l = 0; l < B.nlev; ++l) {
     const size_t n = B.L[l].nodes;
@@ -351,7 +624,61 @@ Work<T>::Work(Batch& b) : B(b) {
   }
 }
 
+// Launch wrapper: profiler marks around one kernel launch.
+#define EQF_RUN(B_, cls_, launch_)                     \
+  do {                                                 \
+    unsigned long long* W = (B_).prof_begin(cls_);     \
+    (void)W;                                           \
+    launch_;                                           \
+    EQF_LAUNCH_CHECK();                                \
+    (B_).prof_end();                                   \
+  } while (0)
+
+// One Chebyshev step on a level (template flags chosen at run time).
+template <class T>
+static void cheb_step(Batch& B, cudaStream_t s, int lev, int nt, const LevelGeom* G,
+                      const Tile* tl, const T* tab, const int* skip, float ratio, int st,
+                      bool first, bool zero, bool dot, const T* b, const T* xin, T* xout, T* d,
+                      double* part) {
+  const int cls = lev > 0 ? KC_COARSE : (zero ? KC_SMOOTH0_FIRST : KC_SMOOTH0);
+  const size_t sm = zero ? 0 : B.L[lev].sm_cheb;
+  if (zero) {
+    if (dot)
+      EQF_RUN(B, cls, (k_cheb<T, true, true, true><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+    else
+      EQF_RUN(B, cls, (k_cheb<T, true, true, false><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+  } else if (first) {
+    if (dot)
+      EQF_RUN(B, cls, (k_cheb<T, true, false, true><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+    else
+      EQF_RUN(B, cls, (k_cheb<T, true, false, false><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+  } else {
+    if (dot)
+      EQF_RUN(B, cls, (k_cheb<T, false, false, true><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, st, b, xin, xout, d, part, W)));
+    else
+      EQF_RUN(B, cls, (k_cheb<T, false, false, false><<<nt, kThreads, sm, s>>>(
+                           G, tl, tab, skip, ratio, st, b, xin, xout, d, part, W)));
+  }
+}
+
+template <class T>
+static const T* level_tab(const Level& L);
+template <>
+const float* level_tab<float>(const Level& L) {
+  return L.tabf.p;
+}
+template <>
+const double* level_tab<double>(const Level& L) {
+  return L.tabd.p;
+}
+
 // V-cycle on level `lev` with rhs lv[lev].b; returns the buffer holding x.
+// With `dot`, the last smoothing step also writes partials of b.x (= r.z on level 0).
 template <class T>
 T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
   const Level& Lv_ = B.L[lev];
@@ -360,71 +687,54 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
   const int* skip = B.d_cg_skip.p;
   const LevelGeom* G = Lv_.dgeom.p;
   const Tile* tl = Lv_.dtiles.p;
+  const T* tab = level_tab<T>(Lv_);
   double* part = B.dpart.p;
   T* cur = v.x.p;
   T* oth = v.y.p;
   const bool coarsest = lev == B.nlev - 1;
   const float ratio = coarsest ? 0.f : (float)B.opts.cheb_ratio;
   const int deg_pre = coarsest ? B.opts.cheb_coarse : B.opts.cheb_pre;
-  // pre-smoothing (or coarsest solve) from zero
-  {
-    const bool last_dot = dot && coarsest && deg_pre == 1;
-    if (last_dot)
-      k_cheb<T, true, true, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur, cur,
-                                                          v.d.p, part);
-    else
-      k_cheb<T, true, true, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
-                                                           cur, v.d.p, part);
-    EQF_LAUNCH_CHECK();
-    for (int st = 1; st < deg_pre; ++st) {
-      const bool ld = dot && coarsest && st == deg_pre - 1;
-      if (ld)
-        k_cheb<T, false, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p, cur,
-                                                              oth, v.d.p, part);
-      else
-        k_cheb<T, false, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
-                                                               cur, oth, v.d.p, part);
-      EQF_LAUNCH_CHECK();
-      std::swap(cur, oth);
-    }
+  if (coarsest && Lv_.sm_coarse && !dot) {
+    // the whole coarsest solve in one CTA per trap
+    EQF_RUN(B, KC_COARSE,
+            (k_coarse_solve<T><<<B.ntraps, kThreads, Lv_.sm_coarse, s>>>(G, tab, skip, deg_pre,
+                                                                          v.b.p, cur)));
+    return cur;
+  }
+  // pre-smoothing (or the coarsest-level solve) from zero
+  cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, 0, true, true,
+               dot && coarsest && deg_pre == 1, v.b.p, cur, cur, v.d.p, part);
+  for (int st = 1; st < deg_pre; ++st) {
+    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, false, false,
+                 dot && coarsest && st == deg_pre - 1, v.b.p, cur, oth, v.d.p, part);
+    std::swap(cur, oth);
   }
   if (coarsest) return cur;
   // residual, restriction, coarse correction, prolongation
-  k_resid<T><<<nt, kThreads, 0, s>>>(G, tl, skip, v.b.p, cur, v.t.p);
-  EQF_LAUNCH_CHECK();
+  const int c0 = lev > 0 ? KC_COARSE : KC_RESID0;
+  EQF_RUN(B, c0,
+          (k_resid<T><<<nt, kThreads, Lv_.sm_resid, s>>>(G, tl, tab, skip, v.b.p, cur, v.t.p,
+                                                          W)));
   const Level& Lc = B.L[lev + 1];
-  k_restrict<T><<<Lc.ntiles(), kThreads, 0, s>>>(Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p,
-                                                  lv[lev + 1].b.p);
-  EQF_LAUNCH_CHECK();
+  EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
+          (k_restrict<T><<<Lc.ntiles(), kThreads, Lc.sm_restrict, s>>>(
+              Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
   T* xc = vcycle(s, lev + 1, false);
-  k_prolong<T><<<nt, kThreads, 0, s>>>(G, Lc.dgeom.p, tl, skip, xc, cur);
-  EQF_LAUNCH_CHECK();
+  EQF_RUN(B, lev > 0 ? KC_COARSE : KC_PROLONG0,
+          (k_prolong<T><<<nt, kThreads, Lv_.sm_prolong, s>>>(G, Lc.dgeom.p, tl, skip, xc, cur,
+                                                              W)));
   // post-smoothing from the corrected iterate
   const int deg_post = B.opts.cheb_post;
   for (int st = 0; st < deg_post; ++st) {
-    const bool ld = dot && st == deg_post - 1;
-    if (st == 0) {
-      if (ld)
-        k_cheb<T, true, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
-                                                             oth, v.d.p, part);
-      else
-        k_cheb<T, true, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, 0, v.b.p, cur,
-                                                              oth, v.d.p, part);
-    } else {
-      if (ld)
-        k_cheb<T, false, false, true><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
-                                                              cur, oth, v.d.p, part);
-      else
-        k_cheb<T, false, false, false><<<nt, kThreads, 0, s>>>(G, tl, skip, ratio, st, v.b.p,
-                                                               cur, oth, v.d.p, part);
-    }
-    EQF_LAUNCH_CHECK();
+    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, st == 0, false,
+                 dot && st == deg_post - 1, v.b.p, cur, oth, v.d.p, part);
     std::swap(cur, oth);
   }
   return cur;
 }
 
-// One refinement sweep: FP64 residual, preconditioned CG on the correction, update.
+// One refinement sweep: FP64 residual, preconditioned CG on the correction,
+// update.  The step reads U[cur] and writes U[1 - cur].
 template <class T>
 void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   const Level& L0 = B.L[0];
@@ -432,86 +742,83 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   const int nb = (B.ntraps + 127) / 128;
   const LevelGeom* G = L0.dgeom.p;
   const Tile* tl = L0.dtiles.p;
+  const T* tab = level_tab<T>(L0);
   double* part = B.dpart.p;
   T* r = lv[0].b.p;  // CG residual = V-cycle rhs on level 0
   const bool fp32 = std::is_same<T, float>::value;
   const double tol_rel = fp32 ? B.opts.inner_tol : 0.0;
   const double tol_abs = fp32 ? 0.0 : B.opts.rtol;
+  double* u_out = B.U[1 - B.cur].p;
+  float* d_out = B.Dd[1 - B.cur].p;
   if (first)
-    k_ir_residual<T, true><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, B.F.p, B.u.p, B.b64.p,
-                                                    r, part, nt);
+    EQF_RUN(B, KC_IR_RESID_FIRST,
+            (k_ir_first<T><<<nt, kThreads, L0.sm_ir, s>>>(
+                G, tl, L0.tabd.p, B.tabM0.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
+                B.b64.p, u_out, d_out, r, part, nt, W)));
   else
-    k_ir_residual<T, false><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, B.F.p, B.u.p, B.b64.p,
-                                                     r, part, nt);
-  EQF_LAUNCH_CHECK();
-  k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
-                            B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p);
-  EQF_LAUNCH_CHECK();
+    EQF_RUN(B, KC_IR_RESID,
+            (k_ir_residual<T, false><<<nt, kThreads, L0.sm_ir, s>>>(
+                G, tl, L0.tabd.p, B.d_ir_done.p, B.b64.p, u_out, d_out, r, part, nt, W)));
+  EQF_RUN(B, KC_SCALAR,
+          (k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
+                                     B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p)));
   EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   T* pin = p0.p;
   T* pout = p1.p;
   for (int it = 0; it < B.opts.max_iters; ++it) {
     T* z = vcycle(s, 0, true);
-    k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p);
-    EQF_LAUNCH_CHECK();
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
     if (it == 0)
-      k_cg_dir<T, true><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, z, pin, pout,
-                                                 q.p, part);
+      EQF_RUN(B, KC_CG_DIR,
+              (k_cg_dir<T, true><<<nt, kThreads, L0.sm_cgdir, s>>>(
+                  G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
     else
-      k_cg_dir<T, false><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, z, pin, pout,
-                                                  q.p, part);
-    EQF_LAUNCH_CHECK();
-    k_s_pq<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p);
-    EQF_LAUNCH_CHECK();
-    k_cg_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p, xs.p, r,
-                                           part);
-    EQF_LAUNCH_CHECK();
-    k_s_rr<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
-                              B.d_cg_skip.p);
-    EQF_LAUNCH_CHECK();
+      EQF_RUN(B, KC_CG_DIR,
+              (k_cg_dir<T, false><<<nt, kThreads, L0.sm_cgdir, s>>>(
+                  G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_pq<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
+    EQF_RUN(B, KC_CG_UPDATE,
+            (k_cg_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p,
+                                                    xs.p, r, part, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_rr<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
+                                       B.d_cg_skip.p)));
     std::swap(pin, pout);
   }
-  k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, B.u.p);
-  EQF_LAUNCH_CHECK();
+  EQF_RUN(B, KC_IR_UPDATE,
+          (k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, u_out, d_out, W)));
 }
 
-__global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
-                          const double* __restrict__ part, int ntiles, double rtol,
-                          CgState* __restrict__ st, int* __restrict__ ir_done,
-                          int* __restrict__ fail) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ntraps || ir_done[t]) return;
-  CgState s = st[t];
-  s.r64 = trap_sum(part + ntiles, range[t]);
-  if (s.r64 <= rtol * rtol * s.bb || s.bb == 0.0)
-    ir_done[t] = 1;
-  else
-    atomicAdd(fail, 1);
-  st[t] = s;
-}
-
-// Final FP64 residual check after the last sweep: marks converged traps and
-// counts the others in d_fail.
+// Final FP64 residual check after the last sweep: marks converged traps, counts
+// the others in d_fail and sets the next step's extrapolation factor.
 template <class T>
 void Work<T>::enqueue_check(cudaStream_t s) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
-  k_ir_residual<T, false><<<nt, kThreads, 0, s>>>(L0.dgeom.p, L0.dtiles.p, B.d_ir_done.p, B.F.p,
-                                                   B.u.p, B.b64.p, lv[0].b.p, B.dpart.p, nt);
-  EQF_LAUNCH_CHECK();
-  k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
-                                                    B.opts.rtol, B.dstate.p, B.d_ir_done.p,
-                                                    B.d_fail.p);
-  EQF_LAUNCH_CHECK();
+  EQF_RUN(B, KC_IR_RESID,
+          (k_ir_residual<T, true><<<nt, kThreads, L0.sm_ir, s>>>(
+              L0.dgeom.p, L0.dtiles.p, L0.tabd.p, B.d_ir_done.p, B.b64.p, B.U[1 - B.cur].p,
+              B.Dd[1 - B.cur].p, lv[0].b.p, B.dpart.p, nt, W)));
+  EQF_RUN(B, KC_SCALAR,
+          (k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
+                                                             B.opts.rtol, B.dstate.p,
+                                                             B.d_ir_done.p, B.d_fail.p)));
 }
 
 void Batch::run_step() {
-  EQF_CK(cudaMemsetAsync(d_ir_done.p, 0, ntraps * sizeof(int), stream));
   for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
   work->enqueue_check(stream);
 }
 
 void Batch::check_fail() {
+  int derr = 0;
+  EQF_CK(cudaMemcpyFromSymbolAsync(&derr, g_eqf_device_error, sizeof(int), 0,
+                                   cudaMemcpyDeviceToHost, stream));
+  sync();
+  if (derr)
+    throw Error(EQF_ERR_CUDA, "a device-side bounded wait gave up (staging copy never landed)");
   int f = 0;
   EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
   sync();
@@ -525,21 +832,22 @@ void Batch::check_fail() {
 void Batch::step(int n) {
   if (cells_dirty) rebuild_cells();
   for (int k = 0; k < n; ++k) {
-    if (opts.use_graph) {
-      if (!graph) {
+    if (opts.use_graph && !prof.on) {
+      cudaGraphExec_t& gx = graph[cur];
+      if (!gx) {
         cudaGraph_t gr;
         EQF_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         run_step();
         EQF_CK(cudaStreamEndCapture(stream, &gr));
-        EQF_CK(cudaGraphInstantiate(&graph, gr, 0));
+        EQF_CK(cudaGraphInstantiate(&gx, gr, 0));
         cudaGraphDestroy(gr);
       }
-      EQF_CK(cudaGraphLaunch(graph, stream));
+      EQF_CK(cudaGraphLaunch(gx, stream));
     } else {
       run_step();
     }
     if (opts.adaptive) {
-      // add sweeps for traps that missed rtol (others are skipped by ir_done)
+      // add sweeps for traps that missed rtol (the others are skipped by ir_done)
       int f = 0;
       for (int extra = 0; extra < 8; ++extra) {
         EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -551,9 +859,11 @@ void Batch::step(int n) {
       }
       if (f != 0) {
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        cur = 1 - cur;
         throw Error(EQF_ERR_NOT_CONVERGED, "trap(s) missed rtol after extra refinement sweeps");
       }
     }
+    cur = 1 - cur;
     ++steps_done;
   }
 }
@@ -740,13 +1050,13 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
   o->adaptive = 1;
   if (precision == EQF_PREC_FP32_IR) {
     o->rtol = 1e-9;
-    o->max_sweeps = 3;
-    o->max_iters = 8;
+    o->max_sweeps = 2;
+    o->max_iters = 6;
     o->inner_tol = 1e-5;
   } else if (precision == EQF_PREC_FP64) {
     o->rtol = 1e-10;
     o->max_sweeps = 1;
-    o->max_iters = 30;
+    o->max_iters = 12;
     o->inner_tol = 0.0;
   } else {
     return EQF_ERR_INVALID;
@@ -850,8 +1160,14 @@ int eqf_set_nodal(eqf_batch* b, int32_t trap, const double* c) {
     EQF_TRAP_CHECK(b, trap);
     EQF_REQUIRE(c != nullptr, "null field");
     Batch& B = *b->impl;
-    EQF_CK(cudaMemcpyAsync(B.u.p + B.L[0].geom[trap].off, c, B.fine_nodes(trap) * sizeof(double),
+    const long long off = B.L[0].geom[trap].off;
+    EQF_CK(cudaMemcpyAsync(B.u_cur() + off, c, B.fine_nodes(trap) * sizeof(double),
                            cudaMemcpyHostToDevice, B.stream));
+    // a new field invalidates the increment history of the initial guess
+    EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_nodes(trap) * sizeof(float), B.stream));
+    EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
+                               offsetof(eqf::CgState, gamma),
+                           0, 2 * sizeof(double), B.stream));
     B.sync();
   });
 }
@@ -884,7 +1200,7 @@ int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
     int ns = 0;
     B.build_segments((int)n, ent.p, counts.p, perm, seg, ns);
     eqf::k_seg_sum<true><<<(ns + 255) / 256, 256, 0, B.stream>>>(ns, seg.p, perm.p, ent.p, dv.p,
-                                                                  B.u.p);
+                                                                  B.u_cur());
     EQF_LAUNCH_CHECK();
     B.sync();
   });
@@ -904,7 +1220,7 @@ int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c) {
     EQF_TRAP_CHECK(b, trap);
     EQF_REQUIRE(c != nullptr, "null output");
     Batch& B = *b->impl;
-    EQF_CK(cudaMemcpyAsync(c, B.u.p + B.L[0].geom[trap].off, B.fine_nodes(trap) * sizeof(double),
+    EQF_CK(cudaMemcpyAsync(c, B.u_cur() + B.L[0].geom[trap].off, B.fine_nodes(trap) * sizeof(double),
                            cudaMemcpyDeviceToHost, B.stream));
     B.sync();
     B.check_fail();
@@ -923,7 +1239,7 @@ int eqf_read_cells(eqf_batch* b, int32_t trap, int64_t n, double* c) {
     out.alloc(n);
     const int c0 = B.cell_first[trap];
     eqf::k_cells_gather<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
-        (int)n, B.d_ent_node.p + 3 * (size_t)c0, B.d_ent_w.p + 3 * (size_t)c0, B.u.p, out.p);
+        (int)n, B.d_ent_node.p + 3 * (size_t)c0, B.d_ent_w.p + 3 * (size_t)c0, B.u_cur(), out.p);
     EQF_LAUNCH_CHECK();
     EQF_CK(cudaMemcpyAsync(c, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, B.stream));
     B.sync();
@@ -936,7 +1252,7 @@ static double trap_reduce(Batch& B, int trap, int what) {
   eqf::DevBuf<double> part;
   part.alloc(tr.count);
   eqf::k_trap_reduce<<<tr.count, eqf::kThreads, 0, B.stream>>>(
-      B.L[0].dgeom.p, B.L[0].dtiles.p, tr.first, B.u.p, what, part.p);
+      B.L[0].dgeom.p, B.L[0].dtiles.p, tr.first, B.u_cur(), what, part.p);
   EQF_LAUNCH_CHECK();
   std::vector<double> h(tr.count);
   EQF_CK(cudaMemcpyAsync(h.data(), part.p, tr.count * sizeof(double), cudaMemcpyDeviceToHost,
@@ -979,6 +1295,106 @@ int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64
     if (sweeps) *sweeps = st.sweeps;
     if (iters) *iters = st.iters;
     if (last_rel_residual) *last_rel_residual = st.bb > 0 ? std::sqrt(st.r64 / st.bb) : 0.0;
+  });
+}
+
+int eqf_set_cell_rates_all(eqf_batch* b, int64_t n, const double* s) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    if (B.cells_dirty) B.rebuild_cells();
+    EQF_REQUIRE(n == B.ncells && (n == 0 || s), "rate count mismatch");
+    if (n == 0) return;
+    EQF_CK(cudaMemcpyAsync(B.d_cell_s.p, s, n * sizeof(double), cudaMemcpyHostToDevice,
+                           B.stream));
+    B.refresh_load();
+    // keep the host copies consistent for later rebuilds
+    for (int t = 0; t < B.ntraps; ++t)
+      std::copy(s + B.cell_first[t], s + B.cell_first[t + 1], B.cell_s[t].begin());
+  });
+}
+
+int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    if (B.cells_dirty) B.rebuild_cells();
+    EQF_REQUIRE(n == B.ncells && (n == 0 || c), "cell count mismatch");
+    if (n == 0) return;
+    if (B.d_cells_out.n < (size_t)n) B.d_cells_out.alloc(n);
+    eqf::k_cells_gather<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
+        (int)n, B.d_ent_node.p, B.d_ent_w.p, B.u_cur(), B.d_cells_out.p);
+    EQF_LAUNCH_CHECK();
+    EQF_CK(cudaMemcpyAsync(c, B.d_cells_out.p, n * sizeof(double), cudaMemcpyDeviceToHost,
+                           B.stream));
+    B.sync();
+    B.check_fail();
+  });
+}
+
+int eqf_stream(eqf_batch* b, void** stream) {
+  if (!b || !stream) return EQF_ERR_INVALID;
+  *stream = (void*)b->impl->stream;
+  return EQF_OK;
+}
+
+int eqf_profile(eqf_batch* b, int32_t enable) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    B.sync();
+    eqf::Prof& P = B.prof;
+    if (enable) {
+      const size_t cap = 1u << 16;
+      if (P.ev.empty()) {
+        P.ev.resize(2 * cap);
+        for (auto& e : P.ev) EQF_CK(cudaEventCreate(&e));
+        P.cls.assign(cap, -1);
+        P.work.alloc(cap);
+      }
+      EQF_CK(cudaMemsetAsync(P.work.p, 0, cap * sizeof(unsigned long long), B.stream));
+      B.sync();
+      P.used = 0;
+      P.overflow = false;
+      P.on = true;
+    } else {
+      P.on = false;
+    }
+  });
+}
+
+int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
+                     int64_t* nodes, double* bytes) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    EQF_REQUIRE(n_classes >= EQF_PROF_CLASSES && ms && launches && nodes && bytes,
+                "profile arrays too short");
+    B.sync();
+    eqf::Prof& P = B.prof;
+    EQF_REQUIRE(!P.overflow, "profiler record pool overflowed (profile fewer steps)");
+    std::vector<unsigned long long> w(P.used);
+    if (P.used)
+      EQF_CK(cudaMemcpy(w.data(), P.work.p, P.used * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost));
+    for (int c = 0; c < n_classes; ++c) {
+      ms[c] = 0.0;
+      launches[c] = 0;
+      nodes[c] = 0;
+      bytes[c] = 0.0;
+    }
+    const int tsize = B.opts.precision == EQF_PREC_FP32_IR ? 4 : 8;
+    for (size_t r = 0; r < P.used; ++r) {
+      float t = 0.f;
+      EQF_CK(cudaEventElapsedTime(&t, P.ev[2 * r], P.ev[2 * r + 1]));
+      const int c = P.cls[r];
+      ms[c] += t;
+      launches[c] += 1;
+      nodes[c] += (int64_t)w[r];
+      double per = 0.0;
+      eqf::class_bytes(c, tsize, per);
+      bytes[c] += per * (double)w[r];
+    }
   });
 }
 

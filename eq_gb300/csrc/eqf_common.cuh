@@ -22,6 +22,16 @@ namespace eqf {
 
 enum : unsigned { WALL_BOTTOM = 1u, WALL_TOP = 2u, WALL_LEFT = 4u, WALL_RIGHT = 8u };
 
+// Lengths and physics of one level in one arithmetic type (kept in both FP32 and
+// FP64 so kernels never convert or divide per node).
+template <class T>
+struct Lens {
+  T hx, hy, hxl, hyl;      // regular spacing and last column/row cell sizes
+  T ihx, ihy, ihxl, ihyl;  // their reciprocals
+  T alpha, beta;           // mass scale (1 + dt*g) and dt*D
+  T adv;                   // advection: dt * v_y(y) = -adv * y
+};
+
 // One trap on one multigrid level.
 struct LevelGeom {
   long long off;      // offset of node (0,0) in the level's arrays
@@ -31,21 +41,35 @@ struct LevelGeom {
   int cx, cy;         // 1 if this level halves x / y relative to the finer level
   int fine_nx, fine_ny;  // cell counts of the finer level (for transfers)
   long long fine_off;    // node offset of this trap on the finer level
-  double hx, hy;         // regular spacing
+  int adv_on;            // advection present (disables the uniform-interior path)
+  double hx, hy;         // regular spacing (host-side construction)
   double hxl, hyl;       // size of the last column / row of cells
   double alpha, beta;    // mass scale (1 + dt*g) and dt*D
-  double adv;            // advection: v_y(y) = -adv * y  (0: none)
+  double adv;            // advection: dt * v_y(y) = -adv * y  (0: none)
+  Lens<double> ld;
+  Lens<float> lf;
   // Uniform-interior stencil (nodes with 2 <= i <= ny-2 and 2 <= j <= nx-2).
   double cC, cE, cN, cD;  // centre, east=west, north=south, NE=SW
-  float fC, fE, fN, fD;
+  double cCinv;           // 1 / cC
+  double mC, mE, mN, mD;  // uniform-interior mass stencil (alpha = 1)
+  float fC, fE, fN, fD, fCinv;
   float lam_max;          // upper bound of spectrum(D^-1 A)
   float lam_min;          // lower estimate (coarsest-level solve)
 };
 
-// A contiguous node range [k0, k1) of one trap on one level (one CTA each).
+template <class T>
+EQF_HD const Lens<T>& lens(const LevelGeom& g);
+template <>
+EQF_HD const Lens<double>& lens<double>(const LevelGeom& g) { return g.ld; }
+template <>
+EQF_HD const Lens<float>& lens<float>(const LevelGeom& g) { return g.lf; }
+
+// Rows [r0, r1) of one trap on one level (one CTA each); k0 = r0*(nx+1) and
+// k1 = r1*(nx+1) are the node range.
 struct Tile {
-  int geom;   // index into the level's LevelGeom array
+  int geom;  // index into the level's LevelGeom array (= trap index)
   int k0, k1;
+  int r0, r1;
 };
 
 template <class T>
@@ -58,8 +82,9 @@ EQF_HD bool is_dirichlet(const LevelGeom& g, int i, int j) {
          ((g.walls & WALL_LEFT) && j == 0) || ((g.walls & WALL_RIGHT) && j == g.nx);
 }
 
+// integer-only: 2 <= i <= ny-2 and 2 <= j <= nx-2, no advection
 EQF_HD bool is_uniform_interior(const LevelGeom& g, int i, int j) {
-  return i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 2 && g.adv == 0.0;
+  return i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 2 && !g.adv_on;
 }
 
 // Full stencil of node (i, j) from the surrounding cell sizes, in arithmetic T.
@@ -69,77 +94,73 @@ EQF_HD bool is_uniform_interior(const LevelGeom& g, int i, int j) {
 // Advection (c2): dt * int v_y d(phi_b)/dy phi_a over each triangle with a P1 v_y.
 template <class T>
 EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
-  const T hx = T(g.hx), hy = T(g.hy);
-  const T hxl = j > 0 ? (j == g.nx ? T(g.hxl) : hx) : T(0);
-  const T hxr = j < g.nx ? (j == g.nx - 1 ? T(g.hxl) : hx) : T(0);
-  const T hyd = i > 0 ? (i == g.ny ? T(g.hyl) : hy) : T(0);
-  const T hyu = i < g.ny ? (i == g.ny - 1 ? T(g.hyl) : hy) : T(0);
-  const T a = T(g.alpha), b = T(g.beta);
+  const Lens<T>& L = lens<T>(g);
+  const T hxl = j > 0 ? (j == g.nx ? L.hxl : L.hx) : T(0);
+  const T hxr = j < g.nx ? (j == g.nx - 1 ? L.hxl : L.hx) : T(0);
+  const T hyd = i > 0 ? (i == g.ny ? L.hyl : L.hy) : T(0);
+  const T hyu = i < g.ny ? (i == g.ny - 1 ? L.hyl : L.hy) : T(0);
+  const T ihxl = j > 0 ? (j == g.nx ? L.ihxl : L.ihx) : T(0);
+  const T ihxr = j < g.nx ? (j == g.nx - 1 ? L.ihxl : L.ihx) : T(0);
+  const T ihyd = i > 0 ? (i == g.ny ? L.ihyl : L.ihy) : T(0);
+  const T ihyu = i < g.ny ? (i == g.ny - 1 ? L.ihyl : L.ihy) : T(0);
+  const T a = L.alpha, hb = T(0.5) * L.beta;
   const T sy = hyd + hyu, sx = hxl + hxr;
+  const T a24 = a * T(1.0 / 24.0), a12 = a * T(1.0 / 12.0);
   Sten<T> s;
-  T ke = hxr > T(0) ? b * sy / (T(2) * hxr) : T(0);
-  T kw = hxl > T(0) ? b * sy / (T(2) * hxl) : T(0);
-  T kn = hyu > T(0) ? b * sx / (T(2) * hyu) : T(0);
-  T ks = hyd > T(0) ? b * sx / (T(2) * hyd) : T(0);
-  s.e = a * hxr * sy / T(24) - ke;
-  s.w = a * hxl * sy / T(24) - kw;
-  s.n = a * hyu * sx / T(24) - kn;
-  s.s = a * hyd * sx / T(24) - ks;
-  s.ne = a * hxr * hyu / T(12);
-  s.sw = a * hxl * hyd / T(12);
-  s.c = a * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu) / T(12) + ke + kw +
-        kn + ks;
-  if (g.adv != 0.0) {
-    // v_y at the node rows: v(y) = -adv*y with y measured on this level's grid
-    const T y0 = (i == g.ny) ? T(g.hy) * T(g.ny - 1) + T(g.hyl) : T(g.hy) * T(i);
+  const T ke = hb * sy * ihxr, kw = hb * sy * ihxl;  // zero where the cell is missing
+  const T kn = hb * sx * ihyu, ks = hb * sx * ihyd;
+  s.e = a24 * hxr * sy - ke;
+  s.w = a24 * hxl * sy - kw;
+  s.n = a24 * hyu * sx - kn;
+  s.s = a24 * hyd * sx - ks;
+  s.ne = a12 * hxr * hyu;
+  s.sw = a12 * hxl * hyd;
+  s.c = a12 * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu) + ke + kw + kn + ks;
+  if (g.adv_on) {
+    // v_y at the node rows: dt*v(y) = -adv*y with y measured on this level's grid
+    const T y0 = (i == g.ny) ? L.hy * T(g.ny - 1) + L.hyl : L.hy * T(i);
     const T yd = y0 - hyd, yu = y0 + hyu;
-    const T va = -T(g.adv) * y0, vd = -T(g.adv) * yd, vu = -T(g.adv) * yu;
-    // C_ab = dt-scaled in adv; each triangle: (area/12) * dphi_b/dy * (v_a + sum v)
+    const T va = -L.adv * y0, vd = -L.adv * yd, vu = -L.adv * yu;
+    // each triangle adds (area/12) * dphi_b/dy * (v_a + sum of its vertex v)
     // Cell UR (x in [0,hxr], y in [0,hyu]), both triangles contain the node.
     if (hxr > T(0) && hyu > T(0)) {
-      const T A = hxr * hyu / T(2);
+      const T A12 = hxr * hyu * T(1.0 / 24.0);
       // lower-right (v0 = node, v1 = E, v3 = NE): dphi/dy: v0 0, v1 -1/hyu, v3 1/hyu
-      T vs = va + va + vu;  // v at (node, E, NE): E is on the node row, NE on the upper
-      T f = A / T(12) * (va + vs);
-      s.e += f * (-T(1) / hyu);
-      s.ne += f * (T(1) / hyu);
+      T f = A12 * (va + (va + va + vu)) * ihyu;
+      s.e -= f;
+      s.ne += f;
       // upper-left (v0 = node, v2 = N, v3 = NE): dphi/dy: v0 -1/hyu, v2 1/hyu, v3 0
-      vs = va + vu + vu;
-      f = A / T(12) * (va + vs);
-      s.c += f * (-T(1) / hyu);
-      s.n += f * (T(1) / hyu);
+      f = A12 * (va + (va + vu + vu)) * ihyu;
+      s.c -= f;
+      s.n += f;
     }
     // Cell LL (x in [-hxl,0], y in [-hyd,0]), node is its v3 corner, both triangles.
     if (hxl > T(0) && hyd > T(0)) {
-      const T A = hxl * hyd / T(2);
+      const T A12 = hxl * hyd * T(1.0 / 24.0);
       // lower-right (v0 = SW, v1 = S, v3 = node): dphi/dy: v0 0, v1 -1/hyd, v3 1/hyd
-      T vs = vd + vd + va;
-      T f = A / T(12) * (va + vs);
-      s.s += f * (-T(1) / hyd);
-      s.c += f * (T(1) / hyd);
+      T f = A12 * (va + (vd + vd + va)) * ihyd;
+      s.s -= f;
+      s.c += f;
       // upper-left (v0 = SW, v2 = W, v3 = node): dphi/dy: v0 -1/hyd, v2 1/hyd, v3 0
-      vs = vd + va + va;
-      f = A / T(12) * (va + vs);
-      s.sw += f * (-T(1) / hyd);
-      s.w += f * (T(1) / hyd);
+      f = A12 * (va + (vd + va + va)) * ihyd;
+      s.sw -= f;
+      s.w += f;
     }
     // Cell LR (x in [0,hxr], y in [-hyd,0]): node is its v2 corner (upper-left tri).
     if (hxr > T(0) && hyd > T(0)) {
-      const T A = hxr * hyd / T(2);
+      const T A12 = hxr * hyd * T(1.0 / 24.0);
       // upper-left (v0 = S, v2 = node, v3 = E): dphi/dy: v0 -1/hyd, v2 1/hyd, v3 0
-      const T vs = vd + va + va;
-      const T f = A / T(12) * (va + vs);
-      s.s += f * (-T(1) / hyd);
-      s.c += f * (T(1) / hyd);
+      const T f = A12 * (va + (vd + va + va)) * ihyd;
+      s.s -= f;
+      s.c += f;
     }
     // Cell UL (x in [-hxl,0], y in [0,hyu]): node is its v1 corner (lower-right tri).
     if (hxl > T(0) && hyu > T(0)) {
-      const T A = hxl * hyu / T(2);
+      const T A12 = hxl * hyu * T(1.0 / 24.0);
       // lower-right (v0 = W, v1 = node, v3 = N): dphi/dy: v0 0, v1 -1/hyu, v3 1/hyu
-      const T vs = va + va + vu;
-      const T f = A / T(12) * (va + vs);
-      s.c += f * (-T(1) / hyu);
-      s.n += f * (T(1) / hyu);
+      const T f = A12 * (va + (va + va + vu)) * ihyu;
+      s.c -= f;
+      s.n += f;
     }
   }
   if (g.walls) {
@@ -172,23 +193,36 @@ EQF_HD Sten<double> stencil_at<double>(const LevelGeom& g, int i, int j) {
   return stencil_general<double>(g, i, j);
 }
 
+// 1 / diagonal of the operator row
+template <class T>
+EQF_HD T inv_diag(const LevelGeom& g, int i, int j, const Sten<T>& s);
+template <>
+EQF_HD float inv_diag<float>(const LevelGeom& g, int i, int j, const Sten<float>& s) {
+  return is_uniform_interior(g, i, j) ? g.fCinv : 1.f / s.c;
+}
+template <>
+EQF_HD double inv_diag<double>(const LevelGeom& g, int i, int j, const Sten<double>& s) {
+  return is_uniform_interior(g, i, j) ? g.cCinv : 1.0 / s.c;
+}
+
 // Mass-matrix stencil (unscaled, alpha = 1, no stiffness): the u0*v part of L.
 template <class T>
 EQF_HD Sten<T> mass_stencil(const LevelGeom& g, int i, int j) {
-  const T hx = T(g.hx), hy = T(g.hy);
-  const T hxl = j > 0 ? (j == g.nx ? T(g.hxl) : hx) : T(0);
-  const T hxr = j < g.nx ? (j == g.nx - 1 ? T(g.hxl) : hx) : T(0);
-  const T hyd = i > 0 ? (i == g.ny ? T(g.hyl) : hy) : T(0);
-  const T hyu = i < g.ny ? (i == g.ny - 1 ? T(g.hyl) : hy) : T(0);
+  const Lens<T>& L = lens<T>(g);
+  const T hxl = j > 0 ? (j == g.nx ? L.hxl : L.hx) : T(0);
+  const T hxr = j < g.nx ? (j == g.nx - 1 ? L.hxl : L.hx) : T(0);
+  const T hyd = i > 0 ? (i == g.ny ? L.hyl : L.hy) : T(0);
+  const T hyu = i < g.ny ? (i == g.ny - 1 ? L.hyl : L.hy) : T(0);
   const T sy = hyd + hyu, sx = hxl + hxr;
+  const T c24 = T(1.0 / 24.0), c12 = T(1.0 / 12.0);
   Sten<T> s;
-  s.e = hxr * sy / T(24);
-  s.w = hxl * sy / T(24);
-  s.n = hyu * sx / T(24);
-  s.s = hyd * sx / T(24);
-  s.ne = hxr * hyu / T(12);
-  s.sw = hxl * hyd / T(12);
-  s.c = (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu) / T(12);
+  s.e = c24 * hxr * sy;
+  s.w = c24 * hxl * sy;
+  s.n = c24 * hyu * sx;
+  s.s = c24 * hyd * sx;
+  s.ne = c12 * hxr * hyu;
+  s.sw = c12 * hxl * hyd;
+  s.c = c12 * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu);
   return s;
 }
 

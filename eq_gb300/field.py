@@ -160,6 +160,41 @@ class TrapBatch:
     def sync(self):
         self._ck(self._lib.eqf_sync(self._h))
 
+    @property
+    def n_cells_total(self) -> int:
+        return int(sum(self._ncells))
+
+    def set_cell_rates_all(self, s: np.ndarray):
+        s = np.ascontiguousarray(s, dtype=np.float64).ravel()
+        self._ck(self._lib.eqf_set_cell_rates_all(self._h, len(s), _dp(s)))
+
+    def read_cells_all(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.n_cells_total)
+        self._ck(self._lib.eqf_read_cells_all(self._h, len(out), _dp(out)))
+        return out
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the batch as an integer (for external CUDA events)."""
+        v = C.c_void_p()
+        self._ck(self._lib.eqf_stream(self._h, C.byref(v)))
+        return int(v.value or 0)
+
+    def profile(self, enable: bool):
+        self._ck(self._lib.eqf_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self) -> Dict[str, Dict[str, float]]:
+        n = len(_lib.PROF_CLASSES)
+        ms = np.zeros(n)
+        bts = np.zeros(n)
+        la = np.zeros(n, dtype=np.int64)
+        nd = np.zeros(n, dtype=np.int64)
+        i64 = C.POINTER(C.c_int64)
+        self._ck(self._lib.eqf_profile_read(self._h, n, _dp(ms), la.ctypes.data_as(i64),
+                                            nd.ctypes.data_as(i64), _dp(bts)))
+        return {name: {"ms": float(ms[i]), "launches": int(la[i]), "nodes": int(nd[i]),
+                       "bytes": float(bts[i])} for i, name in enumerate(_lib.PROF_CLASSES)}
+
 
 @dataclass
 class DiffusionParams:

@@ -148,6 +148,32 @@ int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64
 /* Waits for queued device work and reports deferred errors (convergence). */
 int eqf_sync(eqf_batch* b);
 
+/* Batch-wide cell I/O for the per-step host exchange (one copy each way): rates
+ * and concentrations of every trap's cells, concatenated in trap order (the
+ * order of the eqf_set_cells calls within a trap).  Replaces the controller's
+ * per-layer vector exchange of src/simulation.cpp:425-463 / 491-505. */
+int eqf_set_cell_rates_all(eqf_batch* b, int64_t n, const double* s);
+int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
+
+/* Built-in profiler (no counterpart in the reference, which only keeps MPI_Wtime
+ * accumulators, src/simulation.h:512-521).  While enabled, steps run without CUDA
+ * graphs and every kernel launch is bracketed by CUDA events on the batch's
+ * stream and counts the nodes it processed.  eqf_profile(b, 1) resets and starts,
+ * eqf_profile(b, 0) stops.  eqf_profile_read returns per kernel class the summed
+ * launch time (ms), launches, processed nodes and algorithmic bytes.  Classes, in
+ * order: finest-level operator smoothing step, finest-level first smoothing step,
+ * finest-level residual, restriction from the finest level, prolongation to the
+ * finest level, coarser levels, CG direction (q = A p), CG update, FP64 residual
+ * (first of a step), FP64 residual, FP64 update, per-trap scalar phases. */
+/* The CUDA stream (cudaStream_t) all work of the batch is queued on, for callers
+ * that time the batch with their own CUDA events or order their own work. */
+int eqf_stream(eqf_batch* b, void** stream);
+
+#define EQF_PROF_CLASSES 12
+int eqf_profile(eqf_batch* b, int32_t enable);
+int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
+                     int64_t* nodes, double* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,59 @@
+"""Timed CPU baseline: the reference's algorithm for the field step on host cores.
+
+TEST/BENCH INFRASTRUCTURE ONLY (used by bench.py's CPU legs).  Per trap and step it
+does what DOLFIN's LinearVariationalSolver::solve does for eQ's hslD form
+(src/fHSL.cpp:104-108): re-assemble the system from the element kernels, apply the
+Dirichlet rows, LU-factor and solve (scipy SuperLU, serial), so traps run one per
+process in a spawn pool over all host cores.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _worker(args):
+    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s) = args
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    from oracle import hsld
+    mesh = hsld.RightMesh(W, H, nx, ny)
+    F = hsld.point_load(mesh, xy, s, scale=dt)
+    u = np.zeros(mesh.n_nodes)
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(steps):
+        o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls)
+        u = o.step(u, F)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return mesh.n_nodes * done, time.perf_counter() - t0
+
+
+def reference_rate(traps, idx, steps_per_trap: int, budget_s: float, timeout_s: float = 600.0):
+    """DOF-steps/s of assemble + factor + solve per step over the sampled traps."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    jobs = [(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls, t.cell_xy, t.cell_s,
+             steps_per_trap, budget_s) for t in (traps[i] for i in idx)]
+    procs = min(cores, len(jobs))
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(processes=procs) as pool:
+        res = pool.map_async(_worker, jobs).get(timeout=timeout_s)
+    wall = time.perf_counter() - t0
+    dofs = sum(r[0] for r in res)
+    # pool throughput over the compute span (process start-up excluded)
+    span = max(r[1] for r in res)
+    return {"value": dofs / max(span, 1e-9), "unit": "DOF-steps/s", "cores": procs,
+            "kind": "port",
+            "sample": f"{len(jobs)} traps stratified by size "
+                      f"({sum(traps[i].n_nodes for i in idx)} nodes), up to {steps_per_trap} "
+                      f"step(s) each: re-assemble + LU factor + solve per step (scipy SuperLU), "
+                      f"one trap per process",
+            "dof_steps": int(dofs), "wall_s": round(wall, 3)}
