@@ -17,6 +17,8 @@ EQF_ERR_CUDA = -2
 EQF_ERR_NOT_CONVERGED = -3
 EQF_ERR_NO_DEVICE = -4
 EQF_ERR_NOMEM = -5
+EQF_ERR_TOO_LARGE = -6
+EQF_NOALLOC_MAX_NODES = 8388608
 
 EQF_WALL_BOTTOM, EQF_WALL_TOP, EQF_WALL_LEFT, EQF_WALL_RIGHT = 1, 2, 4, 8
 EQF_PREC_FP64, EQF_PREC_FP32_IR = 0, 1
@@ -27,7 +29,7 @@ EXPORTS = (
     "eqf_set_cells", "eqf_set_cell_rates", "eqf_set_nodal", "eqf_add_nodal", "eqf_step",
     "eqf_read_nodal", "eqf_read_cells", "eqf_boundary_flux", "eqf_total_mass", "eqf_stats",
     "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
-    "eqf_profile_read", "eqf_stream",
+    "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
@@ -87,6 +89,9 @@ def load() -> C.CDLL:
         "eqf_read_cells_all": (C.c_int, [C.c_void_p, C.c_int64, dp]),
         "eqf_profile": (C.c_int, [C.c_void_p, C.c_int32]),
         "eqf_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
+        "eqf_field_integral_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double,
+                                                 C.c_double, C.c_int32, C.c_double, C.c_void_p,
+                                                 dp]),
         "eqf_profile_read": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p, i64p, dp]),
     }
     for name, (res, args) in sig.items():

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libeqfield.so")
-SOURCES = [os.path.join(CSRC, "eqf_batch.cu")]
+SOURCES = [os.path.join(CSRC, "eqf_batch.cu"), os.path.join(CSRC, "eqf_noalloc.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("eqf_common.cuh", "eqf_kernels.cuh",
                                                    "eqf_cells.cuh")] + \
     [os.path.join(ROOT, "include", "eqfield.h")]

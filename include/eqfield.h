@@ -38,6 +38,7 @@ extern "C" {
 #define EQF_ERR_NOT_CONVERGED (-3)  /* a trap missed its tolerance within the schedule */
 #define EQF_ERR_NO_DEVICE (-4)      /* no CUDA device visible */
 #define EQF_ERR_NOMEM (-5)          /* device allocation failed */
+#define EQF_ERR_TOO_LARGE (-6)      /* input beyond the fixed maximum of an allocation-free call */
 
 /* Dirichlet walls (c = 0); unset walls are zero-flux.  The reference's trap types
  * (src/fHSL.h:456-504, decoded at src/fHSL.cpp:557-569) map to:
@@ -173,6 +174,27 @@ int eqf_stream(eqf_batch* b, void** stream);
 int eqf_profile(eqf_batch* b, int32_t enable);
 int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
                      int64_t* nodes, double* bytes);
+
+/* Allocation-free field integral.  No counterpart in the reference: this is an
+ * extra entry point for callers that may not allocate device memory when they
+ * need a figure (a simulation running under its own device-memory budget or
+ * allocator, or code that must not trigger the device-wide synchronisation a
+ * cudaMalloc/cudaFree can cause).  It computes, for a nodal field d_field in the
+ * caller's device memory (grid order, nx x ny squares on [0, width] x [0, height]):
+ *   what 0: the total amount 1^T M c            (as eqf_total_mass)
+ *   what 1: -int grad c . n ds over the boundary (as eqf_boundary_flux / (D*dt))
+ * multiplied by `scale`, into *out (host), on `stream` (a cudaStream_t, NULL for
+ * the default stream), and waits for the result.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: its scratch is a fixed device array in
+ * the library (about 32 KB per GPU, held until exit), sized for at most
+ * EQF_NOALLOC_MAX_NODES nodes; larger fields return EQF_ERR_TOO_LARGE.  The first
+ * call on each device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them. */
+#define EQF_NOALLOC_MAX_NODES 8388608
+int eqf_field_integral_noalloc(const double* d_field, int32_t nx, int32_t ny, double width,
+                               double height, int32_t what, double scale, void* stream,
+                               double* out);
 
 #ifdef __cplusplus
 }
