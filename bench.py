@@ -147,8 +147,9 @@ def run_ours(args, rank, world, local_rank):
     import torch
     from eq_gb300 import field as F
 
+    from eq_gb300 import shard
     torch.cuda.set_device(local_rank)
-    traps = make_workload(args.workload, args.seed + rank, args.traps)
+    traps = make_workload(args.workload, shard.rank_seed(args.seed, rank), args.traps)
     tps = trap_params_of(traps)
     nodes = sum(t.n_nodes for t in traps)
     ncells = sum(t.n_cells for t in traps)
@@ -184,12 +185,9 @@ def run_ours(args, rank, world, local_rank):
     sweeps_ps = sum(a["sweeps"] - z["sweeps"] for a, z in zip(st1, st0)) / len(probe) / args.steps
     iters_ps = sum(a["iters"] - z["iters"] for a, z in zip(st1, st0)) / len(probe) / args.steps
     total_ms = ev[0].elapsed_time(ev[-1])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    dof_steps = nodes * args.steps
-    value = dof_steps * world / (total_ms / 1e3)
+    total_ms = shard.max_over_ranks(total_ms)
+    dof_steps = shard.sum_over_ranks(nodes * args.steps)
+    value = dof_steps / (total_ms / 1e3)
 
     # ---- relL2 of the chosen form against the plain FP64 form (sampled traps),
     #      and the plain FP64 single-trap throughput (traps one by one)

@@ -273,7 +273,7 @@ struct Prof {
 struct WorkBase {
   virtual ~WorkBase() = default;
   virtual void enqueue_sweep(cudaStream_t s, bool first) = 0;
-  virtual void enqueue_check(cudaStream_t s) = 0;
+  virtual void enqueue_check(cudaStream_t s, bool update_gamma) = 0;
 };
 
 class Batch;
@@ -288,7 +288,7 @@ struct Work : WorkBase {
   DevBuf<T> xs, p0, p1, q;  // fine CG: correction, directions, A p
   explicit Work(Batch& b);
   void enqueue_sweep(cudaStream_t s, bool first) override;
-  void enqueue_check(cudaStream_t s) override;
+  void enqueue_check(cudaStream_t s, bool update_gamma) override;
   T* vcycle(cudaStream_t s, int lev, bool dot);
 };
 
@@ -354,7 +354,8 @@ class Batch {
   void rebuild_cells();
   void refresh_load();
   void build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
-                      DevBuf<int>& seg_start, int& nseg_out);
+                      DevBuf<int>& seg_start, int& nseg_out, const double* xy, const double* s,
+                      const double* val);
   long long fine_nodes(int t) const {
     return (long long)(L[0].geom[t].nx + 1) * (L[0].geom[t].ny + 1);
   }
@@ -745,9 +746,11 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   const T* tab = level_tab<T>(L0);
   double* part = B.dpart.p;
   T* r = lv[0].b.p;  // CG residual = V-cycle rhs on level 0
+  // FP32 inner solve: stop at inner_tol relative reduction, or once the correction
+  // residual is below 0.3 rtol |b| (the outer check then passes); FP64: rtol |b|.
   const bool fp32 = std::is_same<T, float>::value;
   const double tol_rel = fp32 ? B.opts.inner_tol : 0.0;
-  const double tol_abs = fp32 ? 0.0 : B.opts.rtol;
+  const double tol_abs = fp32 ? 0.3 * B.opts.rtol : B.opts.rtol;
   double* u_out = B.U[1 - B.cur].p;
   float* d_out = B.Dd[1 - B.cur].p;
   if (first)
@@ -794,7 +797,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
 // Final FP64 residual check after the last sweep: marks converged traps, counts
 // the others in d_fail and sets the next step's extrapolation factor.
 template <class T>
-void Work<T>::enqueue_check(cudaStream_t s) {
+void Work<T>::enqueue_check(cudaStream_t s, bool update_gamma) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
   EQF_RUN(B, KC_IR_RESID,
@@ -804,12 +807,13 @@ void Work<T>::enqueue_check(cudaStream_t s) {
   EQF_RUN(B, KC_SCALAR,
           (k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
                                                              B.opts.rtol, B.dstate.p,
-                                                             B.d_ir_done.p, B.d_fail.p)));
+                                                             B.d_ir_done.p, B.d_fail.p,
+                                                             update_gamma ? 1 : 0)));
 }
 
 void Batch::run_step() {
   for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
-  work->enqueue_check(stream);
+  work->enqueue_check(stream, true);
 }
 
 void Batch::check_fail() {
@@ -855,7 +859,7 @@ void Batch::step(int n) {
         if (f == 0) break;
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
         work->enqueue_sweep(stream, false);
-        work->enqueue_check(stream);
+        work->enqueue_check(stream, false);
       }
       if (f != 0) {
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
@@ -886,7 +890,8 @@ void Batch::scan(int n, const int* in, int* out) {
 // Deterministic sort of entries by node: counting sort, then each bucket ordered
 // by entry index; segments = buckets.  d_counts holds per-node counts on entry.
 void Batch::build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
-                           DevBuf<int>& seg_start, int& nseg_out) {
+                           DevBuf<int>& seg_start, int& nseg_out, const double* xy,
+                           const double* s, const double* val) {
   const long long N = L[0].nodes;
   DevBuf<int> start, cursor, head, head_scan;
   start.alloc(N + 1);
@@ -901,14 +906,14 @@ void Batch::build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& pe
   EQF_LAUNCH_CHECK();
   k_cells_heads<<<gb, bs, 0, stream>>>(nent, d_node, start.p, perm.p, head.p);
   EQF_LAUNCH_CHECK();
-  k_cells_bucket_sort<<<gb, bs, 0, stream>>>(nent, d_node, start.p, head.p, perm.p);
-  EQF_LAUNCH_CHECK();
   scan(nent, head.p, head_scan.p);
   int ns = 0;
   EQF_CK(cudaMemcpyAsync(&ns, head_scan.p + nent, sizeof(int), cudaMemcpyDeviceToHost, stream));
   sync();
   seg_start.alloc(ns + 1);
   k_cells_segments<<<gb, bs, 0, stream>>>(nent, head.p, head_scan.p, seg_start.p, ns);
+  EQF_LAUNCH_CHECK();
+  k_seg_sort<<<(ns + 255) / 256, 256, 0, stream>>>(ns, seg_start.p, perm.p, xy, s, val);
   EQF_LAUNCH_CHECK();
   sync();
   nseg_out = ns;
@@ -958,13 +963,18 @@ void Batch::rebuild_cells() {
                                                            d_cell_xy.p, d_ent_node.p, d_ent_w.p,
                                                            counts.p);
   EQF_LAUNCH_CHECK();
-  build_segments(nent, d_ent_node.p, counts.p, d_perm, d_seg_start, nseg);
+  build_segments(nent, d_ent_node.p, counts.p, d_perm, d_seg_start, nseg, d_cell_xy.p,
+                 d_cell_s.p, nullptr);
   refresh_load();
 }
 
 // F = dt * sum_i s_i phi(x_i) from the current rates (segments fixed)
 void Batch::refresh_load() {
   if (ncells == 0) return;
+  // rates changed: restore the canonical order of every node's contributions
+  k_seg_sort<<<(nseg + 255) / 256, 256, 0, stream>>>(nseg, d_seg_start.p, d_perm.p, d_cell_xy.p,
+                                                     d_cell_s.p, nullptr);
+  EQF_LAUNCH_CHECK();
   k_cells_values<<<(ncells + 255) / 256, 256, 0, stream>>>(ncells, d_ent_w.p, d_cell_s.p,
                                                            d_scale.p, d_cell_trap.p, d_ent_val.p);
   EQF_LAUNCH_CHECK();
@@ -1049,7 +1059,7 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
   o->use_graph = 0;
   o->adaptive = 1;
   if (precision == EQF_PREC_FP32_IR) {
-    o->rtol = 1e-9;
+    o->rtol = 1e-8;
     o->max_sweeps = 2;
     o->max_iters = 6;
     o->inner_tol = 1e-5;
@@ -1198,7 +1208,7 @@ int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
         (int)n, B.L[0].geom[trap].off, dn.p, ent.p, counts.p);
     EQF_LAUNCH_CHECK();
     int ns = 0;
-    B.build_segments((int)n, ent.p, counts.p, perm, seg, ns);
+    B.build_segments((int)n, ent.p, counts.p, perm, seg, ns, nullptr, nullptr, dv.p);
     eqf::k_seg_sum<true><<<(ns + 255) / 256, 256, 0, B.stream>>>(ns, seg.p, perm.p, ent.p, dv.p,
                                                                   B.u_cur());
     EQF_LAUNCH_CHECK();

@@ -84,22 +84,39 @@ __global__ void k_cells_heads(int nent, const int* __restrict__ ent_node,
   head[p] = start[ent_node[perm[p]]] == p ? 1 : 0;
 }
 
-// Order each node's bucket by entry index (buckets hold a handful of entries);
-// one thread per bucket, so the per-node summation order is fixed.
-__global__ void k_cells_bucket_sort(int nent, const int* __restrict__ ent_node,
-                                    const int* __restrict__ start, const int* __restrict__ head,
-                                    int* __restrict__ perm) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nent || !head[p]) return;
-  const int b = start[ent_node[perm[p]] + 1];
-  for (int a = p + 1; a < b; ++a) {
-    const int v = perm[a];
-    int q = a - 1;
-    while (q >= p && perm[q] > v) {
-      perm[q + 1] = perm[q];
-      --q;
+// Canonical order of each segment (the entries of one node): by the contributing
+// cell's (x, y, rate), or by the value for explicit nodal increments, then by entry
+// index.  The summation order then depends only on the set of contributions, so
+// the deposit is bit-identical under any permutation of the cells.  One thread per
+// segment; segments hold a handful of entries.
+__device__ __forceinline__ bool entry_less(int e1, int e2, const double* __restrict__ xy,
+                                           const double* __restrict__ s,
+                                           const double* __restrict__ val) {
+  if (xy) {
+    const int c1 = e1 / 3, c2 = e2 / 3;
+    if (xy[2 * c1] != xy[2 * c2]) return xy[2 * c1] < xy[2 * c2];
+    if (xy[2 * c1 + 1] != xy[2 * c2 + 1]) return xy[2 * c1 + 1] < xy[2 * c2 + 1];
+    if (s[c1] != s[c2]) return s[c1] < s[c2];
+  } else if (val[e1] != val[e2]) {
+    return val[e1] < val[e2];
+  }
+  return e1 < e2;
+}
+
+__global__ void k_seg_sort(int nseg, const int* __restrict__ seg_start, int* __restrict__ perm,
+                           const double* __restrict__ xy, const double* __restrict__ s,
+                           const double* __restrict__ val) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nseg) return;
+  const int a = seg_start[q], b = seg_start[q + 1];
+  for (int i = a + 1; i < b; ++i) {
+    const int v = perm[i];
+    int j = i - 1;
+    while (j >= a && entry_less(v, perm[j], xy, s, val)) {
+      perm[j + 1] = perm[j];
+      --j;
     }
-    perm[q + 1] = v;
+    perm[j + 1] = v;
   }
 }
 

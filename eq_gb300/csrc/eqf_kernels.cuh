@@ -800,10 +800,12 @@ __global__ void k_s_ir(int ntraps, const TileRange* __restrict__ range,
 
 // After the final check: convergence verdict and the next extrapolation factor
 // gamma = |d_n| / |d_{n-1}| (clamped), from the increments of the last two steps.
+// update_gamma is 0 for the extra checks of adaptive sweeps: the factor belongs to
+// the step, so a trap's guess never depends on what the other traps needed.
 __global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
                           const double* __restrict__ part, int ntiles, double rtol,
                           CgState* __restrict__ st, int* __restrict__ ir_done,
-                          int* __restrict__ fail) {
+                          int* __restrict__ fail, int update_gamma) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps) return;
   CgState s = st[t];
@@ -813,6 +815,10 @@ __global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
       ir_done[t] = 1;
     else
       atomicAdd(fail, 1);
+  }
+  if (!update_gamma) {
+    st[t] = s;
+    return;
   }
   const double dn2 = trap_sum(part + 2 * ntiles, range[t]);
   double gm = 0.0;

@@ -92,7 +92,11 @@ class RightMesh:
 
 def _geometry(mesh: RightMesh):
     """Per-triangle Jacobian pieces in the order fenics/hslD.h:3158-3169 uses them."""
-    c = mesh.coords[mesh.cells]  # (T, 3, 2)
+    return _geometry_of(mesh.coords[mesh.cells])
+
+
+def _geometry_of(c: np.ndarray):
+    """Same for explicit triangles c (T, 3, 2)."""
     J_c0 = c[:, 1, 0] - c[:, 0, 0]
     J_c1 = c[:, 2, 0] - c[:, 0, 0]
     J_c2 = c[:, 1, 1] - c[:, 0, 1]
@@ -151,6 +155,69 @@ def tabulate_advection(mesh: RightMesh, dt: float, vx: np.ndarray, vy: np.ndarra
     conv = (np.einsum('q,qa,tq,tb->tab', _QW, _QPHI, vxq, gx)
             + np.einsum('q,qa,tq,tb->tab', _QW, _QPHI, vyq, gy))
     return dt * adet[:, None, None] * conv
+
+
+# --- single-element tensors (the unit the reference's generated kernels compute) ---
+_MASS_REF = np.array([[2.0, 1.0, 1.0], [1.0, 2.0, 1.0], [1.0, 1.0, 2.0]]) / 24.0
+
+
+def element_a(coords, D11, D22, D12, D, dt) -> np.ndarray:
+    """Bilinear cell tensor of hslD on one triangle (cf. fenics/hslD.h:3123-3262)."""
+    c = np.asarray(coords, dtype=np.float64).reshape(1, 3, 2)
+    _, adet, gx, gy = _geometry_of(c)
+    t = [float(np.einsum('q,qc,c->', _QW, _QPHI, np.asarray(v, dtype=np.float64)))
+         for v in (D11, D22, D12)]
+    stiff = (t[0] * np.outer(gx[0], gx[0]) + t[1] * np.outer(gy[0], gy[0])
+             + t[2] * (np.outer(gx[0], gy[0]) + np.outer(gy[0], gx[0])))
+    return D * dt * adet[0] * stiff + adet[0] * _MASS_REF
+
+
+def element_L(coords, u0, dt, f) -> np.ndarray:
+    """Linear cell tensor (u0 + dt f) v on one triangle (cf. fenics/hslD.h:3446-3533)."""
+    c = np.asarray(coords, dtype=np.float64).reshape(1, 3, 2)
+    _, adet, _, _ = _geometry_of(c)
+    return adet[0] * _MASS_REF @ np.asarray(u0, dtype=np.float64) + dt * f * adet[0] / 6.0
+
+
+def _facet_vertices(facet: int):
+    """Local vertices of facet `facet` (the edge opposite vertex `facet`)."""
+    return [v for v in range(3) if v != facet]
+
+
+def facet_a(coords, facet, dt, r) -> np.ndarray:
+    """Robin facet tensor dt r u v on one exterior facet (cf. fenics/hslD.h:3264-3445)."""
+    c = np.asarray(coords, dtype=np.float64)
+    a, b = _facet_vertices(facet)
+    L = float(np.hypot(*(c[b] - c[a])))
+    A = np.zeros((3, 3))
+    A[np.ix_([a, b], [a, b])] = dt * r * L * np.array([[1 / 3, 1 / 6], [1 / 6, 1 / 3]])
+    return A
+
+
+def facet_L(coords, facet, dt, r, s) -> np.ndarray:
+    """Robin facet load dt r s v (cf. fenics/hslD.h:3534-3693)."""
+    c = np.asarray(coords, dtype=np.float64)
+    a, b = _facet_vertices(facet)
+    L = float(np.hypot(*(c[b] - c[a])))
+    out = np.zeros(3)
+    out[[a, b]] = dt * r * s * L / 2.0
+    return out
+
+
+def facet_flux(coords, u, facet) -> float:
+    """-grad(u).n |e| of a P1 field on one exterior facet (cf. fenics/boundary.ufl:11)."""
+    c = np.asarray(coords, dtype=np.float64).reshape(1, 3, 2)
+    _, _, gx, gy = _geometry_of(c)
+    u = np.asarray(u, dtype=np.float64)
+    grad = np.array([gx[0] @ u, gy[0] @ u])
+    a, b = _facet_vertices(facet)
+    e = c[0, b] - c[0, a]
+    L = float(np.hypot(*e))
+    n = np.array([e[1], -e[0]]) / L
+    # outward: away from the opposite vertex
+    if np.dot(n, c[0, facet] - c[0, a]) > 0:
+        n = -n
+    return float(-np.dot(grad, n) * L)
 
 
 def robin_facets(mesh: RightMesh, wall: int):

@@ -1,0 +1,109 @@
+"""The C ABI library without a GPU: it builds, loads, exports every declared symbol,
+its structs match the header, and argument errors come back as status codes."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from eq_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "eqfield.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(eqf_\w+)\s*\(", text)))
+
+
+def test_header_declares_what_the_binding_knows():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_function(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (eqf_\w+)$", out, flags=re.M))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+
+
+def test_struct_layout_matches_header():
+    src = r'''
+#include <stddef.h>
+#include <stdio.h>
+#include "eqfield.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(eqf_trap_params), offsetof(eqf_trap_params, walls),
+         offsetof(eqf_trap_params, adv_len), offsetof(eqf_trap_params, dt));
+  printf("%zu %zu %zu %zu\n", sizeof(eqf_solver_opts), offsetof(eqf_solver_opts, adaptive),
+         offsetof(eqf_solver_opts, cheb_ratio), offsetof(eqf_solver_opts, inner_tol));
+  return 0;
+}'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "layout.c")
+        exe = os.path.join(d, "layout")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), c, "-o", exe],
+                       check=True)
+        lines = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    tp = [int(v) for v in lines[0].split()]
+    so = [int(v) for v in lines[1].split()]
+    T, S = _lib.TrapParams, _lib.SolverOpts
+    assert tp == [C.sizeof(T), T.walls.offset, T.adv_len.offset, T.dt.offset]
+    assert so == [C.sizeof(S), S.adaptive.offset, S.cheb_ratio.offset, S.inner_tol.offset]
+
+
+def test_default_opts_without_gpu(lib):
+    o = _lib.SolverOpts()
+    assert lib.eqf_default_opts(_lib.EQF_PREC_FP32_IR, C.byref(o)) == _lib.EQF_OK
+    assert o.precision == _lib.EQF_PREC_FP32_IR and o.rtol > 0 and o.max_iters >= 1
+    assert lib.eqf_default_opts(7, C.byref(o)) == _lib.EQF_ERR_INVALID
+
+
+def test_invalid_arguments_are_status_codes(lib):
+    h = C.c_void_p()
+    o = _lib.SolverOpts()
+    lib.eqf_default_opts(_lib.EQF_PREC_FP64, C.byref(o))
+    assert lib.eqf_create(0, None, C.byref(o), C.byref(h)) == _lib.EQF_ERR_INVALID
+    assert b"trap" in lib.eqf_last_error(None)
+    bad = (_lib.TrapParams * 1)(_lib.TrapParams(1.0, 1.0, 0, 4, 1.0, 0.1, 0.0, 0.0, 1.0, 1))
+    assert lib.eqf_create(1, bad, C.byref(o), C.byref(h)) == _lib.EQF_ERR_INVALID
+    assert lib.eqf_step(None, 1) == _lib.EQF_ERR_INVALID
+    assert lib.eqf_destroy(None) == _lib.EQF_ERR_INVALID
+
+
+def test_create_reports_missing_device(lib):
+    """On a machine without a GPU the library refuses loudly (no CPU fallback)."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is visible")
+    except ImportError:
+        pass
+    h = C.c_void_p()
+    o = _lib.SolverOpts()
+    lib.eqf_default_opts(_lib.EQF_PREC_FP64, C.byref(o))
+    tp = (_lib.TrapParams * 1)(_lib.TrapParams(4.0, 2.0, 8, 4, 1.0, 0.1, 0.0, 0.0, 1.0, 1))
+    rc = lib.eqf_create(1, tp, C.byref(o), C.byref(h))
+    assert rc in (_lib.EQF_ERR_NO_DEVICE, _lib.EQF_ERR_CUDA)
+    assert lib.eqf_last_error(None)
+
+
+def test_noalloc_rejects_oversize_before_touching_a_device(lib):
+    out = C.c_double(-1.0)
+    rc = lib.eqf_field_integral_noalloc(C.c_void_p(16), 4096, 4096, 1.0, 1.0, 0, 1.0, None,
+                                        C.byref(out))
+    assert rc == _lib.EQF_ERR_TOO_LARGE and out.value == -1.0
+    assert lib.eqf_field_integral_noalloc(None, 4, 4, 1.0, 1.0, 0, 1.0, None,
+                                          C.byref(out)) == _lib.EQF_ERR_INVALID
