@@ -45,7 +45,8 @@ class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("rtol", C.c_double), ("max_sweeps", C.c_int32),
                 ("max_iters", C.c_int32), ("inner_tol", C.c_double), ("cheb_pre", C.c_int32),
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
-                ("use_graph", C.c_int32), ("adaptive", C.c_int32)]
+                ("use_graph", C.c_int32), ("adaptive", C.c_int32),
+                ("tile_nodes", C.c_int32)]
 
 
 class EqfError(RuntimeError):

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -76,7 +77,7 @@ struct DevBuf {
   }
 };
 
-constexpr int kTileNodes = 2048;
+constexpr int kTileNodes = 4096;
 constexpr int kMaxLevels = 16;
 
 static inline long long align_up(long long v, long long a) { return (v + a - 1) / a * a; }
@@ -168,7 +169,7 @@ static size_t staged_bytes(long long ka, long long kb, int tsize, long long nall
   long long b = ((kb + V - 1) / V) * V;
   b = std::min(b, nalloc);
   const long long nb = b > a ? (b - a) * tsize : 0;
-  return (size_t)((nb + 15) & ~15ll);
+  return (size_t)((nb + 15) & ~15ll) + 16;  // + the 16-byte pad Stager leaves after a range
 }
 
 // Class tables: the stencil of every (row class, column class) pair of a trap on
@@ -202,7 +203,7 @@ static size_t guarded_bytes(long long ka, long long kb, int tsize) {
   const long long V = 16 / tsize;
   const long long wa = ka >= 0 ? (ka / V) * V : -(((-ka) + V - 1) / V) * V;
   const long long wb = ((kb + V - 1) / V) * V;
-  return (size_t)(((wb - wa) * tsize + 15) & ~15ll);
+  return (size_t)(((wb - wa) * tsize + 15) & ~15ll) + 16;  // + pad as in Stager
 }
 
 struct Level {
@@ -215,6 +216,7 @@ struct Level {
   DevBuf<double> tabd;  // same in FP64
   // dynamic shared memory per staged kernel (max over this level's tiles)
   size_t sm_cheb = 0, sm_resid = 0, sm_cgdir = 0, sm_ir = 0;
+
   size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
   size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
   size_t sm_coarse = 0;    // single-CTA coarsest solve (0 = not possible)
@@ -317,6 +319,8 @@ class Batch {
   long long steps_done = 0;
   Prof prof;
   int cur_cls = -1;
+  int num_sms = 1;
+
   // profiling hooks: begin() returns the node counter of this launch (or null)
   unsigned long long* prof_begin(int c) {
     if (!prof.on) return nullptr;
@@ -371,6 +375,11 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     throw Error(EQF_ERR_NO_DEVICE, "no CUDA device visible");
   EQF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  {
+    int dev = 0;
+    EQF_CK(cudaGetDevice(&dev));
+    EQF_CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
   build_levels();
   const long long N0 = L[0].nodes;
   for (int q = 0; q < 2; ++q) {
@@ -462,7 +471,8 @@ void Batch::build_levels() {
   }
   // offsets, fine offsets and row tiles (about kTileNodes nodes each, whole rows)
   const int tsz = opts.precision == EQF_PREC_FP32_IR ? 4 : 8;
-  const long long target = tsz == 4 ? kTileNodes : kTileNodes / 2;
+  const long long target =
+      opts.tile_nodes > 0 ? opts.tile_nodes : (tsz == 4 ? kTileNodes : kTileNodes / 2);
   for (int l = 0; l < nlev; ++l) {
     long long off = 0;
     for (int t = 0; t < ntraps; ++t) {
@@ -512,11 +522,14 @@ void Batch::build_levels() {
       (void)n;
       const long long ka = (long long)tl.k0 - P - 1;  // guarded halo window
       const long long kb = (long long)tl.k1 + P + 1;
-      const size_t halo = guarded_bytes(ka, kb, tsz);
+      // quad kernels: a wider halo (qhalo_lo / qhalo_hi) and the staged class table
+      const size_t halo = guarded_bytes((long long)tl.k0 - P - 8, (long long)tl.k1 + P + 8, tsz);
       const size_t own = staged_bytes(tl.k0, tl.k1, tsz, na);
-      Lv.sm_cheb = std::max(Lv.sm_cheb, kSmemHeader + halo + 2 * own);
-      Lv.sm_resid = std::max(Lv.sm_resid, kSmemHeader + halo + own);
-      Lv.sm_cgdir = std::max(Lv.sm_cgdir, kSmemHeader + 2 * halo);
+      const size_t tab = (size_t)kTabPerTrap * tsz;
+      Lv.sm_cheb = std::max(Lv.sm_cheb, kSmemHeader + halo + 2 * own + tab);
+      Lv.sm_resid = std::max(Lv.sm_resid, kSmemHeader + halo + own + tab);
+      Lv.sm_cgdir = std::max(Lv.sm_cgdir, kSmemHeader + 2 * halo + tab);
+
       // first refinement residual: u (FP64, halo), F (FP64), d (FP32, halo)
       Lv.sm_ir = std::max(Lv.sm_ir, kSmemHeader + guarded_bytes(ka, kb, 8) +
                                         staged_bytes(tl.k0, tl.k1, 8, na) +
@@ -576,31 +589,28 @@ void Batch::build_levels() {
 }
 
 // ---------------------------------------------------------------------------
+template <class K>
+static void smem_attrs(K kernel, int mx) {
+  EQF_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  EQF_CK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
 template <class T>
 static void allow_dyn_smem() {
   const int mx = (int)kMaxDynSmem;
-  EQF_CK(cudaFuncSetAttribute(k_cheb<T, true, false, true>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_cheb<T, true, false, false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_cheb<T, false, false, true>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_cheb<T, false, false, false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_resid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_restrict<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_prolong<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_coarse_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              mx));
-  EQF_CK(cudaFuncSetAttribute(k_cg_dir<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              mx));
-  EQF_CK(cudaFuncSetAttribute(k_cg_dir<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              mx));
-  EQF_CK(cudaFuncSetAttribute(k_ir_first<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_ir_residual<T, true>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-  EQF_CK(cudaFuncSetAttribute(k_ir_residual<T, false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  smem_attrs(k_cheb<T, true, false, true>, mx);
+  smem_attrs(k_cheb<T, true, false, false>, mx);
+  smem_attrs(k_cheb<T, false, false, true>, mx);
+  smem_attrs(k_cheb<T, false, false, false>, mx);
+  smem_attrs(k_resid<T>, mx);
+  smem_attrs(k_restrict<T>, mx);
+  smem_attrs(k_prolong<T>, mx);
+  smem_attrs(k_coarse_solve<T>, mx);
+  smem_attrs(k_cg_dir<T, true>, mx);
+  smem_attrs(k_cg_dir<T, false>, mx);
+  smem_attrs(k_ir_first<T>, mx);
+  smem_attrs(k_ir_residual<T, true>, mx);
+  smem_attrs(k_ir_residual<T, false>, mx);
 }
 
 template <class T>
@@ -1092,6 +1102,7 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
     EQF_REQUIRE(o.max_sweeps >= 1 && o.max_iters >= 1 && o.cheb_post >= 1 && o.cheb_pre >= 1 &&
                     o.cheb_coarse >= 1 && o.cheb_ratio > 1.0 && o.rtol > 0.0,
                 "invalid solver options");
+    EQF_REQUIRE(o.tile_nodes >= 0 && o.tile_nodes <= 32768, "tile_nodes outside [0, 32768]");
     for (int t = 0; t < n_traps; ++t) {
       const auto& p = traps[t];
       EQF_REQUIRE(p.nx >= 1 && p.ny >= 1 && p.width > 0 && p.height > 0 && p.dt > 0 &&

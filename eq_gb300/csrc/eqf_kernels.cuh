@@ -23,6 +23,12 @@ namespace eqf {
 constexpr int kThreads = 256;
 constexpr int kTabStride = 8;                 // c, e, w, n, s, ne, sw, 1/c
 constexpr int kTabPerTrap = 25 * kTabStride;  // 5 x 5 node classes
+// Resident CTAs per SM the staged stencil kernels are compiled for (register cap):
+// FP32 tiles are small enough in shared memory for six per SM.
+template <class T>
+constexpr int kStencilCtas = sizeof(T) == 4 ? 4 : 2;
+
+extern __shared__ __align__(16) char eqf_smem[];
 
 // Device-side error flag: set when a bounded wait gives up (never expected).
 __device__ int g_eqf_device_error = 0;
@@ -63,58 +69,40 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
 
 // A staged range of one array: node k (trap-relative) lives at p[k - a].
 template <class T>
+struct Q4;
+template <class T>
 struct View {
   const T* p;
   int a;
   __device__ __forceinline__ T operator[](int k) const { return p[k - a]; }
+  __device__ __forceinline__ Q4<T> quad(int k) const;  // k a multiple of 4
+  __device__ __forceinline__ void row(int k0, T (&out)[5]) const;
 };
 
 constexpr int kMaxStaged = 4;
-constexpr int kMaxGuards = 2 * kMaxStaged;
 
 // Plans up to kMaxStaged ranges in dynamic shared memory; thread 0 then issues
 // them as bulk copies.  Ranges are widened to 16-byte boundaries; trap segments
 // are padded to 32 elements, so a widened range stays inside the allocation.
 // Guarded ranges may reach outside [0, nalloc): those parts are zero-filled.
+// Every add() takes one copy slot and two guard slots, so the slot indices are
+// compile-time constants and the bookkeeping stays in registers.
 struct Stager {
   uint64_t* bar;
   char* cur;
   uint32_t total;
-  int n, ng;
+  int n;
   const void* src[kMaxStaged];
   void* dst[kMaxStaged];
   uint32_t bytes[kMaxStaged];
-  char* gptr[kMaxGuards];  // zero-fill regions (16-byte granules)
-  uint32_t gbytes[kMaxGuards];
+  char* gptr[2 * kMaxStaged];  // zero-fill regions (16-byte granules)
+  uint32_t gbytes[2 * kMaxStaged];
 
   __device__ __forceinline__ explicit Stager(char* smem) {
     bar = reinterpret_cast<uint64_t*>(smem);
     cur = smem + 16;
     total = 0;
     n = 0;
-    ng = 0;
-  }
-  __device__ __forceinline__ void copy(const void* s, void* d, uint32_t nb) {
-    if (nb) {
-      src[n] = s;
-      dst[n] = d;
-      bytes[n] = nb;
-      ++n;
-      total += nb;
-    }
-  }
-  // nodes [ka, kb) of `base` (trap-relative, inside [0, nalloc))
-  template <class T>
-  __device__ __forceinline__ View<T> add(const T* base, int ka, int kb, int nalloc) {
-    constexpr int V = 16 / sizeof(T);
-    const int a = (ka / V) * V;
-    int b = ((kb + V - 1) / V) * V;
-    b = b < nalloc ? b : nalloc;
-    T* d = reinterpret_cast<T*>(cur);
-    const uint32_t nb = b > a ? (uint32_t)(b - a) * (uint32_t)sizeof(T) : 0u;
-    copy(base + a, d, nb);
-    cur += (nb + 15u) & ~15u;
-    return View<T>{d, a};
   }
   // nodes [ka, kb) with ka possibly < 0 and kb possibly > nalloc; the parts
   // outside [0, nalloc) read as zero
@@ -126,39 +114,56 @@ struct Stager {
     const int ca = wa > 0 ? wa : 0;
     const int cb = wb < nalloc ? wb : nalloc;
     T* d = reinterpret_cast<T*>(cur);
-    if (cb > ca) copy(base + ca, d + (ca - wa), (uint32_t)(cb - ca) * sizeof(T));
-    if (ca > wa) {
-      gptr[ng] = reinterpret_cast<char*>(d);
-      gbytes[ng++] = (uint32_t)(ca - wa) * sizeof(T);
-    }
+    const uint32_t nb = cb > ca ? (uint32_t)(cb - ca) * (uint32_t)sizeof(T) : 0u;
+    src[n] = base + ca;
+    dst[n] = d + (ca - wa);
+    bytes[n] = nb;
+    total += nb;
+    gptr[2 * n] = reinterpret_cast<char*>(d);
+    gbytes[2 * n] = ca > wa ? (uint32_t)(ca - wa) * sizeof(T) : 0u;
     const int lo = cb > ca ? cb : ca;
-    if (wb > lo) {
-      gptr[ng] = reinterpret_cast<char*>(d + (lo - wa));
-      gbytes[ng++] = (uint32_t)(wb - lo) * sizeof(T);
-    }
-    cur += ((uint32_t)(wb - wa) * sizeof(T) + 15u) & ~15u;
+    gptr[2 * n + 1] = reinterpret_cast<char*>(d + (lo - wa));
+    gbytes[2 * n + 1] = wb > lo ? (uint32_t)(wb - lo) * sizeof(T) : 0u;
+    ++n;
+    // +16 bytes: vector row loads may read up to 8 bytes past the window (unused)
+    cur += (((uint32_t)(wb - wa) * sizeof(T) + 15u) & ~15u) + 16u;
     return View<T>{d, wa};
+  }
+  // nodes [ka, kb) of `base` (trap-relative, inside [0, nalloc))
+  template <class T>
+  __device__ __forceinline__ View<T> add(const T* base, int ka, int kb, int nalloc) {
+    return add_guarded<T>(base, ka, kb, nalloc);
   }
   // Zero the guards, issue the copies and wait for them (bounded).  Returns
   // false, uniformly for the CTA, if the wait gave up (device error flag set).
   __device__ __forceinline__ bool run() {
     if (threadIdx.x == 0) mbar_init(bar, 1);
-    for (int q = 0; q < ng; ++q) {
-      uint4* z = reinterpret_cast<uint4*>(gptr[q]);
-      for (uint32_t e = threadIdx.x; e < gbytes[q] / 16u; e += blockDim.x)
-        z[e] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (int q = 0; q < 2 * kMaxStaged; ++q) {
+      if (q < 2 * n && gbytes[q]) {
+        uint4* z = reinterpret_cast<uint4*>(gptr[q]);
+        for (uint32_t e = threadIdx.x; e < gbytes[q] / 16u; e += blockDim.x)
+          z[e] = make_uint4(0u, 0u, 0u, 0u);
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       mbar_expect_tx(bar, total);
-      for (int q = 0; q < n; ++q) bulk_copy_g2s(dst[q], src[q], bytes[q], bar);
+#pragma unroll
+      for (int q = 0; q < kMaxStaged; ++q)
+        if (q < n && bytes[q]) bulk_copy_g2s(dst[q], src[q], bytes[q], bar);
     }
-    bool ok = false;
-    for (int it = 0; it < (1 << 22) && !ok; ++it) ok = mbar_try_wait(bar, 0);
-    if (!ok) {
-      // give the copies in flight one more bounded chance to land before leaving
-      for (int it = 0; it < (1 << 20) && !ok; ++it) ok = mbar_try_wait(bar, 0);
-      if (!ok) atomicExch(&g_eqf_device_error, 1);
+    // One thread waits on the mbarrier (the others sleep in the barrier below
+    // instead of spinning); the barrier then publishes the copied data CTA-wide.
+    bool ok = true;
+    if (threadIdx.x == 0) {
+      ok = false;
+      for (int it = 0; it < (1 << 22) && !ok; ++it) ok = mbar_try_wait(bar, 0);
+      if (!ok) {
+        // give the copies in flight one more bounded chance to land before leaving
+        for (int it = 0; it < (1 << 20) && !ok; ++it) ok = mbar_try_wait(bar, 0);
+        if (!ok) atomicExch(&g_eqf_device_error, 1);
+      }
     }
     return __syncthreads_and(ok ? 1 : 0) != 0;
   }
@@ -216,20 +221,56 @@ __device__ __forceinline__ Interior<double> interior<double>(const LevelGeom& g)
   return Interior<double>{g.cC, g.cE, g.cN, g.cD, g.cCinv};
 }
 
-// Advection rows: the full stencil from the cell sizes and the local velocity
-// (out of line; only traps with advection take it, uniformly per CTA).
-template <class T, class X>
-__device__ __noinline__ T apply_general(const LevelGeom& g, const X& x, int k, int i, int j,
-                                        T& idiag) {
+// One fixed evaluation order (explicit fused multiply-adds), shared by every code
+// path, so a node's value never depends on which path evaluated it: the seven
+// weights (c, e, w, n, s, ne, sw) are applied in that order.
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class T>
+__device__ __forceinline__ T st_table(const T* c, T x0, T xe, T xw, T xn, T xs, T xne, T xsw) {
+  return fma_(c[6], xsw, fma_(c[5], xne, fma_(c[4], xs, fma_(c[3], xn, fma_(c[2], xw,
+              fma_(c[1], xe, c[0] * x0))))));
+}
+// The same order with the interior weights (e = w, n = s, ne = sw).
+template <class T>
+__device__ __forceinline__ T st_interior(const Interior<T>& ci, T x0, T xe, T xw, T xn, T xs,
+                                         T xne, T xsw) {
+  return fma_(ci.d, xsw, fma_(ci.d, xne, fma_(ci.n, xs, fma_(ci.n, xn, fma_(ci.e, xw,
+              fma_(ci.e, xe, ci.c * x0))))));
+}
+
+// Advection rows and traps: the full stencil from the cell sizes and the local
+// velocity (out of line; only traps with advection take it, uniformly per CTA).
+// (i, j) are clamped into the grid: nodes outside it are never stored.
+template <class T>
+__device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&c)[8]) {
+  i = i < 0 ? 0 : (i > g.ny ? g.ny : i);
+  j = j < 0 ? 0 : (j > g.nx ? g.nx : j);
   const Sten<T> s = stencil_general<T>(g, i, j);
-  idiag = T(1) / s.c;
+  c[0] = s.c;
+  c[1] = s.e;
+  c[2] = s.w;
+  c[3] = s.n;
+  c[4] = s.s;
+  c[5] = s.ne;
+  c[6] = s.sw;
+  c[7] = T(1) / s.c;
+}
+template <class T, class X>
+__device__ __forceinline__ T apply_general(const LevelGeom& g, const X& x, int k, int i, int j,
+                                           T& idiag) {
+  T c[8];
+  coef_general<T>(g, i, j, c);
+  idiag = c[7];
   const int P = g.nx + 1;
-  return s.c * x[k] + s.e * x[k + 1] + s.w * x[k - 1] + s.n * x[k + P] + s.s * x[k - P] +
-         s.ne * x[k + P + 1] + s.sw * x[k - P - 1];
+  return st_table(c, x[k], x[k + 1], x[k - 1], x[k + P], x[k - P], x[k + P + 1], x[k - P - 1]);
 }
 template <class T>
-__device__ __noinline__ T inv_diag_general(const LevelGeom& g, int i, int j) {
-  return T(1) / stencil_general<T>(g, i, j).c;
+__device__ __forceinline__ T inv_diag_general(const LevelGeom& g, int i, int j) {
+  T c[8];
+  coef_general<T>(g, i, j, c);
+  return c[7];
 }
 
 // (A x)_k and 1/diagonal of node (i, j).  Every neighbour index must be readable
@@ -243,13 +284,13 @@ __device__ __forceinline__ T apply_tab(const LevelGeom& g, const Interior<T>& ci
   const int P = g.nx + 1;
   const T x0 = x[k], xe = x[k + 1], xw = x[k - 1], xn = x[k + P], xs = x[k - P];
   const T xne = x[k + P + 1], xsw = x[k - P - 1];
-  if (__all_sync(__activemask(), is_uniform_interior(g, i, j))) {
+  if (is_uniform_interior(g, i, j)) {
     idiag = ci.ic;
-    return ci.c * x0 + ci.e * (xe + xw) + ci.n * (xn + xs) + ci.d * (xne + xsw);
+    return st_interior(ci, x0, xe, xw, xn, xs, xne, xsw);
   }
   const T* c = tab + node_class(g, i, j) * kTabStride;
   idiag = c[7];
-  return c[0] * x0 + c[1] * xe + c[2] * xw + c[3] * xn + c[4] * xs + c[5] * xne + c[6] * xsw;
+  return st_table(c, x0, xe, xw, xn, xs, xne, xsw);
 }
 
 template <class T>
@@ -257,6 +298,226 @@ __device__ __forceinline__ T inv_diag_tab(const LevelGeom& g, const Interior<T>&
                                           const T* __restrict__ tab, int i, int j) {
   if (g.adv_on) return inv_diag_general<T>(g, i, j);
   return is_uniform_interior(g, i, j) ? ci.ic : tab[node_class(g, i, j) * kTabStride + 7];
+}
+
+// ---------------------------------------------------------------------------
+// Aligned quads: nodes [4q, 4q+4) of a trap (trap segments start 128-byte
+// aligned, so a quad is one 16-byte vector in FP32).
+template <class T>
+struct Q4 {
+  T v[4];
+};
+template <class T>
+__device__ __forceinline__ Q4<T> vld4(const T* p);  // p 16-byte aligned (FP32) / 32 (FP64)
+template <>
+__device__ __forceinline__ Q4<float> vld4<float>(const float* p) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  return Q4<float>{{a.x, a.y, a.z, a.w}};
+}
+template <>
+__device__ __forceinline__ Q4<double> vld4<double>(const double* p) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  return Q4<double>{{a.x, a.y, b.x, b.y}};
+}
+template <class T>
+__device__ __forceinline__ void vst4(T* p, const Q4<T>& q);
+template <>
+__device__ __forceinline__ void vst4<float>(float* p, const Q4<float>& q) {
+  *reinterpret_cast<float4*>(p) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
+}
+template <>
+__device__ __forceinline__ void vst4<double>(double* p, const Q4<double>& q) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(q.v[0], q.v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(q.v[2], q.v[3]);
+}
+template <class T>
+__device__ __forceinline__ Q4<T> ld4(const View<T>& w, int k) {
+  return vld4<T>(w.p + (k - w.a));
+}
+template <class T>
+__device__ __forceinline__ Q4<T> View<T>::quad(int k) const {
+  return vld4<T>(p + (k - a));
+}
+
+template <class T>
+__device__ __forceinline__ void row5(const View<T>& w, int k0, T (&out)[5]);
+template <class T>
+__device__ __forceinline__ void View<T>::row(int k0, T (&out)[5]) const {
+  row5<T>(*this, k0, out);
+}
+
+// Five consecutive values x[k0 .. k0+4] of a staged FP32 row.  Two aligned
+// 16-byte loads and a select on the (warp-uniform) misalignment keep shared
+// memory free of bank conflicts; FP64 views load scalars.
+template <class T>
+__device__ __forceinline__ void row5(const View<T>& w, int k0, T (&out)[5]) {
+#pragma unroll
+  for (int e = 0; e < 5; ++e) out[e] = w[k0 + e];
+}
+template <>
+__device__ __forceinline__ void row5<float>(const View<float>& w, int k0, float (&out)[5]) {
+  const int rel = k0 - w.a;
+  const int m = rel & 3;
+  const float4* base = reinterpret_cast<const float4*>(w.p + (rel - m));
+  const float4 A = base[0], B = base[1];
+  switch (m) {
+    case 0: out[0] = A.x; out[1] = A.y; out[2] = A.z; out[3] = A.w; out[4] = B.x; break;
+    case 1: out[0] = A.y; out[1] = A.z; out[2] = A.w; out[3] = B.x; out[4] = B.y; break;
+    case 2: out[0] = A.z; out[1] = A.w; out[2] = B.x; out[3] = B.y; out[4] = B.z; break;
+    default: out[0] = A.w; out[1] = B.x; out[2] = B.y; out[3] = B.z; out[4] = B.w; break;
+  }
+}
+
+// Walks the quads q = q0 + tid, q0 + tid + bd, ... of a tile, keeping
+// (i, j) of the quad's first node 4q with one division per thread.
+struct QuadWalk {
+  int q, i, j, qi, qj, P;
+  __device__ __forceinline__ QuadWalk(const LevelGeom& g, int q0) {
+    P = g.nx + 1;
+    q = q0 + threadIdx.x;
+    const int k = 4 * q;
+    i = k / P;
+    j = k - i * P;
+    const int step = 4 * blockDim.x;
+    qi = step / P;
+    qj = step - qi * P;
+  }
+  __device__ __forceinline__ void next() {
+    q += blockDim.x;
+    i += qi;
+    j += qj;
+    if (j >= P) {
+      j -= P;
+      ++i;
+    }
+  }
+};
+
+// Geometry scalars a quad loop needs, held in registers.
+struct QuadGeom {
+  int k0, k1, ilo, ihi, jhi;  // tile range; interior rows [2, ny-2]; last interior quad start
+  __device__ __forceinline__ QuadGeom(const LevelGeom& g, const Tile& t) {
+    k0 = t.k0;
+    k1 = t.k1;
+    ilo = 2;
+    ihi = g.adv_on ? -1 : g.ny - 2;  // advection: no uniform interior
+    jhi = g.nx - 5;
+  }
+  // The quad lies inside the tile and all four nodes are uniform-interior nodes.
+  __device__ __forceinline__ bool interior(int k, int i, int j) const {
+    return k >= k0 && k + 4 <= k1 && i >= ilo && i <= ihi && j >= 2 && j <= jhi;
+  }
+};
+
+// Node (i, j) of node kk = 4q + e, from the quad's first node (i0, j0).
+__device__ __forceinline__ void quad_node(int P, int i0, int j0, int e, int& i, int& j) {
+  i = i0;
+  j = j0 + e;
+  while (j >= P) {
+    j -= P;
+    ++i;
+  }
+}
+
+// Class of a node whose row may lie outside the grid (nodes of a quad that reach
+// past the trap's last row are never stored; their class only has to be valid).
+__device__ __forceinline__ int node_class_clamped(const LevelGeom& g, int i, int j) {
+  i = i < 0 ? 0 : (i > g.ny ? g.ny : i);
+  return node_class(g, i, j);
+}
+
+// The trap's class table in shared memory, with the interior class replaced by
+// the interior weights, so that a node of the interior class evaluates to the same
+// bits through the table as through the interior constants.  Call before
+// Stager::run (whose barrier publishes it).
+template <class T>
+__device__ __forceinline__ const T* stage_table(Stager& st, const T* __restrict__ tab,
+                                                const Interior<T>& ci) {
+  T* s = reinterpret_cast<T*>(st.cur);
+  st.cur += kTabPerTrap * sizeof(T);
+  for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) {
+    T v = tab[e];
+    const int q = e - 12 * kTabStride;
+    if (q >= 0 && q < kTabStride)
+      v = q == 0 ? ci.c : (q <= 2 ? ci.e : (q <= 4 ? ci.n : (q <= 6 ? ci.d : ci.ic)));
+    s[e] = v;
+  }
+  return s;
+}
+
+// Quad halo window: one row and nine nodes each side, so that every vector load of
+// a quad that overlaps the tile (quads start 4-aligned, up to 3 nodes before the
+// tile) stays inside the staged, zero-guarded window.
+__device__ __forceinline__ int qhalo_lo(const LevelGeom& g, const Tile& t) {
+  return t.k0 - g.nx - 9;
+}
+__device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
+  return t.k1 + g.nx + 9;
+}
+
+// A x and 1/diagonal on a quad.  Every quad makes the same 13 loads (centre
+// vector, two row ends, five above, five below); only the weights differ:
+// interior quads use the interior constants, the others (walls, row ends, ragged
+// last cells, advection traps) take per-node weights from the staged class table.
+template <class T, class X>
+__device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T>& ci,
+                                            const T* __restrict__ stab, const X& x, int k,
+                                            int P, int i0, int j0, bool inner, Q4<T>& xc,
+                                            Q4<T>& id) {
+  xc = x.quad(k);
+  const T xw = x[k - 1], xe = x[k + 4];
+  T nr[5], sr[5];
+  x.row(k + P, nr);      // nr[e]: N of node e, NE of node e-1
+  x.row(k - P - 1, sr);  // sr[e]: SW of node e, S of node e-1
+  Q4<T> ax;
+  if (inner) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const T w = e == 0 ? xw : xc.v[e - 1];
+      const T ee = e == 3 ? xe : xc.v[e + 1];
+      ax.v[e] = st_interior(ci, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
+      id.v[e] = ci.ic;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      int i, j;
+      quad_node(P, i0, j0, e, i, j);
+      T c[8];
+      if (g.adv_on) {
+        coef_general<T>(g, i, j, c);
+      } else {
+        const T* t = stab + node_class_clamped(g, i, j) * kTabStride;
+        const Q4<T> lo = vld4<T>(t), hi = vld4<T>(t + 4);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          c[q] = lo.v[q];
+          c[4 + q] = hi.v[q];
+        }
+      }
+      const T w = e == 0 ? xw : xc.v[e - 1];
+      const T ee = e == 3 ? xe : xc.v[e + 1];
+      ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
+      id.v[e] = c[7];
+    }
+  }
+  return ax;
+}
+
+// A quad's nodes that lie in [k0, k1): masked loads of a tile-range view.
+template <class T>
+__device__ __forceinline__ Q4<T> quad_masked(const View<T>& v, int k, int k0, int k1) {
+  Q4<T> r;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) r.v[e] = (k + e >= k0 && k + e < k1) ? v[k + e] : T(0);
+  return r;
+}
+template <class T>
+__device__ __forceinline__ void store_masked(T* p, const Q4<T>& q, int k, int k0, int k1) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (k + e >= k0 && k + e < k1) p[k + e] = q.v[e];
 }
 
 __device__ __forceinline__ double block_sum(double v) {
@@ -279,8 +540,6 @@ __device__ __forceinline__ double block_sum(double v) {
 __device__ __forceinline__ void count_work(unsigned long long* work, const Tile& t) {
   if (work && threadIdx.x == 0) atomicAdd(work, (unsigned long long)(t.k1 - t.k0));
 }
-
-extern __shared__ __align__(16) char eqf_smem[];
 
 // halo window of a tile: one row plus one node each side (may leave the trap)
 __device__ __forceinline__ int halo_lo(const LevelGeom& g, const Tile& t) {
@@ -308,6 +567,13 @@ __device__ __forceinline__ ChebCoef cheb_coef(float lmin, float lmax, int step) 
   return ChebCoef{rho * rho_old, 2.f * rho / delta};
 }
 
+// d_new = c_res (b - Ax) / diag (+ c_old d_old), one fixed evaluation order
+template <class T, bool FIRST>
+__device__ __forceinline__ T cheb_dir(const ChebCoef& cc, T bk, T ax, T id, T dold) {
+  const T base = (T(cc.c_res) * (bk - ax)) * id;
+  return FIRST ? base : fma_(T(cc.c_old), dold, base);
+}
+
 // Chebyshev-Jacobi step on one level.
 //   ZERO (x_in = 0): x_out = d = D^-1 b / theta            (streaming, no staging)
 //   FIRST:           d = D^-1 (b - A x_in) / theta; x_out = x_in + d
@@ -315,7 +581,7 @@ __device__ __forceinline__ ChebCoef cheb_coef(float lmin, float lmax, int step) 
 // `ratio` > 0 selects the smoothing interval [lmax/ratio, lmax], else the full
 // interval [lmin, lmax] (coarsest-level solve).  DOT adds a partial of b.x_out.
 template <class T, bool FIRST, bool ZERO, bool DOT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_cheb(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, float ratio, int step,
            const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
@@ -334,33 +600,79 @@ __global__ void __launch_bounds__(kThreads)
   const T* bs = b + g.off;
   T* xo = xout + g.off;
   T* ds = d + g.off;
+  const int P = g.nx + 1;
+  const QuadGeom qg(g, tile);
   T acc = T(0);
   if (ZERO) {
-    for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-      const T bk = bs[w.k];
-      const T dn = T(cc.c_res) * bk * inv_diag_tab<T>(g, ci, tab, w.i, w.j);
-      xo[w.k] = dn;
-      ds[w.k] = dn;
-      if (DOT) acc += bk * dn;
+    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+      const int k = 4 * w.q;
+      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+      const Q4<T> bq = full ? vld4<T>(bs + k) : quad_masked<T>(View<T>{bs, 0}, k, tile.k0, tile.k1);
+      Q4<T> id;
+      if (qg.interior(k, w.i, w.j)) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) id.v[e] = ci.ic;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          int i, j;
+          quad_node(P, w.i, w.j, e, i, j);
+          i = i > g.ny ? g.ny : i;
+          id.v[e] = inv_diag_tab<T>(g, ci, tab, i, j);
+        }
+      }
+      Q4<T> dn;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        dn.v[e] = (T(cc.c_res) * bq.v[e]) * id.v[e];
+        if (DOT) acc += bq.v[e] * dn.v[e];
+      }
+      if (full) {
+        vst4<T>(xo + k, dn);
+        vst4<T>(ds + k, dn);
+      } else {
+        store_masked<T>(xo, dn, k, tile.k0, tile.k1);
+        store_masked<T>(ds, dn, k, tile.k0, tile.k1);
+      }
     }
   } else {
     Stager st(eqf_smem);
     const int na = padded_len(g);
-    const View<T> xv = st.add_guarded(xin + g.off, halo_lo(g, tile), halo_hi(g, tile), na);
+    const View<T> xv = st.add_guarded(xin + g.off, qhalo_lo(g, tile), qhalo_hi(g, tile), na);
     const View<T> bv = st.add(bs, tile.k0, tile.k1, na);
     View<T> dv = bv;
     if (!FIRST) dv = st.add(static_cast<const T*>(ds), tile.k0, tile.k1, na);
+    const T* stab = stage_table<T>(st, tab, ci);
     if (!st.run()) return;
-    for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-      const T bk = bv[w.k];
-      T id;
-      const T r = bk - apply_tab<T>(g, ci, tab, xv, w.k, w.i, w.j, id);
-      T dn = T(cc.c_res) * r * id;
-      if (!FIRST) dn += T(cc.c_old) * dv[w.k];
-      const T xn = xv[w.k] + dn;
-      xo[w.k] = xn;
-      ds[w.k] = dn;
-      if (DOT) acc += bk * xn;
+    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+      const int k = 4 * w.q;
+      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+      Q4<T> xc, id;
+      const Q4<T> ax = apply_quad<T>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j),
+                                     xc, id);
+      Q4<T> bq, dq;
+      if (full) {
+        bq = bv.quad(k);
+        if (!FIRST) dq = dv.quad(k);
+      } else {
+        bq = quad_masked<T>(bv, k, tile.k0, tile.k1);
+        if (!FIRST) dq = quad_masked<T>(dv, k, tile.k0, tile.k1);
+      }
+      if (FIRST) dq = bq;
+      Q4<T> dn, xn;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        dn.v[e] = cheb_dir<T, FIRST>(cc, bq.v[e], ax.v[e], id.v[e], dq.v[e]);
+        xn.v[e] = xc.v[e] + dn.v[e];
+        if (DOT) acc += bq.v[e] * xn.v[e];
+      }
+      if (full) {
+        vst4<T>(xo + k, xn);
+        vst4<T>(ds + k, dn);
+      } else {
+        store_masked<T>(xo, xn, k, tile.k0, tile.k1);
+        store_masked<T>(ds, dn, k, tile.k0, tile.k1);
+      }
     }
   }
   if (DOT) {
@@ -371,7 +683,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // t = b - A x
 template <class T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_resid(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
             const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
             const T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
@@ -379,17 +691,31 @@ __global__ void __launch_bounds__(kThreads)
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
-  Stager st(eqf_smem);
-  const int na = padded_len(g);
-  const View<T> xv = st.add_guarded(x + g.off, halo_lo(g, tile), halo_hi(g, tile), na);
-  const View<T> bv = st.add(b + g.off, tile.k0, tile.k1, na);
-  if (!st.run()) return;
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
+  Stager st(eqf_smem);
+  const int na = padded_len(g);
+  const View<T> xv = st.add_guarded(x + g.off, qhalo_lo(g, tile), qhalo_hi(g, tile), na);
+  const View<T> bv = st.add(b + g.off, tile.k0, tile.k1, na);
+  const T* stab = stage_table<T>(st, tab, ci);
+  if (!st.run()) return;
   T* ts = t + g.off;
-  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-    T id;
-    ts[w.k] = bv[w.k] - apply_tab<T>(g, ci, tab, xv, w.k, w.i, w.j, id);
+  const int P = g.nx + 1;
+  const QuadGeom qg(g, tile);
+  for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+    const int k = 4 * w.q;
+    const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+    Q4<T> xc, id;
+    const Q4<T> ax =
+        apply_quad<T>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j), xc, id);
+    const Q4<T> bq = full ? bv.quad(k) : quad_masked<T>(bv, k, tile.k0, tile.k1);
+    Q4<T> r;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
+    if (full)
+      vst4<T>(ts + k, r);
+    else
+      store_masked<T>(ts, r, k, tile.k0, tile.k1);
   }
 }
 
@@ -551,7 +877,34 @@ struct CgState {
 // p_out = z (FIRST) or z + beta p_in; q = A p_out; partial dot(p_out, q).
 // p is ping-ponged because neighbours of p_out are recomputed from p_in.
 template <class T, bool FIRST>
-__global__ void __launch_bounds__(kThreads)
+struct PNew {  // p_out = z + beta p_in evaluated on the fly from the staged z, p_in
+  View<T> z, p;
+  T beta;
+  __device__ __forceinline__ T operator[](int k) const {
+    return FIRST ? z[k] : fma_(beta, p[k], z[k]);
+  }
+  __device__ __forceinline__ Q4<T> quad(int k) const {
+    Q4<T> a = z.quad(k);
+    if (!FIRST) {
+      const Q4<T> b = p.quad(k);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) a.v[e] = fma_(beta, b.v[e], a.v[e]);
+    }
+    return a;
+  }
+  __device__ __forceinline__ void row(int k0, T (&out)[5]) const {
+    z.row(k0, out);
+    if (!FIRST) {
+      T pr[5];
+      p.row(k0, pr);
+#pragma unroll
+      for (int e = 0; e < 5; ++e) out[e] = fma_(beta, pr[e], out[e]);
+    }
+  }
+};
+
+template <class T, bool FIRST>
+__global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_cg_dir(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
              const T* __restrict__ tabs, const int* __restrict__ skip,
              const CgState* __restrict__ st, const T* __restrict__ z, const T* __restrict__ pin,
@@ -567,36 +920,43 @@ __global__ void __launch_bounds__(kThreads)
   const T beta = FIRST ? T(0) : T(st[g.trap].beta);
   Stager sg(eqf_smem);
   const int na = padded_len(g);
-  const int ka = halo_lo(g, tile), kb = halo_hi(g, tile);
+  const int ka = qhalo_lo(g, tile), kb = qhalo_hi(g, tile);
   const View<T> zv = sg.add_guarded(z + g.off, ka, kb, na);
   View<T> pv = zv;
   if (!FIRST) pv = sg.add_guarded(pin + g.off, ka, kb, na);
-  if (!sg.run()) return;
-  struct PV {
-    View<T> z, p;
-    T beta;
-    __device__ __forceinline__ T operator[](int k) const {
-      return FIRST ? z[k] : z[k] + beta * p[k];
-    }
-  } pnew{zv, pv, beta};
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
+  const T* stab = stage_table<T>(sg, tab, ci);
+  if (!sg.run()) return;
+  const PNew<T, FIRST> pnew{zv, pv, beta};
   T* po = pout + g.off;
   T* qs = q + g.off;
+  const int P = g.nx + 1;
+  const QuadGeom qg(g, tile);
   T acc = T(0);
-  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-    const T pc = pnew[w.k];
-    T id;
-    const T a = apply_tab<T>(g, ci, tab, pnew, w.k, w.i, w.j, id);
-    po[w.k] = pc;
-    qs[w.k] = a;
-    acc += pc * a;
+  for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+    const int k = 4 * w.q;
+    Q4<T> pc, id;
+    const Q4<T> a =
+        apply_quad<T>(g, ci, stab, pnew, k, P, w.i, w.j, qg.interior(k, w.i, w.j), pc, id);
+    if (k >= tile.k0 && k + 4 <= tile.k1) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
+      vst4<T>(po + k, pc);
+      vst4<T>(qs + k, a);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (k + e >= tile.k0 && k + e < tile.k1) acc += pc.v[e] * a.v[e];
+      store_masked<T>(po, pc, k, tile.k0, tile.k1);
+      store_masked<T>(qs, a, k, tile.k0, tile.k1);
+    }
   }
   const double t = block_sum(double(acc));
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// x += alpha p; r -= alpha q; partial dot(r, r)   (streaming)
+// x += alpha p; r -= alpha q; partial dot(r, r)   (streaming, quads)
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_cg_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
@@ -613,12 +973,29 @@ __global__ void __launch_bounds__(kThreads)
   const T alpha = T(st[g.trap].alpha);
   const long long o = g.off;
   T acc = T(0);
-#pragma unroll 4
-  for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) {
-    x[o + k] += alpha * p[o + k];
-    const T rn = r[o + k] - alpha * q[o + k];
-    r[o + k] = rn;
-    acc += rn * rn;
+  const int qa = tile.k0 >> 2, qb = (tile.k1 + 3) >> 2;
+  for (int qq = qa + threadIdx.x; qq < qb; qq += blockDim.x) {
+    const int k = 4 * qq;
+    if (k >= tile.k0 && k + 4 <= tile.k1) {
+      const Q4<T> pq = vld4<T>(p + o + k), qv = vld4<T>(q + o + k);
+      Q4<T> xq = vld4<T>(x + o + k), rq = vld4<T>(r + o + k);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        xq.v[e] = fma_(alpha, pq.v[e], xq.v[e]);
+        rq.v[e] = fma_(-alpha, qv.v[e], rq.v[e]);
+        acc += rq.v[e] * rq.v[e];
+      }
+      vst4<T>(x + o + k, xq);
+      vst4<T>(r + o + k, rq);
+    } else {
+      for (int kk = k; kk < k + 4; ++kk) {
+        if (kk < tile.k0 || kk >= tile.k1) continue;
+        x[o + kk] = fma_(alpha, p[o + kk], x[o + kk]);
+        const T rn = fma_(-alpha, q[o + kk], r[o + kk]);
+        r[o + kk] = rn;
+        acc += rn * rn;
+      }
+    }
   }
   const double t = block_sum(double(acc));
   if (threadIdx.x == 0) part[blockIdx.x] = t;
@@ -742,7 +1119,7 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// u += x; d += x (the inner-solve correction)   (streaming)
+// u += x; d += x (the inner-solve correction)   (streaming, quads)
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
@@ -753,11 +1130,28 @@ __global__ void __launch_bounds__(kThreads)
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
   const long long o = g.off;
-#pragma unroll 4
-  for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) {
-    const T v = x[o + k];
-    u[o + k] += double(v);
-    d[o + k] += float(v);
+  const int qa = tile.k0 >> 2, qb = (tile.k1 + 3) >> 2;
+  for (int qq = qa + threadIdx.x; qq < qb; qq += blockDim.x) {
+    const int k = 4 * qq;
+    if (k >= tile.k0 && k + 4 <= tile.k1) {
+      const Q4<T> xq = vld4<T>(x + o + k);
+      Q4<double> uq = vld4<double>(u + o + k);
+      Q4<float> dq = vld4<float>(d + o + k);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        uq.v[e] += double(xq.v[e]);
+        dq.v[e] += float(xq.v[e]);
+      }
+      vst4<double>(u + o + k, uq);
+      vst4<float>(d + o + k, dq);
+    } else {
+      for (int kk = k; kk < k + 4; ++kk) {
+        if (kk < tile.k0 || kk >= tile.k1) continue;
+        const T v = x[o + kk];
+        u[o + kk] += double(v);
+        d[o + kk] += float(v);
+      }
+    }
   }
 }
 

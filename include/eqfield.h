@@ -79,6 +79,7 @@ typedef struct eqf_solver_opts {
   double cheb_ratio;  /* smoothing interval [lmax/ratio, lmax] */
   int32_t use_graph;  /* capture steps as CUDA graphs */
   int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
+  int32_t tile_nodes; /* target nodes per row tile of the finest level (0: default) */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;
