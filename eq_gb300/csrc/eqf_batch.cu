@@ -21,6 +21,7 @@
 #include "eqf_cells.cuh"
 #include "eqf_common.cuh"
 #include "eqf_kernels.cuh"
+#include "eqf_refine.cuh"
 
 namespace eqf {
 
@@ -216,6 +217,7 @@ struct Level {
   DevBuf<double> tabd;  // same in FP64
   // dynamic shared memory per staged kernel (max over this level's tiles)
   size_t sm_cheb = 0, sm_resid = 0, sm_cgdir = 0, sm_ir = 0;
+  size_t sm_irf1 = 0, sm_irf = 0;  // pair-arithmetic refinement residuals (FP32 form)
 
   size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
   size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
@@ -310,7 +312,8 @@ class Batch {
   DevBuf<float> Dd[2];  // step increments (previous / current), for the initial guess
   int cur = 0;
   DevBuf<double> b64, F;  // refinement rhs, load
-  DevBuf<double> tabA0, tabM0;  // finest-level FP64 operator and mass tables
+  DevBuf<double> tabM0;         // finest-level FP64 mass table
+  DevBuf<float2> tabA2, tabM2;  // finest-level operator / mass tables as float pairs
   double* u_cur() { return U[cur].p; }
   std::unique_ptr<WorkBase> work;
   cudaStream_t stream = nullptr;
@@ -510,6 +513,31 @@ void Batch::build_levels() {
         build_table<double, true>(L[0].geom[t], tm.data() + (size_t)t * kTabPerTrap);
       tabM0.alloc(tm.size());
       tabM0.upload(tm.data(), tm.size(), stream);
+      // float pairs (h, l), h + l = the FP64 weight to ~2^-48; the interior class
+      // holds the interior weights, as the FP64 kernels use them
+      std::vector<float2> a2(tm.size()), m2(tm.size());
+      auto pr = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+      };
+      for (int t = 0; t < ntraps; ++t) {
+        const LevelGeom& g = L[0].geom[t];
+        const size_t o = (size_t)t * kTabPerTrap;
+        for (int e = 0; e < kTabPerTrap; ++e) {
+          a2[o + e] = pr(td[o + e]);
+          m2[o + e] = pr(tm[o + e]);
+        }
+        const double ia[8] = {g.cC, g.cE, g.cE, g.cN, g.cN, g.cD, g.cD, g.cCinv};
+        const double im[8] = {g.mC, g.mE, g.mE, g.mN, g.mN, g.mD, g.mD, 0.0};
+        for (int q = 0; q < kTabStride; ++q) {
+          a2[o + 12 * kTabStride + q] = pr(ia[q]);
+          m2[o + 12 * kTabStride + q] = pr(im[q]);
+        }
+      }
+      tabA2.alloc(a2.size());
+      tabA2.upload(a2.data(), a2.size(), stream);
+      tabM2.alloc(m2.size());
+      tabM2.upload(m2.data(), m2.size(), stream);
     }
     sync();  // host vectors go out of scope
   }
@@ -531,6 +559,10 @@ void Batch::build_levels() {
       Lv.sm_cgdir = std::max(Lv.sm_cgdir, kSmemHeader + 2 * halo + tab);
 
       // first refinement residual: u (FP64, halo), F (FP64), d (FP32, halo)
+      const size_t ptab = (size_t)kTabPerTrap * 8;
+      Lv.sm_irf1 = std::max(Lv.sm_irf1, kSmemHeader + guarded_bytes(ka, kb, 8) +
+                                            guarded_bytes(ka, kb, 4) + 2 * ptab);
+      Lv.sm_irf = std::max(Lv.sm_irf, kSmemHeader + guarded_bytes(ka, kb, 8) + ptab);
       Lv.sm_ir = std::max(Lv.sm_ir, kSmemHeader + guarded_bytes(ka, kb, 8) +
                                         staged_bytes(tl.k0, tl.k1, 8, na) +
                                         guarded_bytes(ka, kb, 4) +
@@ -563,7 +595,7 @@ void Batch::build_levels() {
     for (size_t v : {Lv.sm_cheb, Lv.sm_resid, Lv.sm_cgdir, Lv.sm_restrict, Lv.sm_prolong})
       if (v > kMaxDynSmem)
         throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
-    if (l == 0 && Lv.sm_ir > kMaxDynSmem)
+    if (l == 0 && std::max(Lv.sm_ir, Lv.sm_irf1) > kMaxDynSmem)
       throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
   }
   {  // single-CTA coarsest solve when every trap's coarsest grid fits
@@ -611,6 +643,9 @@ static void allow_dyn_smem() {
   smem_attrs(k_ir_first<T>, mx);
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
+  smem_attrs(k_irf_first, mx);
+  smem_attrs(k_irf_residual<true>, mx);
+  smem_attrs(k_irf_residual<false>, mx);
 }
 
 template <class T>
@@ -763,15 +798,29 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   const double tol_abs = fp32 ? 0.3 * B.opts.rtol : B.opts.rtol;
   double* u_out = B.U[1 - B.cur].p;
   float* d_out = B.Dd[1 - B.cur].p;
-  if (first)
-    EQF_RUN(B, KC_IR_RESID_FIRST,
-            (k_ir_first<T><<<nt, kThreads, L0.sm_ir, s>>>(
-                G, tl, L0.tabd.p, B.tabM0.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
-                B.b64.p, u_out, d_out, r, part, nt, W)));
-  else
-    EQF_RUN(B, KC_IR_RESID,
-            (k_ir_residual<T, false><<<nt, kThreads, L0.sm_ir, s>>>(
-                G, tl, L0.tabd.p, B.d_ir_done.p, B.b64.p, u_out, d_out, r, part, nt, W)));
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 form: residuals in float-pair arithmetic, rhs b kept as pairs
+    float2* b2 = reinterpret_cast<float2*>(B.b64.p);
+    if (first)
+      EQF_RUN(B, KC_IR_RESID_FIRST,
+              (k_irf_first<<<nt, kThreads, L0.sm_irf1, s>>>(
+                  G, tl, B.tabA2.p, B.tabM2.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
+                  b2, u_out, d_out, r, part, nt, W)));
+    else
+      EQF_RUN(B, KC_IR_RESID,
+              (k_irf_residual<false><<<nt, kThreads, L0.sm_irf, s>>>(
+                  G, tl, B.tabA2.p, B.d_ir_done.p, b2, u_out, d_out, r, part, nt, W)));
+  } else {
+    if (first)
+      EQF_RUN(B, KC_IR_RESID_FIRST,
+              (k_ir_first<T><<<nt, kThreads, L0.sm_ir, s>>>(
+                  G, tl, L0.tabd.p, B.tabM0.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
+                  B.b64.p, u_out, d_out, r, part, nt, W)));
+    else
+      EQF_RUN(B, KC_IR_RESID,
+              (k_ir_residual<T, false><<<nt, kThreads, L0.sm_ir, s>>>(
+                  G, tl, L0.tabd.p, B.d_ir_done.p, B.b64.p, u_out, d_out, r, part, nt, W)));
+  }
   EQF_RUN(B, KC_SCALAR,
           (k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
                                      B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p)));
@@ -810,10 +859,17 @@ template <class T>
 void Work<T>::enqueue_check(cudaStream_t s, bool update_gamma) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
-  EQF_RUN(B, KC_IR_RESID,
-          (k_ir_residual<T, true><<<nt, kThreads, L0.sm_ir, s>>>(
-              L0.dgeom.p, L0.dtiles.p, L0.tabd.p, B.d_ir_done.p, B.b64.p, B.U[1 - B.cur].p,
-              B.Dd[1 - B.cur].p, lv[0].b.p, B.dpart.p, nt, W)));
+  if constexpr (std::is_same<T, float>::value)
+    EQF_RUN(B, KC_IR_RESID,
+            (k_irf_residual<true><<<nt, kThreads, L0.sm_irf, s>>>(
+                L0.dgeom.p, L0.dtiles.p, B.tabA2.p, B.d_ir_done.p,
+                reinterpret_cast<const float2*>(B.b64.p), B.U[1 - B.cur].p, B.Dd[1 - B.cur].p,
+                lv[0].b.p, B.dpart.p, nt, W)));
+  else
+    EQF_RUN(B, KC_IR_RESID,
+            (k_ir_residual<T, true><<<nt, kThreads, L0.sm_ir, s>>>(
+                L0.dgeom.p, L0.dtiles.p, L0.tabd.p, B.d_ir_done.p, B.b64.p, B.U[1 - B.cur].p,
+                B.Dd[1 - B.cur].p, lv[0].b.p, B.dpart.p, nt, W)));
   EQF_RUN(B, KC_SCALAR,
           (k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
                                                              B.opts.rtol, B.dstate.p,

@@ -1119,6 +1119,17 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Exact conversion to double: floats by repacking their bits (no FP64-pipe convert).
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  const unsigned long long s = (unsigned long long)(b & 0x80000000u) << 32;
+  const unsigned long long ex = e == 0xFFu ? 0x7FFull : (unsigned long long)(e + 896u);
+  const unsigned long long m = (unsigned long long)(b & 0x7FFFFFu) << 29;
+  return __longlong_as_double(e == 0u ? s : (s | (ex << 52) | m));
+}
+
 // u += x; d += x (the inner-solve correction)   (streaming, quads)
 template <class T>
 __global__ void __launch_bounds__(kThreads)
@@ -1139,7 +1150,7 @@ __global__ void __launch_bounds__(kThreads)
       Q4<float> dq = vld4<float>(d + o + k);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        uq.v[e] += double(xq.v[e]);
+        uq.v[e] += to_double(xq.v[e]);
         dq.v[e] += float(xq.v[e]);
       }
       vst4<double>(u + o + k, uq);
@@ -1148,7 +1159,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int kk = k; kk < k + 4; ++kk) {
         if (kk < tile.k0 || kk >= tile.k1) continue;
         const T v = x[o + kk];
-        u[o + kk] += double(v);
+        u[o + kk] += to_double(v);
         d[o + kk] += float(v);
       }
     }

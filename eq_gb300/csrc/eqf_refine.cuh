@@ -1,0 +1,288 @@
+// Refinement residuals of the FP32 form in double-float arithmetic.
+//
+// GB300 executes FP64 at 1/64 of the FP32 rate, so the residual r = b - A u of the
+// iterative refinement (two seven-point stencils per node in the first pass) is
+// evaluated on the FP32 pipe instead: every value is an unevaluated sum h + l of
+// two floats ("pair", about 47 significant bits), products are split exactly with
+// fused multiply-adds and the sums carry their rounding errors (two-sum).  The
+// conversions between doubles and pairs are done with integer bit operations, so
+// the kernels issue almost no FP64 instructions (one add per stored double and one
+// multiply-add per squared-norm term).
+//
+// Accuracy: a pair carries a relative error below 2^-47 (7e-15).  The residual of a
+// stencil with cancellation factor C = sum|a_ij u_j| / |(A u)_i| is accurate to
+// about 7 C 2^-47 |A u|; for the diffusion operators here (C up to ~1e4) that is
+// 1e-9 of |b| or better, two orders below the tolerances the refinement is run to
+// (rtol >= 1e-8), so the outer convergence test is unaffected.  Values of magnitude
+// below 2^-126 (1.2e-38) flush to zero and values from 2^128 on become infinite.
+//
+// The plain FP64 form keeps its FP64 kernels (eqf_kernels.cuh).
+#pragma once
+#include "eqf_kernels.cuh"
+
+namespace eqf {
+
+struct DF {
+  float h, l;
+};
+
+// Exact float -> double by repacking the bits (denormals flush to signed zero).
+__device__ __forceinline__ double f2d(float f) { return to_double(f); }
+
+// double -> pair: h = v truncated to 24 significant bits, l = the next 23 bits
+// (|h + l - v| < 2^-46 |v|).  |v| < 2^-126 gives (0, 0); |v| >= 2^128 (+-inf, 0).
+__device__ __forceinline__ DF df_split(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const uint32_t wh = (uint32_t)(u >> 32), wl = (uint32_t)u;
+  const uint32_t sg = wh & 0x80000000u;
+  const int e = (int)((wh >> 20) & 0x7FFu);
+  const uint32_t hb = sg | ((uint32_t)(e - 896) << 23) | ((wh & 0xFFFFFu) << 3) | (wl >> 29);
+  // l = (low 29 mantissa bits >> 6) * 2^(e - 1069); the integer part is < 2^23,
+  // so the magic-number conversion below is exact
+  const uint32_t r = (wl & 0x1FFFFFFFu) >> 6;
+  const float rf = __fsub_rn(__uint_as_float(0x4B000000u | r), 8388608.0f);
+  const float sc = __uint_as_float((uint32_t)(e - 942) << 23);
+  const float l = __uint_as_float(__float_as_uint(__fmul_rn(rf, sc)) | sg);
+  DF o;
+  if (e < 897) {
+    o.h = 0.f;
+    o.l = 0.f;
+  } else if (e > 1150) {
+    o.h = __uint_as_float(sg | 0x7F800000u);
+    o.l = 0.f;
+  } else {
+    o.h = __uint_as_float(hb);
+    // below 2^-80 the integer scale would leave the float range: FP64 fallback
+    o.l = e >= 943 ? l : __double2float_rn(v - f2d(o.h));
+  }
+  return o;
+}
+
+// pair -> double (one FP64 add)
+__device__ __forceinline__ double df_to_double(DF a) { return __dadd_rn(f2d(a.h), f2d(a.l)); }
+
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+__device__ __forceinline__ DF df_norm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return DF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float err;
+  const float s = two_sum(a.h, b.h, err);
+  return df_norm(s, __fadd_rn(err, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+
+// Sum of pair products c_m x_m: the high products are added with two-sum, every
+// rounding error (of the products and of the sums) goes into e.
+struct DFAcc {
+  float s, e;
+  __device__ __forceinline__ void first(DF c, DF x) {
+    s = __fmul_rn(c.h, x.h);
+    e = __fmaf_rn(c.h, x.l, __fmaf_rn(c.l, x.h, __fmaf_rn(c.h, x.h, -s)));
+  }
+  __device__ __forceinline__ void add(DF c, DF x) {
+    const float p = __fmul_rn(c.h, x.h);
+    const float pe = __fmaf_rn(c.h, x.l, __fmaf_rn(c.l, x.h, __fmaf_rn(c.h, x.h, -p)));
+    float err;
+    s = two_sum(s, p, err);
+    e = __fadd_rn(e, __fadd_rn(err, pe));
+  }
+  __device__ __forceinline__ DF result() const { return df_norm(s, e); }
+};
+
+// Per-trap pair tables: 25 classes x 8 pairs (c, e, w, n, s, ne, sw, unused), the
+// interior class holding the interior weights (same layout as the FP64 tables).
+__device__ __forceinline__ const float2* stage_pair_table(Stager& st, const float2* tab) {
+  float2* s = reinterpret_cast<float2*>(st.cur);
+  st.cur += kTabPerTrap * sizeof(float2);
+  for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) s[e] = tab[e];
+  return s;
+}
+
+// (A x)_k for node (i, j) from a pair window x (node k at x[k - a]).
+__device__ __forceinline__ DF df_apply(const LevelGeom& g, const float2* __restrict__ stab,
+                                       bool general, const float2* x, int a, int k, int i,
+                                       int j) {
+  const int P = g.nx + 1;
+  DF c[7];
+  if (general) {
+    double cg[8];
+    coef_general<double>(g, i, j, cg);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) c[m] = df_split(cg[m]);
+  } else {
+    const float2* t = stab + node_class(g, i, j) * kTabStride;
+#pragma unroll
+    for (int m = 0; m < 7; ++m) c[m] = DF{t[m].x, t[m].y};
+  }
+  const int idx[7] = {k, k + 1, k - 1, k + P, k - P, k + P + 1, k - P - 1};
+  DFAcc acc;
+  {
+    const float2 v = x[idx[0] - a];
+    acc.first(c[0], DF{v.x, v.y});
+  }
+#pragma unroll
+  for (int m = 1; m < 7; ++m) {
+    const float2 v = x[idx[m] - a];
+    acc.add(c[m], DF{v.x, v.y});
+  }
+  return acc.result();
+}
+
+// Converts the staged doubles of window [ka, kb) to pairs in place (same 8 bytes).
+__device__ __forceinline__ void window_to_pairs(const View<double>& v, int ka, int kb) {
+  double* p = const_cast<double*>(v.p);
+  for (int k = ka + (int)threadIdx.x; k < kb; k += blockDim.x) {
+    const DF d = df_split(p[k - v.a]);
+    reinterpret_cast<float2*>(p)[k - v.a] = make_float2(d.h, d.l);
+  }
+}
+
+// First refinement residual of a step in the FP32 form (partials: [0] |b|^2,
+// [1] |r|^2):  b = F + M u_in (stored as pairs), u0 = u_in + gamma d_in,
+// u_out = u0, d_out = u0 - u_in, r = b - A u0.  Dirichlet rows: b = 0, r = 0.
+__global__ void __launch_bounds__(kThreads)
+    k_irf_first(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+                const float2* __restrict__ tabA, const float2* __restrict__ tabM,
+                const CgState* __restrict__ st, const double* __restrict__ F,
+                const double* __restrict__ u_in, const float* __restrict__ d_in,
+                float2* __restrict__ b2, double* __restrict__ u_out, float* __restrict__ d_out,
+                float* __restrict__ r, double* __restrict__ part, int ntiles,
+                unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];
+  const LevelGeom& g = G[tile.geom];
+  count_work(work, tile);
+  Stager sg(eqf_smem);
+  const int na = padded_len(g);
+  const int ka = halo_lo(g, tile), kb = halo_hi(g, tile);
+  const View<double> uv = sg.add_guarded(u_in + g.off, ka, kb, na);
+  const View<float> dv = sg.add_guarded(d_in + g.off, ka, kb, na);
+  const float2* sA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
+  const float2* sM = stage_pair_table(sg, tabM + (size_t)g.trap * kTabPerTrap);
+  if (!sg.run()) return;
+  window_to_pairs(uv, ka, kb);
+  __syncthreads();
+  const float2* xw = reinterpret_cast<const float2*>(uv.p);
+  const int xa = uv.a;
+  const double* Fs = F + g.off;
+  float2* bs = b2 + g.off;
+  double abb = 0.0, arr = 0.0;
+  // b = F + M u_in
+  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+    const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
+    DF bk{0.f, 0.f};
+    if (!dir) bk = df_add(df_split(Fs[w.k]), df_apply(g, sM, false, xw, xa, w.k, w.i, w.j));
+    bs[w.k] = make_float2(bk.h, bk.l);
+    const double bh = f2d(bk.h);
+    abb = __fma_rn(bh, bh, abb);
+  }
+  __syncthreads();  // every read of u_in done: the window becomes u0 in place
+  {
+    const DF gm = df_split(st[g.trap].gamma);
+    float2* x = const_cast<float2*>(xw);
+    double* uo = u_out + g.off;
+    float* dout = d_out + g.off;
+    for (int k = ka + (int)threadIdx.x; k < kb; k += blockDim.x) {
+      const float2 u = x[k - xa];
+      const float dk = dv[k];
+      const float p = __fmul_rn(gm.h, dk);
+      const float pe = __fmaf_rn(gm.l, dk, __fmaf_rn(gm.h, dk, -p));
+      const DF u0 = df_add(DF{u.x, u.y}, df_norm(p, pe));
+      x[k - xa] = make_float2(u0.h, u0.l);
+      if (k >= tile.k0 && k < tile.k1) {
+        uo[k] = df_to_double(u0);
+        dout[k] = __fadd_rn(p, pe);
+      }
+    }
+  }
+  __syncthreads();
+  const bool general = g.adv_on != 0;
+  float* rs = r + g.off;
+  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+    const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
+    float rk = 0.f;
+    if (!dir) {
+      const float2 b = bs[w.k];
+      const DF res = df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, xa, w.k, w.i, w.j)));
+      rk = __fadd_rn(res.h, res.l);
+    }
+    rs[w.k] = rk;
+    const double rd = f2d(rk);
+    arr = __fma_rn(rd, rd, arr);
+  }
+  const double tb = block_sum(abb);
+  const double tr = block_sum(arr);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = tb;
+    part[ntiles + blockIdx.x] = tr;
+  }
+}
+
+// Later residuals of a step in the FP32 form: r = b - A u (partial [1] |r|^2).
+// With FINAL the residual is only measured and every trap also reports |d|^2
+// (partial [2]) for the next step's extrapolation factor.
+template <bool FINAL>
+__global__ void __launch_bounds__(kThreads)
+    k_irf_residual(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+                   const float2* __restrict__ tabA, const int* __restrict__ skip,
+                   const float2* __restrict__ b2, const double* __restrict__ u,
+                   const float* __restrict__ dcur, float* __restrict__ r,
+                   double* __restrict__ part, int ntiles, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];
+  const LevelGeom& g = G[tile.geom];
+  const bool skipped = skip && skip[g.trap];
+  if (skipped && !FINAL) {
+    if (threadIdx.x == 0) part[ntiles + blockIdx.x] = 0.0;
+    return;
+  }
+  double arr = 0.0, add = 0.0;
+  if (FINAL) {
+    const float* ds = dcur + g.off;
+    for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) {
+      const double v = f2d(ds[k]);
+      add = __fma_rn(v, v, add);
+    }
+  }
+  if (!skipped) {
+    count_work(work, tile);
+    Stager sg(eqf_smem);
+    const int na = padded_len(g);
+    const int ka = halo_lo(g, tile), kb = halo_hi(g, tile);
+    const View<double> uv = sg.add_guarded(u + g.off, ka, kb, na);
+    const float2* sA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
+    if (!sg.run()) return;
+    window_to_pairs(uv, ka, kb);
+    __syncthreads();
+    const float2* xw = reinterpret_cast<const float2*>(uv.p);
+    const bool general = g.adv_on != 0;
+    const float2* bs = b2 + g.off;
+    float* rs = r + g.off;
+    for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+      const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
+      float rk = 0.f;
+      if (!dir) {
+        const float2 b = bs[w.k];
+        const DF res =
+            df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, uv.a, w.k, w.i, w.j)));
+        rk = __fadd_rn(res.h, res.l);
+      }
+      if (!FINAL) rs[w.k] = rk;
+      const double rd = f2d(rk);
+      arr = __fma_rn(rd, rd, arr);
+    }
+  }
+  const double tr = block_sum(arr);
+  const double td = FINAL ? block_sum(add) : 0.0;
+  if (threadIdx.x == 0) {
+    part[ntiles + blockIdx.x] = tr;
+    if (FINAL) part[2 * ntiles + blockIdx.x] = td;
+  }
+}
+
+}  // namespace eqf
