@@ -22,6 +22,7 @@ EQF_NOALLOC_MAX_NODES = 8388608
 
 EQF_WALL_BOTTOM, EQF_WALL_TOP, EQF_WALL_LEFT, EQF_WALL_RIGHT = 1, 2, 4, 8
 EQF_PREC_FP64, EQF_PREC_FP32_IR = 0, 1
+EQF_KRYLOV_AUTO, EQF_KRYLOV_CG, EQF_KRYLOV_BICGSTAB = 0, 1, 2
 
 # every entry point declared in include/eqfield.h
 EXPORTS = (
@@ -29,7 +30,7 @@ EXPORTS = (
     "eqf_set_cells", "eqf_set_cell_rates", "eqf_set_nodal", "eqf_add_nodal", "eqf_step",
     "eqf_read_nodal", "eqf_read_cells", "eqf_boundary_flux", "eqf_total_mass", "eqf_stats",
     "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
-    "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc",
+    "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc", "eqf_couple_species",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
@@ -46,7 +47,7 @@ class SolverOpts(C.Structure):
                 ("max_iters", C.c_int32), ("inner_tol", C.c_double), ("cheb_pre", C.c_int32),
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
                 ("use_graph", C.c_int32), ("adaptive", C.c_int32),
-                ("tile_nodes", C.c_int32)]
+                ("tile_nodes", C.c_int32), ("krylov", C.c_int32)]
 
 
 class EqfError(RuntimeError):
@@ -94,6 +95,8 @@ def load() -> C.CDLL:
                                                  C.c_double, C.c_int32, C.c_double, C.c_void_p,
                                                  dp]),
         "eqf_profile_read": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p, i64p, dp]),
+        "eqf_couple_species": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int32),
+                                         C.c_double, C.c_double, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

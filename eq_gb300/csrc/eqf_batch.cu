@@ -22,6 +22,7 @@
 #include "eqf_common.cuh"
 #include "eqf_kernels.cuh"
 #include "eqf_refine.cuh"
+#include "eqf_bicgstab.cuh"
 
 namespace eqf {
 
@@ -290,10 +291,12 @@ struct Work : WorkBase {
   };
   std::vector<Lv> lv;
   DevBuf<T> xs, p0, p1, q;  // fine CG: correction, directions, A p
+  DevBuf<T> rh;             // BiCGSTAB shadow residual (only when BiCGSTAB is used)
   explicit Work(Batch& b);
   void enqueue_sweep(cudaStream_t s, bool first) override;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
-  T* vcycle(cudaStream_t s, int lev, bool dot);
+  T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr);
+  void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs);
 };
 
 class Batch {
@@ -323,6 +326,7 @@ class Batch {
   Prof prof;
   int cur_cls = -1;
   int num_sms = 1;
+  bool use_bicgstab = false;  // nonsymmetric operator (advection) or requested
 
   // profiling hooks: begin() returns the node counter of this launch (or null)
   unsigned long long* prof_begin(int c) {
@@ -352,6 +356,25 @@ class Batch {
   DevBuf<int> d_cell_trap, d_ent_node, d_perm, d_seg_start;
   DevBuf<double> d_cell_xy, d_cell_s, d_ent_w, d_ent_val, d_scale, d_cells_out;
   std::vector<int> cell_first;  // first cell index of each trap in the batch arrays
+  // two-species couplings (species 1 on t1, species 2 on t2, same cells)
+  struct Coupling {
+    int t1, t2;
+    CouplingLaw law;
+    std::vector<int> sender;
+  };
+  std::vector<Coupling> couplings;
+  int ncp = 0;  // coupled cells over all couplings
+  DevBuf<int> d_cp_i1, d_cp_i2, d_cp_sender, d_cp_law;
+  DevBuf<double> d_cp_prod, d_cp_c;
+  DevBuf<CouplingLaw> d_cp_laws;
+  void enqueue_coupling();
+  void drop_graphs() {
+    for (auto& gx : graph)
+      if (gx) {
+        cudaGraphExecDestroy(gx);
+        gx = nullptr;
+      }
+  }
 
   explicit Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o);
   ~Batch();
@@ -384,6 +407,9 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
     EQF_CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   }
   build_levels();
+  bool adv = false;
+  for (const auto& p : params) adv = adv || (p.adv_u != 0.0 && p.adv_len > 0.0);
+  use_bicgstab = opts.krylov == EQF_KRYLOV_BICGSTAB || (opts.krylov == EQF_KRYLOV_AUTO && adv);
   const long long N0 = L[0].nodes;
   for (int q = 0; q < 2; ++q) {
     U[q].alloc(N0);
@@ -644,6 +670,8 @@ static void allow_dyn_smem() {
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
   smem_attrs(k_irf_first, mx);
+  smem_attrs(k_apply_dot<T, 1>, mx);
+  smem_attrs(k_apply_dot<T, 2>, mx);
   smem_attrs(k_irf_residual<true>, mx);
   smem_attrs(k_irf_residual<false>, mx);
 }
@@ -667,6 +695,10 @@ Work<T>::Work(Batch& b) : B(b) {
   for (DevBuf<T>* v : {&xs, &p0, &p1, &q}) {
     v->alloc(n0);
     EQF_CK(cudaMemsetAsync(v->p, 0, n0 * sizeof(T), B.stream));
+  }
+  if (B.use_bicgstab) {
+    rh.alloc(n0);
+    EQF_CK(cudaMemsetAsync(rh.p, 0, n0 * sizeof(T), B.stream));
   }
 }
 
@@ -723,12 +755,14 @@ const double* level_tab<double>(const Level& L) {
   return L.tabd.p;
 }
 
-// V-cycle on level `lev` with rhs lv[lev].b; returns the buffer holding x.
+// V-cycle on level `lev` with rhs lv[lev].b (rhs0 on level 0 when given); returns
+// the buffer holding x.
 // With `dot`, the last smoothing step also writes partials of b.x (= r.z on level 0).
 template <class T>
-T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
+T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   const Level& Lv_ = B.L[lev];
   Lv& v = lv[lev];
+  const T* bl = (lev == 0 && rhs0) ? rhs0 : v.b.p;  // this level's rhs
   const int nt = Lv_.ntiles();
   const int* skip = B.d_cg_skip.p;
   const LevelGeom* G = Lv_.dgeom.p;
@@ -744,22 +778,22 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
     // the whole coarsest solve in one CTA per trap
     EQF_RUN(B, KC_COARSE,
             (k_coarse_solve<T><<<B.ntraps, kThreads, Lv_.sm_coarse, s>>>(G, tab, skip, deg_pre,
-                                                                          v.b.p, cur)));
+                                                                          bl, cur)));
     return cur;
   }
   // pre-smoothing (or the coarsest-level solve) from zero
   cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, 0, true, true,
-               dot && coarsest && deg_pre == 1, v.b.p, cur, cur, v.d.p, part);
+               dot && coarsest && deg_pre == 1, bl, cur, cur, v.d.p, part);
   for (int st = 1; st < deg_pre; ++st) {
     cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, false, false,
-                 dot && coarsest && st == deg_pre - 1, v.b.p, cur, oth, v.d.p, part);
+                 dot && coarsest && st == deg_pre - 1, bl, cur, oth, v.d.p, part);
     std::swap(cur, oth);
   }
   if (coarsest) return cur;
   // residual, restriction, coarse correction, prolongation
   const int c0 = lev > 0 ? KC_COARSE : KC_RESID0;
   EQF_RUN(B, c0,
-          (k_resid<T><<<nt, kThreads, Lv_.sm_resid, s>>>(G, tl, tab, skip, v.b.p, cur, v.t.p,
+          (k_resid<T><<<nt, kThreads, Lv_.sm_resid, s>>>(G, tl, tab, skip, bl, cur, v.t.p,
                                                           W)));
   const Level& Lc = B.L[lev + 1];
   EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
@@ -773,7 +807,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot) {
   const int deg_post = B.opts.cheb_post;
   for (int st = 0; st < deg_post; ++st) {
     cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, st == 0, false,
-                 dot && st == deg_post - 1, v.b.p, cur, oth, v.d.p, part);
+                 dot && st == deg_post - 1, bl, cur, oth, v.d.p, part);
     std::swap(cur, oth);
   }
   return cur;
@@ -825,6 +859,13 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
           (k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
                                      B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p)));
   EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
+  if (B.use_bicgstab) {
+    bicgstab(s, r, tol_rel, tol_abs);
+    EQF_RUN(B, KC_IR_UPDATE,
+            (k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, u_out, d_out,
+                                                    W)));
+    return;
+  }
   T* pin = p0.p;
   T* pout = p1.p;
   for (int it = 0; it < B.opts.max_iters; ++it) {
@@ -853,6 +894,62 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
           (k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, u_out, d_out, W)));
 }
 
+// Right-preconditioned BiCGSTAB on the correction x (xs) from residual r (the
+// V-cycle is the preconditioner); ceil(max_iters / 2) iterations of two
+// preconditioner applications each.
+template <class T>
+void Work<T>::bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs) {
+  const Level& L0 = B.L[0];
+  const int nt = L0.ntiles();
+  const int nb = (B.ntraps + 127) / 128;
+  const LevelGeom* G = L0.dgeom.p;
+  const Tile* tl = L0.dtiles.p;
+  const T* tab = level_tab<T>(L0);
+  double* part = B.dpart.p;
+  int* skip = B.d_cg_skip.p;
+  CgState* st = B.dstate.p;
+  T* p = p0.p;
+  T* v = p1.p;
+  T* t = q.p;
+  const int iters = (B.opts.max_iters + 1) / 2;
+  for (int it = 0; it < iters; ++it) {
+    if (it == 0) {
+      EQF_RUN(B, KC_CG_UPDATE,
+              (k_bs_dir<T, true><<<nt, kThreads, 0, s>>>(G, tl, skip, st, r, v, p, rh.p, part,
+                                                         W)));
+      EQF_RUN(B, KC_SCALAR,
+              (k_s_bs_rho0<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, st, skip)));
+    } else {
+      EQF_RUN(B, KC_CG_UPDATE,
+              (k_bs_dir<T, false><<<nt, kThreads, 0, s>>>(G, tl, skip, st, r, v, p, rh.p, part,
+                                                          W)));
+    }
+    const T* ph = vcycle(s, 0, false, p);
+    EQF_RUN(B, KC_CG_DIR,
+            (k_apply_dot<T, 1><<<nt, kThreads, L0.sm_resid, s>>>(G, tl, tab, skip, ph, rh.p, v,
+                                                                  part, nt, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_bs_alpha<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, st, skip)));
+    EQF_RUN(B, KC_CG_UPDATE,
+            (k_bs_half<T><<<nt, kThreads, 0, s>>>(G, tl, skip, st, ph, v, xs.p, r, part, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_bs_half<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, st,
+                                            skip)));
+    const T* sh = vcycle(s, 0, false, r);
+    EQF_RUN(B, KC_CG_DIR,
+            (k_apply_dot<T, 2><<<nt, kThreads, L0.sm_resid, s>>>(G, tl, tab, skip, sh, r, t,
+                                                                  part, nt, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_bs_omega<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, st, skip)));
+    EQF_RUN(B, KC_CG_UPDATE,
+            (k_bs_full<T><<<nt, kThreads, 0, s>>>(G, tl, skip, st, sh, t, rh.p, xs.p, r, part,
+                                                  nt, W)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_s_bs_rho<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, tol_rel, tol_abs, st,
+                                           skip)));
+  }
+}
+
 // Final FP64 residual check after the last sweep: marks converged traps, counts
 // the others in d_fail and sets the next step's extrapolation factor.
 template <class T>
@@ -877,7 +974,22 @@ void Work<T>::enqueue_check(cudaStream_t s, bool update_gamma) {
                                                              update_gamma ? 1 : 0)));
 }
 
+// Per-step sources of coupled species: gather every cell's concentration from the
+// field at the start of the step, apply the sender/receiver law, re-deposit.
+void Batch::enqueue_coupling() {
+  if (ncp == 0) return;
+  EQF_RUN(*this, KC_SCALAR,
+          (k_cells_gather<<<(ncells + 255) / 256, 256, 0, stream>>>(ncells, d_ent_node.p, d_ent_w.p,
+                                                                  u_cur(), d_cp_c.p)));
+  EQF_RUN(*this, KC_SCALAR,
+          (k_cells_qs_sources<<<(ncp + 255) / 256, 256, 0, stream>>>(
+              ncp, d_cp_i1.p, d_cp_i2.p, d_cp_sender.p, d_cp_prod.p, d_cp_law.p, d_cp_laws.p,
+              d_cp_c.p, d_cell_s.p)));
+  refresh_load();
+}
+
 void Batch::run_step() {
+  enqueue_coupling();
   for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
   work->enqueue_check(stream, true);
 }
@@ -987,6 +1099,8 @@ void Batch::build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& pe
 
 void Batch::rebuild_cells() {
   cells_dirty = false;
+  ncp = 0;
+  drop_graphs();
   cell_first.assign(ntraps + 1, 0);
   for (int t = 0; t < ntraps; ++t) cell_first[t + 1] = cell_first[t] + (int)cell_s[t].size();
   ncells = cell_first[ntraps];
@@ -1031,7 +1145,45 @@ void Batch::rebuild_cells() {
   EQF_LAUNCH_CHECK();
   build_segments(nent, d_ent_node.p, counts.p, d_perm, d_seg_start, nseg, d_cell_xy.p,
                  d_cell_s.p, nullptr);
+  // coupled cells: index maps, sender flags, production rates, laws
+  ncp = 0;
+  std::vector<int> i1, i2, snd, law_of;
+  std::vector<double> prod;
+  std::vector<CouplingLaw> laws;
+  for (size_t c = 0; c < couplings.size(); ++c) {
+    const Coupling& cp = couplings[c];
+    const int n = (int)cell_s[cp.t1].size();
+    if (n != (int)cell_s[cp.t2].size() || n != (int)cp.sender.size())
+      throw Error(EQF_ERR_INVALID, "coupled traps' cells changed after eqf_couple_species");
+    laws.push_back(cp.law);
+    for (int i = 0; i < n; ++i) {
+      i1.push_back(cell_first[cp.t1] + i);
+      i2.push_back(cell_first[cp.t2] + i);
+      snd.push_back(cp.sender[i]);
+      prod.push_back(cell_s[cp.t1][i]);
+      law_of.push_back((int)c);
+    }
+  }
+  ncp = (int)i1.size();
+  if (ncp > 0) {
+    d_cp_i1.alloc(ncp);
+    d_cp_i1.upload(i1.data(), ncp, stream);
+    d_cp_i2.alloc(ncp);
+    d_cp_i2.upload(i2.data(), ncp, stream);
+    d_cp_sender.alloc(ncp);
+    d_cp_sender.upload(snd.data(), ncp, stream);
+    d_cp_law.alloc(ncp);
+    d_cp_law.upload(law_of.data(), ncp, stream);
+    d_cp_prod.alloc(ncp);
+    d_cp_prod.upload(prod.data(), ncp, stream);
+    d_cp_laws.alloc(laws.size());
+    d_cp_laws.upload(laws.data(), laws.size(), stream);
+    d_cp_c.alloc(ncells);
+  }
+  // captured steps hold pointers to the cell arrays just reallocated
+  drop_graphs();
   refresh_load();
+  sync();
 }
 
 // F = dt * sum_i s_i phi(x_i) from the current rates (segments fixed)
@@ -1159,6 +1311,8 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
                     o.cheb_coarse >= 1 && o.cheb_ratio > 1.0 && o.rtol > 0.0,
                 "invalid solver options");
     EQF_REQUIRE(o.tile_nodes >= 0 && o.tile_nodes <= 32768, "tile_nodes outside [0, 32768]");
+    EQF_REQUIRE(o.krylov >= EQF_KRYLOV_AUTO && o.krylov <= EQF_KRYLOV_BICGSTAB,
+                "unknown Krylov method");
     for (int t = 0; t < n_traps; ++t) {
       const auto& p = traps[t];
       EQF_REQUIRE(p.nx >= 1 && p.ny >= 1 && p.width > 0 && p.height > 0 && p.dt > 0 &&
@@ -1211,6 +1365,35 @@ int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const
     b->impl->cell_xy[trap].assign(xy, xy + 2 * n);
     b->impl->cell_s[trap].assign(s, s + n);
     b->impl->cells_dirty = true;
+  });
+}
+
+int eqf_couple_species(eqf_batch* b, int32_t trap1, int32_t trap2, const int32_t* sender,
+                       double vmax, double K, double uptake) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap1);
+    EQF_TRAP_CHECK(b, trap2);
+    Batch& B = *b->impl;
+    EQF_REQUIRE(trap1 != trap2, "a species cannot be coupled to itself");
+    const auto &p1 = B.params[trap1], &p2 = B.params[trap2];
+    EQF_REQUIRE(p1.nx == p2.nx && p1.ny == p2.ny && p1.width == p2.width &&
+                    p1.height == p2.height,
+                "coupled species must share the trap mesh");
+    for (const auto& c : B.couplings)
+      EQF_REQUIRE(c.t1 != trap1 && c.t2 != trap1 && c.t1 != trap2 && c.t2 != trap2,
+                  "trap already coupled");
+    EQF_REQUIRE(std::isfinite(vmax) && std::isfinite(K) && K > 0 && std::isfinite(uptake) &&
+                    uptake >= 0,
+                "bad coupling law");
+    const size_t n = B.cell_s[trap1].size();
+    EQF_REQUIRE(n == 0 || sender, "null sender flags");
+    Batch::Coupling c{trap1, trap2, eqf::CouplingLaw{vmax, K, uptake}, {}};
+    c.sender.assign(sender, sender + n);
+    B.cell_xy[trap2] = B.cell_xy[trap1];
+    B.cell_s[trap2].assign(n, 0.0);
+    B.couplings.push_back(std::move(c));
+    B.cells_dirty = true;
   });
 }
 

@@ -177,20 +177,26 @@ __global__ void k_cells_gather(int ncells, const int* __restrict__ ent_node,
   out[c] = acc;
 }
 
-// Two-species sender/receiver sources from the gathered concentrations:
+// Two-species sender/receiver sources from the concentrations gathered at the
+// cell centres (cells_c, indexed like the batch cell arrays).  Coupled cell q has
+// index i1[q] in species 1's trap and i2[q] in species 2's trap:
 //   s1 = sender * prod1 - uptake * c1
 //   s2 = (1 - sender) * vmax * c1 / (K + c1) - uptake * c2
-__global__ void k_cells_qs_sources(int ncells, const int* __restrict__ sender,
-                                   const double* __restrict__ prod1, const double* __restrict__ c1,
-                                   const double* __restrict__ c2, double vmax, double K,
-                                   double uptake, double* __restrict__ s1,
-                                   double* __restrict__ s2) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  const double a = c1[c], b = c2[c];
-  const int snd = sender[c];
-  s1[c] = (snd ? prod1[c] : 0.0) - uptake * a;
-  s2[c] = (snd ? 0.0 : vmax * a / (K + a)) - uptake * b;
+struct CouplingLaw {
+  double vmax, K, uptake;
+};
+__global__ void k_cells_qs_sources(int n, const int* __restrict__ i1, const int* __restrict__ i2,
+                                   const int* __restrict__ sender,
+                                   const double* __restrict__ prod1,
+                                   const int* __restrict__ law_of, const CouplingLaw* __restrict__ law,
+                                   const double* __restrict__ cells_c, double* __restrict__ rate) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const CouplingLaw L = law[law_of[q]];
+  const double c1 = cells_c[i1[q]], c2 = cells_c[i2[q]];
+  const int snd = sender[q];
+  rate[i1[q]] = (snd ? prod1[q] : 0.0) - L.uptake * c1;
+  rate[i2[q]] = (snd ? 0.0 : L.vmax * c1 / (L.K + c1)) - L.uptake * c2;
 }
 
 // ---------------------------------------------------------------------------

@@ -871,6 +871,7 @@ struct CgState {
   double rz, pq, rr, rr0, alpha, beta, bb, r64;
   double gamma;     // extrapolation factor of the initial guess
   double dn2_prev;  // |increment|^2 of the previous step
+  double omega;     // BiCGSTAB: stabilisation factor (rz = rho, pq = rhat.v)
   int iters, sweeps, it_in_sweep, pad;
 };
 

@@ -24,6 +24,8 @@ from ._lib import EqfError, SolverOpts, TrapParams
 
 WALL_BOTTOM, WALL_TOP, WALL_LEFT, WALL_RIGHT = 1, 2, 4, 8
 FP64, FP32_IR = _lib.EQF_PREC_FP64, _lib.EQF_PREC_FP32_IR
+KRYLOV_AUTO, KRYLOV_CG, KRYLOV_BICGSTAB = (_lib.EQF_KRYLOV_AUTO, _lib.EQF_KRYLOV_CG,
+                                           _lib.EQF_KRYLOV_BICGSTAB)
 
 # trapType -> Dirichlet walls under boundaryType DIRICHLET_0 (src/fHSL.cpp:557-569)
 TRAP_TYPES = {"NOWALLED": 15, "THREEWALLED": WALL_BOTTOM, "TWOWALLED": WALL_BOTTOM | WALL_TOP,
@@ -104,6 +106,18 @@ class TrapBatch:
             raise ValueError("xy and s lengths differ")
         self._ck(self._lib.eqf_set_cells(self._h, trap, len(s), _dp(xy), _dp(s)))
         self._ncells[trap] = len(s)
+
+    def couple_species(self, trap1: int, trap2: int, sender: np.ndarray, vmax: float = 0.5,
+                       K: float = 0.1, uptake: float = 0.05):
+        """Sender/receiver pair: species 1 on trap1 (cells and senders' rates from
+        set_cells(trap1, ...)), species 2 on trap2 (same mesh; gets the same cells)."""
+        snd = np.ascontiguousarray(sender, dtype=np.int32).ravel()
+        if len(snd) != self._ncells[trap1]:
+            raise ValueError("one sender flag per cell of trap1")
+        self._ck(self._lib.eqf_couple_species(self._h, trap1, trap2,
+                                              snd.ctypes.data_as(C.POINTER(C.c_int32)),
+                                              float(vmax), float(K), float(uptake)))
+        self._ncells[trap2] = len(snd)
 
     def set_cell_rates(self, trap: int, s: np.ndarray):
         s = np.ascontiguousarray(s, dtype=np.float64).ravel()

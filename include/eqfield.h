@@ -68,6 +68,11 @@ typedef struct eqf_trap_params {
   uint32_t walls;       /* EQF_WALL_* bits */
 } eqf_trap_params;
 
+/* Krylov method of the inner solve (eqf_solver_opts.krylov). */
+#define EQF_KRYLOV_AUTO 0
+#define EQF_KRYLOV_CG 1
+#define EQF_KRYLOV_BICGSTAB 2
+
 /* Solver options shared by a batch. */
 typedef struct eqf_solver_opts {
   int32_t precision;  /* EQF_PREC_* */
@@ -80,6 +85,7 @@ typedef struct eqf_solver_opts {
   int32_t use_graph;  /* capture steps as CUDA graphs */
   int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
   int32_t tile_nodes; /* target nodes per row tile of the finest level (0: default) */
+  int32_t krylov;     /* EQF_KRYLOV_*: AUTO = BiCGSTAB iff some trap has advection */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;
@@ -108,6 +114,21 @@ int eqf_num_nodes(const eqf_batch* b, int32_t trap, int64_t* n_nodes);
  * onto the containing triangles and applied every step until replaced.
  * Replaces the deposit writeHSL (src/abm/eQabm.cpp:338-359) for point cells. */
 int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const double* s);
+
+/* Couples trap2 to trap1 as the sender/receiver quorum-sensing pair: species 1
+ * lives on trap1, species 2 on trap2 (same mesh).  The cells are those set on
+ * trap1 by eqf_set_cells (their rates s are the senders' production of species 1);
+ * trap2 gets the same positions.  sender[i] (1 = sender, 0 = receiver) for each
+ * of trap1's cells.  Every step, from the concentrations c1, c2 gathered at the
+ * cell centres at the start of the step, the point sources
+ *   s1_i = sender_i * s_i - uptake * c1_i
+ *   s2_i = (1 - sender_i) * vmax * c1_i / (K + c1_i) - uptake * c2_i
+ * are deposited for the two species (explicit in time).  No reference counterpart:
+ * a config extension whose per-cell exchange is evaluated like the membrane term
+ * of the reference's strains (src/Strain.h:312-313).  The cells of both traps must
+ * not be replaced afterwards. */
+int eqf_couple_species(eqf_batch* b, int32_t trap1, int32_t trap2, const int32_t* sender,
+                       double vmax, double K, double uptake);
 
 /* Replaces the source rates of the cells set by eqf_set_cells (same order),
  * keeping their positions and sort order. */
