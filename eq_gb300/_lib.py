@@ -31,6 +31,8 @@ EXPORTS = (
     "eqf_read_nodal", "eqf_read_cells", "eqf_boundary_flux", "eqf_total_mass", "eqf_stats",
     "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
     "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc", "eqf_couple_species",
+    "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
+    "eqf_footprint_estimate", "eqf_fail_count_async",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
@@ -97,6 +99,13 @@ def load() -> C.CDLL:
         "eqf_profile_read": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p, i64p, dp]),
         "eqf_couple_species": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int32),
                                          C.c_double, C.c_double, C.c_double]),
+        "eqf_poll": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "eqf_read_cells_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp]),
+        "eqf_read_nodal_async": (C.c_int, [C.c_void_p, C.c_int32, dp]),
+        "eqf_set_active": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "eqf_fail_count_async": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "eqf_footprint_estimate": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_int64,
+                                             i64p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

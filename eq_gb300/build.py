@@ -12,10 +12,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libeqfield.so")
-SOURCES = [os.path.join(CSRC, "eqf_batch.cu"), os.path.join(CSRC, "eqf_noalloc.cu")]
+SOURCES = [os.path.join(CSRC, f) for f in ("eqf_batch.cu", "eqf_noalloc.cu", "eqf_server.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("eqf_common.cuh", "eqf_kernels.cuh",
-                                                   "eqf_cells.cuh")] + \
-    [os.path.join(ROOT, "include", "eqfield.h")]
+                                                   "eqf_cells.cuh", "eqf_refine.cuh",
+                                                   "eqf_bicgstab.cuh")] + \
+    [os.path.join(ROOT, "include", h) for h in ("eqfield.h", "eqserve.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -310,6 +310,7 @@ class Batch {
   DevBuf<TileRange> drange;
   DevBuf<CgState> dstate;
   DevBuf<int> d_ir_done, d_cg_skip, d_fail;
+  DevBuf<int> d_frozen;  // per trap: nonzero = inactive (skipped by every kernel of a step)
   DevBuf<double> dpart;
   DevBuf<double> U[2];  // fine FP64 field; a step reads U[cur] and writes U[1 - cur]
   DevBuf<float> Dd[2];  // step increments (previous / current), for the initial guess
@@ -424,6 +425,8 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
   dstate.alloc(ntraps);
   EQF_CK(cudaMemsetAsync(dstate.p, 0, ntraps * sizeof(CgState), stream));
   d_ir_done.alloc(ntraps);
+  d_frozen.alloc(ntraps);
+  EQF_CK(cudaMemsetAsync(d_frozen.p, 0, ntraps * sizeof(int), stream));
   d_cg_skip.alloc(ntraps);
   d_fail.alloc(1);
   EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
@@ -445,20 +448,64 @@ Batch::~Batch() {
   if (stream) cudaStreamDestroy(stream);
 }
 
-void Batch::build_levels() {
-  // level count: coarsen until the Fourier number beta/h^2 drops below ~1
-  int nl = 1;
-  for (const auto& p : params) {
-    const double hmin = std::min(p.width / p.nx, p.height / p.ny);
-    const double beta = p.dt * p.D;
-    int k = 0;
-    double h = hmin;
-    while (beta / (h * h) > 1.0 && k < kMaxLevels - 1) {
-      h *= 2;
-      ++k;
-    }
-    nl = std::max(nl, k + 1);
+// Multigrid levels a trap needs: coarsen until the Fourier number beta/h^2 drops
+// below ~1 (a batch uses the maximum over its traps).
+static int trap_levels(const eqf_trap_params& p) {
+  const double hmin = std::min(p.width / p.nx, p.height / p.ny);
+  const double beta = p.dt * p.D;
+  int k = 0;
+  double h = hmin;
+  while (beta / (h * h) > 1.0 && k < kMaxLevels - 1) {
+    h *= 2;
+    ++k;
   }
+  return k + 1;
+}
+
+}  // namespace eqf
+
+// Multigrid depth of a trap (host helper shared with the serving loop).
+int eqf_internal_trap_levels(const eqf_trap_params& p) { return eqf::trap_levels(p); }
+
+namespace eqf {
+
+// Device bytes of a batch (steady state plus the transient of the cell rebuild),
+// from the same level shapes and buffers as the construction below.
+static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solver_opts& o,
+                             long long ncells) {
+  int nlev = 1;
+  bool adv = false;
+  for (int t = 0; t < n; ++t) {
+    nlev = std::max(nlev, trap_levels(traps[t]));
+    adv = adv || (traps[t].adv_u != 0.0 && traps[t].adv_len > 0.0);
+  }
+  const double T = o.precision == EQF_PREC_FP32_IR ? 4.0 : 8.0;
+  double n0 = 0, nall = 0;
+  for (int t = 0; t < n; ++t) {
+    long long nx = traps[t].nx, ny = traps[t].ny;
+    for (int l = 0; l < nlev; ++l) {
+      if (l > 0) {
+        if (nx >= 4) nx = (nx + 1) / 2;
+        if (ny >= 4) ny = (ny + 1) / 2;
+      }
+      const double nn = (double)(((nx + 1) * (ny + 1) + 31) / 32 * 32);
+      if (l == 0) n0 += nn;
+      nall += nn;
+    }
+  }
+  const bool bicg = o.krylov == EQF_KRYLOV_BICGSTAB || (o.krylov == EQF_KRYLOV_AUTO && adv);
+  double bytes = 40.0 * n0                    // U[2], Dd[2], rhs, load
+                 + T * (4 + (bicg ? 1 : 0)) * n0  // Krylov vectors
+                 + 5.0 * T * nall               // multigrid level vectors
+                 + 12.0 * n0                    // cell rebuild transient (counts, scans)
+                 + 140.0 * (double)ncells       // cell arrays, entries, segments, readout
+                 + 64.0 * 1024;
+  return (size_t)bytes;
+}
+
+void Batch::build_levels() {
+  int nl = 1;
+  for (const auto& p : params) nl = std::max(nl, trap_levels(p));
   nlev = nl;
   L.resize(nlev);
   for (int l = 0; l < nlev; ++l) L[l].geom.resize(ntraps);
@@ -839,7 +886,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
       EQF_RUN(B, KC_IR_RESID_FIRST,
               (k_irf_first<<<nt, kThreads, L0.sm_irf1, s>>>(
                   G, tl, B.tabA2.p, B.tabM2.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
-                  b2, u_out, d_out, r, part, nt, W)));
+                  b2, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
     else
       EQF_RUN(B, KC_IR_RESID,
               (k_irf_residual<false><<<nt, kThreads, L0.sm_irf, s>>>(
@@ -849,7 +896,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
       EQF_RUN(B, KC_IR_RESID_FIRST,
               (k_ir_first<T><<<nt, kThreads, L0.sm_ir, s>>>(
                   G, tl, L0.tabd.p, B.tabM0.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
-                  B.b64.p, u_out, d_out, r, part, nt, W)));
+                  B.b64.p, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
     else
       EQF_RUN(B, KC_IR_RESID,
               (k_ir_residual<T, false><<<nt, kThreads, L0.sm_ir, s>>>(
@@ -857,7 +904,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   }
   EQF_RUN(B, KC_SCALAR,
           (k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
-                                     B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p)));
+                                     B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p, B.d_frozen.p)));
   EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs);
@@ -1365,6 +1412,101 @@ int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const
     b->impl->cell_xy[trap].assign(xy, xy + 2 * n);
     b->impl->cell_s[trap].assign(s, s + n);
     b->impl->cells_dirty = true;
+  });
+}
+
+int eqf_footprint_estimate(int32_t n_traps, const eqf_trap_params* traps,
+                           const eqf_solver_opts* opts, int64_t n_cells, int64_t* bytes) {
+  if (n_traps < 1 || !traps || !bytes || n_cells < 0) return EQF_ERR_INVALID;
+  eqf_solver_opts o;
+  if (opts)
+    o = *opts;
+  else
+    eqf_default_opts(EQF_PREC_FP64, &o);
+  for (int t = 0; t < n_traps; ++t)
+    if (traps[t].nx < 1 || traps[t].ny < 1 || !(traps[t].width > 0) || !(traps[t].height > 0))
+      return EQF_ERR_INVALID;
+  *bytes = (int64_t)eqf::estimate_bytes(n_traps, traps, o, n_cells);
+  return EQF_OK;
+}
+
+int eqf_set_active(eqf_batch* b, int32_t trap, int32_t active) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    const long long off = B.L[0].geom[trap].off;
+    const size_t n = (size_t)B.fine_nodes(trap);
+    if (!active) {
+      // both field buffers hold the frozen field, so reads see it whatever the parity
+      EQF_CK(cudaMemcpyAsync(B.U[1 - B.cur].p + off, B.U[B.cur].p + off, n * sizeof(double),
+                             cudaMemcpyDeviceToDevice, B.stream));
+    } else {
+      // a resumed trap starts a fresh increment history for its initial guess
+      for (int q = 0; q < 2; ++q)
+        EQF_CK(cudaMemsetAsync(B.Dd[q].p + off, 0, n * sizeof(float), B.stream));
+      EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
+                                 offsetof(eqf::CgState, gamma),
+                             0, 2 * sizeof(double), B.stream));
+    }
+    // stream-ordered, no host memory involved: the call does not wait
+    EQF_CK(cudaMemsetAsync(B.d_frozen.p + trap, active ? 0 : 1, sizeof(int), B.stream));
+  });
+}
+
+int eqf_poll(eqf_batch* b, int32_t* idle) {
+  if (!b || !idle) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    const cudaError_t q = cudaStreamQuery(B.stream);
+    if (q == cudaErrorNotReady) {
+      *idle = 0;
+      return;
+    }
+    EQF_CK(q);
+    *idle = 1;
+    B.check_fail();
+  });
+}
+
+int eqf_read_cells_async(eqf_batch* b, int32_t trap, int64_t n, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    if (B.cells_dirty) B.rebuild_cells();
+    EQF_REQUIRE(n == (int64_t)B.cell_s[trap].size() && (n == 0 || c), "cell count mismatch");
+    if (n == 0) return;
+    if (B.d_cells_out.n < (size_t)B.ncells) {
+      B.sync();
+      B.d_cells_out.alloc(B.ncells);
+    }
+    const int c0 = B.cell_first[trap];
+    eqf::k_cells_gather<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
+        (int)n, B.d_ent_node.p + 3 * (size_t)c0, B.d_ent_w.p + 3 * (size_t)c0, B.u_cur(),
+        B.d_cells_out.p + c0);
+    EQF_LAUNCH_CHECK();
+    EQF_CK(cudaMemcpyAsync(c, B.d_cells_out.p + c0, n * sizeof(double), cudaMemcpyDeviceToHost,
+                           B.stream));
+  });
+}
+
+int eqf_fail_count_async(eqf_batch* b, int32_t* count) {
+  if (!b || !count) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    EQF_CK(cudaMemcpyAsync(count, B.d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, B.stream));
+  });
+}
+
+int eqf_read_nodal_async(eqf_batch* b, int32_t trap, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(c != nullptr, "null output");
+    Batch& B = *b->impl;
+    EQF_CK(cudaMemcpyAsync(c, B.u_cur() + B.L[0].geom[trap].off,
+                           B.fine_nodes(trap) * sizeof(double), cudaMemcpyDeviceToHost, B.stream));
   });
 }
 

@@ -1019,9 +1019,13 @@ __global__ void __launch_bounds__(kThreads)
                const double* __restrict__ u_in, const float* __restrict__ d_in,
                double* __restrict__ b64, double* __restrict__ u_out, float* __restrict__ d_out,
                T* __restrict__ r, double* __restrict__ part, int ntiles,
-               unsigned long long* work) {
+               const int* __restrict__ frozen, unsigned long long* work) {
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
+  if (frozen[g.trap]) {
+    if (threadIdx.x == 0) part[blockIdx.x] = part[ntiles + blockIdx.x] = 0.0;
+    return;
+  }
   count_work(work, tile);
   const double gamma = st[g.trap].gamma;
   Stager sg(eqf_smem);
@@ -1183,9 +1187,14 @@ __device__ __forceinline__ double trap_sum(const double* part, TileRange tr) {
 __global__ void k_s_ir(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, int ntiles, int first_sweep, double rtol,
                        CgState* __restrict__ st, int* __restrict__ ir_done,
-                       int* __restrict__ cg_skip) {
+                       int* __restrict__ cg_skip, const int* __restrict__ frozen) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps) return;
+  if (frozen[t]) {  // inactive trap: nothing to solve
+    ir_done[t] = 1;
+    cg_skip[t] = 1;
+    return;
+  }
   if (first_sweep) ir_done[t] = 0;
   if (ir_done[t]) {
     cg_skip[t] = 1;

@@ -5,9 +5,9 @@
 // evaluated on the FP32 pipe instead: every value is an unevaluated sum h + l of
 // two floats ("pair", about 47 significant bits), products are split exactly with
 // fused multiply-adds and the sums carry their rounding errors (two-sum).  The
-// conversions between doubles and pairs are done with integer bit operations, so
-// the kernels issue almost no FP64 instructions (one add per stored double and one
-// multiply-add per squared-norm term).
+// conversions between doubles and pairs are done with integer bit operations and
+// the squared norms are accumulated in FP32, so the kernels issue almost no FP64
+// instructions (one add per stored double, one per thread for the norms).
 //
 // Accuracy: a pair carries a relative error below 2^-47 (7e-15).  The residual of a
 // stencil with cancellation factor C = sum|a_ij u_j| / |(A u)_i| is accurate to
@@ -28,6 +28,12 @@ struct DF {
 
 // Exact float -> double by repacking the bits (denormals flush to signed zero).
 __device__ __forceinline__ double f2d(float f) { return to_double(f); }
+
+// Low part of a value below 2^-80, where the integer scale below would leave the
+// float range (rare: out of line so the common path carries no FP64 instructions).
+__device__ __noinline__ float df_low_tiny(double v, float h) {
+  return __double2float_rn(v - f2d(h));
+}
 
 // double -> pair: h = v truncated to 24 significant bits, l = the next 23 bits
 // (|h + l - v| < 2^-46 |v|).  |v| < 2^-126 gives (0, 0); |v| >= 2^128 (+-inf, 0).
@@ -53,7 +59,8 @@ __device__ __forceinline__ DF df_split(double v) {
   } else {
     o.h = __uint_as_float(hb);
     // below 2^-80 the integer scale would leave the float range: FP64 fallback
-    o.l = e >= 943 ? l : __double2float_rn(v - f2d(o.h));
+    o.l = l;
+    if (e < 943) o.l = df_low_tiny(v, o.h);
   }
   return o;
 }
@@ -94,6 +101,24 @@ struct DFAcc {
     e = __fadd_rn(e, __fadd_rn(err, pe));
   }
   __device__ __forceinline__ DF result() const { return df_norm(s, e); }
+};
+
+// Sum of squares in FP32 without underflow: values below 2^-40 are squared after
+// scaling by 2^64 into a second accumulator (2^-128 times its sum is added back in
+// FP64 once per thread).
+struct SqAcc {
+  float big = 0.f, tiny = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const bool small = fabsf(v) < 9.094947e-13f;  // 2^-40
+    const float w = small ? v * 1.8446744e19f : v;  // 2^64
+    if (small)
+      tiny = __fmaf_rn(w, w, tiny);
+    else
+      big = __fmaf_rn(w, w, big);
+  }
+  __device__ __forceinline__ double total() const {
+    return f2d(big) + f2d(tiny) * 2.9387358770557188e-39;  // 2^-128
+  }
 };
 
 // Per-trap pair tables: 25 classes x 8 pairs (c, e, w, n, s, ne, sw, unused), the
@@ -154,9 +179,13 @@ __global__ void __launch_bounds__(kThreads)
                 const double* __restrict__ u_in, const float* __restrict__ d_in,
                 float2* __restrict__ b2, double* __restrict__ u_out, float* __restrict__ d_out,
                 float* __restrict__ r, double* __restrict__ part, int ntiles,
-                unsigned long long* work) {
+                const int* __restrict__ frozen, unsigned long long* work) {
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
+  if (frozen[g.trap]) {  // inactive trap: its field is left as it is
+    if (threadIdx.x == 0) part[blockIdx.x] = part[ntiles + blockIdx.x] = 0.0;
+    return;
+  }
   count_work(work, tile);
   Stager sg(eqf_smem);
   const int na = padded_len(g);
@@ -172,15 +201,14 @@ __global__ void __launch_bounds__(kThreads)
   const int xa = uv.a;
   const double* Fs = F + g.off;
   float2* bs = b2 + g.off;
-  double abb = 0.0, arr = 0.0;
+  SqAcc abb, arr;
   // b = F + M u_in
   for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
     const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
     DF bk{0.f, 0.f};
     if (!dir) bk = df_add(df_split(Fs[w.k]), df_apply(g, sM, false, xw, xa, w.k, w.i, w.j));
     bs[w.k] = make_float2(bk.h, bk.l);
-    const double bh = f2d(bk.h);
-    abb = __fma_rn(bh, bh, abb);
+    abb.add(bk.h);
   }
   __syncthreads();  // every read of u_in done: the window becomes u0 in place
   {
@@ -213,11 +241,10 @@ __global__ void __launch_bounds__(kThreads)
       rk = __fadd_rn(res.h, res.l);
     }
     rs[w.k] = rk;
-    const double rd = f2d(rk);
-    arr = __fma_rn(rd, rd, arr);
+    arr.add(rk);
   }
-  const double tb = block_sum(abb);
-  const double tr = block_sum(arr);
+  const double tb = block_sum(abb.total());
+  const double tr = block_sum(arr.total());
   if (threadIdx.x == 0) {
     part[blockIdx.x] = tb;
     part[ntiles + blockIdx.x] = tr;
@@ -241,13 +268,10 @@ __global__ void __launch_bounds__(kThreads)
     if (threadIdx.x == 0) part[ntiles + blockIdx.x] = 0.0;
     return;
   }
-  double arr = 0.0, add = 0.0;
+  SqAcc arr, add;
   if (FINAL) {
     const float* ds = dcur + g.off;
-    for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) {
-      const double v = f2d(ds[k]);
-      add = __fma_rn(v, v, add);
-    }
+    for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) add.add(ds[k]);
   }
   if (!skipped) {
     count_work(work, tile);
@@ -273,12 +297,11 @@ __global__ void __launch_bounds__(kThreads)
         rk = __fadd_rn(res.h, res.l);
       }
       if (!FINAL) rs[w.k] = rk;
-      const double rd = f2d(rk);
-      arr = __fma_rn(rd, rd, arr);
+      arr.add(rk);
     }
   }
-  const double tr = block_sum(arr);
-  const double td = FINAL ? block_sum(add) : 0.0;
+  const double tr = block_sum(arr.total());
+  const double td = FINAL ? block_sum(add.total()) : 0.0;
   if (threadIdx.x == 0) {
     part[ntiles + blockIdx.x] = tr;
     if (FINAL) part[2 * ntiles + blockIdx.x] = td;

@@ -1,0 +1,535 @@
+// eqserve: continuous-batching request loop over eqfield batches (include/eqserve.h).
+//
+// Host code only.  A cohort is one eqfield batch (its own CUDA stream) holding the
+// traps of the requests admitted together; cohorts step concurrently.  Per cohort
+// step: CUDA event, one graph-replayed step, asynchronous readout + freeze of the
+// requests that finish at that step, a copy of the convergence-failure counter,
+// CUDA event.  eqs_progress only queries events, so it never waits for the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/eqfield.h"
+#include "../../include/eqserve.h"
+
+// Multigrid depth of a trap (eqf_batch.cu).
+int eqf_internal_trap_levels(const eqf_trap_params& p);
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+  int64_t id = -1;
+  eqs_request r{};
+  std::vector<double> xy, s;
+  std::vector<int32_t> sender;
+  int64_t n_nodes = 0;
+  double t_submit = 0, t_admit = -1, t_done = -1;
+  int status = EQF_OK;
+  int cohort = -1;
+  int trap0 = -1;
+  double* h_cells = nullptr;  // pinned: n_species * n_cells
+  double* h_nodal = nullptr;  // pinned: n_species * n_nodes (when asked for)
+  bool done = false;
+  bool taken = false;  // result handed out (the object lives until its cohort is released)
+  int64_t klass = 0;   // cohort class: multigrid depth and symmetric / advective operator
+  int ntraps() const { return r.n_species; }
+};
+
+struct StepMark {
+  int step = 0;
+  cudaEvent_t start = nullptr, end = nullptr;
+  int32_t* fail = nullptr;  // pinned: the batch's failure counter after this step
+};
+
+struct Cohort {
+  int id = 0;
+  eqf_batch* b = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<Req*> reqs;
+  int steps_target = 0, launched = 0;
+  std::deque<StepMark> inflight;
+  int64_t bytes = 0;
+  int remaining = 0;
+  int32_t fails_seen = 0;
+};
+
+}  // namespace
+
+struct eqs_server {
+  eqs_config cfg{};
+  std::string err;
+  Clock::time_point t0 = Clock::now();
+  double last_progress = 0;
+  int64_t next_id = 0;
+  int next_cohort = 0;
+  std::deque<Req*> pending;
+  std::map<int64_t, std::unique_ptr<Req>> reqs;
+  std::vector<std::unique_ptr<Cohort>> cohorts;
+  std::vector<int64_t> done_ids;
+  std::vector<float> step_ms;
+  eqs_stats st{};
+
+  double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+struct Fail {
+  int code;
+  std::string msg;
+};
+
+void ck(int rc, const char* what) {
+  if (rc != EQF_OK) throw Fail{rc, std::string(what) + " failed (" + std::to_string(rc) + ")"};
+}
+void ckb(int rc, eqf_batch* b) {
+  if (rc != EQF_OK) throw Fail{rc, eqf_last_error(b)};
+}
+void ckc(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw Fail{EQF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+template <class F>
+int guarded(eqs_server* s, F&& f) {
+  try {
+    f();
+    return EQF_OK;
+  } catch (const Fail& e) {
+    if (s) s->err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (s) s->err = "host allocation failed";
+    return EQF_ERR_NOMEM;
+  }
+}
+
+void trap_list(const std::vector<Req*>& rs, std::vector<eqf_trap_params>& tp, int64_t& cells) {
+  tp.clear();
+  cells = 0;
+  for (const Req* q : rs) {
+    for (int k = 0; k < q->r.n_species; ++k) tp.push_back(q->r.species[k]);
+    cells += q->r.n_cells * q->r.n_species;
+  }
+}
+
+int64_t estimate(const eqs_server* s, const std::vector<Req*>& rs) {
+  std::vector<eqf_trap_params> tp;
+  int64_t cells = 0, bytes = 0;
+  trap_list(rs, tp, cells);
+  ck(eqf_footprint_estimate((int32_t)tp.size(), tp.data(), &s->cfg.opts, cells, &bytes),
+     "eqf_footprint_estimate");
+  return bytes;
+}
+
+void release_cohort(eqs_server* s, Cohort& c) {
+  for (StepMark& m : c.inflight) {
+    cudaEventDestroy(m.start);
+    cudaEventDestroy(m.end);
+    cudaFreeHost(m.fail);
+  }
+  c.inflight.clear();
+  if (c.b) eqf_destroy(c.b);
+  c.b = nullptr;
+  s->st.bytes_in_use -= c.bytes;
+}
+
+// Marks a request finished (results are in its pinned buffers).
+void finish(eqs_server* s, Req* q, int status) {
+  if (q->done) return;
+  q->done = true;
+  q->status = status;
+  q->t_done = s->now();
+  s->done_ids.push_back(q->id);
+  if (status == EQF_OK) {
+    s->st.completed += 1;
+    s->st.dof_steps += (double)q->n_nodes * q->r.n_species * q->r.steps;
+  } else {
+    s->st.failed += 1;
+  }
+}
+
+void fail_cohort(eqs_server* s, Cohort& c, int code) {
+  for (Req* q : c.reqs)
+    if (!q->done) finish(s, q, code);
+  c.remaining = 0;
+}
+
+// Queues one step of a cohort with its readouts and bookkeeping.
+void launch_step(eqs_server* s, Cohort& c) {
+  StepMark m;
+  m.step = c.launched + 1;
+  ckc(cudaEventCreate(&m.start), "cudaEventCreate");
+  ckc(cudaEventCreate(&m.end), "cudaEventCreate");
+  ckc(cudaMallocHost(&m.fail, sizeof(int32_t)), "cudaMallocHost");
+  *m.fail = 0;
+  ckc(cudaEventRecord(m.start, c.stream), "cudaEventRecord");
+  ckb(eqf_step(c.b, 1), c.b);
+  for (Req* q : c.reqs) {
+    if (q->r.steps != m.step) continue;
+    for (int k = 0; k < q->r.n_species; ++k) {
+      if (q->r.n_cells > 0)
+        ckb(eqf_read_cells_async(c.b, q->trap0 + k, q->r.n_cells, q->h_cells + k * q->r.n_cells),
+            c.b);
+      if (q->h_nodal) ckb(eqf_read_nodal_async(c.b, q->trap0 + k, q->h_nodal + k * q->n_nodes), c.b);
+      ckb(eqf_set_active(c.b, q->trap0 + k, 0), c.b);
+    }
+  }
+  ckb(eqf_fail_count_async(c.b, m.fail), c.b);
+  ckc(cudaEventRecord(m.end, c.stream), "cudaEventRecord");
+  c.inflight.push_back(m);
+  c.launched = m.step;
+}
+
+void retire(eqs_server* s, Cohort& c) {
+  while (!c.inflight.empty()) {
+    StepMark& m = c.inflight.front();
+    const cudaError_t e = cudaEventQuery(m.end);
+    if (e == cudaErrorNotReady) break;
+    if (e != cudaSuccess) {
+      s->err = cudaGetErrorString(e);
+      fail_cohort(s, c, EQF_ERR_CUDA);
+      return;
+    }
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, m.start, m.end) == cudaSuccess) s->step_ms.push_back(ms);
+    const int32_t fails = *m.fail;
+    const int status = fails > c.fails_seen ? EQF_ERR_NOT_CONVERGED : EQF_OK;
+    if (status != EQF_OK) {
+      // the counter is per batch: every request still running at this step is suspect
+      for (Req* q : c.reqs)
+        if (!q->done && q->r.steps >= m.step) q->status = status;
+      c.fails_seen = fails;
+    }
+    for (Req* q : c.reqs)
+      if (q->r.steps == m.step && !q->done) {
+        finish(s, q, q->status);
+        c.remaining -= 1;
+      }
+    cudaEventDestroy(m.start);
+    cudaEventDestroy(m.end);
+    cudaFreeHost(m.fail);
+    c.inflight.pop_front();
+  }
+}
+
+// Forms one cohort from the head of the queue within the budget: the oldest request
+// and the following ones of its class, in arrival order.  Cohorts are class-pure
+// (same multigrid depth and Krylov method), so a request's result is the same bits
+// whichever requests share its cohort.
+bool admit(eqs_server* s) {
+  std::vector<Req*> take;
+  int traps = 0;
+  const int64_t free_bytes = s->cfg.hbm_budget - s->st.bytes_in_use;
+  int64_t bytes = 0;
+  const int64_t klass = s->pending.front()->klass;
+  for (auto it = s->pending.begin(); it != s->pending.end();) {
+    Req* q = *it;
+    if (q->klass != klass) {
+      ++it;
+      continue;
+    }
+    if (traps + q->ntraps() > s->cfg.max_cohort_traps) break;
+    take.push_back(q);
+    const int64_t b = estimate(s, take);
+    if (b > free_bytes) {
+      take.pop_back();
+      break;
+    }
+    bytes = b;
+    traps += q->ntraps();
+    it = s->pending.erase(it);
+  }
+  if (take.empty()) return false;
+  std::unique_ptr<Cohort> c(new Cohort);
+  c->id = s->next_cohort++;
+  c->reqs = take;
+  c->bytes = bytes;
+  c->remaining = (int)take.size();
+  std::vector<eqf_trap_params> tp;
+  int64_t cells = 0;
+  trap_list(take, tp, cells);
+  eqf_solver_opts o = s->cfg.opts;
+  o.adaptive = 0;
+  o.use_graph = 1;
+  const int rc = eqf_create((int32_t)tp.size(), tp.data(), &o, &c->b);
+  if (rc != EQF_OK) {
+    // put the requests back in arrival order and retry once memory frees up; with
+    // nothing running no memory will free up: the oldest request fails
+    for (Req* q : take) s->pending.push_back(q);
+    std::sort(s->pending.begin(), s->pending.end(),
+              [](const Req* a, const Req* b) { return a->id < b->id; });
+    if ((rc == EQF_ERR_NOMEM || rc == EQF_ERR_CUDA) && !s->cohorts.empty()) return false;
+    Req* q = s->pending.front();
+    s->pending.pop_front();
+    s->err = eqf_last_error(nullptr);
+    finish(s, q, rc);
+    return true;
+  }
+  s->st.bytes_in_use += bytes;
+  s->st.bytes_peak = std::max(s->st.bytes_peak, s->st.bytes_in_use);
+  void* stream = nullptr;
+  ckb(eqf_stream(c->b, &stream), c->b);
+  c->stream = (cudaStream_t)stream;
+  int t = 0;
+  const double now = s->now();
+  for (Req* q : take) {
+    q->trap0 = t;
+    q->cohort = c->id;
+    q->t_admit = now;
+    if (q->r.n_cells > 0) {
+      ckb(eqf_set_cells(c->b, t, q->r.n_cells, q->xy.data(), q->s.data()), c->b);
+      if (q->r.n_species == 2)
+        ckb(eqf_couple_species(c->b, t, t + 1, q->sender.data(), q->r.vmax, q->r.K,
+                               q->r.uptake),
+            c->b);
+    }
+    ckc(cudaMallocHost(&q->h_cells, sizeof(double) * std::max<int64_t>(
+                                        1, q->r.n_cells * q->r.n_species)),
+        "cudaMallocHost");
+    if (q->r.want_nodal)
+      ckc(cudaMallocHost(&q->h_nodal, sizeof(double) * q->n_nodes * q->r.n_species),
+          "cudaMallocHost");
+    c->steps_target = std::max(c->steps_target, q->r.steps);
+    t += q->ntraps();
+  }
+  s->st.admitted += (int64_t)take.size();
+  s->st.cohorts += 1;
+  s->cohorts.push_back(std::move(c));
+  return true;
+}
+
+void progress(eqs_server* s) {
+  const double now = s->now();
+  bool running = false;
+  for (auto& c : s->cohorts) running = running || c->b;
+  if (running) s->st.busy_s += now - s->last_progress;
+  s->last_progress = now;
+  // retire finished steps, release finished cohorts
+  for (auto& c : s->cohorts) retire(s, *c);
+  for (auto& c : s->cohorts)
+    if (c->b && c->remaining == 0 && c->inflight.empty()) {
+      const int rc = eqf_sync(c->b);
+      if (rc == EQF_ERR_NOT_CONVERGED)
+        for (Req* q : c->reqs) q->status = rc;
+      release_cohort(s, *c);
+      for (Req* q : c->reqs)
+        if (q->taken) s->reqs.erase(q->id);
+    }
+  s->cohorts.erase(std::remove_if(s->cohorts.begin(), s->cohorts.end(),
+                                  [](const std::unique_ptr<Cohort>& c) { return !c->b; }),
+                   s->cohorts.end());
+  // admit: an idle GPU, enough waiting requests, or a request waiting too long
+  while (!s->pending.empty() && (int)s->cohorts.size() < s->cfg.max_cohorts) {
+    const bool idle = s->cohorts.empty();
+    const bool enough = (int)s->pending.size() >= s->cfg.min_batch;
+    const bool late = (now - s->pending.front()->t_submit) * 1e3 >= s->cfg.max_wait_ms;
+    if (!(idle || enough || late)) break;
+    if (!admit(s)) break;
+  }
+  // keep every cohort's queue filled
+  for (auto& c : s->cohorts) {
+    try {
+      while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight)
+        launch_step(s, *c);
+    } catch (const Fail& f) {
+      s->err = f.msg;
+      fail_cohort(s, *c, f.code);
+    }
+  }
+  int64_t run = 0;
+  for (auto& c : s->cohorts) run += (int64_t)c->reqs.size();
+  s->st.pending = (int64_t)s->pending.size();
+  s->st.running = run;
+}
+
+double percentile(std::vector<float> v, double p) {
+  if (v.empty()) return 0.0;
+  std::sort(v.begin(), v.end());
+  const double pos = p * (double)(v.size() - 1);
+  const size_t i = (size_t)pos;
+  const double f = pos - (double)i;
+  return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+int eqs_default_config(eqs_config* c) {
+  if (!c) return EQF_ERR_INVALID;
+  std::memset(c, 0, sizeof(*c));
+  eqf_default_opts(EQF_PREC_FP32_IR, &c->opts);
+  c->opts.max_sweeps = 3;  // no host round trip per step: one spare sweep instead
+  c->hbm_budget = (int64_t)150 << 30;
+  c->max_cohorts = 8;
+  c->max_cohort_traps = 256;
+  c->min_batch = 16;
+  c->max_wait_ms = 20.0;
+  c->steps_in_flight = 2;
+  return EQF_OK;
+}
+
+int eqs_create(const eqs_config* cfg, eqs_server** out) {
+  if (!cfg || !out) return EQF_ERR_INVALID;
+  if (cfg->hbm_budget <= 0 || cfg->max_cohorts < 1 || cfg->max_cohort_traps < 2 ||
+      cfg->min_batch < 1 || cfg->steps_in_flight < 1 || !(cfg->max_wait_ms >= 0))
+    return EQF_ERR_INVALID;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return EQF_ERR_NO_DEVICE;
+  eqs_server* s = new (std::nothrow) eqs_server;
+  if (!s) return EQF_ERR_NOMEM;
+  s->cfg = *cfg;
+  *out = s;
+  return EQF_OK;
+}
+
+int eqs_destroy(eqs_server* s) {
+  if (!s) return EQF_ERR_INVALID;
+  for (auto& c : s->cohorts)
+    if (c->b) {
+      eqf_sync(c->b);
+      release_cohort(s, *c);
+    }
+  for (auto& kv : s->reqs) {
+    if (kv.second->h_cells) cudaFreeHost(kv.second->h_cells);
+    if (kv.second->h_nodal) cudaFreeHost(kv.second->h_nodal);
+  }
+  delete s;
+  return EQF_OK;
+}
+
+const char* eqs_last_error(const eqs_server* s) { return s ? s->err.c_str() : ""; }
+
+int eqs_submit(eqs_server* s, const eqs_request* r, int64_t* id) {
+  if (!s || !r || !id) return EQF_ERR_INVALID;
+  return guarded(s, [&] {
+    if (!(r->n_species == 1 || r->n_species == 2) || r->steps < 1 || r->n_cells < 0 ||
+        (r->n_cells > 0 && (!r->xy || !r->s)) ||
+        (r->n_species == 2 && r->n_cells > 0 && !r->sender))
+      throw Fail{EQF_ERR_INVALID, "bad request"};
+    const eqf_trap_params& p = r->species[0];
+    if (p.nx < 1 || p.ny < 1 || !(p.width > 0) || !(p.height > 0))
+      throw Fail{EQF_ERR_INVALID, "bad trap"};
+    if (r->n_species == 2) {
+      const eqf_trap_params& p2 = r->species[1];
+      if (p2.nx != p.nx || p2.ny != p.ny || p2.width != p.width || p2.height != p.height)
+        throw Fail{EQF_ERR_INVALID, "the two species must share the mesh"};
+    }
+    std::unique_ptr<Req> q(new Req);
+    q->r = *r;
+    q->xy.assign(r->xy, r->xy + 2 * r->n_cells);
+    q->s.assign(r->s, r->s + r->n_cells);
+    if (r->n_species == 2) q->sender.assign(r->sender, r->sender + r->n_cells);
+    q->r.xy = q->xy.data();
+    q->r.s = q->s.data();
+    q->r.sender = q->sender.data();
+    q->n_nodes = (int64_t)(p.nx + 1) * (p.ny + 1);
+    int levels = 0;
+    bool adv = false;
+    for (int k = 0; k < r->n_species; ++k) {
+      levels = std::max(levels, eqf_internal_trap_levels(r->species[k]));
+      adv = adv || (r->species[k].adv_u != 0.0 && r->species[k].adv_len > 0.0);
+    }
+    q->klass = 2 * (int64_t)levels + (adv ? 1 : 0);
+    if (estimate(s, {q.get()}) > s->cfg.hbm_budget)
+      throw Fail{EQF_ERR_TOO_LARGE, "request larger than the server's memory budget"};
+    q->id = s->next_id++;
+    q->t_submit = s->now();
+    *id = q->id;
+    s->pending.push_back(q.get());
+    s->reqs[q->id] = std::move(q);
+    s->st.submitted += 1;
+  });
+}
+
+int eqs_progress(eqs_server* s) {
+  if (!s) return EQF_ERR_INVALID;
+  return guarded(s, [&] { progress(s); });
+}
+
+int eqs_take_done(eqs_server* s, int64_t* ids, int32_t cap, int32_t* n) {
+  if (!s || !n || cap < 0 || (cap > 0 && !ids)) return EQF_ERR_INVALID;
+  const int32_t k = (int32_t)std::min<size_t>((size_t)cap, s->done_ids.size());
+  std::copy(s->done_ids.begin(), s->done_ids.begin() + k, ids);
+  s->done_ids.erase(s->done_ids.begin(), s->done_ids.begin() + k);
+  *n = k;
+  return EQF_OK;
+}
+
+int eqs_result(eqs_server* s, int64_t id, double* cells, double* nodal, eqs_result_info* info) {
+  if (!s) return EQF_ERR_INVALID;
+  return guarded(s, [&] {
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) throw Fail{EQF_ERR_INVALID, "unknown request id"};
+    Req* q = it->second.get();
+    if (!q->done) throw Fail{EQF_ERR_INVALID, "request not finished"};
+    if (cells && q->h_cells && q->r.n_cells > 0)
+      std::memcpy(cells, q->h_cells, sizeof(double) * q->r.n_cells * q->r.n_species);
+    if (nodal && q->h_nodal)
+      std::memcpy(nodal, q->h_nodal, sizeof(double) * q->n_nodes * q->r.n_species);
+    if (info) {
+      info->t_submit = q->t_submit;
+      info->t_admit = q->t_admit;
+      info->t_done = q->t_done;
+      info->steps = q->r.steps;
+      info->status = q->status;
+      info->n_nodes = q->n_nodes;
+      info->n_cells = q->r.n_cells;
+      info->n_species = q->r.n_species;
+      info->cohort = q->cohort;
+    }
+    // no copy writes these buffers after the request finished
+    if (q->h_cells) cudaFreeHost(q->h_cells);
+    if (q->h_nodal) cudaFreeHost(q->h_nodal);
+    q->h_cells = q->h_nodal = nullptr;
+    q->taken = true;
+    // the object itself stays while a live cohort still refers to it
+    bool live = false;
+    for (auto& c : s->cohorts)
+      for (Req* r : c->reqs) live = live || r == q;
+    if (!live) s->reqs.erase(it);
+  });
+}
+
+int eqs_get_stats(eqs_server* s, eqs_stats* out) {
+  if (!s || !out) return EQF_ERR_INVALID;
+  *out = s->st;
+  out->step_samples = (int64_t)s->step_ms.size();
+  out->step_ms_p50 = percentile(s->step_ms, 0.50);
+  out->step_ms_p99 = percentile(s->step_ms, 0.99);
+  out->step_ms_p999 = percentile(s->step_ms, 0.999);
+  return EQF_OK;
+}
+
+int eqs_drain(eqs_server* s) {
+  if (!s) return EQF_ERR_INVALID;
+  return guarded(s, [&] {
+    for (;;) {
+      progress(s);
+      if (s->pending.empty() && s->cohorts.empty()) break;
+      bool any = false;
+      for (auto& c : s->cohorts) any = any || !c->inflight.empty();
+      if (any) {
+        // wait for the oldest step of some cohort instead of spinning
+        for (auto& c : s->cohorts)
+          if (!c->inflight.empty()) {
+            cudaEventSynchronize(c->inflight.front().end);
+            break;
+          }
+      }
+    }
+  });
+}
+
+}  // extern "C"

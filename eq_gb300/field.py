@@ -53,6 +53,18 @@ def default_opts(precision: int = FP64, **over) -> SolverOpts:
     return o
 
 
+def footprint_estimate(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
+                       n_cells: int = 0) -> int:
+    """Device bytes a batch of these traps would hold (eqf_footprint_estimate)."""
+    lib = _lib.load()
+    arr = (TrapParams * len(traps))(*traps)
+    out = C.c_int64()
+    rc = lib.eqf_footprint_estimate(len(traps), arr, C.byref(opts) if opts is not None else None,
+                                    int(n_cells), C.byref(out))
+    _check(lib, None, rc)
+    return out.value
+
+
 def trap_params(W, H, nx, ny, D, dt, decay=0.0, walls=WALL_BOTTOM, adv_u=0.0,
                 adv_len=1.0) -> TrapParams:
     return TrapParams(float(W), float(H), int(nx), int(ny), float(D), float(dt), float(decay),

@@ -171,6 +171,31 @@ int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64
 /* Waits for queued device work and reports deferred errors (convergence). */
 int eqf_sync(eqf_batch* b);
 
+/* Asynchronous use (no reference counterpart; the serving loop of eqserve.h is
+ * built on these).  With opts.adaptive = 0, eqf_step only queues the steps on the
+ * batch's stream and returns.  eqf_poll sets *idle to 1 once all queued work has
+ * finished (and then reports deferred errors, as eqf_sync), else 0, without
+ * waiting.  eqf_read_cells_async / eqf_read_nodal_async queue the readout of a
+ * trap's current state into host memory (pinned for the copy to overlap), valid
+ * once eqf_poll reports idle or after eqf_sync; a second asynchronous cell readout
+ * of the same trap before then overwrites the first's device staging.
+ * eqf_set_active(b, t, 0) freezes trap t: the following steps skip it entirely
+ * and its field stays as it is; eqf_set_active(b, t, 1) resumes it (with a fresh
+ * initial-guess history).  Frozen traps keep their device memory. */
+int eqf_poll(eqf_batch* b, int32_t* idle);
+int eqf_read_cells_async(eqf_batch* b, int32_t trap, int64_t n, double* c);
+int eqf_read_nodal_async(eqf_batch* b, int32_t trap, double* c);
+int eqf_set_active(eqf_batch* b, int32_t trap, int32_t active);
+/* Queues a copy of the batch's count of trap-steps that missed rtol so far into
+ * *count (host memory), valid like the asynchronous readouts above. */
+int eqf_fail_count_async(eqf_batch* b, int32_t* count);
+
+/* Device bytes a batch of these traps with n_cells cells in total would hold
+ * (including the transient of the first cell upload), for admission control.
+ * Needs no device. */
+int eqf_footprint_estimate(int32_t n_traps, const eqf_trap_params* traps,
+                           const eqf_solver_opts* opts, int64_t n_cells, int64_t* bytes);
+
 /* Batch-wide cell I/O for the per-step host exchange (one copy each way): rates
  * and concentrations of every trap's cells, concatenated in trap order (the
  * order of the eqf_set_cells calls within a trap).  Replaces the controller's

@@ -107,3 +107,71 @@ def test_noalloc_rejects_oversize_before_touching_a_device(lib):
     assert rc == _lib.EQF_ERR_TOO_LARGE and out.value == -1.0
     assert lib.eqf_field_integral_noalloc(None, 4, 4, 1.0, 1.0, 0, 1.0, None,
                                           C.byref(out)) == _lib.EQF_ERR_INVALID
+
+
+SERVE_HEADER = os.path.join(ROOT, "include", "eqserve.h")
+
+
+def test_serving_header_matches_binding_and_exports(lib):
+    from eq_gb300 import serve
+    text = re.sub(r"/\*.*?\*/", "", open(SERVE_HEADER).read(), flags=re.S)
+    declared = sorted(set(re.findall(r"\b(eqs_\w+)\s*\(", text)))
+    assert declared == sorted(serve.EXPORTS)
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (eqs_\w+)$", out, flags=re.M))
+    assert not [f for f in declared if f not in exported]
+
+
+def test_serving_struct_layout_matches_header():
+    from eq_gb300 import serve
+    src = r'''
+#include <stddef.h>
+#include <stdio.h>
+#include "eqserve.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(eqs_config), offsetof(eqs_config, hbm_budget),
+         offsetof(eqs_config, max_wait_ms), offsetof(eqs_config, steps_in_flight));
+  printf("%zu %zu %zu %zu\n", sizeof(eqs_request), offsetof(eqs_request, n_cells),
+         offsetof(eqs_request, vmax), offsetof(eqs_request, want_nodal));
+  printf("%zu %zu\n", sizeof(eqs_result_info), offsetof(eqs_result_info, cohort));
+  printf("%zu %zu\n", sizeof(eqs_stats), offsetof(eqs_stats, bytes_peak));
+  return 0;
+}'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "layout.c")
+        exe = os.path.join(d, "layout")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), c, "-o", exe],
+                       check=True)
+        lines = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = [[int(v) for v in ln.split()] for ln in lines[:4]]
+    S = serve
+    assert got[0] == [C.sizeof(S.ServerConfig), S.ServerConfig.hbm_budget.offset,
+                      S.ServerConfig.max_wait_ms.offset, S.ServerConfig.steps_in_flight.offset]
+    assert got[1] == [C.sizeof(S.Request), S.Request.n_cells.offset, S.Request.vmax.offset,
+                      S.Request.want_nodal.offset]
+    assert got[2] == [C.sizeof(S.ResultInfo), S.ResultInfo.cohort.offset]
+    assert got[3] == [C.sizeof(S.Stats), S.Stats.bytes_peak.offset]
+
+
+def test_serving_without_a_device_reports_no_device(lib):
+    from eq_gb300 import serve
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is visible")
+    except ImportError:
+        pass
+    cfg = serve.default_config()
+    h = C.c_void_p()
+    assert serve._bind(lib).eqs_create(C.byref(cfg), C.byref(h)) == _lib.EQF_ERR_NO_DEVICE
+
+
+def test_footprint_estimate_needs_no_device(lib):
+    from eq_gb300 import field as F
+    t = F.trap_params(40.0, 20.0, 160, 80, 490.0, 0.1, 0.01)
+    small = F.footprint_estimate([t], F.default_opts(F.FP32_IR), 300)
+    big = F.footprint_estimate([t, t], F.default_opts(F.FP64), 600)
+    assert 13041 * 60 < small < 13041 * 400
+    assert big > 2 * small
