@@ -155,7 +155,13 @@ def run_ours(args, rank, world, local_rank):
     ncells = sum(t.n_cells for t in traps)
 
     opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, tile_nodes=args.tile_nodes)
-    b = F.TrapBatch(tps, opts)
+    # the autotuner picks the row tile target and smoother degrees per size bucket
+    table = None
+    if args.tune_budget > 0 and args.tile_nodes == 0:
+        t_tune = time.perf_counter()
+        table = F.autotune(tps, opts, budget_s=args.tune_budget)
+        tune_s = time.perf_counter() - t_tune
+    b = F.TrapBatch(tps, opts, tune=table)
     for i, t in enumerate(traps):
         b.set_cells(i, t.cell_xy, t.cell_s)
     stream = torch.cuda.ExternalStream(b.stream_handle())
@@ -285,6 +291,8 @@ def run_ours(args, rank, world, local_rank):
             "p50_step_ms": float(np.percentile(sm, 50)), "p99_step_ms": float(np.percentile(sm, 99)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-ir",
             "data": "synthetic (seeded PCG64; the reference publishes no dataset)",
+            "autotune": ({"seconds": round(tune_s, 2), "buckets": F.tune_table_dict(table)}
+                         if table is not None else None),
             "config": {"workload": args.workload, "traps": len(traps), "nodes": nodes,
                        "cells": ncells, "seed": args.seed, "precision": "FP32 inner + FP64 refinement",
                        "rtol": opts.rtol, "graphs": True,
@@ -497,6 +505,8 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
     ap.add_argument("--audit-budget", type=float, default=30.0,
                     help="serving: CPU seconds for the oracle audit")
+    ap.add_argument("--tune-budget", type=float, default=20.0,
+                    help="seconds for the autotuner before the timed run (0: no tuning)")
     ap.add_argument("--tile-nodes", type=int, default=0,
                     help="target nodes per finest-level row tile (0: the library default)")
     ap.add_argument("--ncu", action="store_true",

@@ -32,7 +32,7 @@ EXPORTS = (
     "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
     "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc", "eqf_couple_species",
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
-    "eqf_footprint_estimate", "eqf_fail_count_async",
+    "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
@@ -50,6 +50,18 @@ class SolverOpts(C.Structure):
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
                 ("use_graph", C.c_int32), ("adaptive", C.c_int32),
                 ("tile_nodes", C.c_int32), ("krylov", C.c_int32)]
+
+
+class TuneBucket(C.Structure):
+    _fields_ = [("max_nodes", C.c_int64), ("tile_nodes", C.c_int32), ("cheb_pre", C.c_int32),
+                ("cheb_post", C.c_int32), ("dof_steps_per_s", C.c_double)]
+
+
+EQF_TUNE_MAX_BUCKETS = 8
+
+
+class TuneTable(C.Structure):
+    _fields_ = [("n", C.c_int32), ("b", TuneBucket * EQF_TUNE_MAX_BUCKETS)]
 
 
 class EqfError(RuntimeError):
@@ -104,6 +116,10 @@ def load() -> C.CDLL:
         "eqf_read_nodal_async": (C.c_int, [C.c_void_p, C.c_int32, dp]),
         "eqf_set_active": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
         "eqf_fail_count_async": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "eqf_create_tuned": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), P(TuneTable),
+                                       P(C.c_void_p)]),
+        "eqf_autotune": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_double,
+                                   P(TuneTable)]),
         "eqf_footprint_estimate": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_int64,
                                              i64p]),
     }

@@ -12,7 +12,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libeqfield.so")
-SOURCES = [os.path.join(CSRC, f) for f in ("eqf_batch.cu", "eqf_noalloc.cu", "eqf_server.cu")]
+SOURCES = [os.path.join(CSRC, f) for f in ("eqf_batch.cu", "eqf_noalloc.cu", "eqf_server.cu",
+                                               "eqf_tune.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("eqf_common.cuh", "eqf_kernels.cuh",
                                                    "eqf_cells.cuh", "eqf_refine.cuh",
                                                    "eqf_bicgstab.cuh")] + \

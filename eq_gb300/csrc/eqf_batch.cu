@@ -377,7 +377,8 @@ class Batch {
       }
   }
 
-  explicit Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o);
+  Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles = nullptr);
+  std::vector<int> tile_target;  // per trap (0: opts.tile_nodes / the default)
   ~Batch();
   void build_levels();
   void step(int n);
@@ -396,8 +397,9 @@ class Batch {
 };
 
 // ---------------------------------------------------------------------------
-Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o)
+Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles)
     : ntraps(n), opts(o), params(p, p + n) {
+  if (tiles) tile_target.assign(tiles, tiles + n);
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     throw Error(EQF_ERR_NO_DEVICE, "no CUDA device visible");
@@ -557,7 +559,9 @@ void Batch::build_levels() {
       const long long P = g.nx + 1;
       const long long n = P * (g.ny + 1);
       if (l > 0) g.fine_off = L[l - 1].geom[t].off;
-      const int R = (int)std::max<long long>(1, target / P);
+      const long long tgt =
+          (!tile_target.empty() && tile_target[t] > 0) ? tile_target[t] : target;
+      const int R = (int)std::max<long long>(1, tgt / P);
       for (int r0 = 0; r0 <= g.ny; r0 += R) {
         const int r1 = std::min(g.ny + 1, r0 + R);
         L[l].tiles.push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
@@ -1339,8 +1343,8 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
   return EQF_OK;
 }
 
-int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
-               eqf_batch** out) {
+static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
+                       const eqf_solver_opts* opts, const int* tiles, eqf_batch** out) {
   if (!out) return EQF_ERR_INVALID;
   *out = nullptr;
   auto* h = new (std::nothrow) eqf_batch();
@@ -1366,7 +1370,10 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
                       p.D >= 0 && p.decay >= 0 && (p.walls & ~15u) == 0,
                   "invalid trap parameters (trap " + std::to_string(t) + ")");
     }
-    h->impl.reset(new Batch(n_traps, traps, o));
+    if (tiles)
+      for (int t = 0; t < n_traps; ++t)
+        EQF_REQUIRE(tiles[t] >= 0 && tiles[t] <= 32768, "tile target outside [0, 32768]");
+    h->impl.reset(new Batch(n_traps, traps, o, tiles));
   });
   if (rc != EQF_OK) {
     g_create_err = h->err;
@@ -1375,6 +1382,45 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
   }
   *out = h;
   return EQF_OK;
+}
+
+int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+               eqf_batch** out) {
+  return create_impl(n_traps, traps, opts, nullptr, out);
+}
+
+// Bucket of a trap in a tuning table: the first whose max_nodes holds it (the last
+// bucket takes everything larger).
+static int tune_bucket(const eqf_tune_table& tb, long long nodes) {
+  for (int i = 0; i < tb.n; ++i)
+    if (nodes <= tb.b[i].max_nodes) return i;
+  return tb.n - 1;
+}
+
+int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+                     const eqf_tune_table* table, eqf_batch** out) {
+  if (!out || !traps || n_traps < 1) return EQF_ERR_INVALID;
+  if (!table || table->n < 1 || table->n > EQF_TUNE_MAX_BUCKETS)
+    return create_impl(n_traps, traps, opts, nullptr, out);
+  eqf_solver_opts o;
+  if (opts)
+    o = *opts;
+  else
+    eqf_default_opts(EQF_PREC_FP64, &o);
+  // tile target per trap from its bucket; smoother degrees from the bucket that
+  // holds most of the batch's nodes
+  std::vector<int> tiles(n_traps);
+  std::vector<long long> mass(table->n, 0);
+  for (int t = 0; t < n_traps; ++t) {
+    const long long nodes = (long long)(traps[t].nx + 1) * (traps[t].ny + 1);
+    const int k = tune_bucket(*table, nodes);
+    tiles[t] = table->b[k].tile_nodes;
+    mass[k] += nodes;
+  }
+  const int kb = (int)(std::max_element(mass.begin(), mass.end()) - mass.begin());
+  if (table->b[kb].cheb_pre > 0) o.cheb_pre = table->b[kb].cheb_pre;
+  if (table->b[kb].cheb_post > 0) o.cheb_post = table->b[kb].cheb_post;
+  return create_impl(n_traps, traps, &o, tiles.data(), out);
 }
 
 int eqf_destroy(eqf_batch* b) {

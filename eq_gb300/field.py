@@ -71,15 +71,41 @@ def trap_params(W, H, nx, ny, D, dt, decay=0.0, walls=WALL_BOTTOM, adv_u=0.0,
                       float(adv_u), float(adv_len), int(walls))
 
 
-class TrapBatch:
-    """A batch of independent traps on the GPU (C ABI handle)."""
+def autotune(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
+             budget_s: float = 20.0) -> _lib.TuneTable:
+    """Per size bucket, the fastest row tile target and Chebyshev degrees
+    (eqf_autotune; runs on the GPU for about budget_s seconds at most)."""
+    lib = _lib.load()
+    arr = (TrapParams * len(traps))(*traps)
+    table = _lib.TuneTable()
+    rc = lib.eqf_autotune(len(traps), arr, C.byref(opts) if opts is not None else None,
+                          float(budget_s), C.byref(table))
+    _check(lib, None, rc)
+    return table
 
-    def __init__(self, traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None):
+
+def tune_table_dict(table: _lib.TuneTable) -> List[Dict[str, float]]:
+    return [{"max_nodes": table.b[i].max_nodes, "tile_nodes": table.b[i].tile_nodes,
+             "cheb_pre": table.b[i].cheb_pre, "cheb_post": table.b[i].cheb_post,
+             "dof_steps_per_s": table.b[i].dof_steps_per_s} for i in range(table.n)]
+
+
+class TrapBatch:
+    """A batch of independent traps on the GPU (C ABI handle).  With a tuning table
+    (autotune) the traps take their size bucket's tile target and the batch its
+    dominant bucket's smoother degrees."""
+
+    def __init__(self, traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
+                 tune: Optional[_lib.TuneTable] = None):
         self._lib = _lib.load()
         arr = (TrapParams * len(traps))(*traps)
         self._h = C.c_void_p()
         o = opts if opts is not None else default_opts()
-        rc = self._lib.eqf_create(len(traps), arr, C.byref(o), C.byref(self._h))
+        if tune is not None:
+            rc = self._lib.eqf_create_tuned(len(traps), arr, C.byref(o), C.byref(tune),
+                                            C.byref(self._h))
+        else:
+            rc = self._lib.eqf_create(len(traps), arr, C.byref(o), C.byref(self._h))
         _check(self._lib, None, rc)
         self.n_traps = len(traps)
         self.params = list(traps)

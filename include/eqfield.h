@@ -99,6 +99,35 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* opts);
 int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
                eqf_batch** out);
 
+/* Autotuning (no reference counterpart).  A tuning table maps trap size buckets
+ * (node count <= max_nodes, ascending; the last bucket takes the rest) to the row
+ * tile target of the finest level and the pre/post Chebyshev degrees that were
+ * fastest for traps of that size (DOF-steps/s at the solver tolerance, measured by
+ * eqf_autotune).  eqf_create_tuned creates a batch whose traps take the tile
+ * target of their bucket and whose smoother takes the degrees of the bucket that
+ * holds most of its nodes. */
+#define EQF_TUNE_MAX_BUCKETS 8
+typedef struct eqf_tune_bucket {
+  int64_t max_nodes;
+  int32_t tile_nodes, cheb_pre, cheb_post;
+  double dof_steps_per_s; /* measured rate of the chosen configuration */
+} eqf_tune_bucket;
+typedef struct eqf_tune_table {
+  int32_t n;
+  eqf_tune_bucket b[EQF_TUNE_MAX_BUCKETS];
+} eqf_tune_table;
+
+int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+                     const eqf_tune_table* table, eqf_batch** out);
+
+/* Measures, for each size bucket, candidate tile targets and Chebyshev degrees on a
+ * batch of the given traps that fall into the bucket (replicated up to a
+ * GPU-filling node count), with random point cells, and writes the fastest into
+ * *table.  Buckets: <= 32k, <= 128k, <= 512k nodes, and larger.  Takes about
+ * budget_s seconds of GPU time at most (unexplored candidates keep the defaults). */
+int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+                 double budget_s, eqf_tune_table* table);
+
 /* Releases all device memory.  Replaces fenicsInterface::finalize / destructor
  * (src/fHSL.cpp:655-661). */
 int eqf_destroy(eqf_batch* b);
