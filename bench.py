@@ -255,12 +255,21 @@ def run_ours(args, rank, world, local_rank):
                 "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
                 "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
 
-    # ---- e2e through the host API: pinned rates in, pinned concentrations out
+    b.close()
+
+    # ---- e2e through the host API: a fresh batch taken through the same warm-up, then
+    #      the same steps as the timed loop, each with the pinned per-cell rates copied
+    #      in and the per-cell concentrations read back
+    b = F.TrapBatch(tps, opts, tune=table)
+    for i, t in enumerate(traps):
+        b.set_cells(i, t.cell_xy, t.cell_s)
+    b.step(args.warmup)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream_handle())
     rates = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
     rates.numpy()[:] = np.concatenate([t.cell_s for t in traps])
     cout = torch.empty(ncells, dtype=torch.float64, pin_memory=True)
-    e2e_steps = max(1, min(args.steps, 10))
-    b.sync()
+    e2e_steps = args.steps
     t0 = time.perf_counter()
     ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ee0.record(stream)
@@ -274,8 +283,7 @@ def run_ours(args, rank, world, local_rank):
     e2e_wall = time.perf_counter() - t0
     e2e = {"value": nodes * e2e_steps / (max(e2e_ms, e2e_wall * 1e3) / 1e3), "unit": UNIT,
            "h2d_bytes_per_step": ncells * 8, "d2h_bytes_per_step": ncells * 8,
-           "steps": e2e_steps}
-
+           "steps": e2e_steps, "timing": "wall clock and CUDA events, the larger"}
     b.close()
 
     out = None
