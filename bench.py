@@ -154,7 +154,8 @@ def run_ours(args, rank, world, local_rank):
     nodes = sum(t.n_nodes for t in traps)
     ncells = sum(t.n_cells for t in traps)
 
-    opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, tile_nodes=args.tile_nodes)
+    opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, tile_nodes=args.tile_nodes,
+                          fuse_levels=0 if args.no_fuse else 1)
     # the autotuner picks the row tile target and smoother degrees per size bucket
     table = None
     if args.tune_budget > 0 and args.tile_nodes == 0:
@@ -513,6 +514,8 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
     ap.add_argument("--audit-budget", type=float, default=30.0,
                     help="serving: CPU seconds for the oracle audit")
+    ap.add_argument("--no-fuse", action="store_true",
+                    help="step-by-step level kernels instead of the temporally blocked ones")
     ap.add_argument("--tune-budget", type=float, default=20.0,
                     help="seconds for the autotuner before the timed run (0: no tuning)")
     ap.add_argument("--tile-nodes", type=int, default=0,

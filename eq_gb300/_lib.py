@@ -49,7 +49,7 @@ class SolverOpts(C.Structure):
                 ("max_iters", C.c_int32), ("inner_tol", C.c_double), ("cheb_pre", C.c_int32),
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
                 ("use_graph", C.c_int32), ("adaptive", C.c_int32),
-                ("tile_nodes", C.c_int32), ("krylov", C.c_int32)]
+                ("tile_nodes", C.c_int32), ("krylov", C.c_int32), ("fuse_levels", C.c_int32)]
 
 
 class TuneBucket(C.Structure):

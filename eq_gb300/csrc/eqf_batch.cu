@@ -23,6 +23,7 @@
 #include "eqf_kernels.cuh"
 #include "eqf_refine.cuh"
 #include "eqf_bicgstab.cuh"
+#include "eqf_fused.cuh"
 
 namespace eqf {
 
@@ -137,6 +138,23 @@ static Lens<T> make_lens(const LevelGeom& g) {
   return L;
 }
 
+// Chebyshev-Jacobi coefficients of steps 0..15 on [lmin, lam_max] (three-term
+// recurrence of the shifted Chebyshev polynomials, rho_s = 1 / (2 sigma - rho_{s-1})).
+static void cheb_table(LevelGeom& g, double lmin) {
+  const double lmax = g.lam_max;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+  const double sigma = theta / delta;
+  g.ch_old[0] = 0.0f;
+  g.ch_res[0] = (float)(1.0 / theta);
+  double rho_prev = 1.0 / sigma;
+  for (int s = 1; s < kMaxChebSteps; ++s) {
+    const double rho = 1.0 / (2.0 * sigma - rho_prev);
+    g.ch_old[s] = (float)(rho * rho_prev);
+    g.ch_res[s] = (float)(2.0 * rho / delta);
+    rho_prev = rho;
+  }
+}
+
 static void interior_constants(LevelGeom& g) {
   g.adv_on = g.adv != 0.0 ? 1 : 0;
   g.ld = make_lens<double>(g);
@@ -219,6 +237,7 @@ struct Level {
   // dynamic shared memory per staged kernel (max over this level's tiles)
   size_t sm_cheb = 0, sm_resid = 0, sm_cgdir = 0, sm_ir = 0;
   size_t sm_irf1 = 0, sm_irf = 0;  // pair-arithmetic refinement residuals (FP32 form)
+  size_t sm_down = 0, sm_up = 0;   // fused level kernels (0: not built for this level)
 
   size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
   size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
@@ -544,6 +563,8 @@ void Batch::build_levels() {
       }
       interior_constants(g);
       spectrum_bounds(g);
+      g.inv_pitch = 1.0f / (float)(g.nx + 1);
+      cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
       L[l].geom[t] = g;
     }
   }
@@ -654,6 +675,19 @@ void Batch::build_levels() {
                                   kSmemHeader + staged_bytes(fr0 * PF, fr1 * PF, tsz,
                                                              align_up(PF * (f.ny + 1), 32)));
       }
+      if (l + 1 < nlev) {  // fused level kernels (windows as fused_win / up_coarse_rows)
+        const FusedWin w = fused_win(tl.k0, tl.k1, (int)P);
+        const LevelGeom& c = L[l + 1].geom[tl.geom];
+        int clo = 0, chi = 0;
+        up_coarse_rows(g, c, w, clo, chi);
+        const long long PC = c.nx + 1;
+        const size_t w1 = guarded_bytes(w.w1a, w.w1b, tsz), w2 = guarded_bytes(w.w2a, w.w2b, tsz);
+        const size_t tab = (size_t)kTabPerTrap * tsz;
+        Lv.sm_down = std::max(Lv.sm_down, kSmemHeader + 2 * w1 + w2 + tab);
+        Lv.sm_up = std::max(Lv.sm_up, kSmemHeader + w1 + 2 * w2 + tab +
+                                          staged_bytes(clo * PC, (chi + 1) * PC, tsz,
+                                                       align_up(PC * (c.ny + 1), 32)));
+      }
       if (l + 1 < nlev) {  // prolongation into level l stages coarse rows lo(r0) .. hi(r1-1)
         const LevelGeom& c = L[l + 1].geom[tl.geom];
         auto f2c_lo = [](int f, int nf, int h) {
@@ -672,6 +706,8 @@ void Batch::build_levels() {
     for (size_t v : {Lv.sm_cheb, Lv.sm_resid, Lv.sm_cgdir, Lv.sm_restrict, Lv.sm_prolong})
       if (v > kMaxDynSmem)
         throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
+    // the fused level kernels are used where their windows fit (else the unfused steps)
+    if (Lv.sm_down > kMaxDynSmem || Lv.sm_up > kMaxDynSmem) Lv.sm_down = Lv.sm_up = 0;
     if (l == 0 && std::max(Lv.sm_ir, Lv.sm_irf1) > kMaxDynSmem)
       throw Error(EQF_ERR_INVALID, "trap rows too wide for shared-memory row tiles");
   }
@@ -721,6 +757,9 @@ static void allow_dyn_smem() {
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
   smem_attrs(k_irf_first, mx);
+  smem_attrs(k_down<T>, mx);
+  smem_attrs(k_up<T, true>, mx);
+  smem_attrs(k_up<T, false>, mx);
   smem_attrs(k_apply_dot<T, 1>, mx);
   smem_attrs(k_apply_dot<T, 2>, mx);
   smem_attrs(k_irf_residual<true>, mx);
@@ -766,7 +805,7 @@ Work<T>::Work(Batch& b) : B(b) {
 // One Chebyshev step on a level (template flags chosen at run time).
 template <class T>
 static void cheb_step(Batch& B, cudaStream_t s, int lev, int nt, const LevelGeom* G,
-                      const Tile* tl, const T* tab, const int* skip, float ratio, int st,
+                      const Tile* tl, const T* tab, const int* skip, int st,
                       bool first, bool zero, bool dot, const T* b, const T* xin, T* xout, T* d,
                       double* part) {
   const int cls = lev > 0 ? KC_COARSE : (zero ? KC_SMOOTH0_FIRST : KC_SMOOTH0);
@@ -774,24 +813,24 @@ static void cheb_step(Batch& B, cudaStream_t s, int lev, int nt, const LevelGeom
   if (zero) {
     if (dot)
       EQF_RUN(B, cls, (k_cheb<T, true, true, true><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
     else
       EQF_RUN(B, cls, (k_cheb<T, true, true, false><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
   } else if (first) {
     if (dot)
       EQF_RUN(B, cls, (k_cheb<T, true, false, true><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
     else
       EQF_RUN(B, cls, (k_cheb<T, true, false, false><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, 0, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
   } else {
     if (dot)
       EQF_RUN(B, cls, (k_cheb<T, false, false, true><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, st, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, st, b, xin, xout, d, part, W)));
     else
       EQF_RUN(B, cls, (k_cheb<T, false, false, false><<<nt, kThreads, sm, s>>>(
-                           G, tl, tab, skip, ratio, st, b, xin, xout, d, part, W)));
+                           G, tl, tab, skip, st, b, xin, xout, d, part, W)));
   }
 }
 
@@ -823,7 +862,6 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   T* cur = v.x.p;
   T* oth = v.y.p;
   const bool coarsest = lev == B.nlev - 1;
-  const float ratio = coarsest ? 0.f : (float)B.opts.cheb_ratio;
   const int deg_pre = coarsest ? B.opts.cheb_coarse : B.opts.cheb_pre;
   if (coarsest && Lv_.sm_coarse && !dot) {
     // the whole coarsest solve in one CTA per trap
@@ -832,11 +870,34 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
                                                                           bl, cur)));
     return cur;
   }
+  if (!coarsest && B.opts.fuse_levels && B.opts.cheb_pre == 2 && B.opts.cheb_post == 2 &&
+      Lv_.sm_down > 0) {
+    // temporally blocked: pre-smoothing + residual, restriction, coarse correction,
+    // prolongation + post-smoothing
+    const int cd = lev > 0 ? KC_COARSE : KC_SMOOTH0;
+    EQF_RUN(B, cd,
+            (k_down<T><<<nt, kThreads, Lv_.sm_down, s>>>(G, tl, tab, skip, bl, cur, v.t.p,
+                                                          W)));
+    const Level& Lc = B.L[lev + 1];
+    EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
+            (k_restrict<T><<<Lc.ntiles(), kThreads, Lc.sm_restrict, s>>>(
+                Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
+    T* xc = vcycle(s, lev + 1, false);
+    if (dot)
+      EQF_RUN(B, cd,
+              (k_up<T, true><<<nt, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, tl, tab, skip, xc, bl,
+                                                            cur, oth, part, W)));
+    else
+      EQF_RUN(B, cd,
+              (k_up<T, false><<<nt, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, tl, tab, skip, xc, bl,
+                                                             cur, oth, part, W)));
+    return oth;
+  }
   // pre-smoothing (or the coarsest-level solve) from zero
-  cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, 0, true, true,
+  cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, 0, true, true,
                dot && coarsest && deg_pre == 1, bl, cur, cur, v.d.p, part);
   for (int st = 1; st < deg_pre; ++st) {
-    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, false, false,
+    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, st, false, false,
                  dot && coarsest && st == deg_pre - 1, bl, cur, oth, v.d.p, part);
     std::swap(cur, oth);
   }
@@ -857,7 +918,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   // post-smoothing from the corrected iterate
   const int deg_post = B.opts.cheb_post;
   for (int st = 0; st < deg_post; ++st) {
-    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, ratio, st, st == 0, false,
+    cheb_step<T>(B, s, lev, nt, G, tl, tab, skip, st, st == 0, false,
                  dot && st == deg_post - 1, bl, cur, oth, v.d.p, part);
     std::swap(cur, oth);
   }
@@ -1327,6 +1388,7 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
   o->cheb_ratio = 5.0;
   o->use_graph = 0;
   o->adaptive = 1;
+  o->fuse_levels = 1;
   if (precision == EQF_PREC_FP32_IR) {
     o->rtol = 1e-8;
     o->max_sweeps = 2;
@@ -1361,6 +1423,9 @@ static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
     EQF_REQUIRE(o.max_sweeps >= 1 && o.max_iters >= 1 && o.cheb_post >= 1 && o.cheb_pre >= 1 &&
                     o.cheb_coarse >= 1 && o.cheb_ratio > 1.0 && o.rtol > 0.0,
                 "invalid solver options");
+    EQF_REQUIRE(o.cheb_pre <= eqf::kMaxChebSteps && o.cheb_post <= eqf::kMaxChebSteps &&
+                    o.cheb_coarse <= eqf::kMaxChebSteps,
+                "Chebyshev degrees above 16");
     EQF_REQUIRE(o.tile_nodes >= 0 && o.tile_nodes <= 32768, "tile_nodes outside [0, 32768]");
     EQF_REQUIRE(o.krylov >= EQF_KRYLOV_AUTO && o.krylov <= EQF_KRYLOV_BICGSTAB,
                 "unknown Krylov method");

@@ -84,26 +84,29 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const int P = g.nx + 1;
   const QuadGeom qg(g, tile);
   T a0 = T(0), a1 = T(0);
-  for (QuadWalk q(g, tile.k0 >> 2); 4 * q.q < tile.k1; q.next()) {
-    const int k = 4 * q.q;
-    const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-    Q4<T> xc, id;
-    const Q4<T> ax =
-        apply_quad<T>(g, ci, stab, xv, k, P, q.i, q.j, qg.interior(k, q.i, q.j), xc, id);
-    const Q4<T> wq = full ? wv.quad(k) : quad_masked<T>(wv, k, tile.k0, tile.k1);
+  pitch_dispatch(P, [&](auto pm_) {
+    constexpr int PM = decltype(pm_)::value;
+    for (QuadWalk q(g, tile.k0 >> 2); 4 * q.q < tile.k1; q.next()) {
+      const int k = 4 * q.q;
+      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+      Q4<T> xc, id;
+      const Q4<T> ax =
+          apply_quad<T, PM>(g, ci, stab, xv, k, P, q.i, q.j, qg.interior(k, q.i, q.j), xc, id);
+      const Q4<T> wq = full ? wv.quad(k) : quad_masked<T>(wv, k, tile.k0, tile.k1);
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const bool in = full || (k + e >= tile.k0 && k + e < tile.k1);
-      if (in) {
-        a0 += wq.v[e] * ax.v[e];
-        if (NDOT == 2) a1 += ax.v[e] * ax.v[e];
+      for (int e = 0; e < 4; ++e) {
+        const bool in = full || (k + e >= tile.k0 && k + e < tile.k1);
+        if (in) {
+          a0 += wq.v[e] * ax.v[e];
+          if (NDOT == 2) a1 += ax.v[e] * ax.v[e];
+        }
       }
+      if (full)
+        vst4<T>(ys + k, ax);
+      else
+        store_masked<T>(ys, ax, k, tile.k0, tile.k1);
     }
-    if (full)
-      vst4<T>(ys + k, ax);
-    else
-      store_masked<T>(ys, ax, k, tile.k0, tile.k1);
-  }
+  });
   const double t0 = block_sum(double(a0));
   const double t1 = NDOT == 2 ? block_sum(double(a1)) : 0.0;
   if (threadIdx.x == 0) {

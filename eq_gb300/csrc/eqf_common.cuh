@@ -55,7 +55,13 @@ struct LevelGeom {
   float fC, fE, fN, fD, fCinv;
   float lam_max;          // upper bound of spectrum(D^-1 A)
   float lam_min;          // lower estimate (coarsest-level solve)
+  float inv_pitch;        // 1 / (nx + 1), for division-free row/column walks
+  // Chebyshev-Jacobi step coefficients on this level's interval ([lam_max/ratio,
+  // lam_max] for smoothing, [lam_min, lam_max] on the coarsest level), step s:
+  // d_new = ch_old[s] d + ch_res[s] D^-1 r
+  float ch_old[16], ch_res[16];
 };
+constexpr int kMaxChebSteps = 16;
 
 template <class T>
 EQF_HD const Lens<T>& lens(const LevelGeom& g);

@@ -16,6 +16,8 @@
 // deterministic: each tile writes one FP64 partial and the per-trap scalar
 // kernels add a trap's partials in tile order.
 #pragma once
+#include <type_traits>
+
 #include "eqf_common.cuh"
 
 namespace eqf {
@@ -76,6 +78,8 @@ struct View {
   int a;
   __device__ __forceinline__ T operator[](int k) const { return p[k - a]; }
   __device__ __forceinline__ Q4<T> quad(int k) const;  // k a multiple of 4
+  // x[k0 .. k0+4]; M = (k0 - a) mod 4, a compile-time constant of the caller
+  template <int M>
   __device__ __forceinline__ void row(int k0, T (&out)[5]) const;
 };
 
@@ -174,6 +178,19 @@ __device__ __forceinline__ int padded_len(const LevelGeom& g) {
   return (n + 31) & ~31;
 }
 
+// (i, j) = floor-divmod(k, P) without an integer division (exact for |k| < 2^22).
+__device__ __forceinline__ void div_pitch(int k, int P, float inv_p, int& i, int& j) {
+  i = __float2int_rd(((float)k + 0.5f) * inv_p);
+  j = k - i * P;
+  if (j < 0) {
+    --i;
+    j += P;
+  } else if (j >= P) {
+    ++i;
+    j -= P;
+  }
+}
+
 // Walks the nodes k = k0 + tid, k0 + tid + bd, ... of a tile while keeping
 // (i, j) = divmod(k, nx + 1) up to date with one division per thread.
 struct NodeWalk {
@@ -182,10 +199,8 @@ struct NodeWalk {
   __device__ __forceinline__ NodeWalk(const LevelGeom& g, int k0) {
     pitch = g.nx + 1;
     k = k0 + threadIdx.x;
-    i = k / pitch;
-    j = k - i * pitch;
-    qi = blockDim.x / pitch;
-    qj = blockDim.x - qi * pitch;
+    div_pitch(k, pitch, g.inv_pitch, i, j);
+    div_pitch((int)blockDim.x, pitch, g.inv_pitch, qi, qj);
   }
   __device__ __forceinline__ void next() {
     k += blockDim.x;
@@ -340,34 +355,45 @@ __device__ __forceinline__ Q4<T> View<T>::quad(int k) const {
   return vld4<T>(p + (k - a));
 }
 
+// Five consecutive values x[k0 .. k0+4] of a staged row.  FP32: two aligned 16-byte
+// loads and a compile-time selection by the misalignment M (the same for every quad
+// of a trap: it only depends on the row pitch), free of shared-memory bank
+// conflicts; FP64 loads scalars.
+template <int M, class T>
+struct Row5 {
+  static __device__ __forceinline__ void load(const View<T>& w, int k0, T (&out)[5]) {
+#pragma unroll
+    for (int e = 0; e < 5; ++e) out[e] = w[k0 + e];
+  }
+};
+template <int M>
+struct Row5<M, float> {
+  static __device__ __forceinline__ void load(const View<float>& w, int k0, float (&out)[5]) {
+    const float4* base = reinterpret_cast<const float4*>(w.p + (k0 - w.a - M));
+    const float4 A = base[0], B = base[1];
+    const float v[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+#pragma unroll
+    for (int e = 0; e < 5; ++e) out[e] = v[M + e];
+  }
+};
 template <class T>
-__device__ __forceinline__ void row5(const View<T>& w, int k0, T (&out)[5]);
-template <class T>
+template <int M>
 __device__ __forceinline__ void View<T>::row(int k0, T (&out)[5]) const {
-  row5<T>(*this, k0, out);
+  Row5<M, T>::load(*this, k0, out);
 }
 
-// Five consecutive values x[k0 .. k0+4] of a staged FP32 row.  Two aligned
-// 16-byte loads and a select on the (warp-uniform) misalignment keep shared
-// memory free of bank conflicts; FP64 views load scalars.
-template <class T>
-__device__ __forceinline__ void row5(const View<T>& w, int k0, T (&out)[5]) {
-#pragma unroll
-  for (int e = 0; e < 5; ++e) out[e] = w[k0 + e];
-}
-template <>
-__device__ __forceinline__ void row5<float>(const View<float>& w, int k0, float (&out)[5]) {
-  const int rel = k0 - w.a;
-  const int m = rel & 3;
-  const float4* base = reinterpret_cast<const float4*>(w.p + (rel - m));
-  const float4 A = base[0], B = base[1];
-  switch (m) {
-    case 0: out[0] = A.x; out[1] = A.y; out[2] = A.z; out[3] = A.w; out[4] = B.x; break;
-    case 1: out[0] = A.y; out[1] = A.z; out[2] = A.w; out[3] = B.x; out[4] = B.y; break;
-    case 2: out[0] = A.z; out[1] = A.w; out[2] = B.x; out[3] = B.y; out[4] = B.z; break;
-    default: out[0] = A.w; out[1] = B.x; out[2] = B.y; out[3] = B.z; out[4] = B.w; break;
+// Runs f(std::integral_constant<int, P mod 4>): kernels instantiate their quad loop
+// for the four row-pitch residues, which fixes the row misalignments at compile time.
+template <class F>
+__device__ __forceinline__ void pitch_dispatch(int P, F&& f) {
+  switch (P & 3) {
+    case 0: f(std::integral_constant<int, 0>{}); break;
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    default: f(std::integral_constant<int, 3>{}); break;
   }
 }
+
 
 // Walks the quads q = q0 + tid, q0 + tid + bd, ... of a tile, keeping
 // (i, j) of the quad's first node 4q with one division per thread.
@@ -376,12 +402,8 @@ struct QuadWalk {
   __device__ __forceinline__ QuadWalk(const LevelGeom& g, int q0) {
     P = g.nx + 1;
     q = q0 + threadIdx.x;
-    const int k = 4 * q;
-    i = k / P;
-    j = k - i * P;
-    const int step = 4 * blockDim.x;
-    qi = step / P;
-    qj = step - qi * P;
+    div_pitch(4 * q, P, g.inv_pitch, i, j);
+    div_pitch(4 * (int)blockDim.x, P, g.inv_pitch, qi, qj);
   }
   __device__ __forceinline__ void next() {
     q += blockDim.x;
@@ -460,7 +482,8 @@ __device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
 // vector, two row ends, five above, five below); only the weights differ:
 // interior quads use the interior constants, the others (walls, row ends, ragged
 // last cells, advection traps) take per-node weights from the staged class table.
-template <class T, class X>
+// PM = P mod 4 (pitch_dispatch); x's base index is a multiple of 4.
+template <class T, int PM, class X>
 __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T>& ci,
                                             const T* __restrict__ stab, const X& x, int k,
                                             int P, int i0, int j0, bool inner, Q4<T>& xc,
@@ -468,8 +491,8 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
   xc = x.quad(k);
   const T xw = x[k - 1], xe = x[k + 4];
   T nr[5], sr[5];
-  x.row(k + P, nr);      // nr[e]: N of node e, NE of node e-1
-  x.row(k - P - 1, sr);  // sr[e]: SW of node e, S of node e-1
+  x.template row<PM>(k + P, nr);           // nr[e]: N of node e, NE of node e-1
+  x.template row<3 - PM>(k - P - 1, sr);   // sr[e]: SW of node e, S of node e-1
   Q4<T> ax;
   if (inner) {
 #pragma unroll
@@ -484,22 +507,20 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
     for (int e = 0; e < 4; ++e) {
       int i, j;
       quad_node(P, i0, j0, e, i, j);
-      T c[8];
+      const T w = e == 0 ? xw : xc.v[e - 1];
+      const T ee = e == 3 ? xe : xc.v[e + 1];
       if (g.adv_on) {
+        T c[8];  // filled out of line (local memory): advective traps only
         coef_general<T>(g, i, j, c);
+        ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
+        id.v[e] = c[7];
       } else {
         const T* t = stab + node_class_clamped(g, i, j) * kTabStride;
         const Q4<T> lo = vld4<T>(t), hi = vld4<T>(t + 4);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          c[q] = lo.v[q];
-          c[4 + q] = hi.v[q];
-        }
+        const T c[8] = {lo.v[0], lo.v[1], lo.v[2], lo.v[3], hi.v[0], hi.v[1], hi.v[2], hi.v[3]};
+        ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
+        id.v[e] = c[7];
       }
-      const T w = e == 0 ? xw : xc.v[e - 1];
-      const T ee = e == 3 ? xe : xc.v[e + 1];
-      ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
-      id.v[e] = c[7];
     }
   }
   return ax;
@@ -550,21 +571,14 @@ __device__ __forceinline__ int halo_hi(const LevelGeom& g, const Tile& t) {
 }
 
 // ---------------------------------------------------------------------------
-// Chebyshev step coefficients for step index `step` (0-based) on [lmin, lmax].
+// Chebyshev step coefficients of one step.
 struct ChebCoef {
   float c_old;  // multiplies the previous direction
   float c_res;  // multiplies D^-1 r
 };
-__device__ __forceinline__ ChebCoef cheb_coef(float lmin, float lmax, int step) {
-  const float theta = 0.5f * (lmax + lmin), delta = 0.5f * (lmax - lmin);
-  const float sigma = theta / delta;
-  if (step == 0) return ChebCoef{0.f, 1.f / theta};
-  float rho_old = 1.f / sigma, rho = rho_old;
-  for (int s = 1; s <= step; ++s) {
-    rho = 1.f / (2.f * sigma - rho_old);
-    if (s < step) rho_old = rho;
-  }
-  return ChebCoef{rho * rho_old, 2.f * rho / delta};
+// Step `s` of the level's Chebyshev table.
+__device__ __forceinline__ ChebCoef cheb_at(const LevelGeom& g, int s) {
+  return ChebCoef{g.ch_old[s], g.ch_res[s]};
 }
 
 // d_new = c_res (b - Ax) / diag (+ c_old d_old), one fixed evaluation order
@@ -578,12 +592,12 @@ __device__ __forceinline__ T cheb_dir(const ChebCoef& cc, T bk, T ax, T id, T do
 //   ZERO (x_in = 0): x_out = d = D^-1 b / theta            (streaming, no staging)
 //   FIRST:           d = D^-1 (b - A x_in) / theta; x_out = x_in + d
 //   otherwise:       d = c_old d + c_res D^-1 (b - A x_in); x_out = x_in + d
-// `ratio` > 0 selects the smoothing interval [lmax/ratio, lmax], else the full
-// interval [lmin, lmax] (coarsest-level solve).  DOT adds a partial of b.x_out.
+// The coefficients come from the level's Chebyshev table (the smoothing interval,
+// or the full interval on the coarsest level).  DOT adds a partial of b.x_out.
 template <class T, bool FIRST, bool ZERO, bool DOT>
 __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_cheb(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
-           const T* __restrict__ tabs, const int* __restrict__ skip, float ratio, int step,
+           const T* __restrict__ tabs, const int* __restrict__ skip, int step,
            const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
            T* __restrict__ d, double* __restrict__ part, unsigned long long* work) {
   const Tile tile = tiles[blockIdx.x];
@@ -593,8 +607,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     return;
   }
   count_work(work, tile);
-  const float lmax = g.lam_max, lmin = ratio > 0.f ? g.lam_max / ratio : g.lam_min;
-  const ChebCoef cc = cheb_coef(lmin, lmax, FIRST ? 0 : step);
+  const ChebCoef cc = cheb_at(g, FIRST ? 0 : step);
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
   const T* bs = b + g.off;
@@ -644,36 +657,39 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     if (!FIRST) dv = st.add(static_cast<const T*>(ds), tile.k0, tile.k1, na);
     const T* stab = stage_table<T>(st, tab, ci);
     if (!st.run()) return;
-    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-      const int k = 4 * w.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-      Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j),
-                                     xc, id);
-      Q4<T> bq, dq;
-      if (full) {
-        bq = bv.quad(k);
-        if (!FIRST) dq = dv.quad(k);
-      } else {
-        bq = quad_masked<T>(bv, k, tile.k0, tile.k1);
-        if (!FIRST) dq = quad_masked<T>(dv, k, tile.k0, tile.k1);
-      }
-      if (FIRST) dq = bq;
-      Q4<T> dn, xn;
+    pitch_dispatch(P, [&](auto pm_) {
+      constexpr int PM = decltype(pm_)::value;
+      for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+        const int k = 4 * w.q;
+        const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+        Q4<T> xc, id;
+        const Q4<T> ax = apply_quad<T, PM>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j),
+                                       xc, id);
+        Q4<T> bq, dq;
+        if (full) {
+          bq = bv.quad(k);
+          if (!FIRST) dq = dv.quad(k);
+        } else {
+          bq = quad_masked<T>(bv, k, tile.k0, tile.k1);
+          if (!FIRST) dq = quad_masked<T>(dv, k, tile.k0, tile.k1);
+        }
+        if (FIRST) dq = bq;
+        Q4<T> dn, xn;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        dn.v[e] = cheb_dir<T, FIRST>(cc, bq.v[e], ax.v[e], id.v[e], dq.v[e]);
-        xn.v[e] = xc.v[e] + dn.v[e];
-        if (DOT) acc += bq.v[e] * xn.v[e];
+        for (int e = 0; e < 4; ++e) {
+          dn.v[e] = cheb_dir<T, FIRST>(cc, bq.v[e], ax.v[e], id.v[e], dq.v[e]);
+          xn.v[e] = xc.v[e] + dn.v[e];
+          if (DOT) acc += bq.v[e] * xn.v[e];
+        }
+        if (full) {
+          vst4<T>(xo + k, xn);
+          vst4<T>(ds + k, dn);
+        } else {
+          store_masked<T>(xo, xn, k, tile.k0, tile.k1);
+          store_masked<T>(ds, dn, k, tile.k0, tile.k1);
+        }
       }
-      if (full) {
-        vst4<T>(xo + k, xn);
-        vst4<T>(ds + k, dn);
-      } else {
-        store_masked<T>(xo, xn, k, tile.k0, tile.k1);
-        store_masked<T>(ds, dn, k, tile.k0, tile.k1);
-      }
-    }
+    });
   }
   if (DOT) {
     const double t = block_sum(double(acc));
@@ -702,21 +718,24 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   T* ts = t + g.off;
   const int P = g.nx + 1;
   const QuadGeom qg(g, tile);
-  for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-    const int k = 4 * w.q;
-    const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-    Q4<T> xc, id;
-    const Q4<T> ax =
-        apply_quad<T>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j), xc, id);
-    const Q4<T> bq = full ? bv.quad(k) : quad_masked<T>(bv, k, tile.k0, tile.k1);
-    Q4<T> r;
+  pitch_dispatch(P, [&](auto pm_) {
+    constexpr int PM = decltype(pm_)::value;
+    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+      const int k = 4 * w.q;
+      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+      Q4<T> xc, id;
+      const Q4<T> ax =
+          apply_quad<T, PM>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j), xc, id);
+      const Q4<T> bq = full ? bv.quad(k) : quad_masked<T>(bv, k, tile.k0, tile.k1);
+      Q4<T> r;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
-    if (full)
-      vst4<T>(ts + k, r);
-    else
-      store_masked<T>(ts, r, k, tile.k0, tile.k1);
-  }
+      for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
+      if (full)
+        vst4<T>(ts + k, r);
+      else
+        store_masked<T>(ts, r, k, tile.k0, tile.k1);
+    }
+  });
 }
 
 // Per-axis map between a coarse level and its finer level.  A fine node either
@@ -847,7 +866,7 @@ __global__ void __launch_bounds__(kThreads)
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
   for (int it = 0; it < deg; ++it) {
-    const ChebCoef cc = cheb_coef(g.lam_min, g.lam_max, it);
+    const ChebCoef cc = cheb_at(g, it);
     const View<T>& xi = (it & 1) ? xbv : xav;
     T* xo = (it & 1) ? xa : xb;
     for (NodeWalk w(g, 0); w.k < n; w.next()) {
@@ -893,11 +912,12 @@ struct PNew {  // p_out = z + beta p_in evaluated on the fly from the staged z, 
     }
     return a;
   }
+  template <int M>
   __device__ __forceinline__ void row(int k0, T (&out)[5]) const {
-    z.row(k0, out);
+    z.template row<M>(k0, out);
     if (!FIRST) {
       T pr[5];
-      p.row(k0, pr);
+      p.template row<M>(k0, pr);
 #pragma unroll
       for (int e = 0; e < 5; ++e) out[e] = fma_(beta, pr[e], out[e]);
     }
@@ -935,24 +955,27 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const int P = g.nx + 1;
   const QuadGeom qg(g, tile);
   T acc = T(0);
-  for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-    const int k = 4 * w.q;
-    Q4<T> pc, id;
-    const Q4<T> a =
-        apply_quad<T>(g, ci, stab, pnew, k, P, w.i, w.j, qg.interior(k, w.i, w.j), pc, id);
-    if (k >= tile.k0 && k + 4 <= tile.k1) {
+  pitch_dispatch(P, [&](auto pm_) {
+    constexpr int PM = decltype(pm_)::value;
+    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
+      const int k = 4 * w.q;
+      Q4<T> pc, id;
+      const Q4<T> a =
+          apply_quad<T, PM>(g, ci, stab, pnew, k, P, w.i, w.j, qg.interior(k, w.i, w.j), pc, id);
+      if (k >= tile.k0 && k + 4 <= tile.k1) {
 #pragma unroll
-      for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
-      vst4<T>(po + k, pc);
-      vst4<T>(qs + k, a);
-    } else {
+        for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
+        vst4<T>(po + k, pc);
+        vst4<T>(qs + k, a);
+      } else {
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
-        if (k + e >= tile.k0 && k + e < tile.k1) acc += pc.v[e] * a.v[e];
-      store_masked<T>(po, pc, k, tile.k0, tile.k1);
-      store_masked<T>(qs, a, k, tile.k0, tile.k1);
+        for (int e = 0; e < 4; ++e)
+          if (k + e >= tile.k0 && k + e < tile.k1) acc += pc.v[e] * a.v[e];
+        store_masked<T>(po, pc, k, tile.k0, tile.k1);
+        store_masked<T>(qs, a, k, tile.k0, tile.k1);
+      }
     }
-  }
+  });
   const double t = block_sum(double(acc));
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }

@@ -86,6 +86,7 @@ typedef struct eqf_solver_opts {
   int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
   int32_t tile_nodes; /* target nodes per row tile of the finest level (0: default) */
   int32_t krylov;     /* EQF_KRYLOV_*: AUTO = BiCGSTAB iff some trap has advection */
+  int32_t fuse_levels; /* temporally blocked V(2,2) level kernels where they fit (1) */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;

@@ -205,3 +205,21 @@ def test_batched_sample_against_oracle(lib):
         for k in range(len(sub)):
             assert rel(b.read_nodal(k), refs[k]["u"][0]) <= 1e-6
             assert rel(b.read_cells(k), refs[k]["cells"][0]) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
+def test_fused_and_unfused_level_kernels_agree(lib, precision):
+    """The temporally blocked level kernels (default) and the step-by-step kernels
+    solve the same systems: both meet the oracle's tolerance and agree closely."""
+    t = wl.scaled(wl.single_large(1), 256, 128, n_cells=2000)
+    ref = hsld.run_trap(t, steps=12)
+    out = []
+    for fuse in (1, 0):
+        with F.TrapBatch([tparams(t)], F.default_opts(precision, use_graph=1,
+                                                      fuse_levels=fuse)) as b:
+            b.set_cells(0, t.cell_xy, t.cell_s)
+            b.step(12)
+            u = b.read_nodal(0)
+            assert rel(u, ref["u"][0]) <= TOL[precision]
+            out.append(u)
+    assert rel(out[0], out[1]) <= TOL[precision]
