@@ -229,6 +229,8 @@ static size_t guarded_bytes(long long ka, long long kb, int tsize) {
 struct Level {
   std::vector<LevelGeom> geom;  // per trap
   std::vector<Tile> tiles;
+  std::vector<Tile2> tiles2;  // 2-D tiles of the fused level kernels
+  DevBuf<Tile2> dtiles2;
   long long nodes = 0;
   DevBuf<LevelGeom> dgeom;
   DevBuf<Tile> dtiles;
@@ -327,6 +329,8 @@ class Batch {
   std::vector<Level> L;
   std::vector<TileRange> range;  // fine tiles per trap
   DevBuf<TileRange> drange;
+  DevBuf<TileRange> drange2;     // fine 2-D tiles per trap (partials of the fused kernels)
+  bool fused0 = false;           // the finest level runs the fused level kernels
   DevBuf<CgState> dstate;
   DevBuf<int> d_ir_done, d_cg_skip, d_fail;
   DevBuf<int> d_frozen;  // per trap: nonzero = inactive (skipped by every kernel of a step)
@@ -407,8 +411,22 @@ class Batch {
   void build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
                       DevBuf<int>& seg_start, int& nseg_out, const double* xy, const double* s,
                       const double* val);
+  // nodes of a trap (the caller's compact grid order, nx+1 per row) ...
   long long fine_nodes(int t) const {
     return (long long)(L[0].geom[t].nx + 1) * (L[0].geom[t].ny + 1);
+  }
+  // ... and the device span of its rows (pitch P per row)
+  long long fine_span(int t) const { return (long long)L[0].geom[t].P * (L[0].geom[t].ny + 1); }
+  // compact host grid <-> pitched device rows
+  void copy_field_to_device(double* dst, const double* src, int t, cudaStream_t s) const {
+    const LevelGeom& g = L[0].geom[t];
+    EQF_CK(cudaMemcpy2DAsync(dst, g.P * sizeof(double), src, (g.nx + 1) * sizeof(double),
+                             (g.nx + 1) * sizeof(double), g.ny + 1, cudaMemcpyHostToDevice, s));
+  }
+  void copy_field_to_host(double* dst, const double* src, int t, cudaStream_t s) const {
+    const LevelGeom& g = L[0].geom[t];
+    EQF_CK(cudaMemcpy2DAsync(dst, (g.nx + 1) * sizeof(double), src, g.P * sizeof(double),
+                             (g.nx + 1) * sizeof(double), g.ny + 1, cudaMemcpyDeviceToHost, s));
   }
   void sync() { EQF_CK(cudaStreamSynchronize(stream)); }
   void check_fail();
@@ -451,7 +469,7 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
   d_cg_skip.alloc(ntraps);
   d_fail.alloc(1);
   EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
-  dpart.alloc(3 * (size_t)L[0].ntiles());
+  dpart.alloc(3 * std::max((size_t)L[0].ntiles(), L[0].tiles2.size()));
   if (opts.precision == EQF_PREC_FP32_IR)
     work.reset(new Work<float>(*this));
   else
@@ -509,7 +527,7 @@ static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solv
         if (nx >= 4) nx = (nx + 1) / 2;
         if (ny >= 4) ny = (ny + 1) / 2;
       }
-      const double nn = (double)(((nx + 1) * (ny + 1) + 31) / 32 * 32);
+      const double nn = (double)((((nx + 1 + 3) & ~3ll) * (ny + 1) + 31) / 32 * 32);
       if (l == 0) n0 += nn;
       nall += nn;
     }
@@ -563,7 +581,8 @@ void Batch::build_levels() {
       }
       interior_constants(g);
       spectrum_bounds(g);
-      g.inv_pitch = 1.0f / (float)(g.nx + 1);
+      g.P = (g.nx + 1 + 3) & ~3;
+      g.inv_pitch = 1.0f / (float)g.P;
       cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
       L[l].geom[t] = g;
     }
@@ -577,9 +596,12 @@ void Batch::build_levels() {
     for (int t = 0; t < ntraps; ++t) {
       LevelGeom& g = L[l].geom[t];
       g.off = off;
-      const long long P = g.nx + 1;
+      const long long P = g.P;
       const long long n = P * (g.ny + 1);
-      if (l > 0) g.fine_off = L[l - 1].geom[t].off;
+      if (l > 0) {
+        g.fine_off = L[l - 1].geom[t].off;
+        g.fine_P = L[l - 1].geom[t].P;
+      }
       const long long tgt =
           (!tile_target.empty() && tile_target[t] > 0) ? tile_target[t] : target;
       const int R = (int)std::max<long long>(1, tgt / P);
@@ -587,6 +609,13 @@ void Batch::build_levels() {
         const int r1 = std::min(g.ny + 1, r0 + R);
         L[l].tiles.push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
       }
+      // 2-D tiles of the fused kernels: column blocks of at most 128 nodes
+      const int CW = (int)std::min<long long>(128, P);
+      const int R2 = (int)std::max<long long>(2, tgt / CW);
+      for (int r0 = 0; r0 <= g.ny; r0 += R2)
+        for (int c0 = 0; c0 < P; c0 += CW)
+          L[l].tiles2.push_back(Tile2{t, r0, std::min(g.ny + 1, r0 + R2), c0,
+                                      (int)std::min<long long>(P, c0 + CW)});
       off = align_up(off + n, 32);
     }
     L[l].nodes = off;
@@ -595,6 +624,8 @@ void Batch::build_levels() {
     L[l].dgeom.upload(L[l].geom.data(), ntraps, stream);
     L[l].dtiles.alloc(L[l].tiles.size());
     L[l].dtiles.upload(L[l].tiles.data(), L[l].tiles.size(), stream);
+    L[l].dtiles2.alloc(L[l].tiles2.size());
+    L[l].dtiles2.upload(L[l].tiles2.data(), L[l].tiles2.size(), stream);
     std::vector<float> tf((size_t)ntraps * kTabPerTrap);
     std::vector<double> td((size_t)ntraps * kTabPerTrap);
     for (int t = 0; t < ntraps; ++t) {
@@ -644,7 +675,7 @@ void Batch::build_levels() {
     Level& Lv = L[l];
     for (const Tile& tl : Lv.tiles) {
       const LevelGeom& g = Lv.geom[tl.geom];
-      const long long P = g.nx + 1, n = P * (g.ny + 1), na = align_up(n, 32);
+      const long long P = g.P, n = P * (g.ny + 1), na = align_up(n, 32);
       (void)n;
       const long long ka = (long long)tl.k0 - P - 1;  // guarded halo window
       const long long kb = (long long)tl.k1 + P + 1;
@@ -668,25 +699,12 @@ void Batch::build_levels() {
       if (l > 0) {  // restriction into level l stages fine rows f(r0)-1 .. f(r1-1)+1
         const LevelGeom& f = L[l - 1].geom[tl.geom];
         auto c2f = [](int K, int nf, int h) { return h ? std::min(2 * K, nf) : K; };
-        const long long PF = f.nx + 1;
+        const long long PF = f.P;
         long long fr0 = std::max(0, c2f(tl.r0, f.ny, g.cy) - 1);
         long long fr1 = std::min(f.ny + 1, c2f(tl.r1 - 1, f.ny, g.cy) + 2);
         Lv.sm_restrict = std::max(Lv.sm_restrict,
                                   kSmemHeader + staged_bytes(fr0 * PF, fr1 * PF, tsz,
                                                              align_up(PF * (f.ny + 1), 32)));
-      }
-      if (l + 1 < nlev) {  // fused level kernels (windows as fused_win / up_coarse_rows)
-        const FusedWin w = fused_win(tl.k0, tl.k1, (int)P);
-        const LevelGeom& c = L[l + 1].geom[tl.geom];
-        int clo = 0, chi = 0;
-        up_coarse_rows(g, c, w, clo, chi);
-        const long long PC = c.nx + 1;
-        const size_t w1 = guarded_bytes(w.w1a, w.w1b, tsz), w2 = guarded_bytes(w.w2a, w.w2b, tsz);
-        const size_t tab = (size_t)kTabPerTrap * tsz;
-        Lv.sm_down = std::max(Lv.sm_down, kSmemHeader + 2 * w1 + w2 + tab);
-        Lv.sm_up = std::max(Lv.sm_up, kSmemHeader + w1 + 2 * w2 + tab +
-                                          staged_bytes(clo * PC, (chi + 1) * PC, tsz,
-                                                       align_up(PC * (c.ny + 1), 32)));
       }
       if (l + 1 < nlev) {  // prolongation into level l stages coarse rows lo(r0) .. hi(r1-1)
         const LevelGeom& c = L[l + 1].geom[tl.geom];
@@ -696,11 +714,24 @@ void Batch::build_levels() {
         auto f2c_hi = [](int f, int nf, int h) {
           return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2 + 1));
         };
-        const long long PC = c.nx + 1;
+        const long long PC = c.P;
         const long long lo = f2c_lo(tl.r0, g.ny, c.cy), hi = f2c_hi(tl.r1 - 1, g.ny, c.cy);
         Lv.sm_prolong = std::max(Lv.sm_prolong,
                                  kSmemHeader + staged_bytes(lo * PC, (hi + 1) * PC, tsz,
                                                             align_up(PC * (c.ny + 1), 32)));
+      }
+    }
+    if (l + 1 < nlev) {  // fused level kernels (windows as in k_down / k_up)
+      const LevelGeom* gc = L[l + 1].geom.data();
+      for (const Tile2& t2 : Lv.tiles2) {
+        const LevelGeom& g = Lv.geom[t2.geom];
+        const Win w1 = win_grow(t2, 2, 8), w2 = win_grow(t2, 1, 4);
+        const Win wc = up_coarse_win(g, gc[t2.geom], w1);
+        const size_t tab = (size_t)kTabPerTrap * tsz;
+        Lv.sm_down = std::max(Lv.sm_down, kSmemHeader + 2 * win_bytes(w1, tsz) +
+                                              win_bytes(w2, tsz) + tab);
+        Lv.sm_up = std::max(Lv.sm_up, kSmemHeader + win_bytes(w1, tsz) + 2 * win_bytes(w2, tsz) +
+                                          win_bytes(wc, tsz) + tab);
       }
     }
     for (size_t v : {Lv.sm_cheb, Lv.sm_resid, Lv.sm_cgdir, Lv.sm_restrict, Lv.sm_prolong})
@@ -715,8 +746,8 @@ void Batch::build_levels() {
     Level& Lc = L[nlev - 1];
     size_t need = 0;
     for (const LevelGeom& g : Lc.geom) {
-      const long long n = (long long)(g.nx + 1) * (g.ny + 1), na = align_up(n, 32);
-      const long long gpad = ((g.nx + 2 + 7) / 8) * 8;
+      const long long n = (long long)g.P * (g.ny + 1), na = align_up(n, 32);
+      const long long gpad = ((g.P + 1 + 7) / 8) * 8;
       need = std::max(need, kSmemHeader + staged_bytes(0, n, tsz, na) +
                                 (size_t)(3 * na + 5 * gpad) * tsz);
     }
@@ -730,6 +761,16 @@ void Batch::build_levels() {
   }
   drange.alloc(ntraps);
   drange.upload(range.data(), ntraps, stream);
+  std::vector<TileRange> range2(ntraps, TileRange{0, 0});
+  for (int i = 0; i < (int)L[0].tiles2.size(); ++i) {
+    const int t = L[0].tiles2[i].geom;
+    if (range2[t].count == 0) range2[t].first = i;
+    range2[t].count++;
+  }
+  drange2.alloc(ntraps);
+  drange2.upload(range2.data(), ntraps, stream);
+  fused0 = nlev > 1 && opts.fuse_levels && opts.cheb_pre == 2 && opts.cheb_post == 2 &&
+           L[0].sm_down > 0;
   sync();
 }
 
@@ -875,9 +916,10 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
     // temporally blocked: pre-smoothing + residual, restriction, coarse correction,
     // prolongation + post-smoothing
     const int cd = lev > 0 ? KC_COARSE : KC_SMOOTH0;
+    const int nt2 = (int)Lv_.tiles2.size();
     EQF_RUN(B, cd,
-            (k_down<T><<<nt, kThreads, Lv_.sm_down, s>>>(G, tl, tab, skip, bl, cur, v.t.p,
-                                                          W)));
+            (k_down<T><<<nt2, kThreads, Lv_.sm_down, s>>>(G, Lv_.dtiles2.p, tab, skip, bl, cur,
+                                                           v.t.p, W)));
     const Level& Lc = B.L[lev + 1];
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
             (k_restrict<T><<<Lc.ntiles(), kThreads, Lc.sm_restrict, s>>>(
@@ -885,12 +927,12 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
     T* xc = vcycle(s, lev + 1, false);
     if (dot)
       EQF_RUN(B, cd,
-              (k_up<T, true><<<nt, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, tl, tab, skip, xc, bl,
-                                                            cur, oth, part, W)));
+              (k_up<T, true><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
+                                                             skip, xc, bl, cur, oth, part, W)));
     else
       EQF_RUN(B, cd,
-              (k_up<T, false><<<nt, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, tl, tab, skip, xc, bl,
-                                                             cur, oth, part, W)));
+              (k_up<T, false><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
+                                                              skip, xc, bl, cur, oth, part, W)));
     return oth;
   }
   // pre-smoothing (or the coarsest-level solve) from zero
@@ -983,7 +1025,8 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   for (int it = 0; it < B.opts.max_iters; ++it) {
     T* z = vcycle(s, 0, true);
     EQF_RUN(B, KC_SCALAR,
-            (k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
+            (k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
+                                       B.dstate.p, B.d_cg_skip.p)));
     if (it == 0)
       EQF_RUN(B, KC_CG_DIR,
               (k_cg_dir<T, true><<<nt, kThreads, L0.sm_cgdir, s>>>(
@@ -1228,7 +1271,7 @@ void Batch::rebuild_cells() {
   std::vector<double> scale(ntraps);
   for (int t = 0; t < ntraps; ++t) {
     const LevelGeom& g = L[0].geom[t];
-    cg[t] = CellGeom{g.off, g.nx, g.ny, g.hx, g.hy};
+    cg[t] = CellGeom{g.off, g.nx, g.ny, g.P, g.hx, g.hy};
     scale[t] = params[t].dt;
     std::copy(cell_xy[t].begin(), cell_xy[t].end(), xy.begin() + 2 * (size_t)cell_first[t]);
     std::copy(cell_s[t].begin(), cell_s[t].end(), sv.begin() + cell_first[t]);
@@ -1321,10 +1364,11 @@ __global__ void k_trap_reduce(const LevelGeom* __restrict__ G, const Tile* __res
   const Tile tile = tiles[first_tile + blockIdx.x];
   const LevelGeom g = G[tile.geom];
   const double* us = u + g.off;
-  const int P = g.nx + 1;
+  const int P = g.P;
   double acc = 0.0;
   for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
     const int k = w.k, i = w.i, j = w.j;
+    if (j > g.nx) continue;  // pad column
     if (what == 0) {  // 1^T M u
       const Sten<double> m = mass_stencil<double>(g, i, j);
       acc += (m.c + m.e + m.w + m.n + m.s + m.ne + m.sw) * us[k];
@@ -1547,7 +1591,7 @@ int eqf_set_active(eqf_batch* b, int32_t trap, int32_t active) {
     EQF_TRAP_CHECK(b, trap);
     Batch& B = *b->impl;
     const long long off = B.L[0].geom[trap].off;
-    const size_t n = (size_t)B.fine_nodes(trap);
+    const size_t n = (size_t)B.fine_span(trap);
     if (!active) {
       // both field buffers hold the frozen field, so reads see it whatever the parity
       EQF_CK(cudaMemcpyAsync(B.U[1 - B.cur].p + off, B.U[B.cur].p + off, n * sizeof(double),
@@ -1616,8 +1660,7 @@ int eqf_read_nodal_async(eqf_batch* b, int32_t trap, double* c) {
     EQF_TRAP_CHECK(b, trap);
     EQF_REQUIRE(c != nullptr, "null output");
     Batch& B = *b->impl;
-    EQF_CK(cudaMemcpyAsync(c, B.u_cur() + B.L[0].geom[trap].off,
-                           B.fine_nodes(trap) * sizeof(double), cudaMemcpyDeviceToHost, B.stream));
+    B.copy_field_to_host(c, B.u_cur() + B.L[0].geom[trap].off, trap, B.stream);
   });
 }
 
@@ -1674,10 +1717,9 @@ int eqf_set_nodal(eqf_batch* b, int32_t trap, const double* c) {
     EQF_REQUIRE(c != nullptr, "null field");
     Batch& B = *b->impl;
     const long long off = B.L[0].geom[trap].off;
-    EQF_CK(cudaMemcpyAsync(B.u_cur() + off, c, B.fine_nodes(trap) * sizeof(double),
-                           cudaMemcpyHostToDevice, B.stream));
+    B.copy_field_to_device(B.u_cur() + off, c, trap, B.stream);
     // a new field invalidates the increment history of the initial guess
-    EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_nodes(trap) * sizeof(float), B.stream));
+    EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
     EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
                                offsetof(eqf::CgState, gamma),
                            0, 2 * sizeof(double), B.stream));
@@ -1707,8 +1749,9 @@ int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
     ent.alloc(n);
     counts.alloc(B.L[0].nodes);
     EQF_CK(cudaMemsetAsync(counts.p, 0, B.L[0].nodes * sizeof(int), B.stream));
+    const eqf::LevelGeom& g0 = B.L[0].geom[trap];
     eqf::k_nodal_entries<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
-        (int)n, B.L[0].geom[trap].off, dn.p, ent.p, counts.p);
+        (int)n, g0.off, g0.nx + 1, g0.P, dn.p, ent.p, counts.p);
     EQF_LAUNCH_CHECK();
     int ns = 0;
     B.build_segments((int)n, ent.p, counts.p, perm, seg, ns, nullptr, nullptr, dv.p);
@@ -1733,8 +1776,7 @@ int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c) {
     EQF_TRAP_CHECK(b, trap);
     EQF_REQUIRE(c != nullptr, "null output");
     Batch& B = *b->impl;
-    EQF_CK(cudaMemcpyAsync(c, B.u_cur() + B.L[0].geom[trap].off, B.fine_nodes(trap) * sizeof(double),
-                           cudaMemcpyDeviceToHost, B.stream));
+    B.copy_field_to_host(c, B.u_cur() + B.L[0].geom[trap].off, trap, B.stream);
     B.sync();
     B.check_fail();
   });

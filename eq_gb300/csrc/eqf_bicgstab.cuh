@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const T* stab = stage_table<T>(sg, tab, ci);
   if (!sg.run()) return;
   T* ys = y + g.off;
-  const int P = g.nx + 1;
+  const int P = g.P;
   const QuadGeom qg(g, tile);
   T a0 = T(0), a1 = T(0);
   pitch_dispatch(P, [&](auto pm_) {

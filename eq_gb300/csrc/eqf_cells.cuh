@@ -17,7 +17,7 @@ namespace eqf {
 
 struct CellGeom {  // per trap: fine-level mesh for locating cells
   long long off;
-  int nx, ny;
+  int nx, ny, P;  // cells along x / y, device row pitch
   double hx, hy;
 };
 
@@ -30,16 +30,16 @@ __device__ __forceinline__ void locate(const CellGeom& g, double x, double y, in
   j = j < 0 ? 0 : (j > g.nx - 1 ? g.nx - 1 : j);
   i = i < 0 ? 0 : (i > g.ny - 1 ? g.ny - 1 : i);
   const double xi = X - j, eta = Y - i;
-  const int v0 = j + i * (g.nx + 1);
+  const int v0 = j + i * g.P;
   node[0] = v0;
-  node[2] = v0 + g.nx + 2;
+  node[2] = v0 + g.P + 1;
   if (xi >= eta) {
     node[1] = v0 + 1;
     wgt[0] = 1.0 - xi;
     wgt[1] = xi - eta;
     wgt[2] = eta;
   } else {
-    node[1] = v0 + g.nx + 1;
+    node[1] = v0 + g.P;
     wgt[0] = 1.0 - eta;
     wgt[1] = eta - xi;
     wgt[2] = xi;
@@ -157,11 +157,14 @@ __global__ void k_cells_values(int ncells, const double* __restrict__ ent_w,
 }
 
 // entries of explicit nodal increments: ent_node = off[trap] + node; counts[node]++
-__global__ void k_nodal_entries(int n, long long off, const long long* __restrict__ node,
-                                int* __restrict__ ent_node, int* __restrict__ counts) {
+// node[e] is a grid-order index (row length nx+1); the device rows have pitch P
+__global__ void k_nodal_entries(int n, long long off, int row, int P,
+                                const long long* __restrict__ node, int* __restrict__ ent_node,
+                                int* __restrict__ counts) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  const int gn = (int)(off + node[e]);
+  const long long k = node[e];
+  const int gn = (int)(off + (k / row) * P + k % row);
   ent_node[e] = gn;
   atomicAdd(&counts[gn], 1);
 }

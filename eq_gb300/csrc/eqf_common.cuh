@@ -3,7 +3,10 @@
 //
 // Mesh: eQ builds each HSL layer on RectangleMesh(p0, p1, nx, ny, "right")
 // (src/fHSL.cpp:164-172): vertex (i, j) at (j*hx, i*hy), natural index
-// k = j + i*(nx+1), each square cut along (i, j)-(i+1, j+1).  The stencil below is
+// j + i*(nx+1), each square cut along (i, j)-(i+1, j+1).  On the device a row is
+// stored with pitch P = nx+1 rounded up to a multiple of 4 (k = j + i*P): every row
+// starts 16-byte aligned, so rows, row segments and 4-node quads are aligned
+// vectors.  The pad columns nx+1 .. P-1 hold zeros and carry all-zero stencils.  The stencil below is
 // the assembled hslD bilinear form (fenics/hslD.ufl:31-49, cell kernel
 // fenics/hslD.h:3123-3262) for an isotropic tensor, written per node from the six
 // incident right triangles, plus the reaction scaling of the mass block.
@@ -36,10 +39,12 @@ struct Lens {
 struct LevelGeom {
   long long off;      // offset of node (0,0) in the level's arrays
   int nx, ny;         // cells along x / y (nodes: (nx+1)*(ny+1))
+  int P;              // row pitch: nx + 1 rounded up to a multiple of 4
   int trap;           // trap index in the batch
   unsigned walls;     // Dirichlet walls (WALL_* bits)
   int cx, cy;         // 1 if this level halves x / y relative to the finer level
   int fine_nx, fine_ny;  // cell counts of the finer level (for transfers)
+  int fine_P;            // row pitch of the finer level
   long long fine_off;    // node offset of this trap on the finer level
   int adv_on;            // advection present (disables the uniform-interior path)
   double hx, hy;         // regular spacing (host-side construction)
@@ -55,7 +60,7 @@ struct LevelGeom {
   float fC, fE, fN, fD, fCinv;
   float lam_max;          // upper bound of spectrum(D^-1 A)
   float lam_min;          // lower estimate (coarsest-level solve)
-  float inv_pitch;        // 1 / (nx + 1), for division-free row/column walks
+  float inv_pitch;        // 1 / P, for division-free row/column walks
   // Chebyshev-Jacobi step coefficients on this level's interval ([lam_max/ratio,
   // lam_max] for smoothing, [lam_min, lam_max] on the coarsest level), step s:
   // d_new = ch_old[s] d + ch_res[s] D^-1 r
@@ -70,8 +75,8 @@ EQF_HD const Lens<double>& lens<double>(const LevelGeom& g) { return g.ld; }
 template <>
 EQF_HD const Lens<float>& lens<float>(const LevelGeom& g) { return g.lf; }
 
-// Rows [r0, r1) of one trap on one level (one CTA each); k0 = r0*(nx+1) and
-// k1 = r1*(nx+1) are the node range.
+// Rows [r0, r1) of one trap on one level (one CTA each); k0 = r0*P and k1 = r1*P
+// are the node range.
 struct Tile {
   int geom;  // index into the level's LevelGeom array (= trap index)
   int k0, k1;

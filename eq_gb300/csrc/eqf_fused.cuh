@@ -1,9 +1,10 @@
-// Temporally blocked multigrid level kernels: each computes several smoothing
-// steps of one row tile in shared memory, on windows that shrink by one row (plus a
-// few nodes) per step, so the level's vectors cross HBM once per half V-cycle.
+// Temporally blocked multigrid level kernels on 2-D tiles: each computes several
+// smoothing steps of one tile (rows [r0, r1) x columns [c0, c1) of one trap) in
+// shared memory, on windows that shrink by one row and four columns per step, so a
+// level's vectors cross HBM once per half V-cycle:
 //
-//   k_down:  x1 = d1 = c0 D^-1 b                     (window W1 = tile +- 2 rows)
-//            x2 = x1 + c_old d1 + c1 D^-1 (b - A x1) (window W2 = tile +- 1 row)
+//   k_down:  x1 = d1 = c0 D^-1 b                     (window W1 = tile + 2 rows, 8 cols)
+//            x2 = x1 + c_old d1 + c1 D^-1 (b - A x1) (window W2 = tile + 1 row, 4 cols)
 //            t  = b - A x2                           (tile)      -> writes x2, t
 //   k_up:    x0 = x + P x_c                          (W1)
 //            x1 = x0 + c0 D^-1 (b - A x0)            (W2)
@@ -11,10 +12,16 @@
 //
 // These are the pre-smoothing (two Chebyshev-Jacobi steps from zero) + residual and
 // the prolongation + post-smoothing (two steps) of a V(2,2) cycle.  k_down evaluates
-// exactly the unfused sequence (same formulas, same operand order: bit-identical);
-// k_up recomputes the first step's direction as x1 - x0 instead of storing it.
+// exactly the step-by-step sequence (same formulas, same operand order); k_up
+// recomputes the first step's direction as x1 - x0 instead of storing it.
 // Algorithmic bytes per node (FP32): k_down reads b, writes x, t (12); k_up reads x,
-// b and a quarter-size x_c, writes x (13) -- against 44 and 45 for the unfused steps.
+// b and a quarter-size x_c, writes x (13) -- against 44 and 45 for the steps one by one.
+//
+// Windows are staged row by row with bulk copies (every device row starts 16-byte
+// aligned: the row pitch is a multiple of 4 nodes); window rows and columns outside
+// the grid are zero-filled and take the all-zero pad class, so they stay zero.  In
+// shared memory a window row is a multiple of 4 nodes long, so the neighbour rows of
+// a quad are at compile-time misalignments (0 above, 3 below).
 #pragma once
 #include "eqf_kernels.cuh"
 
@@ -24,46 +31,137 @@ namespace eqf {
 template <class T>
 constexpr int kFusedCtas = sizeof(T) == 4 ? 3 : 2;
 
-// Windows of the fused kernels (node ranges, multiples of 4), identical on host and
-// device.  W1 = tile +- (2 rows + 16 nodes), W2 = tile +- (1 row + 8 nodes): every
-// quad of W2 reads its neighbours inside W1, every quad of the tile inside W2.
-struct FusedWin {
-  int w1a, w1b, w2a, w2b;
+// One 2-D tile of a level: rows [r0, r1), columns [c0, c1) (multiples of 4, c1 <= P).
+struct Tile2 {
+  int geom;
+  int r0, r1, c0, c1;
 };
-EQF_HD FusedWin fused_win(int k0, int k1, int P) {
-  FusedWin w;
-  w.w1a = (k0 - 2 * P - 16) & ~3;
-  w.w1b = (k1 + 2 * P + 16 + 3) & ~3;
-  w.w2a = (k0 - P - 8) & ~3;
-  w.w2b = (k1 + P + 8 + 3) & ~3;
+
+// A staged window: rows [ra, rb), columns [ca, cb) of a trap's array, `S = cb - ca`
+// nodes per shared-memory row.
+struct Win {
+  int ra, rb, ca, cb;
+  EQF_HD int S() const { return cb - ca; }
+  EQF_HD int count() const { return (rb - ra) * (cb - ca); }
+};
+EQF_HD Win win_grow(const Tile2& t, int rows, int cols) {
+  return Win{t.r0 - rows, t.r1 + rows, t.c0 - cols, t.c1 + cols};
+}
+
+// Coarse window of the prolongation into the fine window w1 (fine rows and columns
+// clamped to the grid), columns widened to multiples of 4.
+EQF_HD Win up_coarse_win(const LevelGeom& g, const LevelGeom& c, const Win& w1) {
+  auto f2c_lo = [](int f, int nf, int h) {
+    return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2));
+  };
+  auto f2c_hi = [](int f, int nf, int h) {
+    return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2 + 1));
+  };
+  auto clampi = [](int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); };
+  const int fa = clampi(w1.ra, 0, g.ny), fb = clampi(w1.rb - 1, 0, g.ny);
+  const int ja = clampi(w1.ca, 0, g.nx), jb = clampi(w1.cb - 1, 0, g.nx);
+  Win w;
+  w.ra = f2c_lo(fa, g.ny, c.cy);
+  w.rb = f2c_hi(fb, g.ny, c.cy) + 1;
+  w.ca = f2c_lo(ja, g.nx, c.cx) & ~3;
+  w.cb = (f2c_hi(jb, g.nx, c.cx) + 1 + 3) & ~3;
   return w;
 }
-EQF_HD int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
 
-// Walks the quads k = ka + 4 tid, ka + 4 (tid + bd), ... of a window that may start
-// before the trap (negative k), keeping (i, j) = floor-divmod(k, P).
-struct WinWalk {
-  int k, i, j, di, dj, P;
-  __device__ __forceinline__ WinWalk(int ka, int P_) : P(P_) {
-    k = ka + 4 * (int)threadIdx.x;
-    i = floor_div(k, P);
-    j = k - i * P;
-    const int st = 4 * (int)blockDim.x;
-    di = st / P;
-    dj = st - di * P;
+// Shared-memory bytes of a window (with the 16-byte pad every region keeps after it).
+EQF_HD size_t win_bytes(const Win& w, int tsize) {
+  return (size_t)(((long long)w.count() * tsize + 15) & ~15ll) + 16;
+}
+
+// One array's window to stage: every thread zero-fills the out-of-grid parts,
+// thread 0 counts the bytes, warp 0 issues one bulk copy per in-grid row segment.
+template <class T>
+struct RowStage {
+  const T* src;  // trap base of the array (node (0,0))
+  T* dst;        // window in shared memory
+  Win w;
+  int P, nrows;  // array row pitch and row count (ny + 1)
+  __device__ __forceinline__ uint32_t row_bytes(int r, int& a, int& b) const {
+    a = w.ca > 0 ? w.ca : 0;
+    b = w.cb < P ? w.cb : P;
+    if (r < 0 || r >= nrows || b <= a) return 0u;
+    return (uint32_t)(b - a) * (uint32_t)sizeof(T);
   }
-  __device__ __forceinline__ void next() {
-    k += 4 * (int)blockDim.x;
-    i += di;
-    j += dj;
-    if (j >= P) {
-      j -= P;
-      ++i;
+  __device__ __forceinline__ void zero_guards() const {
+    const int S = w.S();
+    const int a = w.ca > 0 ? w.ca : 0, b = w.cb < P ? w.cb : P;
+    for (int r = w.ra + (int)(threadIdx.x >> 5); r < w.rb; r += (int)(blockDim.x >> 5)) {
+      T* row = dst + (r - w.ra) * S;
+      const bool in = r >= 0 && r < nrows && b > a;
+      for (int c = (int)(threadIdx.x & 31); c < S; c += 32) {
+        const int col = w.ca + c;
+        if (!in || col < a || col >= b) row[c] = T(0);
+      }
+    }
+  }
+  __device__ __forceinline__ uint32_t total() const {
+    uint32_t t = 0;
+    for (int r = w.ra; r < w.rb; ++r) {
+      int a, b;
+      t += row_bytes(r, a, b);
+    }
+    return t;
+  }
+  __device__ __forceinline__ void issue(uint64_t* bar) const {  // warp 0
+    for (int r = w.ra + (int)threadIdx.x; r < w.rb; r += 32) {
+      int a, b;
+      const uint32_t n = row_bytes(r, a, b);
+      if (n)
+        bulk_copy_g2s(dst + (r - w.ra) * w.S() + (a - w.ca), src + (size_t)r * P + a, n, bar);
     }
   }
 };
 
-// The quad's nodes are all uniform-interior nodes (no tile bounds involved).
+// Stages the windows on one mbarrier; returns false, uniformly for the CTA, if the
+// bounded wait gave up (device error flag set).
+template <class T, int N>
+__device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st)[N]) {
+#pragma unroll
+  for (int q = 0; q < N; ++q) st[q].zero_guards();
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    uint32_t tot = 0;
+#pragma unroll
+    for (int q = 0; q < N; ++q) tot += st[q].total();
+    mbar_expect_tx(bar, tot);
+  }
+  __syncwarp();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int q = 0; q < N; ++q) st[q].issue(bar);
+  }
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    ok = false;
+    for (int it = 0; it < (1 << 22) && !ok; ++it) ok = mbar_try_wait(bar, 0);
+    if (!ok) {
+      for (int it = 0; it < (1 << 20) && !ok; ++it) ok = mbar_try_wait(bar, 0);
+      if (!ok) atomicExch(&g_eqf_device_error, 1);
+    }
+  }
+  return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+// Quads of a window: quad q at window row q / QW, columns 4 (q % QW) .. +3.
+struct WinQuads {
+  int QW, n;
+  float inv;
+  __device__ __forceinline__ explicit WinQuads(const Win& w) {
+    QW = w.S() >> 2;
+    n = (w.rb - w.ra) * QW;
+    inv = 1.0f / (float)QW;
+  }
+  __device__ __forceinline__ void at(int q, int& row, int& cq) const {
+    div_pitch(q, QW, inv, row, cq);
+  }
+};
+
+// The quad's nodes are all uniform-interior nodes.
 __device__ __forceinline__ bool quad_interior(const LevelGeom& g, int i, int j) {
   return !g.adv_on && i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 5;
 }
@@ -71,8 +169,8 @@ __device__ __forceinline__ bool quad_interior(const LevelGeom& g, int i, int j) 
 // 1 / diagonal of the quad's nodes (the same values every stencil path uses).
 template <class T>
 __device__ __forceinline__ Q4<T> inv_diag_quad(const LevelGeom& g, const Interior<T>& ci,
-                                               const T* __restrict__ stab, int P, int i0,
-                                               int j0, bool inner) {
+                                               const T* __restrict__ stab, int i, int j0,
+                                               bool inner) {
   Q4<T> id;
   if (inner) {
 #pragma unroll
@@ -80,27 +178,16 @@ __device__ __forceinline__ Q4<T> inv_diag_quad(const LevelGeom& g, const Interio
   } else {
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      int i, j;
-      quad_node(P, i0, j0, e, i, j);
       if (g.adv_on) {
         T c[8];
-        coef_general<T>(g, i, j, c);
+        coef_general<T>(g, i, j0 + e, c);
         id.v[e] = c[7];
       } else {
-        id.v[e] = stab[node_class_clamped(g, i, j) * kTabStride + 7];
+        id.v[e] = stab[node_class_clamped(g, i, j0 + e) * kTabStride + 7];
       }
     }
   }
   return id;
-}
-
-// Zeroes the nodes of a quad that lie outside the trap's grid [0, n).
-template <class T>
-__device__ __forceinline__ void mask_outside(Q4<T>& q, int k, int n) {
-  if (k >= 0 && k + 4 <= n) return;
-#pragma unroll
-  for (int e = 0; e < 4; ++e)
-    if (k + e < 0 || k + e >= n) q.v[e] = T(0);
 }
 
 template <class T>
@@ -109,202 +196,205 @@ __device__ __forceinline__ T* carve(Stager& st, int count) {
   st.cur += (((uint32_t)count * sizeof(T) + 15u) & ~15u) + 16u;
   return p;
 }
+// Local index of node (i, j) in window w.
+__device__ __forceinline__ int wl(const Win& w, int i, int j) {
+  return (i - w.ra) * w.S() + (j - w.ca);
+}
 
-// Pre-smoothing (two steps from zero) and residual of one row tile.
+// Pre-smoothing (two steps from zero) and residual of one tile.
 template <class T>
 __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
-    k_down(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+    k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
-           T* __restrict__ x, T* __restrict__ t,
-           unsigned long long* work) {
-  const Tile tile = tiles[blockIdx.x];
+           T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+  const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
-  count_work(work, tile);
+  if (work && threadIdx.x == 0)
+    atomicAdd(work, (unsigned long long)(tile.r1 - tile.r0) * (tile.c1 - tile.c0));
   const ChebCoef c0 = cheb_at(g, 0), c1 = cheb_at(g, 1);
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
-  const int P = g.nx + 1, n = P * (g.ny + 1), na = padded_len(g);
-  const FusedWin w = fused_win(tile.k0, tile.k1, P);
-  Stager st(eqf_smem);
-  const View<T> bv = st.add_guarded(b + g.off, w.w1a, w.w1b, na);
-  T* x1p = carve<T>(st, w.w1b - w.w1a);
-  T* x2p = carve<T>(st, w.w2b - w.w2a);
+  const int P = g.P;
+  const Win w1 = win_grow(tile, 2, 8), w2 = win_grow(tile, 1, 4);
+  const Win wt = win_grow(tile, 0, 0);
+  Stager st(eqf_smem);  // used for the layout (barrier + regions) and the class table
+  T* bp = carve<T>(st, w1.count());
+  T* x1p = carve<T>(st, w1.count());
+  T* x2p = carve<T>(st, w2.count());
   const T* stab = stage_table<T>(st, tab, ci);
-  if (!st.run()) return;
-  const View<T> x1v{x1p, w.w1a}, x2v{x2p, w.w2a};
+  const RowStage<T> rs[1] = {{b + g.off, bp, w1, P, g.ny + 1}};
+  if (!stage_rows<T, 1>(st.bar, rs)) return;
+  const int S1 = w1.S(), S2 = w2.S();
   // step 1 from zero (pointwise) on W1
-  for (WinWalk q(w.w1a, P); q.k < w.w1b; q.next()) {
-    const Q4<T> bq = bv.quad(q.k);
-    const Q4<T> id = inv_diag_quad<T>(g, ci, stab, P, q.i, q.j, quad_interior(g, q.i, q.j));
-    Q4<T> d;
+  {
+    const WinQuads wq(w1);
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = w1.ra + row, j = w1.ca + 4 * cq, kl = row * S1 + 4 * cq;
+      const Q4<T> bq = vld4<T>(bp + kl);
+      const Q4<T> id = inv_diag_quad<T>(g, ci, stab, i, j, quad_interior(g, i, j));
+      Q4<T> d;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) d.v[e] = (T(c0.c_res) * bq.v[e]) * id.v[e];
-    mask_outside(d, q.k, n);
-    vst4<T>(x1p + (q.k - w.w1a), d);
+      for (int e = 0; e < 4; ++e) d.v[e] = (T(c0.c_res) * bq.v[e]) * id.v[e];
+      vst4<T>(x1p + kl, d);
+    }
   }
   __syncthreads();
   // step 2 on W2 (d1 = x1)
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (WinWalk q(w.w2a, P); q.k < w.w2b; q.next()) {
+  {
+    const WinQuads wq(w2);
+    const View<T> x1v{x1p, 0};
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = w2.ra + row, j = w2.ca + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, PM>(g, ci, stab, x1v, q.k, P, q.i, q.j,
-                                     quad_interior(g, q.i, q.j), xc, id);
-      const Q4<T> bq = bv.quad(q.k);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w1, i, j), S1, i, j,
+                                        quad_interior(g, i, j), xc, id);
+      const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
         xn.v[e] = xc.v[e] + cheb_dir<T, false>(c1, bq.v[e], ax.v[e], id.v[e], xc.v[e]);
-      mask_outside(xn, q.k, n);
-      vst4<T>(x2p + (q.k - w.w2a), xn);
+      vst4<T>(x2p + row * S2 + 4 * cq, xn);
     }
-  });
+  }
   __syncthreads();
   // residual on the tile; store x2 and t
-  T* xs = x + g.off;
-  T* ts = t + g.off;
-  const QuadGeom qg(g, tile);
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (QuadWalk q(g, tile.k0 >> 2); 4 * q.q < tile.k1; q.next()) {
-      const int k = 4 * q.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+  {
+    const WinQuads wq(wt);
+    const View<T> x2v{x2p, 0};
+    T* xs = x + g.off;
+    T* ts = t + g.off;
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = tile.r0 + row, j = tile.c0 + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax =
-          apply_quad<T, PM>(g, ci, stab, x2v, k, P, q.i, q.j, qg.interior(k, q.i, q.j), xc, id);
-      const Q4<T> bq = bv.quad(k);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x2v, wl(w2, i, j), S2, i, j,
+                                        quad_interior(g, i, j), xc, id);
+      const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> r;
 #pragma unroll
       for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
-      if (full) {
-        vst4<T>(xs + k, xc);
-        vst4<T>(ts + k, r);
-      } else {
-        store_masked<T>(xs, xc, k, tile.k0, tile.k1);
-        store_masked<T>(ts, r, k, tile.k0, tile.k1);
-      }
+      const size_t k = (size_t)i * P + j;
+      vst4<T>(xs + k, xc);
+      vst4<T>(ts + k, r);
     }
-  });
+  }
 }
 
-// Coarse rows a fused up-kernel tile stages: those the prolongation of the fine rows
-// of W1 (clamped to the grid) reads.
-EQF_HD void up_coarse_rows(const LevelGeom& g, const LevelGeom& c, const FusedWin& w, int& lo,
-                           int& hi) {
-  const int P = g.nx + 1;
-  int fa = floor_div(w.w1a, P), fb = floor_div(w.w1b - 1, P);
-  fa = fa < 0 ? 0 : (fa > g.ny ? g.ny : fa);
-  fb = fb < 0 ? 0 : (fb > g.ny ? g.ny : fb);
-  auto f2c_lo = [](int f, int nf, int h) {
-    return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2));
-  };
-  auto f2c_hi = [](int f, int nf, int h) {
-    return !h ? f : ((f & 1) == 0 ? f / 2 : (f == nf ? (f + 1) / 2 : (f - 1) / 2 + 1));
-  };
-  lo = f2c_lo(fa, g.ny, c.cy);
-  hi = f2c_hi(fb, g.ny, c.cy);
-}
-
-// Prolongation and post-smoothing (two steps) of one row tile: reads x (xin) and the
+// Prolongation and post-smoothing (two steps) of one tile: reads x (xin) and the
 // coarse correction, writes x2 to xout (another buffer: neighbouring tiles still
 // stage xin).  DOT adds a partial of b.x2 (r.z of the Krylov iteration).
 template <class T, bool DOT>
 __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_up(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
-         const Tile* __restrict__ tiles, const T* __restrict__ tabs,
-         const int* __restrict__ skip, const T* __restrict__ xc,
-         const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
-         double* __restrict__ part, unsigned long long* work) {
-  const Tile tile = tiles[blockIdx.x];
+         const Tile2* __restrict__ tiles, const T* __restrict__ tabs,
+         const int* __restrict__ skip, const T* __restrict__ xc, const T* __restrict__ b,
+         const T* __restrict__ xin, T* __restrict__ xout, double* __restrict__ part,
+         unsigned long long* work) {
+  const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
     if (DOT && threadIdx.x == 0) part[blockIdx.x] = 0.0;
     return;
   }
-  count_work(work, tile);
+  if (work && threadIdx.x == 0)
+    atomicAdd(work, (unsigned long long)(tile.r1 - tile.r0) * (tile.c1 - tile.c0));
   const LevelGeom& c = Gc[tile.geom];
   const ChebCoef c0 = cheb_at(g, 0), c1 = cheb_at(g, 1);
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
-  const int P = g.nx + 1, n = P * (g.ny + 1), na = padded_len(g);
-  const int PC = c.nx + 1;
-  const FusedWin w = fused_win(tile.k0, tile.k1, P);
-  int clo, chi;
-  up_coarse_rows(g, c, w, clo, chi);
+  const int P = g.P;
+  const Win w1 = win_grow(tile, 2, 8), w2 = win_grow(tile, 1, 4);
+  const Win wt = win_grow(tile, 0, 0);
+  const Win wc = up_coarse_win(g, c, w1);
   Stager st(eqf_smem);
-  const View<T> xv = st.add_guarded(xin + g.off, w.w1a, w.w1b, na);
-  const View<T> bv = st.add_guarded(b + g.off, w.w2a, w.w2b, na);
-  const View<T> cv = st.add(xc + c.off, clo * PC, (chi + 1) * PC, padded_len(c));
-  T* x1p = carve<T>(st, w.w2b - w.w2a);
+  T* xp = carve<T>(st, w1.count());
+  T* bp = carve<T>(st, w2.count());
+  T* cp = carve<T>(st, wc.count());
+  T* x1p = carve<T>(st, w2.count());
   const T* stab = stage_table<T>(st, tab, ci);
-  if (!st.run()) return;
-  // x0 = x + P x_c on W1 (in place; nodes outside the grid stay zero)
+  const RowStage<T> rs[3] = {{xin + g.off, xp, w1, P, g.ny + 1},
+                             {b + g.off, bp, w2, P, g.ny + 1},
+                             {xc + c.off, cp, wc, c.P, c.ny + 1}};
+  if (!stage_rows<T, 3>(st.bar, rs)) return;
+  const int S1 = w1.S(), S2 = w2.S(), SC = wc.S();
+  // x0 = x + P x_c on the in-grid nodes of W1 (in place)
   {
-    T* x0 = const_cast<T*>(xv.p);
-    const int ka = w.w1a > 0 ? w.w1a : 0, kb = w.w1b < n ? w.w1b : n;
-    for (int k = ka + (int)threadIdx.x; k < kb; k += blockDim.x) {
-      const int i = k / P, j = k - i * P;
+    const int n1 = w1.count();
+    const float inv1 = 1.0f / (float)S1;
+    for (int e = threadIdx.x; e < n1; e += blockDim.x) {
+      int row, col;
+      div_pitch(e, S1, inv1, row, col);
+      const int i = w1.ra + row, j = w1.ca + col;
+      if (i < 0 || i > g.ny || j < 0 || j > g.nx) continue;
       int i0, i1, j0, j1;
       fine_to_coarse(i, g.ny, c.cy, i0, i1);
       fine_to_coarse(j, g.nx, c.cx, j0, j1);
+      const T* cr0 = cp + (i0 - wc.ra) * SC - wc.ca;
+      const T* cr1 = cp + (i1 - wc.ra) * SC - wc.ca;
       T v;
       if (i0 == i1 && j0 == j1)
-        v = cv[j0 + i0 * PC];
+        v = cr0[j0];
       else if (i0 == i1)
-        v = T(0.5) * (cv[j0 + i0 * PC] + cv[j1 + i0 * PC]);
+        v = T(0.5) * (cr0[j0] + cr0[j1]);
       else if (j0 == j1)
-        v = T(0.5) * (cv[j0 + i0 * PC] + cv[j0 + i1 * PC]);
+        v = T(0.5) * (cr0[j0] + cr1[j0]);
       else
-        v = T(0.5) * (cv[j0 + i0 * PC] + cv[j1 + i1 * PC]);
-      x0[k - xv.a] += v;
+        v = T(0.5) * (cr0[j0] + cr1[j1]);  // on the coarse diagonal
+      xp[e] += v;
     }
   }
   __syncthreads();
-  const View<T> x1v{x1p, w.w2a};
   // first step (no previous direction) on W2
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (WinWalk q(w.w2a, P); q.k < w.w2b; q.next()) {
+  {
+    const WinQuads wq(w2);
+    const View<T> xv{xp, 0};
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = w2.ra + row, j = w2.ca + 4 * cq;
       Q4<T> x0q, id;
-      const Q4<T> ax = apply_quad<T, PM>(g, ci, stab, xv, q.k, P, q.i, q.j,
-                                     quad_interior(g, q.i, q.j), x0q, id);
-      const Q4<T> bq = bv.quad(q.k);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, wl(w1, i, j), S1, i, j,
+                                        quad_interior(g, i, j), x0q, id);
+      const Q4<T> bq = vld4<T>(bp + row * S2 + 4 * cq);
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
         xn.v[e] = x0q.v[e] + cheb_dir<T, true>(c0, bq.v[e], ax.v[e], id.v[e], T(0));
-      mask_outside(xn, q.k, n);
-      vst4<T>(x1p + (q.k - w.w2a), xn);
+      vst4<T>(x1p + row * S2 + 4 * cq, xn);
     }
-  });
+  }
   __syncthreads();
   // second step on the tile, d1 = x1 - x0
-  T* xo = xout + g.off;
-  const QuadGeom qg(g, tile);
   T acc = T(0);
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (QuadWalk q(g, tile.k0 >> 2); 4 * q.q < tile.k1; q.next()) {
-      const int k = 4 * q.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
+  {
+    const WinQuads wq(wt);
+    const View<T> x1v{x1p, 0};
+    T* xo = xout + g.off;
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = tile.r0 + row, j = tile.c0 + 4 * cq;
       Q4<T> x1q, id;
-      const Q4<T> ax =
-          apply_quad<T, PM>(g, ci, stab, x1v, k, P, q.i, q.j, qg.interior(k, q.i, q.j), x1q, id);
-      const Q4<T> bq = bv.quad(k);
-      const Q4<T> x0q = xv.quad(k);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w2, i, j), S2, i, j,
+                                        quad_interior(g, i, j), x1q, id);
+      const Q4<T> bq = vld4<T>(bp + wl(w2, i, j));
+      const Q4<T> x0q = vld4<T>(xp + wl(w1, i, j));
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        xn.v[e] = x1q.v[e] + cheb_dir<T, false>(c1, bq.v[e], ax.v[e], id.v[e], x1q.v[e] - x0q.v[e]);
-        if (DOT && (full || (k + e >= tile.k0 && k + e < tile.k1))) acc += bq.v[e] * xn.v[e];
+        xn.v[e] =
+            x1q.v[e] + cheb_dir<T, false>(c1, bq.v[e], ax.v[e], id.v[e], x1q.v[e] - x0q.v[e]);
+        if (DOT) acc += bq.v[e] * xn.v[e];
       }
-      if (full)
-        vst4<T>(xo + k, xn);
-      else
-        store_masked<T>(xo, xn, k, tile.k0, tile.k1);
+      vst4<T>(xo + (size_t)i * P + j, xn);
     }
-  });
+  }
   if (DOT) {
     const double s = block_sum(double(acc));
     if (threadIdx.x == 0) part[blockIdx.x] = s;

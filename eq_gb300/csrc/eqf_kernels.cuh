@@ -24,7 +24,9 @@ namespace eqf {
 
 constexpr int kThreads = 256;
 constexpr int kTabStride = 8;                 // c, e, w, n, s, ne, sw, 1/c
-constexpr int kTabPerTrap = 25 * kTabStride;  // 5 x 5 node classes
+constexpr int kTabClasses = 26;                // 5 x 5 node classes + the pad class
+constexpr int kClassPad = 25;                  // pad columns: all-zero row
+constexpr int kTabPerTrap = kTabClasses * kTabStride;
 // Resident CTAs per SM the staged stencil kernels are compiled for (register cap):
 // FP32 tiles are small enough in shared memory for six per SM.
 template <class T>
@@ -174,7 +176,7 @@ struct Stager {
 };
 
 __device__ __forceinline__ int padded_len(const LevelGeom& g) {
-  const int n = (g.nx + 1) * (g.ny + 1);
+  const int n = g.P * (g.ny + 1);
   return (n + 31) & ~31;
 }
 
@@ -192,12 +194,12 @@ __device__ __forceinline__ void div_pitch(int k, int P, float inv_p, int& i, int
 }
 
 // Walks the nodes k = k0 + tid, k0 + tid + bd, ... of a tile while keeping
-// (i, j) = divmod(k, nx + 1) up to date with one division per thread.
+// (i, j) = divmod(k, P) up to date with no division.
 struct NodeWalk {
   int k, i, j;
   int qi, qj, pitch;
   __device__ __forceinline__ NodeWalk(const LevelGeom& g, int k0) {
-    pitch = g.nx + 1;
+    pitch = g.P;
     k = k0 + threadIdx.x;
     div_pitch(k, pitch, g.inv_pitch, i, j);
     div_pitch((int)blockDim.x, pitch, g.inv_pitch, qi, qj);
@@ -216,6 +218,7 @@ struct NodeWalk {
 // ---------------------------------------------------------------------------
 // Stencil evaluation.
 __device__ __forceinline__ int node_class(const LevelGeom& g, int i, int j) {
+  if (j > g.nx) return kClassPad;
   const int ci = i < 2 ? i : (i > g.ny - 2 ? 4 - (g.ny - i) : 2);
   const int cj = j < 2 ? j : (j > g.nx - 2 ? 4 - (g.nx - j) : 2);
   return ci * 5 + cj;
@@ -257,11 +260,14 @@ __device__ __forceinline__ T st_interior(const Interior<T>& ci, T x0, T xe, T xw
 
 // Advection rows and traps: the full stencil from the cell sizes and the local
 // velocity (out of line; only traps with advection take it, uniformly per CTA).
-// (i, j) are clamped into the grid: nodes outside it are never stored.
+// Pad columns and nodes outside the grid get an all-zero row.
 template <class T>
 __device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&c)[8]) {
-  i = i < 0 ? 0 : (i > g.ny ? g.ny : i);
-  j = j < 0 ? 0 : (j > g.nx ? g.nx : j);
+  if (j > g.nx || j < 0 || i < 0 || i > g.ny) {  // pad column or outside the grid
+#pragma unroll
+    for (int q = 0; q < 8; ++q) c[q] = T(0);
+    return;
+  }
   const Sten<T> s = stencil_general<T>(g, i, j);
   c[0] = s.c;
   c[1] = s.e;
@@ -278,7 +284,7 @@ __device__ __forceinline__ T apply_general(const LevelGeom& g, const X& x, int k
   T c[8];
   coef_general<T>(g, i, j, c);
   idiag = c[7];
-  const int P = g.nx + 1;
+  const int P = g.P;
   return st_table(c, x[k], x[k + 1], x[k - 1], x[k + P], x[k - P], x[k + P + 1], x[k - P - 1]);
 }
 template <class T>
@@ -296,7 +302,7 @@ __device__ __forceinline__ T apply_tab(const LevelGeom& g, const Interior<T>& ci
                                        const T* __restrict__ tab, const X& x, int k, int i,
                                        int j, T& idiag) {
   if (!MASS && g.adv_on) return apply_general<T, X>(g, x, k, i, j, idiag);
-  const int P = g.nx + 1;
+  const int P = g.P;
   const T x0 = x[k], xe = x[k + 1], xw = x[k - 1], xn = x[k + P], xs = x[k - P];
   const T xne = x[k + P + 1], xsw = x[k - P - 1];
   if (is_uniform_interior(g, i, j)) {
@@ -400,7 +406,7 @@ __device__ __forceinline__ void pitch_dispatch(int P, F&& f) {
 struct QuadWalk {
   int q, i, j, qi, qj, P;
   __device__ __forceinline__ QuadWalk(const LevelGeom& g, int q0) {
-    P = g.nx + 1;
+    P = g.P;
     q = q0 + threadIdx.x;
     div_pitch(4 * q, P, g.inv_pitch, i, j);
     div_pitch(4 * (int)blockDim.x, P, g.inv_pitch, qi, qj);
@@ -433,19 +439,17 @@ struct QuadGeom {
 };
 
 // Node (i, j) of node kk = 4q + e, from the quad's first node (i0, j0).
+// Rows are padded to a multiple of 4 nodes, so a quad never leaves its row.
 __device__ __forceinline__ void quad_node(int P, int i0, int j0, int e, int& i, int& j) {
+  (void)P;
   i = i0;
   j = j0 + e;
-  while (j >= P) {
-    j -= P;
-    ++i;
-  }
 }
 
-// Class of a node whose row may lie outside the grid (nodes of a quad that reach
-// past the trap's last row are never stored; their class only has to be valid).
+// Class of a node that may lie outside the grid (guard rows and columns of staged
+// windows): those take the all-zero pad class, so they stay exactly zero.
 __device__ __forceinline__ int node_class_clamped(const LevelGeom& g, int i, int j) {
-  i = i < 0 ? 0 : (i > g.ny ? g.ny : i);
+  if (i < 0 || i > g.ny || j < 0) return kClassPad;
   return node_class(g, i, j);
 }
 
@@ -472,10 +476,10 @@ __device__ __forceinline__ const T* stage_table(Stager& st, const T* __restrict_
 // a quad that overlaps the tile (quads start 4-aligned, up to 3 nodes before the
 // tile) stays inside the staged, zero-guarded window.
 __device__ __forceinline__ int qhalo_lo(const LevelGeom& g, const Tile& t) {
-  return t.k0 - g.nx - 9;
+  return t.k0 - g.P - 8;
 }
 __device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
-  return t.k1 + g.nx + 9;
+  return t.k1 + g.P + 8;
 }
 
 // A x and 1/diagonal on a quad.  Every quad makes the same 13 loads (centre
@@ -564,10 +568,10 @@ __device__ __forceinline__ void count_work(unsigned long long* work, const Tile&
 
 // halo window of a tile: one row plus one node each side (may leave the trap)
 __device__ __forceinline__ int halo_lo(const LevelGeom& g, const Tile& t) {
-  return t.k0 - g.nx - 2;
+  return t.k0 - g.P - 1;
 }
 __device__ __forceinline__ int halo_hi(const LevelGeom& g, const Tile& t) {
-  return t.k1 + g.nx + 2;
+  return t.k1 + g.P + 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -613,7 +617,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const T* bs = b + g.off;
   T* xo = xout + g.off;
   T* ds = d + g.off;
-  const int P = g.nx + 1;
+  const int P = g.P;
   const QuadGeom qg(g, tile);
   T acc = T(0);
   if (ZERO) {
@@ -716,7 +720,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const T* stab = stage_table<T>(st, tab, ci);
   if (!st.run()) return;
   T* ts = t + g.off;
-  const int P = g.nx + 1;
+  const int P = g.P;
   const QuadGeom qg(g, tile);
   pitch_dispatch(P, [&](auto pm_) {
     constexpr int PM = decltype(pm_)::value;
@@ -772,18 +776,18 @@ __global__ void __launch_bounds__(kThreads)
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
-  const int nfx = g.fine_nx, nfy = g.fine_ny, PF = nfx + 1;
+  const int nfx = g.fine_nx, nfy = g.fine_ny, PF = g.fine_P;
   int fr0 = coarse_to_fine(tile.r0, nfy, g.cy) - 1;
   int fr1 = coarse_to_fine(tile.r1 - 1, nfy, g.cy) + 2;
   fr0 = fr0 < 0 ? 0 : fr0;
   fr1 = fr1 > nfy + 1 ? nfy + 1 : fr1;
-  const int naf = (((nfx + 1) * (nfy + 1)) + 31) & ~31;
+  const int naf = ((PF * (nfy + 1)) + 31) & ~31;
   Stager st(eqf_smem);
   const View<T> t = st.add(tf + g.fine_off, fr0 * PF, fr1 * PF, naf);
   if (!st.run()) return;
   T* b = bc + g.off;
   for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-    if (g.walls && is_dirichlet(g, w.i, w.j)) {
+    if (w.j > g.nx || (g.walls && is_dirichlet(g, w.i, w.j))) {  // pad column or wall
       b[w.k] = T(0);
       continue;
     }
@@ -816,7 +820,7 @@ __global__ void __launch_bounds__(kThreads)
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
   const LevelGeom& c = Gc[tile.geom];
-  const int PC = c.nx + 1;
+  const int PC = c.P;
   int lo0, hi0, lo1, hi1;
   fine_to_coarse(tile.r0, g.ny, c.cy, lo0, hi0);
   fine_to_coarse(tile.r1 - 1, g.ny, c.cy, lo1, hi1);
@@ -825,6 +829,7 @@ __global__ void __launch_bounds__(kThreads)
   if (!st.run()) return;
   T* xs = xf + g.off;
   for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+    if (w.j > g.nx) continue;  // pad column stays zero
     int i0, i1, j0, j1;
     fine_to_coarse(w.i, g.ny, c.cy, i0, i1);
     fine_to_coarse(w.j, g.nx, c.cx, j0, j1);
@@ -851,9 +856,9 @@ __global__ void __launch_bounds__(kThreads)
                    T* __restrict__ xout) {
   const LevelGeom& g = G[blockIdx.x];
   if (skip && skip[g.trap]) return;
-  const int n = (g.nx + 1) * (g.ny + 1);
+  const int n = g.P * (g.ny + 1);
   const int na = padded_len(g);
-  const int gpad = ((g.nx + 2 + 7) / 8) * 8;
+  const int gpad = ((g.P + 1 + 7) / 8) * 8;
   Stager st(eqf_smem);
   const View<T> bv = st.add(b + g.off, 0, n, na);
   T* xa = reinterpret_cast<T*>(st.cur) + gpad;
@@ -952,7 +957,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const PNew<T, FIRST> pnew{zv, pv, beta};
   T* po = pout + g.off;
   T* qs = q + g.off;
-  const int P = g.nx + 1;
+  const int P = g.P;
   const QuadGeom qg(g, tile);
   T acc = T(0);
   pitch_dispatch(P, [&](auto pm_) {

@@ -134,7 +134,7 @@ __device__ __forceinline__ const float2* stage_pair_table(Stager& st, const floa
 __device__ __forceinline__ DF df_apply(const LevelGeom& g, const float2* __restrict__ stab,
                                        bool general, const float2* x, int a, int k, int i,
                                        int j) {
-  const int P = g.nx + 1;
+  const int P = g.P;
   DF c[7];
   if (general) {
     double cg[8];
