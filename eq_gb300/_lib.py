@@ -35,7 +35,8 @@ EXPORTS = (
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
-                "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar")
+                "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
+                "down0", "up0")
 
 
 class TrapParams(C.Structure):

@@ -266,6 +266,8 @@ enum KClass : int {
   KC_IR_RESID,        // FP64 r = b - A u
   KC_IR_UPDATE,       // FP64 u += x
   KC_SCALAR,          // per-trap scalar phases
+  KC_DOWN0,           // finest level, fused pre-smoothing + residual
+  KC_UP0,             // finest level, fused prolongation + post-smoothing
   KC_COUNT
 };
 static_assert(KC_COUNT == EQF_PROF_CLASSES, "profiler class count");
@@ -280,9 +282,11 @@ static void class_bytes(int cls, int tsize, double& per_node) {
     case KC_PROLONG0: per_node = 2.25 * tsize; break;      // x in/out; 1/4 coarse in
     case KC_CG_DIR: per_node = 4.0 * tsize; break;         // z, p in; p', q out
     case KC_CG_UPDATE: per_node = 6.0 * tsize; break;      // x, p, r, q in; x, r out
-    case KC_IR_RESID_FIRST: per_node = 24.0 + tsize; break;  // F, u in; b out; r out
+    case KC_IR_RESID_FIRST: per_node = 40.0 + tsize; break;  // F, u, d in; b, u, d, r out
     case KC_IR_RESID: per_node = 16.0 + tsize; break;      // b, u in; r out
-    case KC_IR_UPDATE: per_node = 16.0 + tsize; break;     // x, u in; u out
+    case KC_IR_UPDATE: per_node = 24.0 + tsize; break;     // x, u, d in; u, d out
+    case KC_DOWN0: per_node = 3.0 * tsize; break;          // b in; x, t out
+    case KC_UP0: per_node = 3.25 * tsize; break;           // x, b, 1/4 coarse in; x out
     default: per_node = 0.0;
   }
 }
@@ -915,9 +919,8 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
       Lv_.sm_down > 0) {
     // temporally blocked: pre-smoothing + residual, restriction, coarse correction,
     // prolongation + post-smoothing
-    const int cd = lev > 0 ? KC_COARSE : KC_SMOOTH0;
     const int nt2 = (int)Lv_.tiles2.size();
-    EQF_RUN(B, cd,
+    EQF_RUN(B, lev > 0 ? KC_COARSE : KC_DOWN0,
             (k_down<T><<<nt2, kThreads, Lv_.sm_down, s>>>(G, Lv_.dtiles2.p, tab, skip, bl, cur,
                                                            v.t.p, W)));
     const Level& Lc = B.L[lev + 1];
@@ -926,11 +929,11 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
                 Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
     T* xc = vcycle(s, lev + 1, false);
     if (dot)
-      EQF_RUN(B, cd,
+      EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
               (k_up<T, true><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
                                                              skip, xc, bl, cur, oth, part, W)));
     else
-      EQF_RUN(B, cd,
+      EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
               (k_up<T, false><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
                                                               skip, xc, bl, cur, oth, part, W)));
     return oth;

@@ -388,16 +388,13 @@ __device__ __forceinline__ void View<T>::row(int k0, T (&out)[5]) const {
   Row5<M, T>::load(*this, k0, out);
 }
 
-// Runs f(std::integral_constant<int, P mod 4>): kernels instantiate their quad loop
-// for the four row-pitch residues, which fixes the row misalignments at compile time.
+// Runs f(std::integral_constant<int, P mod 4>), the row misalignment of the quad
+// loops.  Device rows are padded to a multiple of 4 nodes, so it is always 0; the
+// parameter keeps the row loads generic over the pitch.
 template <class F>
 __device__ __forceinline__ void pitch_dispatch(int P, F&& f) {
-  switch (P & 3) {
-    case 0: f(std::integral_constant<int, 0>{}); break;
-    case 1: f(std::integral_constant<int, 1>{}); break;
-    case 2: f(std::integral_constant<int, 2>{}); break;
-    default: f(std::integral_constant<int, 3>{}); break;
-  }
+  (void)P;
+  f(std::integral_constant<int, 0>{});
 }
 
 

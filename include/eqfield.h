@@ -241,13 +241,15 @@ int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
  * launch time (ms), launches, processed nodes and algorithmic bytes.  Classes, in
  * order: finest-level operator smoothing step, finest-level first smoothing step,
  * finest-level residual, restriction from the finest level, prolongation to the
- * finest level, coarser levels, CG direction (q = A p), CG update, FP64 residual
- * (first of a step), FP64 residual, FP64 update, per-trap scalar phases. */
+ * finest level, coarser levels, CG direction (q = A p), CG update, refinement
+ * residual (first of a step), refinement residual, refinement update, per-trap
+ * scalar phases, finest-level fused pre-smoothing + residual, finest-level fused
+ * prolongation + post-smoothing. */
 /* The CUDA stream (cudaStream_t) all work of the batch is queued on, for callers
  * that time the batch with their own CUDA events or order their own work. */
 int eqf_stream(eqf_batch* b, void** stream);
 
-#define EQF_PROF_CLASSES 12
+#define EQF_PROF_CLASSES 14
 int eqf_profile(eqf_batch* b, int32_t enable);
 int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
                      int64_t* nodes, double* bytes);
