@@ -33,10 +33,15 @@ EXPORTS = (
     "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc", "eqf_couple_species",
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
+    "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
 )
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
-                "down0", "up0")
+                "down0", "up0", "rod_exchange")
+
+# rod cells (eqf_set_rods): per cell and layer modes, and the eqf_rod record
+EQF_MAX_ROD_LAYERS = 4
+EQF_ROD_HELD, EQF_ROD_CIRCUIT, EQF_ROD_INERT = 0, 1, 2
 
 
 class TrapParams(C.Structure):
@@ -63,6 +68,19 @@ EQF_TUNE_MAX_BUCKETS = 8
 
 class TuneTable(C.Structure):
     _fields_ = [("n", C.c_int32), ("b", TuneBucket * EQF_TUNE_MAX_BUCKETS)]
+
+
+class RodLaw(C.Structure):
+    _fields_ = [("nodes_per_micron", C.c_double), ("dt", C.c_double),
+                ("membrane_rate", C.c_double * EQF_MAX_ROD_LAYERS)]
+
+
+def rod_dtype():
+    """numpy record layout of eqf_rod (20 doubles, 160 bytes)."""
+    import numpy as np
+    return np.dtype([("center", "<f8", (2,)), ("pole_a", "<f8", (2,)), ("pole_b", "<f8", (2,)),
+                     ("body_pos", "<f8", (2,)), ("body_rot", "<f8", (2,)), ("verts", "<f8", (8,)),
+                     ("length", "<f8"), ("reserved", "<f8")])
 
 
 class EqfError(RuntimeError):
@@ -123,6 +141,12 @@ def load() -> C.CDLL:
                                    P(TuneTable)]),
         "eqf_footprint_estimate": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_int64,
                                              i64p]),
+        "eqf_set_rods": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32), P(RodLaw), C.c_int64,
+                                   C.c_void_p, dp, dp, P(C.c_uint8)]),
+        "eqf_update_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, dp]),
+        "eqf_read_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp, P(C.c_int32)]),
+        "eqf_exchange_rods": (C.c_int, [C.c_void_p]),
+        "eqf_rod_waves": (C.c_int, [C.c_void_p, P(C.c_int32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -24,6 +24,7 @@
 #include "eqf_refine.cuh"
 #include "eqf_bicgstab.cuh"
 #include "eqf_fused.cuh"
+#include "eqf_rods.cuh"
 
 namespace eqf {
 
@@ -268,6 +269,7 @@ enum KClass : int {
   KC_SCALAR,          // per-trap scalar phases
   KC_DOWN0,           // finest level, fused pre-smoothing + residual
   KC_UP0,             // finest level, fused prolongation + post-smoothing
+  KC_ROD,             // rod-cell exchange waves (gather, membrane exchange, deposit)
   KC_COUNT
 };
 static_assert(KC_COUNT == EQF_PROF_CLASSES, "profiler class count");
@@ -396,6 +398,24 @@ class Batch {
   DevBuf<double> d_cp_prod, d_cp_c;
   DevBuf<CouplingLaw> d_cp_laws;
   void enqueue_coupling();
+  // rod cells of the agent-based model (eqf_set_rods), one set per simulation
+  struct RodSet {
+    std::vector<int> layers;
+    eqf_rod_law law{};
+    RodLawDev dev{};
+    int n = 0, nent = 0, waves = 0, waves_cap = 0, grid = 0;
+    long long span = 0;  // lattice nodes of the layers' trap in device layout
+    DevBuf<eqf_rod> rods;
+    DevBuf<RodLawDev> dlaw;
+    DevBuf<int> fp_off, fp_node, ent_cell, wave_cells, wave_off;
+    DevBuf<int> cover, start, cursor, flag;  // wave analysis scratch
+    DevBuf<double> ihsl, prod, ehsl;
+    DevBuf<unsigned char> mode;
+  };
+  std::vector<std::unique_ptr<RodSet>> rod_sets;
+  RodSet* rod_set_of(int layer0);
+  void rod_analyse(RodSet& rs);
+  void enqueue_rods();
   void drop_graphs() {
     for (auto& gx : graph)
       if (gx) {
@@ -1146,7 +1166,131 @@ void Batch::enqueue_coupling() {
   refresh_load();
 }
 
+// ---------------------------------------------------------------------------
+// Rod cells: footprints and dependency waves (at every geometry update), and the
+// per-step exchange (one launch per wave, captured with the step).
+
+Batch::RodSet* Batch::rod_set_of(int layer0) {
+  for (auto& rs : rod_sets)
+    if (rs->layers[0] == layer0) return rs.get();
+  return nullptr;
+}
+
+void Batch::rod_analyse(RodSet& rs) {
+  const int n = rs.n, bs = 256;
+  bool moved = false;  // pointers or launch counts captured in a step change
+  rs.grid = std::max(1, std::min((n * 32 + bs - 1) / bs, num_sms * 16));
+  DevBuf<int> count;
+  count.alloc(n);
+  k_rod_footprint<false><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, count.p, nullptr,
+                                                     nullptr, nullptr);
+  EQF_LAUNCH_CHECK();
+  scan(n, count.p, rs.fp_off.p);
+  int nent = 0;
+  EQF_CK(cudaMemcpyAsync(&nent, rs.fp_off.p + n, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  sync();
+  if ((size_t)nent > rs.fp_node.n) {
+    const size_t cap = (size_t)nent + (size_t)nent / 4 + 64;
+    rs.fp_node.alloc(cap);
+    rs.ent_cell.alloc(cap);
+    moved = true;
+  }
+  rs.nent = nent;
+  k_rod_footprint<true><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, nullptr,
+                                                    rs.fp_off.p, rs.fp_node.p, rs.ent_cell.p);
+  EQF_LAUNCH_CHECK();
+  // does any node lie in two footprints?
+  const int ge = (nent + bs - 1) / bs, gc = (n + bs - 1) / bs;
+  EQF_CK(cudaMemsetAsync(rs.cover.p, 0, rs.span * sizeof(int), stream));
+  EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
+  k_rod_cover<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.cover.p, rs.flag.p);
+  EQF_LAUNCH_CHECK();
+  int shared = 0;
+  EQF_CK(cudaMemcpyAsync(&shared, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  sync();
+  std::vector<int> woff;
+  if (!shared) {
+    k_rod_iota<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p);
+    EQF_LAUNCH_CHECK();
+    woff = {0, n};
+  } else {
+    // bucket the entries by node, each bucket in cell order; wave = longest chain
+    scan((int)rs.span, rs.cover.p, rs.start.p);
+    EQF_CK(cudaMemsetAsync(rs.cursor.p, 0, rs.span * sizeof(int), stream));
+    DevBuf<int> perm, pred, succ, wave, wcount, wstart;
+    perm.alloc(nent);
+    pred.alloc(nent);
+    succ.alloc(nent);
+    wave.alloc(n);
+    wcount.alloc(n);
+    k_rod_place<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cursor.p, perm.p);
+    EQF_LAUNCH_CHECK();
+    k_rod_bucket_order<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cover.p,
+                                              perm.p);
+    EQF_LAUNCH_CHECK();
+    k_rod_preds<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, perm.p, rs.ent_cell.p,
+                                       pred.p, succ.p);
+    EQF_LAUNCH_CHECK();
+    EQF_CK(cudaMemsetAsync(wave.p, 0, n * sizeof(int), stream));
+    for (int it = 0;; ++it) {
+      if (it > n) throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
+      int changed = 0;
+      EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
+      k_rod_relax<<<ge, bs, 0, stream>>>(nent, pred.p, succ.p, wave.p, rs.flag.p);
+      EQF_LAUNCH_CHECK();
+      EQF_CK(cudaMemcpyAsync(&changed, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      sync();
+      if (!changed) break;
+    }
+    EQF_CK(cudaMemsetAsync(wcount.p, 0, n * sizeof(int), stream));
+    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
+    k_rod_wave_count<<<gc, bs, 0, stream>>>(n, wave.p, wcount.p, rs.flag.p);
+    EQF_LAUNCH_CHECK();
+    int wmax = 0;
+    EQF_CK(cudaMemcpyAsync(&wmax, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    sync();
+    const int waves = wmax + 1;
+    wstart.alloc(waves + 1);
+    scan(waves, wcount.p, wstart.p);
+    EQF_CK(cudaMemsetAsync(wcount.p, 0, waves * sizeof(int), stream));
+    k_rod_wave_place<<<gc, bs, 0, stream>>>(n, wave.p, wstart.p, wcount.p, rs.wave_cells.p);
+    EQF_LAUNCH_CHECK();
+    woff.resize(waves + 1);
+    EQF_CK(cudaMemcpyAsync(woff.data(), wstart.p, (waves + 1) * sizeof(int),
+                           cudaMemcpyDeviceToHost, stream));
+    sync();
+  }
+  rs.waves = (int)woff.size() - 1;
+  if (rs.waves > rs.waves_cap) {
+    rs.waves_cap = rs.waves;
+    moved = true;
+  }
+  // launches past the last wave (kept in captured steps) see empty ranges
+  woff.resize(rs.waves_cap + 1, n);
+  if (rs.wave_off.n < woff.size()) {
+    rs.wave_off.alloc(woff.size());
+    moved = true;
+  }
+  EQF_CK(cudaMemcpyAsync(rs.wave_off.p, woff.data(), woff.size() * sizeof(int),
+                         cudaMemcpyHostToDevice, stream));
+  sync();
+  if (moved) drop_graphs();
+}
+
+void Batch::enqueue_rods() {
+  for (auto& up : rod_sets) {
+    RodSet& rs = *up;
+    for (int w = 0; w < rs.waves_cap; ++w)
+      EQF_RUN(*this, KC_ROD,
+              (k_rod_exchange<<<rs.grid, 256, 0, stream>>>(
+                  w, rs.wave_off.p, rs.wave_cells.p, rs.rods.p, rs.dlaw.p, rs.fp_off.p,
+                  rs.fp_node.p, rs.ihsl.p, rs.prod.p, rs.mode.p, rs.ehsl.p, d_frozen.p,
+                  u_cur())));
+  }
+}
+
 void Batch::run_step() {
+  enqueue_rods();
   enqueue_coupling();
   for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
   work->enqueue_check(stream, true);
@@ -1888,6 +2032,219 @@ int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c) {
     B.sync();
     B.check_fail();
   });
+}
+
+// Rod cells (eqfield.h: eqf_set_rods and the calls after it).
+namespace {
+
+// eQ::Cell::DEFAULT_CELL_WIDTH_MICRONS (src/eQcell.h:42)
+constexpr double kRodCellWidth = 1.0;
+
+void check_rods(const eqf_trap_params& p, const eqf_rod* rods, int64_t n) {
+  auto in_trap = [&](const double* xy) {
+    return std::isfinite(xy[0]) && std::isfinite(xy[1]) && xy[0] >= 0.0 && xy[1] >= 0.0 &&
+           xy[0] <= p.width && xy[1] <= p.height;
+  };
+  for (int64_t c = 0; c < n; ++c) {
+    const eqf_rod& r = rods[c];
+    EQF_REQUIRE(in_trap(r.center) && in_trap(r.pole_a) && in_trap(r.pole_b),
+                "rod centre or pole outside the trap");
+    bool fin = std::isfinite(r.length) && std::isfinite(r.body_pos[0]) &&
+               std::isfinite(r.body_pos[1]) && std::isfinite(r.body_rot[0]) &&
+               std::isfinite(r.body_rot[1]);
+    for (double v : r.verts) fin = fin && std::isfinite(v);
+    EQF_REQUIRE(fin, "non-finite rod geometry");
+    EQF_REQUIRE(r.length >= kRodCellWidth, "rod shorter than its width");
+  }
+}
+
+}  // namespace
+
+int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eqf_rod_law* law,
+                 int64_t n_cells, const eqf_rod* rods, const double* ihsl,
+                 const double* production, const uint8_t* mode) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    EQF_REQUIRE(n_layers >= 1 && n_layers <= EQF_MAX_ROD_LAYERS && layers && law,
+                "bad rod layers or law");
+    for (int l = 0; l < n_layers; ++l) {
+      EQF_TRAP_CHECK(b, layers[l]);
+      for (int m = 0; m < l; ++m) EQF_REQUIRE(layers[m] != layers[l], "repeated rod layer");
+    }
+    const eqf_trap_params& p0 = B.params[layers[0]];
+    for (int l = 1; l < n_layers; ++l) {
+      const eqf_trap_params& p = B.params[layers[l]];
+      EQF_REQUIRE(p.nx == p0.nx && p.ny == p0.ny && p.width == p0.width &&
+                      p.height == p0.height,
+                  "rod layers must share the mesh");
+    }
+    const double npm = law->nodes_per_micron;
+    EQF_REQUIRE(std::isfinite(npm) && npm > 0.0 && std::isfinite(law->dt) && law->dt >= 0.0,
+                "bad rod law");
+    for (int l = 0; l < n_layers; ++l)
+      EQF_REQUIRE(std::isfinite(law->membrane_rate[l]), "non-finite membrane rate");
+    // eQabm's lattice, nodesWide = size_t(W*npm) + 1 and nodesHigh = size_t(H*npm) + 1
+    // (src/abm/eQabm.cpp:30-31), must be the mesh's nodes, with W*npm and H*npm
+    // integral so that every point of the trap rounds to a lattice node
+    EQF_REQUIRE(p0.width * npm == (double)p0.nx && p0.height * npm == (double)p0.ny,
+                "rod coupling needs nx = W*npm and ny = H*npm exactly");
+    size_t slot = B.rod_sets.size();
+    for (size_t q = 0; q < B.rod_sets.size(); ++q) {
+      const auto& rs = *B.rod_sets[q];
+      if (rs.layers[0] == layers[0]) {
+        slot = q;
+        continue;
+      }
+      for (int l = 0; l < n_layers; ++l)
+        for (int t : rs.layers)
+          EQF_REQUIRE(t != layers[l], "trap already belongs to another rod set");
+    }
+    EQF_REQUIRE(n_cells >= 0 && n_cells <= (1 << 26), "bad rod cell count");
+    if (n_cells == 0) {
+      if (slot < B.rod_sets.size()) B.rod_sets.erase(B.rod_sets.begin() + slot);
+      B.drop_graphs();
+      return;
+    }
+    EQF_REQUIRE(rods && ihsl && production && mode, "null rod arrays");
+    check_rods(p0, rods, n_cells);
+    const int64_t ns = n_cells * n_layers;
+    for (int64_t i = 0; i < ns; ++i)
+      EQF_REQUIRE(std::isfinite(ihsl[i]) && ihsl[i] >= 0.0 && std::isfinite(production[i]) &&
+                      mode[i] <= EQF_ROD_INERT,
+                  "bad rod state");
+    auto rs = std::make_unique<Batch::RodSet>();
+    rs->layers.assign(layers, layers + n_layers);
+    rs->law = *law;
+    rs->n = (int)n_cells;
+    const eqf::LevelGeom& g = B.L[0].geom[layers[0]];
+    eqf::RodLawDev& d = rs->dev;
+    d.npm = npm;
+    d.dt = law->dt;
+    for (int l = 0; l < eqf::kRodLayers; ++l) {
+      d.km[l] = l < n_layers ? law->membrane_rate[l] : 0.0;
+      d.lay_off[l] = l < n_layers ? B.L[0].geom[layers[l]].off : 0;
+    }
+    d.trap0 = layers[0];
+    d.nlayers = n_layers;
+    d.nx = g.nx;
+    d.ny = g.ny;
+    d.P = g.P;
+    // nodesToEdge = size_t(round(npm * W / 2)) (src/abm/eQabm.cpp:75)
+    d.nte = (int)std::round(npm * kRodCellWidth / 2.0);
+    // eQ::Cell (src/eQcell.h:51-59), same expressions
+    const double pole_radius = kRodCellWidth / 2.0;
+    d.k.cyl = M_PI * (pole_radius * pole_radius);
+    d.k.pole = 4.0 / 3.0 * M_PI * (pole_radius * pole_radius * pole_radius);
+    d.k.nm_per_molecule = 1.0 / 0.602;
+    rs->span = B.fine_span(layers[0]);
+    const size_t n = (size_t)n_cells, n4 = n * eqf::kRodLayers;
+    rs->rods.alloc(n);
+    rs->dlaw.alloc(1);
+    rs->fp_off.alloc(n + 1);
+    rs->wave_cells.alloc(n);
+    rs->cover.alloc(rs->span);
+    rs->start.alloc(rs->span + 1);
+    rs->cursor.alloc(rs->span);
+    rs->flag.alloc(1);
+    rs->ihsl.alloc(n4);
+    rs->prod.alloc(n4);
+    rs->ehsl.alloc(n4);
+    rs->mode.alloc(n4);
+    std::vector<double> hi(n4, 0.0), hp(n4, 0.0);
+    std::vector<unsigned char> hm(n4, EQF_ROD_INERT);
+    for (size_t c = 0; c < n; ++c)
+      for (int l = 0; l < n_layers; ++l) {
+        hi[c * eqf::kRodLayers + l] = ihsl[c * n_layers + l];
+        hp[c * eqf::kRodLayers + l] = production[c * n_layers + l];
+        hm[c * eqf::kRodLayers + l] = mode[c * n_layers + l];
+      }
+    rs->rods.upload(rods, n, B.stream);
+    rs->dlaw.upload(&rs->dev, 1, B.stream);
+    rs->ihsl.upload(hi.data(), n4, B.stream);
+    rs->prod.upload(hp.data(), n4, B.stream);
+    rs->mode.upload(hm.data(), n4, B.stream);
+    EQF_CK(cudaMemsetAsync(rs->ehsl.p, 0, n4 * sizeof(double), B.stream));
+    B.rod_analyse(*rs);
+    if (slot < B.rod_sets.size())
+      B.rod_sets[slot] = std::move(rs);
+    else
+      B.rod_sets.push_back(std::move(rs));
+    B.drop_graphs();  // captured steps hold the previous set's pointers
+  });
+}
+
+int eqf_update_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, const eqf_rod* rods,
+                    const double* production) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    Batch::RodSet* rs = B.rod_set_of(layer0);
+    EQF_REQUIRE(rs != nullptr, "no rod set on this layer");
+    EQF_REQUIRE(n_cells == rs->n && rods, "rod count mismatch");
+    check_rods(B.params[layer0], rods, n_cells);
+    const int nl = (int)rs->layers.size();
+    const size_t n = (size_t)n_cells, n4 = n * eqf::kRodLayers;
+    if (production) {
+      for (int64_t i = 0; i < n_cells * nl; ++i)
+        EQF_REQUIRE(std::isfinite(production[i]), "non-finite production");
+      std::vector<double> hp(n4, 0.0);
+      for (size_t c = 0; c < n; ++c)
+        for (int l = 0; l < nl; ++l) hp[c * eqf::kRodLayers + l] = production[c * nl + l];
+      EQF_CK(cudaMemcpyAsync(rs->prod.p, hp.data(), n4 * sizeof(double), cudaMemcpyHostToDevice,
+                             B.stream));
+      B.sync();  // hp is released on return
+    }
+    EQF_CK(cudaMemcpyAsync(rs->rods.p, rods, n * sizeof(eqf_rod), cudaMemcpyHostToDevice,
+                           B.stream));
+    B.rod_analyse(*rs);
+  });
+}
+
+int eqf_read_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, double* ihsl, double* ehsl,
+                  int32_t* points) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    Batch::RodSet* rs = B.rod_set_of(layer0);
+    EQF_REQUIRE(rs != nullptr, "no rod set on this layer");
+    EQF_REQUIRE(n_cells == rs->n, "rod count mismatch");
+    const int nl = (int)rs->layers.size();
+    const size_t n = (size_t)n_cells, n4 = n * eqf::kRodLayers;
+    std::vector<double> hi(n4), he(n4);
+    std::vector<int> off(n + 1);
+    EQF_CK(cudaMemcpyAsync(hi.data(), rs->ihsl.p, n4 * sizeof(double), cudaMemcpyDeviceToHost,
+                           B.stream));
+    EQF_CK(cudaMemcpyAsync(he.data(), rs->ehsl.p, n4 * sizeof(double), cudaMemcpyDeviceToHost,
+                           B.stream));
+    EQF_CK(cudaMemcpyAsync(off.data(), rs->fp_off.p, (n + 1) * sizeof(int),
+                           cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    for (size_t c = 0; c < n; ++c) {
+      for (int l = 0; l < nl; ++l) {
+        if (ihsl) ihsl[c * nl + l] = hi[c * eqf::kRodLayers + l];
+        if (ehsl) ehsl[c * nl + l] = he[c * eqf::kRodLayers + l];
+      }
+      if (points) points[c] = off[c + 1] - off[c];
+    }
+  });
+}
+
+int eqf_exchange_rods(eqf_batch* b) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    B.enqueue_rods();
+    B.sync();
+  });
+}
+
+int eqf_rod_waves(eqf_batch* b, int32_t* waves) {
+  if (!b || !waves) return EQF_ERR_INVALID;
+  int w = 0;
+  for (const auto& rs : b->impl->rod_sets) w = std::max(w, rs->waves);
+  *waves = w;
+  return EQF_OK;
 }
 
 int eqf_stream(eqf_batch* b, void** stream) {

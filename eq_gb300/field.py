@@ -178,6 +178,60 @@ class TrapBatch:
     def step(self, n: int = 1):
         self._ck(self._lib.eqf_step(self._h, int(n)))
 
+    # --- rod cells of the agent-based model (eqf_set_rods) -----------------------
+    def set_rods(self, layers: Sequence[int], rods: np.ndarray, ihsl: np.ndarray,
+                 production: np.ndarray, mode: np.ndarray, nodes_per_micron: float,
+                 dt: float, membrane_rate: Sequence[float]):
+        """Rod cells (records of ``_lib.rod_dtype()``) coupled to the layers ``layers``
+        the reference's way; ihsl / production / mode are (n_cells, n_layers)."""
+        nl = len(layers)
+        lay = np.ascontiguousarray(layers, dtype=np.int32)
+        rods = np.ascontiguousarray(rods, dtype=_lib.rod_dtype())
+        n = len(rods)
+        ih = np.ascontiguousarray(ihsl, dtype=np.float64).reshape(n, nl)
+        pr = np.ascontiguousarray(production, dtype=np.float64).reshape(n, nl)
+        md = np.ascontiguousarray(mode, dtype=np.uint8).reshape(n, nl)
+        law = _lib.RodLaw()
+        law.nodes_per_micron = float(nodes_per_micron)
+        law.dt = float(dt)
+        for l, k in enumerate(membrane_rate):
+            law.membrane_rate[l] = float(k)
+        self._ck(self._lib.eqf_set_rods(
+            self._h, nl, lay.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(law), n,
+            rods.ctypes.data if n else None, _dp(ih), _dp(pr),
+            md.ctypes.data_as(C.POINTER(C.c_uint8))))
+        self._rods = getattr(self, "_rods", {})
+        self._rods[int(layers[0])] = (n, nl)
+
+    def update_rods(self, layer0: int, rods: np.ndarray,
+                    production: Optional[np.ndarray] = None):
+        rods = np.ascontiguousarray(rods, dtype=_lib.rod_dtype())
+        pr = None
+        if production is not None:
+            pr = _dp(np.ascontiguousarray(production, dtype=np.float64).ravel())
+        self._ck(self._lib.eqf_update_rods(self._h, int(layer0), len(rods), rods.ctypes.data,
+                                           pr))
+
+    def read_rods(self, layer0: int):
+        """(ihsl, ehsl, points): intracellular HSL (molecules) and the last gathered
+        footprint mean per cell and layer, and the footprint size per cell."""
+        n, nl = self._rods[int(layer0)]
+        ih = np.empty((n, nl))
+        eh = np.empty((n, nl))
+        pts = np.empty(n, dtype=np.int32)
+        self._ck(self._lib.eqf_read_rods(self._h, int(layer0), n, _dp(ih), _dp(eh),
+                                         pts.ctypes.data_as(C.POINTER(C.c_int32))))
+        return ih, eh, pts
+
+    def exchange_rods(self):
+        """One pass of the cell loop without a solve."""
+        self._ck(self._lib.eqf_exchange_rods(self._h))
+
+    def rod_waves(self) -> int:
+        w = C.c_int32()
+        self._ck(self._lib.eqf_rod_waves(self._h, C.byref(w)))
+        return w.value
+
     def read_nodal(self, trap: int, out: Optional[np.ndarray] = None) -> np.ndarray:
         if out is None:
             out = np.empty(self.num_nodes(trap))

@@ -152,3 +152,107 @@ WORKLOADS = {
     "single_large": single_large,
     "two_species": two_species,
 }
+
+
+# --- rod cells of the agent-based model (eqf_set_rods) ----------------------------
+
+ROD_HELD, ROD_CIRCUIT, ROD_INERT = 0, 1, 2
+
+
+def rod_records(cx, cy, angle, length, W: float, H: float) -> np.ndarray:
+    """eqf_rod records of freshly created cells: the first body half at the centre
+    with the cell's angle, its box of half-length (L - 1)/2 and half-width 1/2 in its
+    own frame (upper-left, upper-right, lower-right, lower-left), as
+    cpmEcoli::cpmEcoli builds it (src/abm/cpmEcoli.cpp:100-180), and the pole centres
+    of Ecoli::updatePoleCenters (src/abm/Ecoli.cpp:36-60): centre + (cos, sin) *
+    (0.5 L - W/2) and centre + (cos, sin) * (-0.5 L - W/2), clamped to the trap."""
+    from ._lib import rod_dtype
+    cx, cy, angle, length = (np.asarray(v, dtype=np.float64).ravel() for v in
+                             (cx, cy, angle, length))
+    n = len(cx)
+    rec = np.zeros(n, dtype=rod_dtype())
+    c, s = np.cos(angle), np.sin(angle)
+    rec["center"][:, 0], rec["center"][:, 1] = cx, cy
+    width = 1.0
+    for key, r in (("pole_a", 1.0), ("pole_b", -1.0)):
+        k = r * 0.5 * length - width / 2.0
+        px, py = cx + c * k, cy + s * k
+        rec[key][:, 0] = np.clip(px, 0.0, W)
+        rec[key][:, 1] = np.clip(py, 0.0, H)
+    rec["body_pos"][:, 0], rec["body_pos"][:, 1] = cx, cy
+    rec["body_rot"][:, 0], rec["body_rot"][:, 1] = c, s
+    off = (length - width) * 0.5
+    rad = width * 0.5
+    rec["verts"] = np.stack([-off, np.full(n, rad), off, np.full(n, rad),
+                             off, np.full(n, -rad), -off, np.full(n, -rad)], axis=1)
+    rec["length"] = length
+    return rec
+
+
+@dataclass
+class RodColony:
+    """One trap with rod cells coupled through their footprints, one field layer per
+    HSL species, each with its own D, decay and membrane rate."""
+    W: float
+    H: float
+    npm: float
+    D: List[float]
+    g: List[float]
+    km: List[float]
+    dt: float
+    steps: int
+    rods: np.ndarray
+    ihsl: np.ndarray  # (n_cells, n_layers) molecules
+    prod: np.ndarray  # (n_cells, n_layers) nM per time unit
+    mode: np.ndarray  # (n_cells, n_layers) ROD_*
+    walls: int = WALL_BOTTOM
+
+    @property
+    def nx(self) -> int:
+        return int(self.W * self.npm)
+
+    @property
+    def ny(self) -> int:
+        return int(self.H * self.npm)
+
+    @property
+    def n_nodes(self) -> int:
+        return (self.nx + 1) * (self.ny + 1)
+
+    @property
+    def n_layers(self) -> int:
+        return len(self.D)
+
+    @property
+    def n_cells(self) -> int:
+        return len(self.rods)
+
+    def dof_steps(self, steps: Optional[int] = None) -> int:
+        return self.n_nodes * self.n_layers * (self.steps if steps is None else steps)
+
+
+def rod_colony(seed: int = 11, W: float = 100.0, H: float = 40.0, npm: float = 4.0,
+               n_cells: int = 1000, steps: int = 200, dt: float = 0.05,
+               len_lo: float = 1.5, len_hi: float = 4.2) -> RodColony:
+    """Sender/receiver colony on two HSL layers (C4-like, C14-like): centres uniform
+    2 um inside the walls, angles uniform, lengths U(len_lo, len_hi) (rods may
+    overlap, as compressed cells do).  Half the cells are senders: layer 0 runs
+    their circuit with production 100 nM/time; receivers run it with production 0
+    (pure membrane exchange); layer 1 is held (the strain does not update it), as
+    sendRecvStrain does with a second HSL.  Membrane rates 3.0 and 2.1 per time
+    unit (the reference's C4/C14 values, src/eQinit.h:12-13)."""
+    rng = _rng(seed)
+    cx = rng.uniform(2.0, W - 2.0, size=n_cells)
+    cy = rng.uniform(2.0, H - 2.0, size=n_cells)
+    ang = rng.uniform(0.0, np.pi, size=n_cells)
+    length = rng.uniform(len_lo, len_hi, size=n_cells)
+    sender = rng.uniform(size=n_cells) < 0.5
+    rods = rod_records(cx, cy, ang, length, W, H)
+    nl = 2
+    prod = np.zeros((n_cells, nl))
+    prod[:, 0] = np.where(sender, 100.0, 0.0)
+    mode = np.full((n_cells, nl), ROD_HELD, dtype=np.uint8)
+    mode[:, 0] = ROD_CIRCUIT
+    return RodColony(W=W, H=H, npm=npm, D=[490.0, 300.0], g=[0.01, 0.02], km=[3.0, 2.1],
+                     dt=dt, steps=steps, rods=rods, ihsl=np.zeros((n_cells, nl)), prod=prod,
+                     mode=mode)

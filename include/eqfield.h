@@ -233,6 +233,77 @@ int eqf_footprint_estimate(int32_t n_traps, const eqf_trap_params* traps,
 int eqf_set_cell_rates_all(eqf_batch* b, int64_t n, const double* s);
 int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
 
+/* ---------------------------------------------------------------------------
+ * Rod cells of the agent-based model, coupled the reference's way.
+ *
+ * Replaces the per-cell loop of eQabm::updateCells (src/abm/eQabm.cpp:234-390):
+ * the interior-node search findInteriorPoints (268-304) with
+ * cpmEcoli::pointIsInCell (src/abm/cpmEcoli.cpp:313-328), the interior-mean
+ * gather readHSL (326-337), the strain's membrane exchange
+ * (Strain::computeConcentrations / pushConcentrations, src/Strain.h:281-345, and
+ * sendRecvStrain::computeProteins, src/Strain.cpp:10-73) and the equal-split
+ * deposit writeHSL into u0 (338-359), with the unit conversions of eQ::Cell
+ * (src/eQcell.h:42-97).  The cells are processed in array order with the
+ * reference's sequential semantics: a cell reads the deposits of every earlier
+ * cell whose footprint shares a node with its own.  Every eqf_step runs the
+ * exchange for all rod cells at the start of each step, before the solve.
+ *
+ * One rod set belongs to one simulation: its layers are traps of the batch with
+ * the same mesh, a lattice of nodes_per_micron nodes per micron in both directions
+ * (W*npm = nx and H*npm = ny exactly, eQabm's nodesWide - 1 and nodesHigh - 1,
+ * src/abm/eQabm.cpp:30-31).  A trap belongs to at most one rod set.
+ */
+#define EQF_MAX_ROD_LAYERS 4
+/* per cell and layer: how the cell's circuit treats that HSL species */
+#define EQF_ROD_HELD 0    /* exchange deposited; intracellular HSL only converted
+                             nM <-> molecules (a species the strain does not update) */
+#define EQF_ROD_CIRCUIT 1 /* iHSL += dt*production - exchange (sender: production =
+                             hslProductionRate; receiver: 0), clamped at 0 */
+#define EQF_ROD_INERT 2   /* no exchange (a strain without an HSL circuit) */
+
+/* One rod cell as the agent-based model holds it.  All lengths in microns. */
+typedef struct eqf_rod {
+  double center[2];   /* Ecoli::getCenter_x/y: the fallback node when no lattice
+                         node lies inside (src/abm/eQabm.cpp:299-303) */
+  double pole_a[2];   /* Ecoli::polePositionA/B, clamped to the trap as
+                         Ecoli::updatePoleCenters does (src/abm/Ecoli.cpp:36-60): */
+  double pole_b[2];   /*   they bound the node search */
+  double body_pos[2]; /* position of the cell's first half (cpBodyGetPosition(bodyA)) */
+  double body_rot[2]; /* its rotation (cos, sin) (cpBodyGetRotation(bodyA)) */
+  double verts[8];    /* cpmEcoli::vertsA[0..3], that half's box in its own frame,
+                         clockwise (x, y pairs) */
+  double length;      /* Ecoli::getLengthMicrons */
+  double reserved;    /* 0 */
+} eqf_rod;
+
+typedef struct eqf_rod_law {
+  double nodes_per_micron; /* parameters["nodesPerMicronSignaling"] */
+  double dt;               /* cell-model time step (the strain's params.dt) */
+  double membrane_rate[EQF_MAX_ROD_LAYERS]; /* parameters["membraneDiffusionRates"] */
+} eqf_rod_law;
+
+/* Sets (replaces) the rod cells of the simulation whose layers are
+ * layers[0..n_layers-1], with their state: ihsl[c*n_layers + l] intracellular
+ * HSL (molecules, as Strain stores iHSL), production[c*n_layers + l] (nM/min) and
+ * mode[c*n_layers + l] (EQF_ROD_*).  n_cells = 0 removes the set. */
+int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eqf_rod_law* law,
+                 int64_t n_cells, const eqf_rod* rods, const double* ihsl,
+                 const double* production, const uint8_t* mode);
+/* Moves the cells of the set whose first layer is layer0 (same count and order);
+ * their intracellular state stays on the device.  production may be NULL (kept). */
+int eqf_update_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, const eqf_rod* rods,
+                    const double* production);
+/* Reads, per cell and layer, the intracellular HSL (molecules) and the mean field
+ * value over the cell's footprint gathered by the last exchange (readHSL; 0 before
+ * the first), and per cell the number of footprint nodes.  Any pointer may be NULL. */
+int eqf_read_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, double* ihsl, double* ehsl,
+                  int32_t* points);
+/* Runs the exchange once now, without a solve (the reference's updateCells alone). */
+int eqf_exchange_rods(eqf_batch* b);
+/* Number of sequential waves the exchange of the current rod cells takes (1 when
+ * no two cells share a footprint node). */
+int eqf_rod_waves(eqf_batch* b, int32_t* waves);
+
 /* Built-in profiler (no counterpart in the reference, which only keeps MPI_Wtime
  * accumulators, src/simulation.h:512-521).  While enabled, steps run without CUDA
  * graphs and every kernel launch is bracketed by CUDA events on the batch's
@@ -244,12 +315,12 @@ int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
  * finest level, coarser levels, CG direction (q = A p), CG update, refinement
  * residual (first of a step), refinement residual, refinement update, per-trap
  * scalar phases, finest-level fused pre-smoothing + residual, finest-level fused
- * prolongation + post-smoothing. */
+ * prolongation + post-smoothing, rod-cell exchange (eqf_set_rods). */
 /* The CUDA stream (cudaStream_t) all work of the batch is queued on, for callers
  * that time the batch with their own CUDA events or order their own work. */
 int eqf_stream(eqf_batch* b, void** stream);
 
-#define EQF_PROF_CLASSES 14
+#define EQF_PROF_CLASSES 15
 int eqf_profile(eqf_batch* b, int32_t enable);
 int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
                      int64_t* nodes, double* bytes);
