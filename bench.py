@@ -142,6 +142,47 @@ def cpu_reference_rate(traps, idx, steps_per_trap: int, budget_s: float):
     return cpu_baseline.reference_rate(traps, idx, steps_per_trap, budget_s)
 
 
+def profiled_roofline(b, stream, prof_steps: int, workload: str):
+    """A short profiled pass (no graphs) of batch b: per kernel class time, launches
+    and algorithmic bytes, and the roofline of the dominant byte-carrying class."""
+    import torch
+    b.profile(True)
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0.record(stream)
+    b.step(prof_steps)
+    pe1.record(stream)
+    b.sync()
+    prof = b.profile_read()
+    b.profile(False)
+    prof_total = pe0.elapsed_time(pe1)
+    launches_per_step = sum(v["launches"] for v in prof.values()) / prof_steps
+    # dominant kernel class among those with algorithmic bytes (the "coarse" and
+    # "scalar" classes collect many small launches and carry no byte count)
+    dom = max((k for k in prof if prof[k]["bytes"] > 0), key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0
+    # DRAM traffic per launch from the committed ncu captures (per kernel class)
+    tclasses = {}
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        if tj.get("workload") == workload:
+            tclasses = tj.get("classes", {})
+    traffic = tclasses.get(dom, {}).get("bytes_per_launch")
+    roofline = {"bound": "hbm", "kernel_class": dom, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "peak_source": peak_kind,
+                "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
+                "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
+    if dom in ("down0", "up0"):
+        roofline["note"] = ("temporally blocked level kernel: several smoothing steps per HBM "
+                            "pass, bytes counted once (compute-bound by design)")
+    return prof, prof_total, launches_per_step, roofline, tclasses
+
+
 # -------------------------------------------------------------------- our arm
 def run_ours(args, rank, world, local_rank):
     import torch
@@ -226,40 +267,9 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- profiled pass (no graphs): per kernel class time / nodes / bytes
     prof_steps = max(2, min(args.steps, 5))
-    b.profile(True)
-    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    pe0.record(stream)
-    b.step(prof_steps)
-    pe1.record(stream)
-    b.sync()
-    prof = b.profile_read()
-    b.profile(False)
-    prof_total = pe0.elapsed_time(pe1)
-    launches_per_step = sum(v["launches"] for v in prof.values()) / prof_steps
-    # dominant kernel class among those with algorithmic bytes (the "coarse" and
-    # "scalar" classes collect many small launches and carry no byte count)
-    dom = max((k for k in prof if prof[k]["bytes"] > 0), key=lambda k: prof[k]["ms"])
-    d = prof[dom]
+    prof, prof_total, launches_per_step, roofline, tclasses = profiled_roofline(
+        b, stream, prof_steps, args.workload)
     peak, peak_kind = measured_peaks()
-    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0
-    # DRAM traffic per launch from the committed ncu captures (per kernel class)
-    tclasses = {}
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tj = json.load(f)
-        if tj.get("workload") == args.workload:
-            tclasses = tj.get("classes", {})
-    traffic = tclasses.get(dom, {}).get("bytes_per_launch")
-    roofline = {"bound": "hbm", "kernel_class": dom, "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": traffic, "peak_source": peak_kind,
-                "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
-                "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
-                "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
-    if dom in ("down0", "up0"):
-        roofline["note"] = ("temporally blocked level kernel: several smoothing steps per HBM "
-                            "pass, bytes counted once (compute-bound by design)")
 
     # ---- the operator kernel alone: the step-by-step smoothing step (k_cheb on the
     #      finest level) in a short profiled pass of an unfused batch
@@ -355,6 +365,174 @@ def run_ours(args, rank, world, local_rank):
             "cpu_baseline": cpu,
         }
     return out
+
+
+# ------------------------------------------------------------- rod-cell colonies
+ROD_METRIC = ("DOF-steps/s of rod-coupled colonies (reference cell loop: footprint, "
+              "gather, membrane exchange, deposit; then the FP32+IR solve)")
+
+
+def rod_colonies(args, rank: int):
+    from eq_gb300 import shard
+    from eq_gb300 import workloads as wl
+    base = shard.rank_seed(args.seed, rank)
+    return [wl.rod_colony(seed=base * 1000 + k) for k in range(args.colonies)]
+
+
+def colony_params(cols):
+    from eq_gb300 import field as F
+    return [F.trap_params(c.W, c.H, c.nx, c.ny, c.D[l], c.dt, c.g[l], c.walls)
+            for c in cols for l in range(c.n_layers)]
+
+
+def colony_batch(cols, opts):
+    from eq_gb300 import field as F
+    b = F.TrapBatch(colony_params(cols), opts)
+    t = 0
+    for c in cols:
+        b.set_rods(list(range(t, t + c.n_layers)), c.rods, c.ihsl, c.prod, c.mode, c.npm,
+                   c.dt, c.km)
+        t += c.n_layers
+    return b
+
+
+def run_rods(args, rank, world, local_rank):
+    import torch
+    from eq_gb300 import field as F
+    from eq_gb300 import shard
+    torch.cuda.set_device(local_rank)
+    cols = rod_colonies(args, rank)
+    dofs = sum(c.n_nodes * c.n_layers for c in cols)
+    ncells = sum(c.n_cells for c in cols)
+    opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1)
+    b = colony_batch(cols, opts)
+    waves = b.rod_waves()
+    stream = torch.cuda.ExternalStream(b.stream_handle())
+    b.step(args.warmup)
+    b.sync()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks = ClockSampler(local_rank)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        b.step(1)
+        ev[k + 1].record(stream)
+    b.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = shard.max_over_ranks(ev[0].elapsed_time(ev[-1]))
+    value = shard.sum_over_ranks(dofs * args.steps) / (total_ms / 1e3)
+    total_steps = args.warmup + args.steps
+    # relL2 of colony 0 against the plain FP64 form (the same colony alone)
+    c0 = cols[0]
+    u32 = [b.read_nodal(l) for l in range(c0.n_layers)]
+    i32 = b.read_rods(0)[0]
+    with colony_batch([c0], F.default_opts(F.FP64, use_graph=1, adaptive=1)) as b64:
+        b64.step(total_steps)
+        u64 = [b64.read_nodal(l) for l in range(c0.n_layers)]
+        i64 = b64.read_rods(0)[0]
+    rel = max(float(np.linalg.norm(a - z) / max(np.linalg.norm(z), 1e-300))
+              for a, z in zip(u32, u64))
+    reli = float(np.linalg.norm(i32 - i64) / max(np.linalg.norm(i64), 1e-300))
+    # profiled pass: the exchange's share and the dominant kernel's roofline
+    prof, prof_total, launches_per_step, roofline, _ = profiled_roofline(
+        b, stream, max(2, min(args.steps, 5)), "rod_colony")
+    ex = prof["rod_exchange"]
+    prof_steps = max(2, min(args.steps, 5))
+    b.close()
+    # e2e through the public API: every step the host re-sends every rod's geometry
+    # (the agent-based model moved them; footprints and waves are recomputed), steps,
+    # and reads every cell's intracellular and gathered HSL back
+    b = colony_batch(cols, opts)
+    b.step(args.warmup)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream_handle())
+    t0 = time.perf_counter()
+    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ee0.record(stream)
+    for _ in range(args.steps):
+        t = 0
+        for c in cols:
+            b.update_rods(t, c.rods)
+            t += c.n_layers
+        b.step(1)
+        t = 0
+        for c in cols:
+            b.read_rods(t)
+            t += c.n_layers
+    ee1.record(stream)
+    b.sync()
+    e2e_ms = max(ee0.elapsed_time(ee1), (time.perf_counter() - t0) * 1e3)
+    b.close()
+    rod_bytes = ncells * 160
+    state_bytes = sum(c.n_cells * c.n_layers * 16 + c.n_cells * 4 for c in cols)
+    e2e = {"value": dofs * args.steps / (e2e_ms / 1e3), "unit": UNIT,
+           "h2d_bytes_per_step": rod_bytes, "d2h_bytes_per_step": state_bytes,
+           "steps": args.steps, "timing": "wall clock and CUDA events, the larger"}
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            from oracle import cpu_baseline
+            cpu = cpu_baseline.rod_colony_rate(cols, args.cpu_steps, args.cpu_budget)
+        sm = sorted(step_ms)
+        out = {
+            "metric": ROD_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "p50_step_ms": float(np.percentile(sm, 50)), "p99_step_ms": float(np.percentile(sm, 99)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+fp64-ir (exchange f64)",
+            "data": "synthetic (seeded PCG64 colonies; the reference publishes no dataset)",
+            "config": {"workload": "rod_colony", "colonies": len(cols),
+                       "trap_um": [cols[0].W, cols[0].H], "nodes_per_micron": cols[0].npm,
+                       "layers": cols[0].n_layers, "dofs": dofs, "rods": ncells,
+                       "rod_waves": waves, "seed": args.seed, "rtol": opts.rtol,
+                       "graphs": True, "l2": "working set below L2 (per-step L2 reuse counted)",
+                       "parallelism": f"independent colonies, {world} replica(s)"},
+            "relL2_vs_fp64": {"nodal_max": rel, "ihsl": reli, "colony": 0,
+                              "steps": total_steps},
+            "exchange": {"ms_per_step": ex["ms"] / prof_steps,
+                         "launches_per_step": ex["launches"] / prof_steps,
+                         "share_of_step": round(ex["ms"] / max(prof_total, 1e-9), 4),
+                         "rod_steps_per_s": ncells * prof_steps / max(ex["ms"] / 1e3, 1e-12)},
+            "roofline": roofline,
+            "profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]}
+                        for k, v in prof.items() if v["launches"]},
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "e2e": e2e, "clocks": clk, "cpu_baseline": cpu,
+        }
+    return out
+
+
+def run_rods_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle import cpu_baseline
+    cols = rod_colonies(args, 0)
+    cores = os.cpu_count() or 1
+    sample = (cols * ((cores + len(cols) - 1) // len(cols)))[:cores]
+    cpu_baseline.rod_colony_rate(sample[:min(len(sample), 2)], 1, args.cpu_budget)  # warm-up
+    vals, last = [], None
+    for _ in range(args.steps):
+        last = cpu_baseline.rod_colony_rate(sample, 1, args.cpu_budget)
+        vals.append(last["value"])
+    value = float(np.median(vals))
+    return {"metric": ROD_METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (seeded PCG64 colonies)",
+            "config": {"workload": "rod_colony", "colonies": len(cols), "sampled": len(sample)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["cores"],
+                             "kind": "port", "sample": last["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's cell loop runs as its plain-C restatement (pinned bit for "
+                    "bit to the reference's own code) and its FEniCS/PETSc solve as assemble + "
+                    "LU per step (no DOLFIN/PETSc/MPI here)"}
 
 
 # --------------------------------------------------------------- reference arm
@@ -508,8 +686,18 @@ def run_serving(args, rank, world, local_rank):
 def run_ncu_target(args):
     """Minimal run for ncu captures: build the batch, step without graphs, exit."""
     from eq_gb300 import field as F
-    traps = make_workload(args.workload, args.seed, args.traps)
     prec = F.FP64 if args.fp64 else F.FP32_IR
+    if args.workload == "rod_colony":
+        cols = rod_colonies(args, 0)
+        b = colony_batch(cols, F.default_opts(prec, use_graph=0, adaptive=1))
+        b.step(args.warmup + args.steps)
+        b.sync()
+        print(json.dumps({"ncu_target": "rod_colony", "colonies": len(cols),
+                          "rods": sum(c.n_cells for c in cols), "waves": b.rod_waves(),
+                          "steps": args.warmup + args.steps}))
+        b.close()
+        return
+    traps = make_workload(args.workload, args.seed, args.traps)
     b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1,
                                                           tile_nodes=args.tile_nodes))
     for i, t in enumerate(traps):
@@ -530,6 +718,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched_uneven")
     ap.add_argument("--traps", type=int, default=512)
+    ap.add_argument("--colonies", type=int, default=16, help="rod_colony: simulations")
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--fp64-sample", type=int, default=8)
     ap.add_argument("--cpu-sample", type=int, default=16)
@@ -571,6 +760,11 @@ def main():
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
+    if args.workload == "rod_colony" and args.impl == "reference":
+        out = run_rods_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
         if out is not None:
@@ -579,7 +773,10 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    out = run_ours(args, rank, world, local_rank)
+    if args.workload == "rod_colony":
+        out = run_rods(args, rank, world, local_rank)
+    else:
+        out = run_ours(args, rank, world, local_rank)
     if world > 1:
         import torch
         torch.distributed.barrier()

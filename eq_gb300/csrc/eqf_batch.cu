@@ -403,18 +403,23 @@ class Batch {
     std::vector<int> layers;
     eqf_rod_law law{};
     RodLawDev dev{};
-    int n = 0, nent = 0, waves = 0, waves_cap = 0, grid = 0;
+    int n = 0, nent = 0, waves = 0, grid = 0;
     long long span = 0;  // lattice nodes of the layers' trap in device layout
     DevBuf<eqf_rod> rods;
     DevBuf<RodLawDev> dlaw;
     DevBuf<int> fp_off, fp_node, ent_cell, wave_cells, wave_off;
     DevBuf<int> cover, start, cursor, flag;  // wave analysis scratch
+    DevBuf<int4> winfo;     // wave order: (cell, footprint offset, size)
+    DevBuf<double> cellk;   // per cell: volume constants
     DevBuf<double> ihsl, prod, ehsl;
     DevBuf<unsigned char> mode;
   };
   std::vector<std::unique_ptr<RodSet>> rod_sets;
+  DevBuf<RodSetDev> d_rod_sets;        // one descriptor per set (blockIdx.y of a wave)
+  int rod_launches = 0, rod_grid = 0;  // wave launches and blocks per set, as captured
   RodSet* rod_set_of(int layer0);
   void rod_analyse(RodSet& rs);
+  void rod_publish();
   void enqueue_rods();
   void drop_graphs() {
     for (auto& gx : graph)
@@ -1178,7 +1183,6 @@ Batch::RodSet* Batch::rod_set_of(int layer0) {
 
 void Batch::rod_analyse(RodSet& rs) {
   const int n = rs.n, bs = 256;
-  bool moved = false;  // pointers or launch counts captured in a step change
   rs.grid = std::max(1, std::min((n * 32 + bs - 1) / bs, num_sms * 16));
   DevBuf<int> count;
   count.alloc(n);
@@ -1193,7 +1197,6 @@ void Batch::rod_analyse(RodSet& rs) {
     const size_t cap = (size_t)nent + (size_t)nent / 4 + 64;
     rs.fp_node.alloc(cap);
     rs.ent_cell.alloc(cap);
-    moved = true;
   }
   rs.nent = nent;
   k_rod_footprint<true><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, nullptr,
@@ -1260,33 +1263,76 @@ void Batch::rod_analyse(RodSet& rs) {
                            cudaMemcpyDeviceToHost, stream));
     sync();
   }
+  k_rod_cell_info<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p, rs.fp_off.p, rs.rods.p, rs.dlaw.p,
+                                         rs.winfo.p, rs.cellk.p);
+  EQF_LAUNCH_CHECK();
   rs.waves = (int)woff.size() - 1;
-  if (rs.waves > rs.waves_cap) {
-    rs.waves_cap = rs.waves;
-    moved = true;
-  }
-  // launches past the last wave (kept in captured steps) see empty ranges
-  woff.resize(rs.waves_cap + 1, n);
-  if (rs.wave_off.n < woff.size()) {
-    rs.wave_off.alloc(woff.size());
-    moved = true;
-  }
+  if (rs.wave_off.n < woff.size()) rs.wave_off.alloc(woff.size() + 8);
   EQF_CK(cudaMemcpyAsync(rs.wave_off.p, woff.data(), woff.size() * sizeof(int),
                          cudaMemcpyHostToDevice, stream));
   sync();
-  if (moved) drop_graphs();
+}
+
+// Device descriptors of every rod set.  A captured step holds only the descriptor
+// array, the launch count and the grid: it is re-captured when one of those changes.
+void Batch::rod_publish() {
+  std::vector<RodSetDev> h;
+  int waves = 0, grid = 1;
+  for (auto& up : rod_sets) {
+    RodSet& rs = *up;
+    RodSetDev d;
+    d.woff = rs.wave_off.p;
+    d.winfo = rs.winfo.p;
+    d.cellk = rs.cellk.p;
+    d.rods = rs.rods.p;
+    d.law = rs.dlaw.p;
+    d.fp_node = rs.fp_node.p;
+    d.ihsl = rs.ihsl.p;
+    d.prod = rs.prod.p;
+    d.mode = rs.mode.p;
+    d.ehsl = rs.ehsl.p;
+    d.waves = rs.waves;
+    h.push_back(d);
+    waves = std::max(waves, rs.waves);
+    grid = std::max(grid, std::min((rs.n + kRodThreads - 1) / kRodThreads, num_sms * 4));
+  }
+  // the exchange's shared-memory stash exceeds the default 48 KB per block
+  EQF_CK(cudaFuncSetAttribute(k_rod_exchange<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)rod_stash_bytes(1)));
+  EQF_CK(cudaFuncSetAttribute(k_rod_exchange<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)rod_stash_bytes(2)));
+  EQF_CK(cudaFuncSetAttribute(k_rod_exchange<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)rod_stash_bytes(3)));
+  EQF_CK(cudaFuncSetAttribute(k_rod_exchange<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)rod_stash_bytes(4)));
+  bool recapture = false;
+  if (d_rod_sets.n != h.size()) {
+    d_rod_sets.alloc(h.size());
+    recapture = true;
+  }
+  if (!h.empty())
+    EQF_CK(cudaMemcpyAsync(d_rod_sets.p, h.data(), h.size() * sizeof(RodSetDev),
+                           cudaMemcpyHostToDevice, stream));
+  sync();
+  if (waves > rod_launches || grid > rod_grid || h.empty()) recapture = true;
+  rod_launches = h.empty() ? 0 : std::max(rod_launches, waves);
+  rod_grid = h.empty() ? 0 : std::max(rod_grid, grid);
+  if (recapture) drop_graphs();
 }
 
 void Batch::enqueue_rods() {
-  for (auto& up : rod_sets) {
-    RodSet& rs = *up;
-    for (int w = 0; w < rs.waves_cap; ++w)
-      EQF_RUN(*this, KC_ROD,
-              (k_rod_exchange<<<rs.grid, 256, 0, stream>>>(
-                  w, rs.wave_off.p, rs.wave_cells.p, rs.rods.p, rs.dlaw.p, rs.fp_off.p,
-                  rs.fp_node.p, rs.ihsl.p, rs.prod.p, rs.mode.p, rs.ehsl.p, d_frozen.p,
-                  u_cur())));
-  }
+  if (rod_launches == 0) return;
+  const dim3 grid(rod_grid, (unsigned)rod_sets.size());
+  int nl = 1;
+  for (const auto& rs : rod_sets) nl = std::max(nl, (int)rs->layers.size());
+  auto kern = nl == 1 ? k_rod_exchange<1>
+              : nl == 2 ? k_rod_exchange<2>
+              : nl == 3 ? k_rod_exchange<3>
+                        : k_rod_exchange<4>;
+  const size_t smem = rod_stash_bytes(nl);  // opted in by rod_publish
+  for (int w = 0; w < rod_launches; ++w)
+    EQF_RUN(*this, KC_ROD,
+            (kern<<<grid, kRodThreads, smem, stream>>>(w, d_rod_sets.p, d_frozen.p, u_cur())));
 }
 
 void Batch::run_step() {
@@ -2103,7 +2149,7 @@ int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eq
     EQF_REQUIRE(n_cells >= 0 && n_cells <= (1 << 26), "bad rod cell count");
     if (n_cells == 0) {
       if (slot < B.rod_sets.size()) B.rod_sets.erase(B.rod_sets.begin() + slot);
-      B.drop_graphs();
+      B.rod_publish();
       return;
     }
     EQF_REQUIRE(rods && ihsl && production && mode, "null rod arrays");
@@ -2143,6 +2189,8 @@ int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eq
     rs->dlaw.alloc(1);
     rs->fp_off.alloc(n + 1);
     rs->wave_cells.alloc(n);
+    rs->winfo.alloc(n);
+    rs->cellk.alloc(3 * n);
     rs->cover.alloc(rs->span);
     rs->start.alloc(rs->span + 1);
     rs->cursor.alloc(rs->span);
@@ -2170,7 +2218,7 @@ int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eq
       B.rod_sets[slot] = std::move(rs);
     else
       B.rod_sets.push_back(std::move(rs));
-    B.drop_graphs();  // captured steps hold the previous set's pointers
+    B.rod_publish();
   });
 }
 
@@ -2198,6 +2246,7 @@ int eqf_update_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, const eqf_rod
     EQF_CK(cudaMemcpyAsync(rs->rods.p, rods, n * sizeof(eqf_rod), cudaMemcpyHostToDevice,
                            B.stream));
     B.rod_analyse(*rs);
+    B.rod_publish();
   });
 }
 

@@ -18,7 +18,8 @@
 // cells deposited on shared nodes.  Here the cells are grouped into waves: a cell's
 // wave is one more than the latest wave of any earlier cell sharing a node with it,
 // so within a wave no two cells touch the same node and every node sees its
-// deposits in cell order.  Each wave is one launch, one warp per cell.
+// deposits in cell order.  Each wave is one launch over every rod set of the
+// batch, one thread per cell.
 //
 // Every floating-point operation is a separately rounded IEEE operation (no fused
 // multiply-add), in the reference's order, so results match the reference's
@@ -269,68 +270,257 @@ __global__ void k_rod_iota(int n, int* __restrict__ cells) {
   if (c < n) cells[c] = c;
 }
 
+// Per cell in wave order: (cell, footprint offset, footprint size), and per cell
+// the eQ::Cell volume constants of its length, evaluated as the reference does:
+// computeCellVolumeActual V = (L - W) * pi r^2 + 4/3 pi r^3,
+// moleculeNumberToNanoMolar(1, L) = (1/V) * nM-per-molecule-per-um^3 and
+// computeExtraCellularVolumeFraction = 1 - V / (L*1*1) (src/eQcell.h:61-93).
+__global__ void k_rod_cell_info(int n, const int* __restrict__ cells,
+                                const int* __restrict__ fp_off, const eqf_rod* __restrict__ rods,
+                                const RodLawDev* __restrict__ law, int4* __restrict__ winfo,
+                                double* __restrict__ cellk) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int c = cells[idx];
+  winfo[idx] = make_int4(c, fp_off[c], fp_off[c + 1] - fp_off[c], 0);
+  const RodConst k = law->k;
+  const double len = rods[c].length;
+  const double V = r_add(r_mul(r_sub(len, 1.0), k.cyl), k.pole);
+  cellk[3 * c] = V;
+  cellk[3 * c + 1] = r_mul(r_div(1.0, V), k.nm_per_molecule);
+  cellk[3 * c + 2] = r_sub(1.0, r_div(V, len));
+}
+
 // --- the per-step exchange ---------------------------------------------------
 
-// One wave of the exchange: one warp per cell of cells[woff[wave] .. woff[wave+1]).
-// State per cell and layer at [c*kRodLayers + l]: ihsl (molecules), prod (nM/min),
-// mode (EQF_ROD_*), ehsl (out: the gathered mean).
-__global__ void k_rod_exchange(int wave, const int* __restrict__ woff,
-                               const int* __restrict__ cells, const eqf_rod* __restrict__ rods,
-                               const RodLawDev* __restrict__ law, const int* __restrict__ fp_off,
-                               const int* __restrict__ fp_node, double* __restrict__ ihsl,
-                               const double* __restrict__ prod,
-                               const unsigned char* __restrict__ mode,
-                               double* __restrict__ ehsl, const int* __restrict__ frozen,
-                               double* __restrict__ U) {
-  const RodLawDev& L = *law;  // per-layer fields are indexed: read them in place
+// What one wave launch needs of a rod set (device copy; the launch indexes it by
+// blockIdx.y, so pointer changes never invalidate a captured step).
+struct RodSetDev {
+  const int* woff;    // woff[w] .. woff[w+1]: cells of wave w
+  const int4* winfo;  // in wave order: (cell, footprint offset, footprint size, 0)
+  const double* cellk;  // per cell: volume, nM per molecule, extracellular fraction
+  const eqf_rod* rods;
+  const RodLawDev* law;
+  const int* fp_node;  // lattice nodes relative to the trap
+  double* ihsl;        // per cell and layer [c*kRodLayers + l]: molecules
+  const double* prod;  // nM per time unit
+  const unsigned char* mode;  // EQF_ROD_*
+  double* ehsl;        // out: the gathered footprint mean
+  int waves;
+};
+
+// The exchange of one cell once its footprint sums are known: the gathered means,
+// the membrane exchange and intracellular update, and the per-node deposit d[l]
+// (dep[l] false: the layer takes no deposit).
+template <int NL>
+__device__ __forceinline__ void rod_exchange_values(const RodSetDev& S, const RodLawDev& L,
+                                                    int c, int K, const double* sum,
+                                                    double* d, bool* dep) {
+  // per-cell volume constants (k_rod_cell_info)
+  const double V = S.cellk[3 * c], nmpm = S.cellk[3 * c + 1], ecf = S.cellk[3 * c + 2];
+  const double Kd = (double)K;
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    // readHSL: the footprint sum over the point count
+    const double e = r_div(sum[l], Kd);
+    const int s = c * kRodLayers + l;
+    const int md = S.mode[s];
+    S.ehsl[s] = e;
+    dep[l] = md != EQF_ROD_INERT;
+    d[l] = 0.0;
+    if (!dep[l]) continue;
+    // computeConcentrations: iHSL *= nanoMolarPerMolecule; dHSL = dt*(k_m*(iHSL - eHSL))
+    const double inm = r_mul(S.ihsl[s], nmpm);
+    const double dH = r_mul(L.dt, r_mul(L.km[l], r_sub(inm, e)));
+    // computeProteins: deltaHSL = dt*alpha - dHSL (circuit) or 0 (held)
+    const double delta = md == EQF_ROD_CIRCUIT ? r_sub(r_mul(L.dt, S.prod[s]), dH) : 0.0;
+    // pushConcentrations: iHSL += deltaHSL, clamped at 0, stored as molecules
+    double inew = r_add(inm, delta);
+    if (inew < 0.0) inew = 0.0;
+    S.ihsl[s] = r_div(inew, nmpm);
+    // writeHSL: molecules / extracellular fraction * npm^2 / K on every node
+    const double number = r_mul(r_div(dH, L.k.nm_per_molecule), V);
+    const double per_um2 = r_div(number, ecf);
+    d[l] = r_div(r_mul(r_mul(per_um2, L.npm), L.npm), Kd);
+  }
+}
+
+// One cell of a wave, NL layers.  The layers share the footprint walk and the
+// node loads are issued B at a time (the sums stay in footprint order).
+template <int NL, int B>
+__device__ __forceinline__ void rod_cell(const RodSetDev& S, const RodLawDev& L, int c, int f0,
+                                         int K, double* __restrict__ U) {
+  const int* __restrict__ fp = S.fp_node + f0;
+  double* u[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) u[l] = U + L.lay_off[l];
+  double sum[NL], d[NL];
+  bool dep[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) sum[l] = 0.0;
+  int k = 0;
+  for (; k + B <= K; k += B) {
+    int n[B];
+    double v[NL][B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) n[q] = fp[k + q];
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[l][q] = u[l][n[q]];
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q) sum[l] = r_add(sum[l], v[l][q]);
+  }
+  if (k < K) {  // the last K - k < B nodes: one predicated round of loads
+    int n[B];
+    double v[NL][B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) n[q] = k + q < K ? fp[k + q] : 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[l][q] = k + q < K ? u[l][n[q]] : 0.0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q)
+        if (k + q < K) sum[l] = r_add(sum[l], v[l][q]);
+  }
+  rod_exchange_values<NL>(S, L, c, K, sum, d, dep);
+  // deposit: the footprint's nodes are distinct, so each group of loads may run
+  // ahead of the group's stores
+  k = 0;
+  for (; k + B <= K; k += B) {
+    int n[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) n[q] = fp[k + q];
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      if (!dep[l]) continue;
+      double v[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[q] = u[l][n[q]];
+#pragma unroll
+      for (int q = 0; q < B; ++q) u[l][n[q]] = r_add(v[q], d[l]);
+    }
+  }
+  if (k < K) {
+    int n[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) n[q] = k + q < K ? fp[k + q] : 0;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      if (!dep[l]) continue;
+      double v[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[q] = k + q < K ? u[l][n[q]] : 0.0;
+#pragma unroll
+      for (int q = 0; q < B; ++q)
+        if (k + q < K) u[l][n[q]] = r_add(v[q], d[l]);
+    }
+  }
+}
+
+// The stashed form for footprints of at most KS nodes: the gather walks the
+// footprint in rounds of B loads with the next round's node indices prefetched,
+// and keeps every value and index in shared memory (this thread's slice, strided
+// by the block size), so the deposit is stores only -- no other cell of the wave
+// touches these nodes.
+constexpr int kRodStash = 64;     // footprint nodes held per thread
+constexpr int kRodThreads = 64;   // threads per block of the exchange
+
+__host__ __device__ constexpr size_t rod_stash_bytes(int nl) {
+  return (size_t)kRodThreads * kRodStash * (nl * sizeof(double) + sizeof(int));
+}
+
+template <int NL, int B>
+__device__ __forceinline__ void rod_cell_stash(const RodSetDev& S, const RodLawDev& L, int c,
+                                               int f0, int K, double* __restrict__ U,
+                                               double* __restrict__ smv, int* __restrict__ smi) {
+  const int t = threadIdx.x, nt = kRodThreads;
+  const int* __restrict__ fp = S.fp_node + f0;
+  double* u[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) u[l] = U + L.lay_off[l];
+  double sum[NL], d[NL];
+  bool dep[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) sum[l] = 0.0;
+  int nn[B];
+#pragma unroll
+  for (int q = 0; q < B; ++q) nn[q] = q < K ? fp[q] : 0;
+  for (int k = 0; k < K; k += B) {
+    int cur[B];
+    double v[NL][B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) cur[q] = nn[q];
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[l][q] = k + q < K ? u[l][cur[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) nn[q] = k + B + q < K ? fp[k + B + q] : 0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      if (k + q < K) {
+        smi[(k + q) * nt + t] = cur[q];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+          sum[l] = r_add(sum[l], v[l][q]);  // footprint order
+          smv[(l * kRodStash + k + q) * nt + t] = v[l][q];
+        }
+      }
+    }
+  }
+  rod_exchange_values<NL>(S, L, c, K, sum, d, dep);
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    if (!dep[l]) continue;
+    for (int q = 0; q < K; ++q)
+      u[l][smi[q * nt + t]] = r_add(smv[(l * kRodStash + q) * nt + t], d[l]);
+  }
+}
+
+// One wave of every rod set: one thread per cell (the cells of a wave touch
+// disjoint nodes).  A cell's gather is a serial sum in footprint order, so one
+// thread per cell lets 32 cells share each double-precision instruction.  NL is
+// the batch's largest layer count; a set with fewer layers takes the matching
+// instantiation of the cell body.
+template <int NL>
+__global__ void __launch_bounds__(kRodThreads) k_rod_exchange(
+    int wave, const RodSetDev* __restrict__ sets, const int* __restrict__ frozen,
+    double* __restrict__ U) {
+  extern __shared__ __align__(16) unsigned char rod_smem[];
+  double* smv = reinterpret_cast<double*>(rod_smem);
+  int* smi = reinterpret_cast<int*>(smv + (size_t)NL * kRodStash * kRodThreads);
+  const RodSetDev S = sets[blockIdx.y];  // by value: its loads issue together
+  if (wave >= S.waves) return;
+  const RodLawDev L = *S.law;
   if (frozen && frozen[L.trap0]) return;
-  const int lane = threadIdx.x & 31;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  const int a = woff[wave], b = woff[wave + 1];
-  for (int idx = a + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); idx < b; idx += warps) {
-    const int c = cells[idx];
-    const int f0 = fp_off[c], K = fp_off[c + 1] - f0;
-    const double len = rods[c].length;
-    // eQ::Cell::computeCellVolumeActual: (L - W) * pi r^2 + 4/3 pi r^3
-    const double V = r_add(r_mul(r_sub(len, 1.0), L.k.cyl), L.k.pole);
-    // moleculeNumberToNanoMolar(1, L) = (1/V) * nM-per-molecule-per-um^3
-    const double nmpm = r_mul(r_div(1.0, V), L.k.nm_per_molecule);
-    // computeExtraCellularVolumeFraction = 1 - V / (L*1*1)
-    const double ecf = r_sub(1.0, r_div(V, len));
-    const double Kd = (double)K;
-    for (int l = 0; l < L.nlayers; ++l) {
-      double* u = U + L.lay_off[l];
-      // readHSL: HSL = 0; HSL += u[node] in footprint order; HSL / K
-      double sum = 0.0;
-      for (int k0 = 0; k0 < K; k0 += 32) {
-        const int k = k0 + lane;
-        const double v = k < K ? u[fp_node[f0 + k]] : 0.0;
-        const int m = K - k0 < 32 ? K - k0 : 32;
-        for (int t = 0; t < m; ++t) sum = r_add(sum, __shfl_sync(0xffffffffu, v, t));
-      }
-      const double e = r_div(sum, Kd);
-      const int s = c * kRodLayers + l;
-      const int md = mode[s];
-      if (lane == 0) ehsl[s] = e;
-      if (md == EQF_ROD_INERT) continue;
-      // computeConcentrations: iHSL *= nanoMolarPerMolecule; dHSL = dt*(k_m*(iHSL - eHSL))
-      const double inm = r_mul(ihsl[s], nmpm);
-      const double dH = r_mul(L.dt, r_mul(L.km[l], r_sub(inm, e)));
-      // computeProteins: deltaHSL = dt*alpha - dHSL (circuit) or 0 (held)
-      const double delta = md == EQF_ROD_CIRCUIT ? r_sub(r_mul(L.dt, prod[s]), dH) : 0.0;
-      // pushConcentrations: iHSL += deltaHSL, clamped at 0, stored as molecules
-      double inew = r_add(inm, delta);
-      if (inew < 0.0) inew = 0.0;
-      // writeHSL: molecules / extracellular fraction * npm^2 / K on every node
-      const double number = r_mul(r_div(dH, L.k.nm_per_molecule), V);
-      const double per_um2 = r_div(number, ecf);
-      const double d = r_div(r_mul(r_mul(per_um2, L.npm), L.npm), Kd);
-      __syncwarp();
-      if (lane == 0) ihsl[s] = r_div(inew, nmpm);
-      for (int k = lane; k < K; k += 32) {
-        double* p = u + fp_node[f0 + k];
-        *p = r_add(*p, d);
-      }
+  const int a = S.woff[wave], b = S.woff[wave + 1];
+  const int nl = L.nlayers;
+  for (int idx = a + blockIdx.x * blockDim.x + threadIdx.x; idx < b;
+       idx += gridDim.x * blockDim.x) {
+    const int4 w = S.winfo[idx];
+    if (w.z <= kRodStash) {
+      if (NL == 1 || nl == 1)
+        rod_cell_stash<1, 16>(S, L, w.x, w.y, w.z, U, smv, smi);
+      else if (NL == 2 || nl == 2)
+        rod_cell_stash<2, 16>(S, L, w.x, w.y, w.z, U, smv, smi);
+      else if (NL == 3 || nl == 3)
+        rod_cell_stash<(NL < 3 ? NL : 3), 8>(S, L, w.x, w.y, w.z, U, smv, smi);
+      else
+        rod_cell_stash<NL, 8>(S, L, w.x, w.y, w.z, U, smv, smi);
+    } else if (NL == 1 || nl == 1) {
+      rod_cell<1, 8>(S, L, w.x, w.y, w.z, U);
+    } else if (NL == 2 || nl == 2) {
+      rod_cell<2, 8>(S, L, w.x, w.y, w.z, U);
+    } else if (NL == 3 || nl == 3) {
+      rod_cell<(NL < 3 ? NL : 3), 8>(S, L, w.x, w.y, w.z, U);
+    } else {
+      rod_cell<NL, 8>(S, L, w.x, w.y, w.z, U);
     }
   }
 }

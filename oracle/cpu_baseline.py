@@ -57,3 +57,55 @@ def reference_rate(traps, idx, steps_per_trap: int, budget_s: float, timeout_s: 
                       f"step(s) each: re-assemble + LU factor + solve per step (scipy SuperLU), "
                       f"one trap per process",
             "dof_steps": int(dofs), "wall_s": round(wall, 3)}
+
+
+def _rod_worker(args):
+    (col, steps, budget_s) = args
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    from oracle import hsld, rods_port
+    nl = col.n_layers
+    fields = np.zeros((nl, col.ny + 1, col.nx + 1))
+    ex = rods_port.Exchanger(fields, col.rods, col.ihsl, col.prod, col.mode, col.npm, col.dt,
+                             col.km)
+    t0 = time.perf_counter()
+    t_ex = 0.0
+    done = 0
+    for _ in range(steps):
+        te = time.perf_counter()
+        ex.run()  # the cell loop: footprints, gather, exchange, deposit into u0
+        t_ex += time.perf_counter() - te
+        for l in range(nl):
+            o = hsld.HsldOracle(col.W, col.H, col.nx, col.ny, col.D[l], col.dt, col.g[l],
+                                col.walls)
+            ex.f[l] = o.step(ex.f[l].ravel()).reshape(ex.f[l].shape)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return col.n_nodes * nl * done, time.perf_counter() - t0, t_ex, done * col.n_cells
+
+
+def rod_colony_rate(colonies, steps: int, budget_s: float, timeout_s: float = 600.0):
+    """DOF-steps/s of the reference's coupled step on host cores: the rod cell loop
+    (plain-C restatement) then, per layer, re-assemble + LU factor + solve
+    (scipy SuperLU), one colony per process."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    jobs = [(c, steps, budget_s) for c in colonies[:max(1, cores)]]
+    procs = min(cores, len(jobs))
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(processes=procs) as pool:
+        res = pool.map_async(_rod_worker, jobs).get(timeout=timeout_s)
+    wall = time.perf_counter() - t0
+    dofs = sum(r[0] for r in res)
+    span = max(r[1] for r in res)
+    t_ex = sum(r[2] for r in res)
+    cell_steps = sum(r[3] for r in res)
+    return {"value": dofs / max(span, 1e-9), "unit": "DOF-steps/s", "cores": procs,
+            "kind": "port",
+            "sample": f"{len(jobs)} colonies ({colonies[0].n_cells} rods, {colonies[0].n_layers} "
+                      f"layers of {colonies[0].n_nodes} nodes each), up to {steps} step(s) "
+                      f"each: rod cell loop in C, then re-assemble + LU factor + solve per "
+                      f"layer (scipy SuperLU), one colony per process",
+            "exchange_cells_per_s_per_core": cell_steps / max(t_ex, 1e-9),
+            "dof_steps": int(dofs), "wall_s": round(wall, 3)}

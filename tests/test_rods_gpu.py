@@ -241,3 +241,37 @@ def test_rod_argument_errors(lib):
                        col.npm, col.dt, col.km[:1])
         with pytest.raises(F.EqfError):   # count changes need eqf_set_rods
             b.update_rods(0, col.rods[:5])
+
+
+def test_several_rod_sets_in_one_batch_bitwise(lib):
+    """Colonies with different wave counts share each wave launch."""
+    cols = [wl.rod_colony(seed=30, W=24.0, H=12.0, npm=2.0, n_cells=40),
+            wl.rod_colony(seed=31, W=20.0, H=10.0, npm=4.0, n_cells=150),
+            wl.rod_colony(seed=32, W=16.0, H=8.0, npm=2.0, n_cells=5)]
+    rng = np.random.Generator(np.random.PCG64(5))
+    params, fields, ihs = [], [], []
+    for c in cols:
+        params += layer_params(c.W, c.H, c.npm, c.n_layers)
+        fields.append([rng.uniform(0, 30, (c.ny + 1, c.nx + 1)) for _ in range(c.n_layers)])
+        ihs.append(rng.uniform(0, 3000, (c.n_cells, c.n_layers)))
+    with F.TrapBatch(params, F.default_opts(F.FP64)) as b:
+        t = 0
+        for c, f, ih in zip(cols, fields, ihs):
+            for l in range(c.n_layers):
+                b.set_nodal(t + l, f[l].ravel())
+            b.set_rods(list(range(t, t + c.n_layers)), c.rods, ih, c.prod, c.mode, c.npm, c.dt,
+                       c.km)
+            t += c.n_layers
+        waves = [oracle_waves(c.rods, c.npm, c.nx, c.ny) for c in cols]
+        assert b.rod_waves() == max(waves) and len(set(waves)) > 1
+        for _ in range(2):
+            b.exchange_rods()
+            for c, f, ih in zip(cols, fields, ihs):
+                ih[:], _, _ = R.exchange(f, c.rods, ih, c.prod, c.mode, c.npm, c.dt, c.km)
+        t = 0
+        for c, f, ih in zip(cols, fields, ihs):
+            gi, _, _ = b.read_rods(t)
+            assert np.array_equal(gi, ih)
+            for l in range(c.n_layers):
+                assert np.array_equal(b.read_nodal(t + l), f[l].ravel())
+            t += c.n_layers

@@ -11,6 +11,7 @@ from eq_gb300 import _lib
 from eq_gb300 import workloads as wl
 from oracle import ref_rods
 from oracle import rods as R
+from oracle import rods_port
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "rods_reference.npz")
 CASES = ("colony", "walls", "grown", "lattice", "stack")
@@ -125,3 +126,18 @@ def test_oracle_matches_reference_on_fresh_colonies(seed):
     assert np.array_equal(e1, e2) and np.array_equal(i1, i2)
     for l in range(nl):
         assert np.array_equal(f[l], f2[l])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_c_restatement_matches_reference_golden_bitwise(name):
+    """The plain-C restatement (the timed CPU baseline) is the same function."""
+    z = np.load(GOLDEN)
+    W, H, npm, dt, rods = golden_case(z, name)
+    ex = rods_port.Exchanger(z[f"{name}/fields_in"], rods, z[f"{name}/ihsl_in"],
+                             z[f"{name}/prod"], z[f"{name}/mode"], npm, dt, z[f"{name}/km"])
+    for p in range(3):
+        ex.run()
+        assert np.array_equal(ex.eh, z[f"{name}/ehsl_{p}"]), p
+        assert np.array_equal(ex.ih, z[f"{name}/ihsl_{p}"]), p
+    assert np.array_equal(ex.f, z[f"{name}/fields_out"])
+    assert np.array_equal(ex.pts, z[f"{name}/points"])
