@@ -34,7 +34,12 @@ EXPORTS = (
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
     "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
+    "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels",
 )
+
+# wall conditions (eqf_set_boundaries)
+EQF_SIDE_BOTTOM, EQF_SIDE_TOP, EQF_SIDE_LEFT, EQF_SIDE_RIGHT = 0, 1, 2, 3
+EQF_BC_NEUMANN, EQF_BC_DIRICHLET, EQF_BC_ROBIN, EQF_BC_CHANNEL = 0, 1, 2, 3
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
                 "down0", "up0", "rod_exchange")
@@ -68,6 +73,16 @@ EQF_TUNE_MAX_BUCKETS = 8
 
 class TuneTable(C.Structure):
     _fields_ = [("n", C.c_int32), ("b", TuneBucket * EQF_TUNE_MAX_BUCKETS)]
+
+
+class Wall(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("value", C.c_double), ("rate", C.c_double)]
+
+
+class Boundaries(C.Structure):
+    _fields_ = [("wall", Wall * 4), ("channel_velocity", C.c_double), ("channel_D", C.c_double),
+                ("channel_rate", C.c_double * 2), ("channel_substeps", C.c_int32),
+                ("well_scaling", C.c_double)]
 
 
 class RodLaw(C.Structure):
@@ -146,6 +161,9 @@ def load() -> C.CDLL:
         "eqf_update_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, dp]),
         "eqf_read_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp, P(C.c_int32)]),
         "eqf_exchange_rods": (C.c_int, [C.c_void_p]),
+        "eqf_set_boundaries": (C.c_int, [C.c_void_p, C.c_int32, P(Boundaries)]),
+        "eqf_read_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),
+        "eqf_set_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),
         "eqf_rod_waves": (C.c_int, [C.c_void_p, P(C.c_int32)]),
     }
     for name, (res, args) in sig.items():

@@ -17,7 +17,7 @@ SOURCES = [os.path.join(CSRC, f) for f in ("eqf_batch.cu", "eqf_noalloc.cu", "eq
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("eqf_common.cuh", "eqf_kernels.cuh",
                                                    "eqf_cells.cuh", "eqf_refine.cuh",
                                                    "eqf_bicgstab.cuh", "eqf_fused.cuh",
-                                                   "eqf_rods.cuh")] + \
+                                                   "eqf_rods.cuh", "eqf_walls.cuh")] + \
     [os.path.join(ROOT, "include", h) for h in ("eqfield.h", "eqserve.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -25,6 +25,7 @@
 #include "eqf_bicgstab.cuh"
 #include "eqf_fused.cuh"
 #include "eqf_rods.cuh"
+#include "eqf_walls.cuh"
 
 namespace eqf {
 
@@ -136,6 +137,7 @@ static Lens<T> make_lens(const LevelGeom& g) {
   L.alpha = (T)g.alpha;
   L.beta = (T)g.beta;
   L.adv = (T)g.adv;
+  for (int w = 0; w < 4; ++w) L.rob[w] = (T)g.rob[w];
   return L;
 }
 
@@ -414,6 +416,23 @@ class Batch {
     DevBuf<double> ihsl, prod, ehsl;
     DevBuf<unsigned char> mode;
   };
+  // wall conditions (eqf_set_boundaries) and the flow channels
+  std::vector<eqf_boundaries> bcs;  // per trap
+  bool walls_active = false;        // some trap carries wall values, Robin loads or channels
+  std::vector<WallDev> hwalls;
+  DevBuf<WallDev> d_walls;
+  DevBuf<double> d_fbase;  // F of the point cells on the wall traps' rims
+  int rim_max = 0;
+  struct Chan {
+    int trap = 0, n = 0, levels = 0;
+    DevBuf<double> k1, k2, bfin, bl, bd, bu, c[2];
+  };
+  std::vector<std::unique_ptr<Chan>> chans;
+  DevBuf<ChanDev> d_chans;
+  int chan_n_max = 0;
+  void setup_walls();
+  void enqueue_walls();
+  void enqueue_channels();
   std::vector<std::unique_ptr<RodSet>> rod_sets;
   DevBuf<RodSetDev> d_rod_sets;        // one descriptor per set (blockIdx.y of a wave)
   int rod_launches = 0, rod_grid = 0;  // wave launches and blocks per set, as captured
@@ -474,6 +493,16 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
     int dev = 0;
     EQF_CK(cudaGetDevice(&dev));
     EQF_CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  bcs.resize(ntraps);
+  for (int t = 0; t < ntraps; ++t) {
+    eqf_boundaries& bc = bcs[t];
+    std::memset(&bc, 0, sizeof(bc));
+    const unsigned bits[4] = {WALL_BOTTOM, WALL_TOP, WALL_LEFT, WALL_RIGHT};
+    for (int w = 0; w < 4; ++w)
+      bc.wall[w].kind = (params[t].walls & bits[w]) ? EQF_BC_DIRICHLET : EQF_BC_NEUMANN;
+    bc.channel_substeps = 1;
+    bc.well_scaling = 1.0;
   }
   build_levels();
   bool adv = false;
@@ -572,6 +601,7 @@ static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solv
 }
 
 void Batch::build_levels() {
+  L.clear();
   int nl = 1;
   for (const auto& p : params) nl = std::max(nl, trap_levels(p));
   nlev = nl;
@@ -589,9 +619,16 @@ void Batch::build_levels() {
     g.alpha = 1.0 + p.dt * p.decay;
     g.beta = p.dt * p.D;
     g.adv = (p.adv_u != 0.0 && p.adv_len > 0.0) ? p.dt * p.adv_u / p.adv_len : 0.0;
+    const eqf_boundaries& bc = bcs[t];
+    for (int w = 0; w < 4; ++w)
+      g.rob[w] = bc.wall[w].kind == EQF_BC_ROBIN ? p.dt * bc.wall[w].rate : 0.0;
+    for (int w = 0; w < 4; ++w)
+      g.dvals = g.dvals || bc.wall[w].kind == EQF_BC_CHANNEL ||
+                (bc.wall[w].kind == EQF_BC_DIRICHLET && bc.wall[w].value != 0.0);
     for (int l = 0; l < nlev; ++l) {
       if (l > 0) {
         LevelGeom c = g;
+        c.dvals = 0;  // coarse levels carry corrections: homogeneous walls
         c.fine_nx = g.nx;
         c.fine_ny = g.ny;
         c.cx = g.nx >= 4;
@@ -1172,6 +1209,179 @@ void Batch::enqueue_coupling() {
 }
 
 // ---------------------------------------------------------------------------
+// Wall conditions with values, Robin loads and flow channels (eqf_set_boundaries).
+
+// Device data of the traps whose walls carry values, Robin loads or channels: their
+// rim slots, and per channel trap the Crank-Nicolson matrices of the sub-step with
+// the parallel-cyclic-reduction multipliers of its left side.
+void Batch::setup_walls() {
+  hwalls.clear();
+  chans.clear();
+  rim_max = 0;
+  chan_n_max = 0;
+  int rim_total = 0;
+  for (int t = 0; t < ntraps; ++t) {
+    const eqf_boundaries& bc = bcs[t];
+    const eqf_trap_params& p = params[t];
+    bool active = false, channel = false;
+    for (int w = 0; w < 4; ++w) {
+      const eqf_wall& wl = bc.wall[w];
+      active = active || wl.kind == EQF_BC_CHANNEL ||
+               (wl.kind != EQF_BC_NEUMANN && wl.value != 0.0);
+      channel = channel || wl.kind == EQF_BC_CHANNEL;
+    }
+    if (!active) continue;
+    WallDev wd{};
+    wd.trap = t;
+    wd.rim0 = rim_total;
+    for (int w = 0; w < 4; ++w) {
+      wd.kind[w] = bc.wall[w].kind;
+      wd.value[w] = bc.wall[w].value;
+      wd.robs[w] = bc.wall[w].kind == EQF_BC_ROBIN ? p.dt * bc.wall[w].rate * bc.wall[w].value : 0.0;
+    }
+    const int nr = rim_count(p.nx, p.ny);
+    rim_total += nr;
+    rim_max = std::max(rim_max, nr);
+    if (channel) {
+      // the channel: nx cells of h_c = W/nx on [0, W], dt_c = dt / substeps
+      auto ch = std::make_unique<Chan>();
+      ch->trap = t;
+      const int n = p.nx + 1;
+      ch->n = n;
+      const double h = p.width / p.nx, dtc = p.dt / bc.channel_substeps;
+      const double D = bc.channel_D, v = bc.channel_velocity;
+      // element matrices of fenics/AdvectionDiffusion.ufl (test row, trial column):
+      // M h/6 [2 1; 1 2], K 1/h [1 -1; -1 1], C (w * du/dx) [-1/2 1/2; -1/2 1/2]
+      std::vector<double> a(n, 0.0), b(n, 0.0), c(n, 0.0), bl(n, 0.0), bd(n, 0.0), bu(n, 0.0);
+      const double me[2][2] = {{h / 3.0, h / 6.0}, {h / 6.0, h / 3.0}};
+      const double ke[2][2] = {{1.0 / h, -1.0 / h}, {-1.0 / h, 1.0 / h}};
+      const double ce[2][2] = {{-0.5, 0.5}, {-0.5, 0.5}};
+      for (int e = 0; e < n - 1; ++e)
+        for (int r = 0; r < 2; ++r)
+          for (int q = 0; q < 2; ++q) {
+            const double op = 0.5 * dtc * (D * ke[r][q] + v * ce[r][q]);
+            const double lhs = me[r][q] + op, rhs = me[r][q] - op;
+            const int i = e + r, jn = e + q;
+            if (jn == i) {
+              b[i] += lhs;
+              bd[i] += rhs;
+            } else if (jn == i + 1) {
+              c[i] += lhs;
+              bu[i] += rhs;
+            } else {
+              a[i] += lhs;
+              bl[i] += rhs;
+            }
+          }
+      // Robin ends: dt_c * r * (0.5 (c0 + c) - 0) w at x = 0 (ds(1)) and x = W (ds(2))
+      b[0] += 0.5 * dtc * bc.channel_rate[0];
+      bd[0] -= 0.5 * dtc * bc.channel_rate[0];
+      b[n - 1] += 0.5 * dtc * bc.channel_rate[1];
+      bd[n - 1] -= 0.5 * dtc * bc.channel_rate[1];
+      // parallel cyclic reduction of the left side: at stride s, row i eliminates
+      // x_{i-s} and x_{i+s} with rows i-s and i+s
+      std::vector<double> k1, k2;
+      int levels = 0;
+      for (int st = 1; st < n; st <<= 1, ++levels) {
+        std::vector<double> na(n, 0.0), nb(n, 0.0), nc(n, 0.0);
+        k1.resize((size_t)(levels + 1) * n);
+        k2.resize((size_t)(levels + 1) * n);
+        for (int i = 0; i < n; ++i) {
+          const double m1 = i - st >= 0 ? a[i] / b[i - st] : 0.0;
+          const double m2 = i + st < n ? c[i] / b[i + st] : 0.0;
+          k1[(size_t)levels * n + i] = m1;
+          k2[(size_t)levels * n + i] = m2;
+          na[i] = i - st >= 0 ? -a[i - st] * m1 : 0.0;
+          nc[i] = i + st < n ? -c[i + st] * m2 : 0.0;
+          nb[i] = b[i] - (i - st >= 0 ? c[i - st] * m1 : 0.0) - (i + st < n ? a[i + st] * m2 : 0.0);
+        }
+        a.swap(na);
+        b.swap(nb);
+        c.swap(nc);
+      }
+      ch->levels = levels;
+      auto up = [&](DevBuf<double>& d, const std::vector<double>& h_) {
+        d.alloc(std::max<size_t>(1, h_.size()));
+        if (!h_.empty()) d.upload(h_.data(), h_.size(), stream);
+      };
+      up(ch->k1, k1);
+      up(ch->k2, k2);
+      up(ch->bfin, b);
+      up(ch->bl, bl);
+      up(ch->bd, bd);
+      up(ch->bu, bu);
+      for (int side = 0; side < 2; ++side)
+        if (bc.wall[side].kind == EQF_BC_CHANNEL) {
+          ch->c[side].alloc(n);
+          EQF_CK(cudaMemsetAsync(ch->c[side].p, 0, n * sizeof(double), stream));
+          wd.chan[side] = ch->c[side].p;
+        }
+      chan_n_max = std::max(chan_n_max, n);
+      chans.push_back(std::move(ch));
+    }
+    hwalls.push_back(wd);
+  }
+  walls_active = !hwalls.empty();
+  d_walls.alloc(hwalls.size());
+  if (walls_active) d_walls.upload(hwalls.data(), hwalls.size(), stream);
+  d_fbase.alloc(std::max(rim_total, 1));
+  EQF_CK(cudaMemsetAsync(d_fbase.p, 0, d_fbase.n * sizeof(double), stream));
+  std::vector<ChanDev> hc;
+  for (const auto& up : chans) {
+    const Chan& ch = *up;
+    const eqf_boundaries& bc = bcs[ch.trap];
+    const eqf_trap_params& p = params[ch.trap];
+    ChanDev d{};
+    d.trap = ch.trap;
+    d.n = ch.n;
+    d.levels = ch.levels;
+    d.substeps = bc.channel_substeps;
+    d.h = p.height / p.ny;
+    d.dtD = p.dt * p.D;
+    d.well = bc.well_scaling;
+    d.k1 = ch.k1.p;
+    d.k2 = ch.k2.p;
+    d.bfin = ch.bfin.p;
+    d.bl = ch.bl.p;
+    d.bd = ch.bd.p;
+    d.bu = ch.bu.p;
+    d.c[0] = ch.c[0].p;
+    d.c[1] = ch.c[1].p;
+    hc.push_back(d);
+  }
+  d_chans.alloc(hc.size());
+  if (!hc.empty()) {
+    d_chans.upload(hc.data(), hc.size(), stream);
+    EQF_CK(cudaFuncSetAttribute(k_channel_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)chan_smem_bytes(chan_n_max)));
+  }
+  // the load vector restarts from the point cells alone (rims included)
+  if (!cells_dirty) {
+    EQF_CK(cudaMemsetAsync(F.p, 0, L[0].nodes * sizeof(double), stream));
+    refresh_load();
+  }
+  drop_graphs();
+  sync();
+}
+
+void Batch::enqueue_walls() {
+  if (!walls_active) return;
+  const dim3 grid((rim_max + 255) / 256, (unsigned)hwalls.size());
+  EQF_RUN(*this, KC_SCALAR,
+          (k_wall_rim<2><<<grid, 256, 0, stream>>>(d_walls.p, L[0].dgeom.p, F.p, d_fbase.p)));
+}
+
+// After the step's solve (the new field is U[1 - cur]): fluxes into the channels and
+// their sub-steps.
+void Batch::enqueue_channels() {
+  if (chans.empty()) return;
+  EQF_RUN(*this, KC_SCALAR,
+          (k_channel_step<<<dim3((unsigned)chans.size(), 2), kChanThreads,
+                            chan_smem_bytes(chan_n_max), stream>>>(
+              d_chans.p, L[0].dgeom.p, U[1 - cur].p, d_frozen.p)));
+}
+
+// ---------------------------------------------------------------------------
 // Rod cells: footprints and dependency waves (at every geometry update), and the
 // per-step exchange (one launch per wave, captured with the step).
 
@@ -1338,6 +1548,7 @@ void Batch::enqueue_rods() {
 void Batch::run_step() {
   enqueue_rods();
   enqueue_coupling();
+  enqueue_walls();
   for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
   work->enqueue_check(stream, true);
 }
@@ -1389,10 +1600,12 @@ void Batch::step(int n) {
       }
       if (f != 0) {
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        enqueue_channels();
         cur = 1 - cur;
         throw Error(EQF_ERR_NOT_CONVERGED, "trap(s) missed rtol after extra refinement sweeps");
       }
     }
+    enqueue_channels();
     cur = 1 - cur;
     ++steps_done;
   }
@@ -1455,6 +1668,7 @@ void Batch::rebuild_cells() {
   EQF_CK(cudaMemsetAsync(F.p, 0, L[0].nodes * sizeof(double), stream));
   if (ncells == 0) {
     nseg = 0;
+    if (walls_active) EQF_CK(cudaMemsetAsync(d_fbase.p, 0, d_fbase.n * sizeof(double), stream));
     sync();
     return;
   }
@@ -1537,6 +1751,9 @@ void Batch::rebuild_cells() {
 // F = dt * sum_i s_i phi(x_i) from the current rates (segments fixed)
 void Batch::refresh_load() {
   if (ncells == 0) return;
+  const dim3 rim_grid((rim_max + 255) / 256, (unsigned)hwalls.size());
+  if (walls_active)  // the rim takes the point cells' load alone, then is kept apart
+    k_wall_rim<0><<<rim_grid, 256, 0, stream>>>(d_walls.p, L[0].dgeom.p, F.p, d_fbase.p);
   // rates changed: restore the canonical order of every node's contributions
   k_seg_sort<<<(nseg + 255) / 256, 256, 0, stream>>>(nseg, d_seg_start.p, d_perm.p, d_cell_xy.p,
                                                      d_cell_s.p, nullptr);
@@ -1547,6 +1764,10 @@ void Batch::refresh_load() {
   k_seg_sum<false><<<(nseg + 255) / 256, 256, 0, stream>>>(nseg, d_seg_start.p, d_perm.p,
                                                            d_ent_node.p, d_ent_val.p, F.p);
   EQF_LAUNCH_CHECK();
+  if (walls_active) {
+    k_wall_rim<1><<<rim_grid, 256, 0, stream>>>(d_walls.p, L[0].dgeom.p, F.p, d_fbase.p);
+    EQF_LAUNCH_CHECK();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2077,6 +2298,101 @@ int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c) {
                            B.stream));
     B.sync();
     B.check_fail();
+  });
+}
+
+// Wall conditions and flow channels (eqfield.h: eqf_set_boundaries).
+int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(bc != nullptr, "null boundaries");
+    Batch& B = *b->impl;
+    const eqf_trap_params& p = B.params[trap];
+    unsigned walls = 0;
+    bool channel = false, active = false;
+    const unsigned bits[4] = {eqf::WALL_BOTTOM, eqf::WALL_TOP, eqf::WALL_LEFT, eqf::WALL_RIGHT};
+    for (int w = 0; w < 4; ++w) {
+      const eqf_wall& wl = bc->wall[w];
+      EQF_REQUIRE(wl.kind >= EQF_BC_NEUMANN && wl.kind <= EQF_BC_CHANNEL, "bad wall kind");
+      EQF_REQUIRE(std::isfinite(wl.value) && std::isfinite(wl.rate), "non-finite wall value");
+      EQF_REQUIRE(wl.kind != EQF_BC_ROBIN || wl.rate >= 0.0, "negative Robin rate");
+      EQF_REQUIRE(wl.kind != EQF_BC_CHANNEL || w <= EQF_SIDE_TOP,
+                  "channels border the bottom and top walls only");
+      if (wl.kind == EQF_BC_DIRICHLET || wl.kind == EQF_BC_CHANNEL) walls |= bits[w];
+      channel = channel || wl.kind == EQF_BC_CHANNEL;
+      active = active || wl.kind == EQF_BC_CHANNEL ||
+               (wl.kind != EQF_BC_NEUMANN && wl.value != 0.0);
+    }
+    if (active) EQF_REQUIRE(p.nx >= 3 && p.ny >= 3, "walls with values need nx, ny >= 3");
+    if (channel) {
+      EQF_REQUIRE(bc->channel_substeps >= 1 && std::isfinite(bc->channel_D) &&
+                      bc->channel_D >= 0.0 && std::isfinite(bc->channel_velocity) &&
+                      std::isfinite(bc->channel_rate[0]) && std::isfinite(bc->channel_rate[1]) &&
+                      bc->channel_rate[0] >= 0.0 && bc->channel_rate[1] >= 0.0 &&
+                      std::isfinite(bc->well_scaling) && bc->well_scaling > 0.0,
+                  "bad channel parameters");
+      EQF_REQUIRE(p.nx + 1 <= eqf::kChanMaxNodes, "channel longer than 4097 nodes");
+      const double hx = p.width / p.nx, hy = p.height / p.ny;
+      EQF_REQUIRE(std::fabs(hx - hy) <= 1e-12 * hx, "channel walls need a square lattice");
+    }
+    if (p.adv_u != 0.0 && p.adv_len > 0.0)
+      EQF_REQUIRE(!active, "walls with values on advective traps are not supported");
+    B.sync();
+    B.bcs[trap] = *bc;
+    B.params[trap].walls = walls;
+    B.build_levels();
+    B.setup_walls();
+    // a new operator invalidates the initial-guess history of that trap
+    const long long off = B.L[0].geom[trap].off;
+    EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
+    EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
+                               offsetof(eqf::CgState, gamma),
+                           0, 2 * sizeof(double), B.stream));
+    B.sync();
+  });
+}
+
+static Batch::Chan* chan_of(Batch& B, int trap) {
+  for (auto& c : B.chans)
+    if (c->trap == trap) return c.get();
+  return nullptr;
+}
+
+int eqf_read_channels(eqf_batch* b, int32_t trap, double* bottom, double* top) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    Batch::Chan* ch = chan_of(B, trap);
+    EQF_REQUIRE(ch != nullptr, "trap has no flow channel");
+    double* out[2] = {bottom, top};
+    for (int s = 0; s < 2; ++s) {
+      if (!out[s]) continue;
+      EQF_REQUIRE(ch->c[s].p != nullptr, "no channel on that wall");
+      EQF_CK(cudaMemcpyAsync(out[s], ch->c[s].p, ch->n * sizeof(double), cudaMemcpyDeviceToHost,
+                             B.stream));
+    }
+    B.sync();
+  });
+}
+
+int eqf_set_channels(eqf_batch* b, int32_t trap, const double* bottom, const double* top) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    Batch::Chan* ch = chan_of(B, trap);
+    EQF_REQUIRE(ch != nullptr, "trap has no flow channel");
+    const double* in[2] = {bottom, top};
+    for (int s = 0; s < 2; ++s) {
+      if (!in[s]) continue;
+      EQF_REQUIRE(ch->c[s].p != nullptr, "no channel on that wall");
+      for (int j = 0; j < ch->n; ++j) EQF_REQUIRE(std::isfinite(in[s][j]), "non-finite channel value");
+      EQF_CK(cudaMemcpyAsync(ch->c[s].p, in[s], ch->n * sizeof(double), cudaMemcpyHostToDevice,
+                             B.stream));
+    }
+    B.sync();
   });
 }
 

@@ -33,6 +33,7 @@ struct Lens {
   T ihx, ihy, ihxl, ihyl;  // their reciprocals
   T alpha, beta;           // mass scale (1 + dt*g) and dt*D
   T adv;                   // advection: dt * v_y(y) = -adv * y
+  T rob[4];                // Robin walls: dt * rate (bottom, top, left, right; 0 = none)
 };
 
 // One trap on one multigrid level.
@@ -51,6 +52,8 @@ struct LevelGeom {
   double hxl, hyl;       // size of the last column / row of cells
   double alpha, beta;    // mass scale (1 + dt*g) and dt*D
   double adv;            // advection: dt * v_y(y) = -adv * y  (0: none)
+  double rob[4];         // Robin walls: dt * rate (bottom, top, left, right; 0 = none)
+  int dvals;             // finest level: Dirichlet rows carry values (b = F there)
   Lens<double> ld;
   Lens<float> lf;
   // Uniform-interior stencil (nodes with 2 <= i <= ny-2 and 2 <= j <= nx-2).
@@ -173,6 +176,28 @@ EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
       s.c -= f;
       s.n += f;
     }
+  }
+  // Robin walls: dt*r*u*v on the wall's facets (fenics/hslD.ufl:36-42, facet
+  // kernels fenics/hslD.h:3264-3445): facet mass |e|/3 on the diagonal, |e|/6 along it
+  if (i == 0 && L.rob[0] != T(0)) {
+    s.c += L.rob[0] * (hxl + hxr) * T(1.0 / 3.0);
+    s.e += L.rob[0] * hxr * T(1.0 / 6.0);
+    s.w += L.rob[0] * hxl * T(1.0 / 6.0);
+  }
+  if (i == g.ny && L.rob[1] != T(0)) {
+    s.c += L.rob[1] * (hxl + hxr) * T(1.0 / 3.0);
+    s.e += L.rob[1] * hxr * T(1.0 / 6.0);
+    s.w += L.rob[1] * hxl * T(1.0 / 6.0);
+  }
+  if (j == 0 && L.rob[2] != T(0)) {
+    s.c += L.rob[2] * (hyd + hyu) * T(1.0 / 3.0);
+    s.n += L.rob[2] * hyu * T(1.0 / 6.0);
+    s.s += L.rob[2] * hyd * T(1.0 / 6.0);
+  }
+  if (j == g.nx && L.rob[3] != T(0)) {
+    s.c += L.rob[3] * (hyd + hyu) * T(1.0 / 3.0);
+    s.n += L.rob[3] * hyu * T(1.0 / 6.0);
+    s.s += L.rob[3] * hyd * T(1.0 / 6.0);
   }
   if (g.walls) {
     if (is_dirichlet(g, i, j)) {

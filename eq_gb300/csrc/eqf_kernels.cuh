@@ -1080,8 +1080,10 @@ __global__ void __launch_bounds__(kThreads)
     double id;
     const double mu = apply_tab<double, View<double>, true>(g, cm, tM, uv, k, w.i, w.j, id);
     const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
-    const double bk = dir ? 0.0 : fv[k] + mu;
-    const double rk = dir ? 0.0 : bk - apply_tab<double>(g, ci, tA, u0, k, w.i, w.j, id);
+    // Dirichlet rows: the identity with the wall value (held in F) or 0
+    const double bk = dir ? (g.dvals ? fv[k] : 0.0) : fv[k] + mu;
+    const double rk = dir ? (g.dvals ? bk - u0[k] : 0.0)
+                          : bk - apply_tab<double>(g, ci, tA, u0, k, w.i, w.j, id);
     bs[k] = bk;
     uo[k] = u0[k];
     dout[k] = (float)(u0[k] - uv[k]);
@@ -1135,8 +1137,8 @@ __global__ void __launch_bounds__(kThreads)
     for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
       double id;
       const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
-      const double rk =
-          dir ? 0.0 : bv[w.k] - apply_tab<double>(g, ci, tA, uv, w.k, w.i, w.j, id);
+      const double rk = dir ? (g.dvals ? bv[w.k] - uv[w.k] : 0.0)
+                            : bv[w.k] - apply_tab<double>(g, ci, tA, uv, w.k, w.i, w.j, id);
       if (!FINAL) rs[w.k] = T(rk);
       arr += rk * rk;
     }

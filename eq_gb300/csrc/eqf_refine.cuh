@@ -206,7 +206,10 @@ __global__ void __launch_bounds__(kThreads)
   for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
     const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
     DF bk{0.f, 0.f};
-    if (!dir) bk = df_add(df_split(Fs[w.k]), df_apply(g, sM, false, xw, xa, w.k, w.i, w.j));
+    if (!dir)
+      bk = df_add(df_split(Fs[w.k]), df_apply(g, sM, false, xw, xa, w.k, w.i, w.j));
+    else if (g.dvals)  // the identity row with the wall value held in F
+      bk = df_split(Fs[w.k]);
     bs[w.k] = make_float2(bk.h, bk.l);
     abb.add(bk.h);
   }
@@ -238,6 +241,10 @@ __global__ void __launch_bounds__(kThreads)
     if (!dir) {
       const float2 b = bs[w.k];
       const DF res = df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, xa, w.k, w.i, w.j)));
+      rk = __fadd_rn(res.h, res.l);
+    } else if (g.dvals) {
+      const float2 b = bs[w.k], x = xw[w.k - xa];
+      const DF res = df_add(DF{b.x, b.y}, df_neg(DF{x.x, x.y}));
       rk = __fadd_rn(res.h, res.l);
     }
     rs[w.k] = rk;
@@ -294,6 +301,10 @@ __global__ void __launch_bounds__(kThreads)
         const float2 b = bs[w.k];
         const DF res =
             df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, uv.a, w.k, w.i, w.j)));
+        rk = __fadd_rn(res.h, res.l);
+      } else if (g.dvals) {
+        const float2 b = bs[w.k], x = xw[w.k - uv.a];
+        const DF res = df_add(DF{b.x, b.y}, df_neg(DF{x.x, x.y}));
         rk = __fadd_rn(res.h, res.l);
       }
       if (!FINAL) rs[w.k] = rk;

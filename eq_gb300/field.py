@@ -178,6 +178,42 @@ class TrapBatch:
     def step(self, n: int = 1):
         self._ck(self._lib.eqf_step(self._h, int(n)))
 
+    # --- wall conditions and flow channels (eqf_set_boundaries) ----------------------
+    def set_boundaries(self, trap: int, walls: Dict[int, tuple],
+                       channel: Optional[dict] = None):
+        """walls[side] = (kind, value, rate) by _lib.EQF_SIDE_* (missing sides: Neumann);
+        channel = {"velocity", "D", "rate": (left, right), "substeps", "well_scaling"}."""
+        bc = _lib.Boundaries()
+        for side in range(4):
+            kind, value, rate = walls.get(side, (_lib.EQF_BC_NEUMANN, 0.0, 0.0))
+            bc.wall[side].kind = int(kind)
+            bc.wall[side].value = float(value)
+            bc.wall[side].rate = float(rate)
+        ch = channel or {}
+        bc.channel_velocity = float(ch.get("velocity", 0.0))
+        bc.channel_D = float(ch.get("D", 0.0))
+        rates = ch.get("rate", (0.0, 0.0))
+        bc.channel_rate[0] = float(rates[0])
+        bc.channel_rate[1] = float(rates[1])
+        bc.channel_substeps = int(ch.get("substeps", 1))
+        bc.well_scaling = float(ch.get("well_scaling", 1.0))
+        self._ck(self._lib.eqf_set_boundaries(self._h, int(trap), C.byref(bc)))
+
+    def read_channels(self, trap: int, bottom: bool = True, top: bool = True):
+        nx = self.params[trap].nx
+        b = np.empty(nx + 1) if bottom else None
+        t = np.empty(nx + 1) if top else None
+        self._ck(self._lib.eqf_read_channels(self._h, int(trap), _dp(b) if b is not None else None,
+                                             _dp(t) if t is not None else None))
+        return b, t
+
+    def set_channels(self, trap: int, bottom: Optional[np.ndarray] = None,
+                     top: Optional[np.ndarray] = None):
+        b = None if bottom is None else np.ascontiguousarray(bottom, dtype=np.float64)
+        t = None if top is None else np.ascontiguousarray(top, dtype=np.float64)
+        self._ck(self._lib.eqf_set_channels(self._h, int(trap), _dp(b) if b is not None else None,
+                                            _dp(t) if t is not None else None))
+
     # --- rod cells of the agent-based model (eqf_set_rods) -----------------------
     def set_rods(self, layers: Sequence[int], rods: np.ndarray, ihsl: np.ndarray,
                  production: np.ndarray, mode: np.ndarray, nodes_per_micron: float,

@@ -234,6 +234,53 @@ int eqf_set_cell_rates_all(eqf_batch* b, int64_t n, const double* s);
 int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
 
 /* ---------------------------------------------------------------------------
+ * Wall conditions and flow channels: the reference's MICROFLUIDIC_TRAP boundary
+ * mode (fenicsInterface::createHSL, src/fHSL.cpp:446-540; setRobinBoundaryConditions,
+ * 331-364; the channels' stepping in stepDiffusion, 54-152).
+ *
+ * Each wall of a trap is Neumann (zero flux), Dirichlet (c = value), Robin (the
+ * hslD terms dt*r*(c - s)*v on ds, fenics/hslD.ufl:31-42) or, for the bottom and top
+ * walls, Dirichlet to a flow channel: a 1D advection-diffusion layer of nx+1 nodes on
+ * [0, W] (fenics/AdvectionDiffusion.ufl: Crank-Nicolson, flow velocity v, Robin rates
+ * at its two ends, fenicsChannel, src/fHSL.h:240-330).  Every step: the trap solve
+ * takes the channels' current values on those walls, then each channel receives the
+ * flux h*(dt*D*grad_j)/well_scaling of every column j (grad from the wall row and the
+ * row next to it, computeBoundaryFlux, src/fHSL.cpp:54-95) spread over `substeps`
+ * Crank-Nicolson sub-steps of dt/substeps.  Where walls meet, the bottom and top
+ * walls' conditions win (the reference applies them last).
+ */
+#define EQF_SIDE_BOTTOM 0
+#define EQF_SIDE_TOP 1
+#define EQF_SIDE_LEFT 2
+#define EQF_SIDE_RIGHT 3
+#define EQF_BC_NEUMANN 0
+#define EQF_BC_DIRICHLET 1 /* c = value */
+#define EQF_BC_ROBIN 2     /* dt*rate*(c - value) on the wall */
+#define EQF_BC_CHANNEL 3   /* c = the flow channel's concentration (bottom, top) */
+typedef struct eqf_wall {
+  int32_t kind; /* EQF_BC_* */
+  double value; /* Dirichlet value / Robin external concentration s */
+  double rate;  /* Robin rate r */
+} eqf_wall;
+typedef struct eqf_boundaries {
+  eqf_wall wall[4];         /* indexed by EQF_SIDE_* */
+  double channel_velocity;  /* flow velocity v (parameters["simulationFlowRate"]) */
+  double channel_D;         /* channel diffusion constant (the layer's D_HSL) */
+  double channel_rate[2];   /* Robin rates at the channel's x = 0 and x = W ends (s = 0) */
+  int32_t channel_substeps; /* parameters["channelSolverNumberIterations"] (>= 1) */
+  double well_scaling;      /* wellScaling of src/fHSL.cpp:47 */
+} eqf_boundaries;
+
+/* Sets the wall conditions of a trap (replacing the walls bitfield of its
+ * eqf_trap_params: a set bit there means EQF_BC_DIRICHLET with value 0).  Channel
+ * walls need a square lattice (W/nx = H/ny).  Rebuilds the batch's operators. */
+int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc);
+/* The trap's bottom and top channel concentrations (nx+1 values each, x = j*W/nx);
+ * either pointer may be NULL.  Channels start at 0. */
+int eqf_read_channels(eqf_batch* b, int32_t trap, double* bottom, double* top);
+int eqf_set_channels(eqf_batch* b, int32_t trap, const double* bottom, const double* top);
+
+/* ---------------------------------------------------------------------------
  * Rod cells of the agent-based model, coupled the reference's way.
  *
  * Replaces the per-cell loop of eQabm::updateCells (src/abm/eQabm.cpp:234-390):

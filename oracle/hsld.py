@@ -344,15 +344,18 @@ class HsldOracle:
         self.A = A
         self.lu = spla.splu(A) if factor else None
 
-    def rhs(self, u: np.ndarray, F: Optional[np.ndarray] = None) -> np.ndarray:
+    def rhs(self, u: np.ndarray, F: Optional[np.ndarray] = None,
+            dvals: Optional[np.ndarray] = None) -> np.ndarray:
         b = self.M @ u + self.robin_load
         if F is not None:
             b = b + F
-        b[self.dir] = 0.0
+        # DirichletBC.apply: the wall rows take the wall values (0 unless given)
+        b[self.dir] = 0.0 if dvals is None else np.asarray(dvals)[self.dir]
         return b
 
-    def step(self, u: np.ndarray, F: Optional[np.ndarray] = None) -> np.ndarray:
-        b = self.rhs(u, F)
+    def step(self, u: np.ndarray, F: Optional[np.ndarray] = None,
+             dvals: Optional[np.ndarray] = None) -> np.ndarray:
+        b = self.rhs(u, F, dvals)
         if self.lu is None:
             return spla.spsolve(self.A, b)
         return self.lu.solve(b)

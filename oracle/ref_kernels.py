@@ -30,13 +30,19 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-LIB = os.path.join(REF_DIR, "libhsld_ref.so")
+LIB = os.path.join(REF_DIR, "libhsld_ref2.so")
 REFERENCE = os.environ.get("EQ_REFERENCE_ROOT", "/root/reference")
 
 HSLD_CLASSES = ["hsld_cell_integral_0_otherwise", "hsld_exterior_facet_integral_0_1",
                 "hsld_exterior_facet_integral_0_2", "hsld_cell_integral_1_otherwise",
                 "hsld_exterior_facet_integral_1_1", "hsld_exterior_facet_integral_1_2"]
 BOUNDARY_CLASSES = ["boundary_exterior_facet_integral_0_otherwise"]
+ADV_CLASSES = ["advectiondiffusion_cell_integral_0_otherwise",
+               "advectiondiffusion_exterior_facet_integral_0_1",
+               "advectiondiffusion_exterior_facet_integral_0_2",
+               "advectiondiffusion_cell_integral_1_otherwise",
+               "advectiondiffusion_exterior_facet_integral_1_1",
+               "advectiondiffusion_exterior_facet_integral_1_2"]
 
 UFC_STUB = r'''
 // Minimal stand-in for the two UFC integral interfaces the generated kernels
@@ -72,7 +78,48 @@ HARNESS = r'''
 #include "ufc_stub.h"
 #include "hsld_integrals.inc"
 #include "boundary_integrals.inc"
+#include "adv_integrals.inc"
 extern "C" {
+// flow channel, bilinear form of AdvectionDiffusion: w = {dt, D, v, r1, r2}
+void ref_adv_a_cell(double dt, double D, double v, const double* coords, double* A) {
+  const double a[1] = {dt}, b[1] = {D}, c[1] = {v}, z[1] = {0.0};
+  const double* w[5] = {a, b, c, z, z};
+  advectiondiffusion_cell_integral_0_otherwise k;
+  k.tabulate_tensor(A, w, coords, 0);
+}
+void ref_adv_a_facet(int marker, double dt, double r, const double* coords, int facet,
+                     double* A) {
+  const double a[1] = {dt}, rv[1] = {r}, z[1] = {0.0};
+  const double* w[5] = {a, z, z, marker == 1 ? rv : z, marker == 2 ? rv : z};
+  if (marker == 1) {
+    advectiondiffusion_exterior_facet_integral_0_1 k;
+    k.tabulate_tensor(A, w, coords, facet, 0);
+  } else {
+    advectiondiffusion_exterior_facet_integral_0_2 k;
+    k.tabulate_tensor(A, w, coords, facet, 0);
+  }
+}
+// linear form: w = {u0[2], dt, D, v, r1, s1, r2, s2}
+void ref_adv_L_cell(const double* u0, double dt, double D, double v, const double* coords,
+                    double* b) {
+  const double a[1] = {dt}, d[1] = {D}, c[1] = {v}, z[1] = {0.0};
+  const double* w[8] = {u0, a, d, c, z, z, z, z};
+  advectiondiffusion_cell_integral_1_otherwise k;
+  k.tabulate_tensor(b, w, coords, 0);
+}
+void ref_adv_L_facet(int marker, const double* u0, double dt, double r, double s,
+                     const double* coords, int facet, double* b) {
+  const double a[1] = {dt}, rv[1] = {r}, sv[1] = {s}, z[1] = {0.0};
+  const double* w[8] = {u0, a, z, z, marker == 1 ? rv : z, marker == 1 ? sv : z,
+                        marker == 2 ? rv : z, marker == 2 ? sv : z};
+  if (marker == 1) {
+    advectiondiffusion_exterior_facet_integral_1_1 k;
+    k.tabulate_tensor(b, w, coords, facet, 0);
+  } else {
+    advectiondiffusion_exterior_facet_integral_1_2 k;
+    k.tabulate_tensor(b, w, coords, facet, 0);
+  }
+}
 // bilinear cell kernel of hslD: w = {D11[3], D22[3], D12[3], D, dt, r1, r2}
 void ref_hsld_a_cell(const double* D11, const double* D22, const double* D12, double D,
                      double dt, const double* coords, double* A) {
@@ -155,6 +202,9 @@ def build_if_available(force: bool = False) -> Optional[str]:
         f.write(_slice_classes(os.path.join(REFERENCE, "fenics", "hslD.h"), HSLD_CLASSES))
     with open(os.path.join(REF_DIR, "boundary_integrals.inc"), "w") as f:
         f.write(_slice_classes(os.path.join(REFERENCE, "fenics", "boundary.h"), BOUNDARY_CLASSES))
+    with open(os.path.join(REF_DIR, "adv_integrals.inc"), "w") as f:
+        f.write(_slice_classes(os.path.join(REFERENCE, "fenics", "AdvectionDiffusion.h"),
+                               ADV_CLASSES))
     src = os.path.join(REF_DIR, "harness.cpp")
     with open(src, "w") as f:
         f.write(HARNESS)
@@ -219,3 +269,38 @@ def flux_facet(coords, u, facet) -> float:
     uu = np.ascontiguousarray(u, dtype=np.float64)
     load().ref_boundary_flux_facet(_p(uu), _p(c), facet, out.ctypes.data_as(C.POINTER(C.c_double)))
     return float(out[0])
+
+
+# ---- flow channel (fenics/AdvectionDiffusion.h) ----
+def adv_a_cell(coords, dt, D, v) -> np.ndarray:
+    A = np.zeros(4)
+    c = np.ascontiguousarray(coords, dtype=np.float64).ravel()
+    load().ref_adv_a_cell(C.c_double(dt), C.c_double(D), C.c_double(v), _p(c),
+                          A.ctypes.data_as(C.POINTER(C.c_double)))
+    return A.reshape(2, 2)
+
+
+def adv_a_facet(marker, dt, r, coords, facet) -> np.ndarray:
+    A = np.zeros(4)
+    c = np.ascontiguousarray(coords, dtype=np.float64).ravel()
+    load().ref_adv_a_facet(marker, C.c_double(dt), C.c_double(r), _p(c), facet,
+                           A.ctypes.data_as(C.POINTER(C.c_double)))
+    return A.reshape(2, 2)
+
+
+def adv_L_cell(coords, u0, dt, D, v) -> np.ndarray:
+    b = np.zeros(2)
+    c = np.ascontiguousarray(coords, dtype=np.float64).ravel()
+    u = np.ascontiguousarray(u0, dtype=np.float64)
+    load().ref_adv_L_cell(_p(u), C.c_double(dt), C.c_double(D), C.c_double(v), _p(c),
+                          b.ctypes.data_as(C.POINTER(C.c_double)))
+    return b
+
+
+def adv_L_facet(marker, coords, u0, dt, r, s, facet) -> np.ndarray:
+    b = np.zeros(2)
+    c = np.ascontiguousarray(coords, dtype=np.float64).ravel()
+    u = np.ascontiguousarray(u0, dtype=np.float64)
+    load().ref_adv_L_facet(marker, _p(u), C.c_double(dt), C.c_double(r), C.c_double(s), _p(c),
+                           facet, b.ctypes.data_as(C.POINTER(C.c_double)))
+    return b
