@@ -119,7 +119,17 @@ def make_workload(name: str, seed: int, n_traps: int):
         return [wl.single_large(seed)]
     if name == "single_small":
         return [wl.single_small(seed)]
+    if name == "microfluidic":
+        return wl.batched_microfluidic(seed=seed, n_traps=n_traps)
     raise ValueError(name)
+
+
+def load_traps(b, traps, first: int = 0):
+    """Wall conditions (when the workload has them) and point cells of each trap."""
+    for i, t in enumerate(traps):
+        if t.bc is not None:
+            b.set_boundaries(first + i, t.bc["walls"], t.bc.get("channel"))
+        b.set_cells(first + i, t.cell_xy, t.cell_s)
 
 
 def trap_params_of(traps):
@@ -204,8 +214,7 @@ def run_ours(args, rank, world, local_rank):
         table = F.autotune(tps, opts, budget_s=args.tune_budget)
         tune_s = time.perf_counter() - t_tune
     b = F.TrapBatch(tps, opts, tune=table)
-    for i, t in enumerate(traps):
-        b.set_cells(i, t.cell_xy, t.cell_s)
+    load_traps(b, traps)
     stream = torch.cuda.ExternalStream(b.stream_handle())
 
     # warm-up (graph capture happens on the first steps)
@@ -248,7 +257,7 @@ def run_ours(args, rank, world, local_rank):
     o64 = F.default_opts(F.FP64, use_graph=1, adaptive=1)
     for i in idx:
         with F.TrapBatch([tps[i]], o64) as b1:
-            b1.set_cells(0, traps[i].cell_xy, traps[i].cell_s)
+            load_traps(b1, [traps[i]])
             s1 = torch.cuda.ExternalStream(b1.stream_handle())
             b1.step(1)
             b1.sync()
@@ -276,8 +285,7 @@ def run_ours(args, rank, world, local_rank):
     op_opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, fuse_levels=0,
                              tile_nodes=args.tile_nodes)
     bo = F.TrapBatch(tps, op_opts, tune=table)
-    for i, t in enumerate(traps):
-        bo.set_cells(i, t.cell_xy, t.cell_s)
+    load_traps(bo, traps)
     bo.step(3)
     bo.profile(True)
     bo.step(2)
@@ -300,8 +308,7 @@ def run_ours(args, rank, world, local_rank):
     #      the same steps as the timed loop, each with the pinned per-cell rates copied
     #      in and the per-cell concentrations read back
     b = F.TrapBatch(tps, opts, tune=table)
-    for i, t in enumerate(traps):
-        b.set_cells(i, t.cell_xy, t.cell_s)
+    load_traps(b, traps)
     b.step(args.warmup)
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream_handle())
@@ -700,8 +707,7 @@ def run_ncu_target(args):
     traps = make_workload(args.workload, args.seed, args.traps)
     b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1,
                                                           tile_nodes=args.tile_nodes))
-    for i, t in enumerate(traps):
-        b.set_cells(i, t.cell_xy, t.cell_s)
+    load_traps(b, traps)
     b.step(args.warmup + args.steps)
     b.sync()
     b.close()

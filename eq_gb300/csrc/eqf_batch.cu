@@ -1352,8 +1352,9 @@ void Batch::setup_walls() {
   d_chans.alloc(hc.size());
   if (!hc.empty()) {
     d_chans.upload(hc.data(), hc.size(), stream);
+    // the attribute belongs to the kernel, not to this batch: always the largest size
     EQF_CK(cudaFuncSetAttribute(k_channel_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)chan_smem_bytes(chan_n_max)));
+                                (int)chan_smem_bytes(kChanMaxNodes)));
   }
   // the load vector restarts from the point cells alone (rims included)
   if (!cells_dirty) {

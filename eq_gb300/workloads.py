@@ -62,6 +62,9 @@ class Trap:
     cell_kind: Optional[np.ndarray] = None  # 1 = sender, 0 = receiver
     adv_u: float = 0.0  # v = (0, -adv_u * y / adv_len)
     adv_len: float = 40.0
+    # wall conditions / flow channels (eqf_set_boundaries): {"walls": {side: (kind,
+    # value, rate)}, "channel": {...}}; None = the walls bitfield above
+    bc: Optional[dict] = None
 
     @property
     def n_nodes(self) -> int:
@@ -256,3 +259,46 @@ def rod_colony(seed: int = 11, W: float = 100.0, H: float = 40.0, npm: float = 4
     return RodColony(W=W, H=H, npm=npm, D=[490.0, 300.0], g=[0.01, 0.02], km=[3.0, 2.1],
                      dt=dt, steps=steps, rods=rods, ihsl=np.zeros((n_cells, nl)), prod=prod,
                      mode=mode)
+
+
+# --- MICROFLUIDIC_TRAP walls (eqf_set_boundaries) -----------------------------------
+
+BC_NEUMANN, BC_DIRICHLET, BC_ROBIN, BC_CHANNEL = 0, 1, 2, 3
+SIDE_BOTTOM, SIDE_TOP, SIDE_LEFT, SIDE_RIGHT = 0, 1, 2, 3
+
+
+def microfluidic_bc(trap: Trap, velocity: float = 100.0, side_channel: float = 20.0,
+                    length_scaling: float = 1.0) -> dict:
+    """The reference's MICROFLUIDIC_TRAP walls for a trap: flow channels on the bottom
+    and top walls, Robin side walls.  Robin rates from the flow over side channels of
+    length side_channel (setRobinBoundaryConditions, src/fHSL.cpp:338-356: v/(1 -
+    exp(-Lv/D)) and v/(exp(Lv/D) - 1)); channel sub-steps ceil(D dt^2 / h^2) with
+    h = length_scaling / npm (checkAdvectionDiffusionStability, src/main.cpp:415-430);
+    wellScaling = 10 (25 / length_scaling) h (src/fHSL.cpp:45-47)."""
+    D, v, dt = trap.D[0], velocity, trap.dt
+    npm = trap.nx / trap.W
+    h = 1.0 / npm
+    if v > 1.0e-6:
+        lv = side_channel * v / D
+        r_left, r_right = v * (1.0 / (1.0 - np.exp(-lv))), v * (1.0 / (np.exp(lv) - 1.0))
+    else:
+        r_left = r_right = D / side_channel
+    hs = length_scaling / npm
+    substeps = int(np.ceil(dt / (hs * hs / (D * dt))))
+    return {"walls": {SIDE_BOTTOM: (BC_CHANNEL, 0.0, 0.0), SIDE_TOP: (BC_CHANNEL, 0.0, 0.0),
+                      SIDE_LEFT: (BC_ROBIN, 0.0, float(r_left)),
+                      SIDE_RIGHT: (BC_ROBIN, 0.0, float(r_right))},
+            "channel": {"velocity": v, "D": D, "rate": (float(r_left), float(r_right)),
+                        "substeps": max(1, substeps),
+                        "well_scaling": 10.0 * (25.0 / length_scaling) * h}}
+
+
+def batched_microfluidic(seed: int = 3, n_traps: int = 512, h: float = 0.25,
+                         steps: int = 200) -> List[Trap]:
+    """The batched_uneven traps with the MICROFLUIDIC_TRAP walls (flow channels on
+    the bottom and top walls, Robin side walls)."""
+    traps = batched_uneven(seed=seed, n_traps=n_traps, h=h, steps=steps)
+    for t in traps:
+        t.walls = 0
+        t.bc = microfluidic_bc(t)
+    return traps

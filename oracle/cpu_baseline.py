@@ -18,18 +18,26 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _worker(args):
-    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s) = args
+    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s, bc) = args
     if ROOT not in sys.path:
         sys.path.insert(0, ROOT)
-    from oracle import hsld
+    from oracle import channel, hsld
     mesh = hsld.RightMesh(W, H, nx, ny)
     F = hsld.point_load(mesh, xy, s, scale=dt)
     u = np.zeros(mesh.n_nodes)
+    chans = None
     t0 = time.perf_counter()
     done = 0
     for _ in range(steps):
-        o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls)
-        u = o.step(u, F)
+        if bc is None:
+            o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls)
+            u = o.step(u, F)
+        else:  # walls and channels re-assembled every step, as the reference does
+            o = channel.MicrofluidicTrap(W, H, nx, ny, D, dt, g, bc["walls"], bc.get("channel"))
+            if chans is not None:
+                o.channels = chans
+            u = o.step(u, F)
+            chans = o.channels
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -41,7 +49,7 @@ def reference_rate(traps, idx, steps_per_trap: int, budget_s: float, timeout_s: 
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     jobs = [(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls, t.cell_xy, t.cell_s,
-             steps_per_trap, budget_s) for t in (traps[i] for i in idx)]
+             steps_per_trap, budget_s, getattr(t, "bc", None)) for t in (traps[i] for i in idx)]
     procs = min(cores, len(jobs))
     t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(processes=procs) as pool:

@@ -144,3 +144,19 @@ def test_boundary_argument_errors(lib):
             b.set_boundaries(1, {_lib.EQF_SIDE_BOTTOM: (_lib.EQF_BC_CHANNEL, 0, 0)}, c.channel)
         with pytest.raises(F.EqfError):  # no channel on this trap
             b.read_channels(1)
+
+
+def test_a_small_batch_does_not_shrink_a_large_channel(lib):
+    """Kernel attributes are per kernel: a later batch with short channels must not
+    cap the shared memory of an earlier one with long channels (2049 nodes)."""
+    big = microfluidic_case(9, 2048, 8, substeps=2)
+    small = microfluidic_case(10, 32, 16, substeps=2)
+    with F.TrapBatch([big.params()], F.default_opts(F.FP64)) as b1:
+        big.configure(b1, 0)
+        with F.TrapBatch([small.params()], F.default_opts(F.FP64)) as b2:
+            small.configure(b2, 0)
+            b2.step(1)
+        b1.step(2)
+        u_ref, ch_ref = big.oracle(2)
+        assert rel(b1.read_nodal(0), u_ref) <= 1e-9
+        assert rel(b1.read_channels(0)[0], ch_ref[chn.BOTTOM]) <= 1e-9
