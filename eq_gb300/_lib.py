@@ -34,12 +34,15 @@ EXPORTS = (
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
     "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
-    "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels",
+    "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels", "eqf_set_well",
+    "eqf_read_well", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
+    "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
+    "eqf_vtk_write_host", "eqf_vtk_close",
 )
 
 # wall conditions (eqf_set_boundaries)
 EQF_SIDE_BOTTOM, EQF_SIDE_TOP, EQF_SIDE_LEFT, EQF_SIDE_RIGHT = 0, 1, 2, 3
-EQF_BC_NEUMANN, EQF_BC_DIRICHLET, EQF_BC_ROBIN, EQF_BC_CHANNEL = 0, 1, 2, 3
+EQF_BC_NEUMANN, EQF_BC_DIRICHLET, EQF_BC_ROBIN, EQF_BC_CHANNEL, EQF_BC_WELL = 0, 1, 2, 3, 4
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
                 "down0", "up0", "rod_exchange")
@@ -164,6 +167,23 @@ def load() -> C.CDLL:
         "eqf_set_boundaries": (C.c_int, [C.c_void_p, C.c_int32, P(Boundaries)]),
         "eqf_read_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),
         "eqf_set_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),
+        "eqf_set_well": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
+        "eqf_trap_info": (C.c_int, [C.c_void_p, C.c_int32, P(TrapParams)]),
+        "eqf_json_open": (C.c_int, [C.c_char_p, C.c_int64, C.c_int32, C.c_int32,
+                                    P(C.c_void_p)]),
+        "eqf_json_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, P(C.c_int32), C.c_double,
+                                     C.c_int64, dp, C.c_int64, i64p, C.c_int32, dp]),
+        "eqf_json_frame_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, C.c_double,
+                                          C.c_int64, dp, C.c_int64, i64p, C.c_int32, dp]),
+        "eqf_json_close": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "eqf_vtk_open": (C.c_int, [C.c_char_p, P(C.c_void_p)]),
+        "eqf_vtk_write": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double]),
+        "eqf_vtk_write_channel": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                            C.c_double]),
+        "eqf_vtk_write_host": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32,
+                                         C.c_int32, dp, C.c_double]),
+        "eqf_vtk_close": (C.c_int, [C.c_void_p]),
+        "eqf_read_well": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p]),
         "eqf_rod_waves": (C.c_int, [C.c_void_p, P(C.c_int32)]),
     }
     for name, (res, args) in sig.items():

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libeqfield.so")
 SOURCES = [os.path.join(CSRC, f) for f in ("eqf_batch.cu", "eqf_noalloc.cu", "eqf_server.cu",
-                                               "eqf_tune.cu")]
+                                               "eqf_tune.cu", "eqf_output.cpp")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("eqf_common.cuh", "eqf_kernels.cuh",
                                                    "eqf_cells.cuh", "eqf_refine.cuh",
                                                    "eqf_bicgstab.cuh", "eqf_fused.cuh",

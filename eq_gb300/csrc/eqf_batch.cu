@@ -433,6 +433,17 @@ class Batch {
   void setup_walls();
   void enqueue_walls();
   void enqueue_channels();
+  // boundary wells (eqf_set_well)
+  struct WellParams {
+    double scale = 0.0, decay = 0.0;
+  };
+  std::vector<WellParams> well;
+  DevBuf<double> d_well_c;
+  DevBuf<long long> d_well_under;
+  std::vector<WellDev> hwells;
+  DevBuf<WellDev> d_wells;
+  void setup_wells();
+  void enqueue_wells();
   std::vector<std::unique_ptr<RodSet>> rod_sets;
   DevBuf<RodSetDev> d_rod_sets;        // one descriptor per set (blockIdx.y of a wave)
   int rod_launches = 0, rod_grid = 0;  // wave launches and blocks per set, as captured
@@ -534,6 +545,11 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
     work.reset(new Work<double>(*this));
   cell_xy.resize(ntraps);
   cell_s.resize(ntraps);
+  well.resize(ntraps);
+  d_well_c.alloc(ntraps);
+  d_well_under.alloc(ntraps);
+  EQF_CK(cudaMemsetAsync(d_well_c.p, 0, ntraps * sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(d_well_under.p, 0, ntraps * sizeof(long long), stream));
   sync();
 }
 
@@ -623,7 +639,7 @@ void Batch::build_levels() {
     for (int w = 0; w < 4; ++w)
       g.rob[w] = bc.wall[w].kind == EQF_BC_ROBIN ? p.dt * bc.wall[w].rate : 0.0;
     for (int w = 0; w < 4; ++w)
-      g.dvals = g.dvals || bc.wall[w].kind == EQF_BC_CHANNEL ||
+      g.dvals = g.dvals || bc.wall[w].kind == EQF_BC_CHANNEL || bc.wall[w].kind == EQF_BC_WELL ||
                 (bc.wall[w].kind == EQF_BC_DIRICHLET && bc.wall[w].value != 0.0);
     for (int l = 0; l < nlev; ++l) {
       if (l > 0) {
@@ -1226,7 +1242,7 @@ void Batch::setup_walls() {
     bool active = false, channel = false;
     for (int w = 0; w < 4; ++w) {
       const eqf_wall& wl = bc.wall[w];
-      active = active || wl.kind == EQF_BC_CHANNEL ||
+      active = active || wl.kind == EQF_BC_CHANNEL || wl.kind == EQF_BC_WELL ||
                (wl.kind != EQF_BC_NEUMANN && wl.value != 0.0);
       channel = channel || wl.kind == EQF_BC_CHANNEL;
     }
@@ -1234,6 +1250,7 @@ void Batch::setup_walls() {
     WallDev wd{};
     wd.trap = t;
     wd.rim0 = rim_total;
+    wd.well = d_well_c.p + t;
     for (int w = 0; w < 4; ++w) {
       wd.kind[w] = bc.wall[w].kind;
       wd.value[w] = bc.wall[w].value;
@@ -1363,6 +1380,32 @@ void Batch::setup_walls() {
   }
   drop_graphs();
   sync();
+}
+
+void Batch::setup_wells() {
+  hwells.clear();
+  for (int t = 0; t < ntraps; ++t) {
+    if (!(well[t].scale > 0.0)) continue;
+    WellDev w{};
+    w.trap = t;
+    w.scale = well[t].scale;
+    w.decay_dt = params[t].dt * well[t].decay;
+    w.Ddt = params[t].D * params[t].dt;
+    w.conc = d_well_c.p + t;
+    w.under = d_well_under.p + t;
+    hwells.push_back(w);
+  }
+  d_wells.alloc(hwells.size());
+  if (!hwells.empty()) d_wells.upload(hwells.data(), hwells.size(), stream);
+  sync();
+}
+
+// After the step (and the channels): the boundary wells take the new field's flux.
+void Batch::enqueue_wells() {
+  if (hwells.empty()) return;
+  EQF_RUN(*this, KC_SCALAR,
+          (k_well_update<<<(unsigned)hwells.size(), kThreads, 0, stream>>>(
+              d_wells.p, L[0].dgeom.p, U[1 - cur].p, d_frozen.p)));
 }
 
 void Batch::enqueue_walls() {
@@ -1602,11 +1645,13 @@ void Batch::step(int n) {
       if (f != 0) {
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
         enqueue_channels();
+        enqueue_wells();
         cur = 1 - cur;
         throw Error(EQF_ERR_NOT_CONVERGED, "trap(s) missed rtol after extra refinement sweeps");
       }
     }
     enqueue_channels();
+    enqueue_wells();
     cur = 1 - cur;
     ++steps_done;
   }
@@ -1959,6 +2004,12 @@ const char* eqf_last_error(const eqf_batch* b) {
 
 #define EQF_TRAP_CHECK(b, trap)                                                     \
   EQF_REQUIRE((trap) >= 0 && (trap) < (b)->impl->ntraps, "trap index out of range")
+
+int eqf_trap_info(const eqf_batch* b, int32_t trap, eqf_trap_params* out) {
+  if (!b || !out || trap < 0 || trap >= b->impl->ntraps) return EQF_ERR_INVALID;
+  *out = b->impl->params[trap];
+  return EQF_OK;
+}
 
 int eqf_num_nodes(const eqf_batch* b, int32_t trap, int64_t* n) {
   if (!b || !n || trap < 0 || trap >= b->impl->ntraps) return EQF_ERR_INVALID;
@@ -2315,14 +2366,15 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc) {
     const unsigned bits[4] = {eqf::WALL_BOTTOM, eqf::WALL_TOP, eqf::WALL_LEFT, eqf::WALL_RIGHT};
     for (int w = 0; w < 4; ++w) {
       const eqf_wall& wl = bc->wall[w];
-      EQF_REQUIRE(wl.kind >= EQF_BC_NEUMANN && wl.kind <= EQF_BC_CHANNEL, "bad wall kind");
+      EQF_REQUIRE(wl.kind >= EQF_BC_NEUMANN && wl.kind <= EQF_BC_WELL, "bad wall kind");
       EQF_REQUIRE(std::isfinite(wl.value) && std::isfinite(wl.rate), "non-finite wall value");
       EQF_REQUIRE(wl.kind != EQF_BC_ROBIN || wl.rate >= 0.0, "negative Robin rate");
       EQF_REQUIRE(wl.kind != EQF_BC_CHANNEL || w <= EQF_SIDE_TOP,
                   "channels border the bottom and top walls only");
-      if (wl.kind == EQF_BC_DIRICHLET || wl.kind == EQF_BC_CHANNEL) walls |= bits[w];
+      if (wl.kind == EQF_BC_DIRICHLET || wl.kind == EQF_BC_CHANNEL || wl.kind == EQF_BC_WELL)
+        walls |= bits[w];
       channel = channel || wl.kind == EQF_BC_CHANNEL;
-      active = active || wl.kind == EQF_BC_CHANNEL ||
+      active = active || wl.kind == EQF_BC_CHANNEL || wl.kind == EQF_BC_WELL ||
                (wl.kind != EQF_BC_NEUMANN && wl.value != 0.0);
     }
     if (active) EQF_REQUIRE(p.nx >= 3 && p.ny >= 3, "walls with values need nx, ny >= 3");
@@ -2351,6 +2403,38 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc) {
                                offsetof(eqf::CgState, gamma),
                            0, 2 * sizeof(double), B.stream));
     B.sync();
+  });
+}
+
+int eqf_set_well(eqf_batch* b, int32_t trap, double well_scaling, double decay_rate) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(std::isfinite(well_scaling) && well_scaling >= 0.0 && std::isfinite(decay_rate) &&
+                    decay_rate >= 0.0,
+                "bad well parameters");
+    Batch& B = *b->impl;
+    B.sync();
+    B.well[trap].scale = well_scaling;
+    B.well[trap].decay = decay_rate;
+    B.setup_wells();
+  });
+}
+
+int eqf_read_well(eqf_batch* b, int32_t trap, double* concentration, int64_t* underflows) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    double c = 0.0;
+    long long u = 0;
+    EQF_CK(cudaMemcpyAsync(&c, B.d_well_c.p + trap, sizeof(double), cudaMemcpyDeviceToHost,
+                           B.stream));
+    EQF_CK(cudaMemcpyAsync(&u, B.d_well_under.p + trap, sizeof(long long),
+                           cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    if (concentration) *concentration = c;
+    if (underflows) *underflows = u;
   });
 }
 

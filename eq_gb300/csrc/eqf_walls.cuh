@@ -33,6 +33,7 @@ struct WallDev {  // one trap whose walls carry values, Robin loads or channels
   double value[4];
   double robs[4];         // dt * rate * s of Robin walls (their load), else 0
   const double* chan[2];  // channel concentrations of the bottom / top walls (or null)
+  const double* well;     // the trap's boundary-well concentration (EQF_BC_WELL walls)
 };
 
 // Rim of an (nx+1) x (ny+1) lattice, nx, ny >= 3: rows 0, 1, ny-1, ny whole, then
@@ -53,13 +54,17 @@ EQF_HD void rim_node(int r, int nx, int ny, int& i, int& j) {
 }
 
 // Value of Dirichlet node (i, j); bottom and top walls win at the corners.
+__device__ __forceinline__ double side_value(const WallDev& w, int side, int j) {
+  const int k = w.kind[side];
+  if (k == EQF_BC_CHANNEL) return w.chan[side][j];
+  if (k == EQF_BC_WELL) return *w.well;
+  return w.value[side];
+}
 __device__ __forceinline__ double wall_value(const WallDev& w, const LevelGeom& g, int i, int j) {
-  if (i == 0 && (g.walls & WALL_BOTTOM))
-    return w.kind[EQF_SIDE_BOTTOM] == EQF_BC_CHANNEL ? w.chan[0][j] : w.value[EQF_SIDE_BOTTOM];
-  if (i == g.ny && (g.walls & WALL_TOP))
-    return w.kind[EQF_SIDE_TOP] == EQF_BC_CHANNEL ? w.chan[1][j] : w.value[EQF_SIDE_TOP];
-  if (j == 0 && (g.walls & WALL_LEFT)) return w.value[EQF_SIDE_LEFT];
-  return w.value[EQF_SIDE_RIGHT];
+  if (i == 0 && (g.walls & WALL_BOTTOM)) return side_value(w, EQF_SIDE_BOTTOM, j);
+  if (i == g.ny && (g.walls & WALL_TOP)) return side_value(w, EQF_SIDE_TOP, j);
+  if (j == 0 && (g.walls & WALL_LEFT)) return side_value(w, EQF_SIDE_LEFT, j);
+  return side_value(w, EQF_SIDE_RIGHT, j);
 }
 
 // F on the rim of every wall trap (blockIdx.y = trap): MODE 0 zeroes it (before the
@@ -192,6 +197,57 @@ __global__ void __launch_bounds__(kChanThreads)
     __syncthreads();
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) c[j] = cc[j];
+}
+
+// --- the boundary well -------------------------------------------------------
+
+struct WellDev {
+  int trap;           // finest-level geometry index
+  double scale;       // well_scaling
+  double decay_dt;    // dt * decay_rate
+  double Ddt;         // D * dt of the trap
+  double* conc;       // the well concentration
+  long long* under;   // underflow count
+};
+
+// One block per well trap: the boundary-flux functional -int grad u . n ds of the new
+// field (each boundary edge with the gradient of the triangle it bounds, as the
+// flux readout), then Simulation::computeBoundaryWell.
+__global__ void k_well_update(const WellDev* __restrict__ wells, const LevelGeom* __restrict__ G,
+                              const double* __restrict__ U, const int* __restrict__ frozen) {
+  const WellDev& w = wells[blockIdx.x];
+  const LevelGeom& g = G[w.trap];
+  if (frozen && frozen[g.trap]) return;
+  const double* u = U + g.off;
+  const int P = g.P, nx = g.nx, ny = g.ny;
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < 2 * (nx + ny); e += blockDim.x) {
+    if (e < nx) {  // bottom edge (0, j)-(0, j+1)
+      const int k = e;
+      acc += (u[k + P + 1] - u[k + 1]) / g.hy * g.hx;
+    } else if (e < 2 * nx) {  // top edge (ny, j)-(ny, j+1)
+      const int k = (e - nx) + ny * P;
+      acc += -(u[k] - u[k - P]) / g.hy * g.hx;
+    } else if (e < 2 * nx + ny) {  // left edge (i, 0)-(i+1, 0)
+      const int k = (e - 2 * nx) * P;
+      acc += (u[k + P + 1] - u[k + P]) / g.hx * g.hy;
+    } else {  // right edge (i, nx)-(i+1, nx)
+      const int k = (e - 2 * nx - ny) * P + nx;
+      acc += -(u[k] - u[k - 1]) / g.hx * g.hy;
+    }
+  }
+  const double total = block_sum(acc);
+  if (threadIdx.x == 0) {
+    const double flux = w.Ddt * total;  // totalBoundaryFlux
+    double c = *w.conc;
+    c += flux / w.scale;
+    c -= w.decay_dt * c;
+    if (c < 0.0) {
+      c = 0.0;
+      *w.under += 1;
+    }
+    *w.conc = c;
+  }
 }
 
 }  // namespace eqf

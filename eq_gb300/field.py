@@ -214,6 +214,17 @@ class TrapBatch:
         self._ck(self._lib.eqf_set_channels(self._h, int(trap), _dp(b) if b is not None else None,
                                             _dp(t) if t is not None else None))
 
+    def set_well(self, trap: int, well_scaling: float, decay_rate: float):
+        """Boundary well of a trap (0 scaling: off); walls of kind EQF_BC_WELL take it."""
+        self._ck(self._lib.eqf_set_well(self._h, int(trap), float(well_scaling),
+                                        float(decay_rate)))
+
+    def read_well(self, trap: int):
+        c = C.c_double()
+        u = C.c_int64()
+        self._ck(self._lib.eqf_read_well(self._h, int(trap), C.byref(c), C.byref(u)))
+        return c.value, u.value
+
     # --- rod cells of the agent-based model (eqf_set_rods) -----------------------
     def set_rods(self, layers: Sequence[int], rods: np.ndarray, ihsl: np.ndarray,
                  production: np.ndarray, mode: np.ndarray, nodes_per_micron: float,

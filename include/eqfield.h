@@ -138,6 +138,8 @@ const char* eqf_last_error(const eqf_batch* b);
 
 /* Node count of a trap. */
 int eqf_num_nodes(const eqf_batch* b, int32_t trap, int64_t* n_nodes);
+/* The parameters a trap was created with (walls as set by eqf_set_boundaries). */
+int eqf_trap_info(const eqf_batch* b, int32_t trap, eqf_trap_params* out);
 
 /* Point cells of trap `trap`: positions xy[2*n] (x, y interleaved) and source
  * rates s[n].  The load dt * sum s_i phi(x_i) is deposited deterministically
@@ -257,6 +259,8 @@ int eqf_read_cells_all(eqf_batch* b, int64_t n, double* c);
 #define EQF_BC_DIRICHLET 1 /* c = value */
 #define EQF_BC_ROBIN 2     /* dt*rate*(c - value) on the wall */
 #define EQF_BC_CHANNEL 3   /* c = the flow channel's concentration (bottom, top) */
+#define EQF_BC_WELL 4      /* c = the trap's boundary-well concentration (the reference's
+                              DIRICHLET_UPDATE walls, src/fHSL.cpp:545-554) */
 typedef struct eqf_wall {
   int32_t kind; /* EQF_BC_* */
   double value; /* Dirichlet value / Robin external concentration s */
@@ -279,6 +283,61 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc);
  * either pointer may be NULL.  Channels start at 0. */
 int eqf_read_channels(eqf_batch* b, int32_t trap, double* bottom, double* top);
 int eqf_set_channels(eqf_batch* b, int32_t trap, const double* bottom, const double* top);
+
+/* Boundary well of a trap (Simulation::computeBoundaryWell, src/simulation.cpp:581-604):
+ * after every step, with the step's totalBoundaryFlux F = D*dt*(-int grad c . n ds),
+ *   w += F / well_scaling;  w -= dt * decay_rate * w;  w < 0 -> w = 0 (an underflow)
+ * well_scaling = 2*10*(15/lengthScaling)*(W + H) and decay_rate = flow rate / W in the
+ * reference (initBoundaryWell, setBoundaryRate: src/simulation.cpp:605-627).  Walls of
+ * kind EQF_BC_WELL take w as their value in the next step.  well_scaling = 0 switches
+ * the well off; it starts at 0. */
+int eqf_set_well(eqf_batch* b, int32_t trap, double well_scaling, double decay_rate);
+int eqf_read_well(eqf_batch* b, int32_t trap, double* concentration, int64_t* underflows);
+
+/* ---------------------------------------------------------------------------
+ * Output in the reference's formats (host-side writers; the reads from a batch are
+ * ordinary synchronous readouts).
+ *
+ * JSON recording: jsonRecording (src/main.cpp:81-192), "jsonSimVersion" v00_02.  The
+ * file is one object with the keys in sorted order, as the reference's JSON library
+ * writes them: cellDataFormat, frames, jsonSimVersion, nodeID, parameters, simNumber,
+ * timeSinceEpoch.  A frame is {"cells", "divisions", "externalHSL", "simTime"}: cells
+ * as [[id, strainType], [x, y, angle, length, spring, HSL (nM) ...]], divisions as
+ * [time, parent id, parent length, daughter id, daughter length]
+ * (eQabm::recordDivisionEvent, src/abm/eQabm.cpp:458-480) and externalHSL as one array
+ * per layer in grid order.  Frames stream to the file as they are recorded.
+ */
+typedef struct eqf_json eqf_json;
+int eqf_json_open(const char* path, int64_t time_since_epoch, int32_t node_id,
+                  int32_t sim_number, eqf_json** out);
+/* One frame with the layers' fields read from the batch: n_div divisions (5 values
+ * each), n_cells cells with ids[2*i] = id, ids[2*i+1] = strain type and n_data values
+ * each in data. */
+int eqf_json_frame(eqf_json* j, eqf_batch* b, int32_t n_layers, const int32_t* layers,
+                   double sim_time, int64_t n_div, const double* divisions, int64_t n_cells,
+                   const int64_t* ids, int32_t n_data, const double* data);
+/* The same with the fields in host memory: n_layers grids of n_nodes values each. */
+int eqf_json_frame_host(eqf_json* j, int32_t n_layers, int64_t n_nodes, const double* fields,
+                        double sim_time, int64_t n_div, const double* divisions,
+                        int64_t n_cells, const int64_t* ids, int32_t n_data, const double* data);
+/* Finishes and closes the file; parameters_json is the "parameters" object as JSON text
+ * (NULL: {}). */
+int eqf_json_close(eqf_json* j, const char* parameters_json);
+
+/* VTK snapshots: what fenicsInterface::writeDiffusionFiles writes through DOLFIN's File
+ * (src/fHSL.cpp:606-632): a .pvd collection (rewritten at every snapshot) and one .vtu
+ * per snapshot (<stem>NNNNNN.vtu beside it) with the mesh and the nodal field "u".
+ * A trap is its "right" triangulation; a channel the nx+1 nodes of its wall as line
+ * cells. */
+typedef struct eqf_vtk eqf_vtk;
+int eqf_vtk_open(const char* pvd_path, eqf_vtk** out);
+int eqf_vtk_write(eqf_vtk* v, eqf_batch* b, int32_t trap, double time);
+int eqf_vtk_write_channel(eqf_vtk* v, eqf_batch* b, int32_t trap, int32_t side, double time);
+/* A field in host memory: ny > 0 a trap of nx x ny squares on [0, W] x [0, H]; ny = 0 a
+ * channel of nx cells on [0, W]. */
+int eqf_vtk_write_host(eqf_vtk* v, double width, double height, int32_t nx, int32_t ny,
+                       const double* field, double time);
+int eqf_vtk_close(eqf_vtk* v);
 
 /* ---------------------------------------------------------------------------
  * Rod cells of the agent-based model, coupled the reference's way.

@@ -32,7 +32,7 @@ import scipy.sparse.linalg as spla
 
 from oracle import hsld
 
-NEUMANN, DIRICHLET, ROBIN, CHANNEL = 0, 1, 2, 3
+NEUMANN, DIRICHLET, ROBIN, CHANNEL, WELL = 0, 1, 2, 3, 4
 BOTTOM, TOP, LEFT, RIGHT = 0, 1, 2, 3
 SIDE_BITS = {BOTTOM: hsld.WALL_BOTTOM, TOP: hsld.WALL_TOP, LEFT: hsld.WALL_LEFT,
              RIGHT: hsld.WALL_RIGHT}
@@ -110,14 +110,19 @@ class MicrofluidicTrap:
     top walls.  walls[side] = (kind, value, rate) by BOTTOM, TOP, LEFT, RIGHT."""
 
     def __init__(self, W, H, nx, ny, D, dt, g, walls: Dict[int, tuple],
-                 channel: Optional[dict] = None):
+                 channel: Optional[dict] = None, well: Optional[tuple] = None):
         self.W, self.H, self.nx, self.ny = W, H, nx, ny
+        # boundary well (Simulation::computeBoundaryWell, src/simulation.cpp:581-604):
+        # (well_scaling, decay_rate); its concentration drives WELL walls
+        self.well = well
+        self.well_c = 0.0
+        self.well_under = 0
         self.D, self.dt = float(D), float(dt)
         self.walls = walls
         bits = 0
         robin = {}
         for side, (kind, value, rate) in walls.items():
-            if kind in (DIRICHLET, CHANNEL):
+            if kind in (DIRICHLET, CHANNEL, WELL):
                 bits |= SIDE_BITS[side]
             elif kind == ROBIN:
                 robin[SIDE_BITS[side]] = (rate, value)
@@ -141,6 +146,8 @@ class MicrofluidicTrap:
                 vals = value
             elif kind == CHANNEL:
                 vals = self.channels[side]
+            elif kind == WELL:
+                vals = self.well_c
             else:
                 continue
             if side == BOTTOM:
@@ -166,4 +173,13 @@ class MicrofluidicTrap:
                     gradc = (U[self.ny - 1, :] - U[self.ny, :]) / h
                 flux = h * (self.dt * self.D * gradc) / ch["well_scaling"]
                 self.channels[side] = self.ch.step(c, flux)
+        if self.well is not None:
+            scale, decay = self.well
+            flux = self.D * self.dt * hsld.boundary_flux_integral(self.mesh, u)
+            c = self.well_c + flux / scale
+            c -= self.dt * decay * c
+            if c < 0.0:
+                c = 0.0
+                self.well_under += 1
+            self.well_c = c
         return u

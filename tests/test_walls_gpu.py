@@ -12,7 +12,7 @@ from oracle import hsld
 pytestmark = pytest.mark.gpu
 TOL = {F.FP64: 1e-9, F.FP32_IR: 1e-6}
 K = {chn.NEUMANN: _lib.EQF_BC_NEUMANN, chn.DIRICHLET: _lib.EQF_BC_DIRICHLET,
-     chn.ROBIN: _lib.EQF_BC_ROBIN, chn.CHANNEL: _lib.EQF_BC_CHANNEL}
+     chn.ROBIN: _lib.EQF_BC_ROBIN, chn.CHANNEL: _lib.EQF_BC_CHANNEL, chn.WELL: _lib.EQF_BC_WELL}
 
 
 def rel(a, b):
@@ -160,3 +160,32 @@ def test_a_small_batch_does_not_shrink_a_large_channel(lib):
         u_ref, ch_ref = big.oracle(2)
         assert rel(b1.read_nodal(0), u_ref) <= 1e-9
         assert rel(b1.read_channels(0)[0], ch_ref[chn.BOTTOM]) <= 1e-9
+
+
+@pytest.mark.parametrize("drive", [False, True])
+def test_boundary_well_against_oracle(lib, drive):
+    """The well integrates the boundary flux every step; with DIRICHLET_UPDATE walls
+    (EQF_BC_WELL) its concentration is the walls' value in the next step."""
+    W, H, nx, ny = 12.0, 6.0, 48, 24
+    scale = 2.0 * 10.0 * 15.0 * (W + H)  # 2*10*(15/lengthScaling)*(W+H)
+    decay = 100.0 / W
+    walls = ({s_: (chn.WELL, 0.0, 0.0) for s_ in range(4)} if drive
+             else {chn.BOTTOM: (chn.DIRICHLET, 0.0, 0.0)})
+    c = Case(W, H, nx, ny, 490.0, 0.05, 0.0, walls, cells=40, seed=11)
+    tr = chn.MicrofluidicTrap(W, H, nx, ny, 490.0, 0.05, 0.0, walls, None, well=(scale, decay))
+    Fl = hsld.point_load(tr.mesh, c.xy, c.s, scale=c.dt)
+    u = np.zeros(tr.mesh.n_nodes)
+    wells = []
+    for _ in range(8):
+        u = tr.step(u, Fl)
+        wells.append(tr.well_c)
+    with F.TrapBatch([c.params()], F.default_opts(F.FP64)) as b:
+        c.configure(b, 0)
+        b.set_well(0, scale, decay)
+        got = []
+        for _ in range(8):
+            b.step(1)
+            got.append(b.read_well(0)[0])
+        assert rel(b.read_nodal(0), u) <= 1e-9
+    assert max(abs(x - y) for x, y in zip(got, wells)) <= 1e-9 * max(abs(x) for x in wells)
+    assert max(wells) > 0
