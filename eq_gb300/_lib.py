@@ -35,7 +35,7 @@ EXPORTS = (
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
     "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
     "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels", "eqf_set_well",
-    "eqf_read_well", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
+    "eqf_read_well", "eqf_set_tensor", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
     "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
     "eqf_vtk_write_host", "eqf_vtk_close",
 )
@@ -169,6 +169,7 @@ def load() -> C.CDLL:
         "eqf_set_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),
         "eqf_set_well": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
         "eqf_trap_info": (C.c_int, [C.c_void_p, C.c_int32, P(TrapParams)]),
+        "eqf_set_tensor": (C.c_int, [C.c_void_p, C.c_int32, dp, dp, dp]),
         "eqf_json_open": (C.c_int, [C.c_char_p, C.c_int64, C.c_int32, C.c_int32,
                                     P(C.c_void_p)]),
         "eqf_json_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, P(C.c_int32), C.c_double,

@@ -119,6 +119,21 @@ static void spectrum_bounds(LevelGeom& g) {
       gmax = std::max(gmax, r);
     }
   }
+  if (g.htens) {
+    // a varying tensor: the Gershgorin bound over every row (setup-time host loop)
+    gmax = 0.0;
+    for (int i = 0; i <= g.ny; ++i)
+      for (int j = 0; j <= g.nx; ++j) {
+        if (g.walls && is_dirichlet(g, i, j)) continue;
+        const Sten<double> s = stencil_general<double>(g, i, j);
+        gmax = std::max(gmax, (std::fabs(s.c) + std::fabs(s.e) + std::fabs(s.w) +
+                               std::fabs(s.n) + std::fabs(s.s) + std::fabs(s.ne) +
+                               std::fabs(s.sw)) / s.c);
+      }
+    g.lam_max = (float)gmax;
+    g.lam_min = (float)(1e-3 * gmax);
+    return;
+  }
   g.lam_max = (float)std::min(gmax, 1.15 * smax);
   g.lam_min = (float)std::max(0.9 * smin, 1e-3 * smax);
 }
@@ -167,6 +182,7 @@ static void interior_constants(LevelGeom& g) {
   q.walls = 0;
   q.adv = 0.0;
   q.adv_on = 0;
+  q.tens = q.htens = nullptr;
   const Sten<double> s = stencil_general<double>(q, 500, 500);
   g.cC = s.c;
   g.cE = s.e;
@@ -433,6 +449,12 @@ class Batch {
   void setup_walls();
   void enqueue_walls();
   void enqueue_channels();
+  // anisotropic tensors (eqf_set_tensor): per trap the caller's D11, D22, D12 in grid
+  // order (empty: isotropic), and per trap and level the pitched copy the stencil reads
+  std::vector<std::vector<double>> tensor;
+  std::map<std::pair<int, int>, std::vector<double>> htens;
+  std::map<std::pair<int, int>, DevBuf<double>> dtens;
+  void level_tensor(LevelGeom& g, int level, int t);
   // boundary wells (eqf_set_well)
   struct WellParams {
     double scale = 0.0, decay = 0.0;
@@ -505,6 +527,7 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
     EQF_CK(cudaGetDevice(&dev));
     EQF_CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   }
+  tensor.resize(ntraps);
   bcs.resize(ntraps);
   for (int t = 0; t < ntraps; ++t) {
     eqf_boundaries& bc = bcs[t];
@@ -616,6 +639,39 @@ static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solv
   return (size_t)bytes;
 }
 
+// The tensor of trap t on `level` (pitched, D11 | D22 | D12): the caller's fields on
+// the finest level, injection from the finer level below (coarse node (I, J) is fine
+// node (2I, 2J), clamped to the last node, on coarsened axes).
+void Batch::level_tensor(LevelGeom& g, int level, int t) {
+  const long long st = (long long)g.P * (g.ny + 1);
+  std::vector<double>& h = htens[{level, t}];
+  h.assign(3 * st, 0.0);
+  if (level == 0) {
+    const std::vector<double>& src = tensor[t];
+    const long long n = (long long)(g.nx + 1) * (g.ny + 1);
+    for (int c = 0; c < 3; ++c)
+      for (int i = 0; i <= g.ny; ++i)
+        for (int j = 0; j <= g.nx; ++j)
+          h[c * st + (long long)i * g.P + j] = src[c * n + (long long)i * (g.nx + 1) + j];
+  } else {
+    const std::vector<double>& f = htens[{level - 1, t}];
+    const int fnx = g.fine_nx, fny = g.fine_ny, fP = (fnx + 1 + 3) & ~3;
+    const long long fst = (long long)fP * (fny + 1);
+    for (int c = 0; c < 3; ++c)
+      for (int i = 0; i <= g.ny; ++i)
+        for (int j = 0; j <= g.nx; ++j) {
+          const int fi = g.cy ? std::min(2 * i, fny) : i, fj = g.cx ? std::min(2 * j, fnx) : j;
+          h[c * st + (long long)i * g.P + j] = f[c * fst + (long long)fi * fP + fj];
+        }
+  }
+  DevBuf<double>& d = dtens[{level, t}];
+  d.alloc(h.size());
+  d.upload(h.data(), h.size(), stream);
+  g.htens = h.data();
+  g.tens = d.p;
+  g.tstride = st;
+}
+
 void Batch::build_levels() {
   L.clear();
   int nl = 1;
@@ -661,10 +717,14 @@ void Batch::build_levels() {
         }
         g = c;
       }
-      interior_constants(g);
-      spectrum_bounds(g);
       g.P = (g.nx + 1 + 3) & ~3;
       g.inv_pitch = 1.0f / (float)g.P;
+      g.tens = g.htens = nullptr;
+      g.tstride = 0;
+      if (!tensor[t].empty()) level_tensor(g, l, t);
+      interior_constants(g);
+      if (g.tens) g.adv_on = 1;  // per-node stencils: every kernel takes the general path
+      spectrum_bounds(g);
       cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
       L[l].geom[t] = g;
     }
@@ -2397,6 +2457,48 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc) {
     B.build_levels();
     B.setup_walls();
     // a new operator invalidates the initial-guess history of that trap
+    const long long off = B.L[0].geom[trap].off;
+    EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
+    EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
+                               offsetof(eqf::CgState, gamma),
+                           0, 2 * sizeof(double), B.stream));
+    B.sync();
+  });
+}
+
+int eqf_set_tensor(eqf_batch* b, int32_t trap, const double* D11, const double* D22,
+                   const double* D12) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    Batch& B = *b->impl;
+    const eqf_trap_params& p = B.params[trap];
+    const bool iso = !D11 && !D22 && !D12;
+    EQF_REQUIRE(iso || (D11 && D22 && D12), "give all three tensor fields or none");
+    const long long n = (long long)(p.nx + 1) * (p.ny + 1);
+    std::vector<double> t;
+    if (!iso) {
+      t.resize(3 * n);
+      for (long long k = 0; k < n; ++k) {
+        const double a = D11[k], c = D22[k], d = D12[k];
+        EQF_REQUIRE(std::isfinite(a) && std::isfinite(c) && std::isfinite(d) && a > 0.0 &&
+                        c > 0.0 && a * c - d * d >= -1e-12 * a * c,
+                    "tensor not symmetric positive definite at a node");
+        t[k] = a;
+        t[n + k] = c;
+        t[2 * n + k] = d;
+      }
+    }
+    B.sync();
+    B.tensor[trap].swap(t);
+    if (iso) {
+      for (auto it = B.htens.begin(); it != B.htens.end();)
+        it = it->first.second == trap ? B.htens.erase(it) : std::next(it);
+      for (auto it = B.dtens.begin(); it != B.dtens.end();)
+        it = it->first.second == trap ? B.dtens.erase(it) : std::next(it);
+    }
+    B.build_levels();
+    B.setup_walls();
     const long long off = B.L[0].geom[trap].off;
     EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
     EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +

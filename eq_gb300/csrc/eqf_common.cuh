@@ -54,6 +54,11 @@ struct LevelGeom {
   double adv;            // advection: dt * v_y(y) = -adv * y  (0: none)
   double rob[4];         // Robin walls: dt * rate (bottom, top, left, right; 0 = none)
   int dvals;             // finest level: Dirichlet rows carry values (b = F there)
+  // Anisotropic tensor (D11, D22, D12 per node, pitched like the field, tstride apart):
+  // device copy for kernels, host copy for host-side setup; null = isotropic
+  const double* tens;
+  const double* htens;
+  long long tstride;
   Lens<double> ld;
   Lens<float> lf;
   // Uniform-interior stencil (nodes with 2 <= i <= ny-2 and 2 <= j <= nx-2).
@@ -101,6 +106,78 @@ EQF_HD bool is_uniform_interior(const LevelGeom& g, int i, int j) {
   return i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 2 && !g.adv_on;
 }
 
+// Tensor (D11, D22, D12) of node (i, j) of this level.
+EQF_HD void tensor_at(const LevelGeom& g, int i, int j, double& d11, double& d22, double& d12) {
+#ifdef __CUDA_ARCH__
+  const double* t = g.tens;
+#else
+  const double* t = g.htens;
+#endif
+  const long long k = (long long)i * g.P + j;
+  d11 = t[k];
+  d22 = t[k + g.tstride];
+  d12 = t[k + 2 * g.tstride];
+}
+
+// One triangle's stiffness beta * area * grad(phi_a) . A grad(phi_b), A the mean of its
+// vertex tensors, added to the node's row: gn the node's gradient, (gb[q], cb[q]) the
+// other two vertices' gradients and the stencil entries they go to.
+template <class T>
+EQF_HD void aniso_tri(T beta_area, const double (&m)[3], T gnx, T gny, T gbx0, T gby0,
+                      T& cb0, T gbx1, T gby1, T& cb1, T& cc) {
+  const T a11 = T(m[0]), a22 = T(m[1]), a12 = T(m[2]);
+  auto form = [&](T ux, T uy, T vx, T vy) {
+    return ux * (a11 * vx + a12 * vy) + uy * (a12 * vx + a22 * vy);
+  };
+  cc += beta_area * form(gnx, gny, gnx, gny);
+  cb0 += beta_area * form(gnx, gny, gbx0, gby0);
+  cb1 += beta_area * form(gnx, gny, gbx1, gby1);
+}
+
+// Stiffness of an anisotropic row from its (up to) six incident right triangles:
+// square UR (the node is v0): (node, E, NE) and (node, N, NE); square LL (v3):
+// (SW, S, node) and (SW, W, node); square LR (v2): (S, node, E); square UL (v1):
+// (W, node, N).  The "right" cut couples no NW / SE pair, so the 7-point shape holds.
+template <class T>
+EQF_HD void aniso_stiffness(const LevelGeom& g, int i, int j, T hxl, T hxr, T hyd, T hyu,
+                            Sten<T>& s) {
+  const T beta = lens<T>(g).beta, half = T(0.5), third = T(1.0 / 3.0);
+  double t0[3];
+  tensor_at(g, i, j, t0[0], t0[1], t0[2]);
+  auto mean3 = [&](int i1, int j1, int i2, int j2, double (&m)[3]) {
+    double u[3], v[3];
+    tensor_at(g, i1, j1, u[0], u[1], u[2]);
+    tensor_at(g, i2, j2, v[0], v[1], v[2]);
+    for (int q = 0; q < 3; ++q) m[q] = (double)(third * (T)(t0[q] + u[q] + v[q]));
+  };
+  T zero = T(0);
+  double m[3];
+  if (hxr > T(0) && hyu > T(0)) {
+    const T ba = beta * half * hxr * hyu, ix = T(1) / hxr, iy = T(1) / hyu;
+    mean3(i, j + 1, i + 1, j + 1, m);  // (node, E, NE)
+    aniso_tri<T>(ba, m, -ix, zero, ix, -iy, s.e, zero, iy, s.ne, s.c);
+    mean3(i + 1, j, i + 1, j + 1, m);  // (node, N, NE)
+    aniso_tri<T>(ba, m, zero, -iy, -ix, iy, s.n, ix, zero, s.ne, s.c);
+  }
+  if (hxl > T(0) && hyd > T(0)) {
+    const T ba = beta * half * hxl * hyd, ix = T(1) / hxl, iy = T(1) / hyd;
+    mean3(i - 1, j - 1, i - 1, j, m);  // (SW, S, node)
+    aniso_tri<T>(ba, m, zero, iy, -ix, zero, s.sw, ix, -iy, s.s, s.c);
+    mean3(i - 1, j - 1, i, j - 1, m);  // (SW, W, node)
+    aniso_tri<T>(ba, m, ix, zero, zero, -iy, s.sw, -ix, iy, s.w, s.c);
+  }
+  if (hxr > T(0) && hyd > T(0)) {
+    const T ba = beta * half * hxr * hyd, ix = T(1) / hxr, iy = T(1) / hyd;
+    mean3(i - 1, j, i, j + 1, m);  // (S, node, E)
+    aniso_tri<T>(ba, m, -ix, iy, zero, -iy, s.s, ix, zero, s.e, s.c);
+  }
+  if (hxl > T(0) && hyu > T(0)) {
+    const T ba = beta * half * hxl * hyu, ix = T(1) / hxl, iy = T(1) / hyu;
+    mean3(i, j - 1, i + 1, j, m);  // (W, node, N)
+    aniso_tri<T>(ba, m, ix, -iy, -ix, zero, s.w, zero, iy, s.n, s.c);
+  }
+}
+
 // Full stencil of node (i, j) from the surrounding cell sizes, in arithmetic T.
 // Mass (scaled by alpha): each triangle of area A adds A/6 on the diagonal and
 // A/12 per edge.  Stiffness (scaled by beta): right triangles couple only along
@@ -121,15 +198,28 @@ EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
   const T sy = hyd + hyu, sx = hxl + hxr;
   const T a24 = a * T(1.0 / 24.0), a12 = a * T(1.0 / 12.0);
   Sten<T> s;
-  const T ke = hb * sy * ihxr, kw = hb * sy * ihxl;  // zero where the cell is missing
-  const T kn = hb * sx * ihyu, ks = hb * sx * ihyd;
-  s.e = a24 * hxr * sy - ke;
-  s.w = a24 * hxl * sy - kw;
-  s.n = a24 * hyu * sx - kn;
-  s.s = a24 * hyd * sx - ks;
-  s.ne = a12 * hxr * hyu;
-  s.sw = a12 * hxl * hyd;
-  s.c = a12 * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu) + ke + kw + kn + ks;
+  if (g.tens) {
+    // mass as below; stiffness per incident triangle with the mean of the vertex
+    // tensors (the P1 tensor integrates exactly to area x mean)
+    s.e = a24 * hxr * sy;
+    s.w = a24 * hxl * sy;
+    s.n = a24 * hyu * sx;
+    s.s = a24 * hyd * sx;
+    s.ne = a12 * hxr * hyu;
+    s.sw = a12 * hxl * hyd;
+    s.c = a12 * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu);
+    aniso_stiffness<T>(g, i, j, hxl, hxr, hyd, hyu, s);
+  } else {
+    const T ke = hb * sy * ihxr, kw = hb * sy * ihxl;  // zero where the cell is missing
+    const T kn = hb * sx * ihyu, ks = hb * sx * ihyd;
+    s.e = a24 * hxr * sy - ke;
+    s.w = a24 * hxl * sy - kw;
+    s.n = a24 * hyu * sx - kn;
+    s.s = a24 * hyd * sx - ks;
+    s.ne = a12 * hxr * hyu;
+    s.sw = a12 * hxl * hyd;
+    s.c = a12 * (T(2) * hxl * hyd + hxr * hyd + hxl * hyu + T(2) * hxr * hyu) + ke + kw + kn + ks;
+  }
   if (g.adv_on) {
     // v_y at the node rows: dt*v(y) = -adv*y with y measured on this level's grid
     const T y0 = (i == g.ny) ? L.hy * T(g.ny - 1) + L.hyl : L.hy * T(i);

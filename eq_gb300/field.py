@@ -214,6 +214,17 @@ class TrapBatch:
         self._ck(self._lib.eqf_set_channels(self._h, int(trap), _dp(b) if b is not None else None,
                                             _dp(t) if t is not None else None))
 
+    def set_tensor(self, trap: int, D11=None, D22=None, D12=None):
+        """Per-node anisotropic tensor (grid order); None restores the isotropic one."""
+        if D11 is None:
+            self._ck(self._lib.eqf_set_tensor(self._h, int(trap), None, None, None))
+            return
+        a, b_, c = (np.ascontiguousarray(v, dtype=np.float64).ravel() for v in (D11, D22, D12))
+        n = self.num_nodes(trap)
+        if not (len(a) == len(b_) == len(c) == n):
+            raise ValueError("one tensor value per node")
+        self._ck(self._lib.eqf_set_tensor(self._h, int(trap), _dp(a), _dp(b_), _dp(c)))
+
     def set_well(self, trap: int, well_scaling: float, decay_rate: float):
         """Boundary well of a trap (0 scaling: off); walls of kind EQF_BC_WELL take it."""
         self._ck(self._lib.eqf_set_well(self._h, int(trap), float(well_scaling),

@@ -302,3 +302,14 @@ def batched_microfluidic(seed: int = 3, n_traps: int = 512, h: float = 0.25,
         t.walls = 0
         t.bc = microfluidic_bc(t)
     return traps
+
+
+# --- anisotropic tensors (eqf_set_tensor) -------------------------------------------
+
+def rotated_tensor(theta: np.ndarray, Dx: float, Dy: float):
+    """D11, D22, D12 of diag(Dx, Dy) turned by theta, as eQabm's setDiffusionTensor
+    forms them (src/abm/eQabm.cpp:306-325): Dx cos^2 + Dy sin^2, Dx sin^2 + Dy cos^2,
+    (Dx - Dy) sin cos."""
+    c, s = np.cos(theta), np.sin(theta)
+    cos2t, sin2t, sincost = c * c, s * s, s * c
+    return Dx * cos2t + Dy * sin2t, Dx * sin2t + Dy * cos2t, (Dx - Dy) * sincost

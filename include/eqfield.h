@@ -284,6 +284,18 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc);
 int eqf_read_channels(eqf_batch* b, int32_t trap, double* bottom, double* top);
 int eqf_set_channels(eqf_batch* b, int32_t trap, const double* bottom, const double* top);
 
+/* Anisotropic diffusion tensor of a trap: per node (grid order) the D11, D22, D12 of
+ * hslD's A = D*[[D11, D12], [D12, D22]] (fenics/hslD.ufl:31), the reference's
+ * D11/D22/D12 vectors (src/fHSL.h:418), filled per cell by setDiffusionTensor
+ * (src/abm/eQabm.cpp:306-325) and sampled by AnisotropicDiffusionTensor
+ * (src/Expressions.h:95-124).  The fields are P1: each triangle's stiffness uses the
+ * mean of its three vertex tensors.  All three NULL restores the isotropic tensor
+ * (1, 1, 0).  The tensor must be symmetric positive definite at every node.  Such
+ * traps take the per-node stencil path; their multigrid levels take the tensor by
+ * injection.  Rebuilds the batch's operators. */
+int eqf_set_tensor(eqf_batch* b, int32_t trap, const double* D11, const double* D22,
+                   const double* D12);
+
 /* Boundary well of a trap (Simulation::computeBoundaryWell, src/simulation.cpp:581-604):
  * after every step, with the step's totalBoundaryFlux F = D*dt*(-int grad c . n ds),
  *   w += F / well_scaling;  w -= dt * decay_rate * w;  w < 0 -> w = 0 (an underflow)
