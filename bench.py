@@ -121,6 +121,8 @@ def make_workload(name: str, seed: int, n_traps: int):
         return [wl.single_small(seed)]
     if name == "microfluidic":
         return wl.batched_microfluidic(seed=seed, n_traps=n_traps)
+    if name == "anisotropic":
+        return wl.batched_anisotropic(seed=seed, n_traps=n_traps)
     raise ValueError(name)
 
 
@@ -129,6 +131,8 @@ def load_traps(b, traps, first: int = 0):
     for i, t in enumerate(traps):
         if t.bc is not None:
             b.set_boundaries(first + i, t.bc["walls"], t.bc.get("channel"))
+        if t.tensor is not None:
+            b.set_tensor(first + i, *t.tensor)
         b.set_cells(first + i, t.cell_xy, t.cell_s)
 
 

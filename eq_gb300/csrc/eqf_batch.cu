@@ -183,6 +183,9 @@ static void interior_constants(LevelGeom& g) {
   q.adv = 0.0;
   q.adv_on = 0;
   q.tens = q.htens = nullptr;
+  q.tensf = nullptr;
+  q.coef_f = nullptr;
+  q.coef_d = nullptr;
   const Sten<double> s = stencil_general<double>(q, 500, 500);
   g.cC = s.c;
   g.cE = s.e;
@@ -447,6 +450,13 @@ class Batch {
   DevBuf<ChanDev> d_chans;
   int chan_n_max = 0;
   void setup_walls();
+  bool ops_dirty = false;  // walls or tensors changed: operators rebuilt before the next use
+  void ensure_ops() {
+    if (!ops_dirty) return;
+    ops_dirty = false;
+    build_levels();
+    setup_walls();
+  }
   void enqueue_walls();
   void enqueue_channels();
   // anisotropic tensors (eqf_set_tensor): per trap the caller's D11, D22, D12 in grid
@@ -454,6 +464,9 @@ class Batch {
   std::vector<std::vector<double>> tensor;
   std::map<std::pair<int, int>, std::vector<double>> htens;
   std::map<std::pair<int, int>, DevBuf<double>> dtens;
+  std::map<std::pair<int, int>, DevBuf<float>> dtensf;
+  std::map<std::pair<int, int>, DevBuf<float>> dcoef_f;
+  std::map<std::pair<int, int>, DevBuf<double>> dcoef_d;
   void level_tensor(LevelGeom& g, int level, int t);
   // boundary wells (eqf_set_well)
   struct WellParams {
@@ -667,8 +680,14 @@ void Batch::level_tensor(LevelGeom& g, int level, int t) {
   DevBuf<double>& d = dtens[{level, t}];
   d.alloc(h.size());
   d.upload(h.data(), h.size(), stream);
+  std::vector<float> hf(h.begin(), h.end());
+  DevBuf<float>& df = dtensf[{level, t}];
+  df.alloc(hf.size());
+  df.upload(hf.data(), hf.size(), stream);
+  sync();  // hf is released on return
   g.htens = h.data();
   g.tens = d.p;
+  g.tensf = df.p;
   g.tstride = st;
 }
 
@@ -720,10 +739,25 @@ void Batch::build_levels() {
       g.P = (g.nx + 1 + 3) & ~3;
       g.inv_pitch = 1.0f / (float)g.P;
       g.tens = g.htens = nullptr;
+      g.tensf = nullptr;
       g.tstride = 0;
+      g.coef_f = nullptr;
+      g.coef_d = nullptr;
       if (!tensor[t].empty()) level_tensor(g, l, t);
       interior_constants(g);
-      if (g.tens) g.adv_on = 1;  // per-node stencils: every kernel takes the general path
+      if (g.tens) {
+        g.adv_on = 1;  // per-node stencils: every kernel takes the general path
+        const long long n = (long long)g.P * (g.ny + 1);
+        DevBuf<float>& cf = dcoef_f[{l, t}];
+        DevBuf<double>& cd = dcoef_d[{l, t}];
+        cf.alloc(8 * n);
+        cd.alloc(8 * n);
+        k_aniso_coefs<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, stream>>>(
+            g, cf.p, cd.p);
+        EQF_LAUNCH_CHECK();
+        g.coef_f = cf.p;
+        g.coef_d = cd.p;
+      }
       spectrum_bounds(g);
       cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
       L[l].geom[t] = g;
@@ -1675,6 +1709,7 @@ void Batch::check_fail() {
 }
 
 void Batch::step(int n) {
+  ensure_ops();
   if (cells_dirty) rebuild_cells();
   for (int k = 0; k < n; ++k) {
     if (opts.use_graph && !prof.on) {
@@ -2454,8 +2489,7 @@ int eqf_set_boundaries(eqf_batch* b, int32_t trap, const eqf_boundaries* bc) {
     B.sync();
     B.bcs[trap] = *bc;
     B.params[trap].walls = walls;
-    B.build_levels();
-    B.setup_walls();
+    B.ops_dirty = true;
     // a new operator invalidates the initial-guess history of that trap
     const long long off = B.L[0].geom[trap].off;
     EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
@@ -2496,9 +2530,14 @@ int eqf_set_tensor(eqf_batch* b, int32_t trap, const double* D11, const double* 
         it = it->first.second == trap ? B.htens.erase(it) : std::next(it);
       for (auto it = B.dtens.begin(); it != B.dtens.end();)
         it = it->first.second == trap ? B.dtens.erase(it) : std::next(it);
+      for (auto it = B.dtensf.begin(); it != B.dtensf.end();)
+        it = it->first.second == trap ? B.dtensf.erase(it) : std::next(it);
+      for (auto it = B.dcoef_f.begin(); it != B.dcoef_f.end();)
+        it = it->first.second == trap ? B.dcoef_f.erase(it) : std::next(it);
+      for (auto it = B.dcoef_d.begin(); it != B.dcoef_d.end();)
+        it = it->first.second == trap ? B.dcoef_d.erase(it) : std::next(it);
     }
-    B.build_levels();
-    B.setup_walls();
+    B.ops_dirty = true;
     const long long off = B.L[0].geom[trap].off;
     EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
     EQF_CK(cudaMemsetAsync(reinterpret_cast<char*>(B.dstate.p + trap) +
@@ -2551,6 +2590,7 @@ int eqf_read_channels(eqf_batch* b, int32_t trap, double* bottom, double* top) {
   return guarded(b, [&] {
     EQF_TRAP_CHECK(b, trap);
     Batch& B = *b->impl;
+    B.ensure_ops();
     Batch::Chan* ch = chan_of(B, trap);
     EQF_REQUIRE(ch != nullptr, "trap has no flow channel");
     double* out[2] = {bottom, top};
@@ -2569,6 +2609,7 @@ int eqf_set_channels(eqf_batch* b, int32_t trap, const double* bottom, const dou
   return guarded(b, [&] {
     EQF_TRAP_CHECK(b, trap);
     Batch& B = *b->impl;
+    B.ensure_ops();
     Batch::Chan* ch = chan_of(B, trap);
     EQF_REQUIRE(ch != nullptr, "trap has no flow channel");
     const double* in[2] = {bottom, top};

@@ -58,7 +58,12 @@ struct LevelGeom {
   // device copy for kernels, host copy for host-side setup; null = isotropic
   const double* tens;
   const double* htens;
+  const float* tensf;  // FP32 copy for the FP32 operator path
   long long tstride;
+  // the per-node stencils of an anisotropic level (c, e, w, n, s, ne, sw, 1/c per node,
+  // pitched), built once per tensor update: the general path reads them
+  const float* coef_f;
+  const double* coef_d;
   Lens<double> ld;
   Lens<float> lf;
   // Uniform-interior stencil (nodes with 2 <= i <= ny-2 and 2 <= j <= nx-2).
@@ -106,26 +111,35 @@ EQF_HD bool is_uniform_interior(const LevelGeom& g, int i, int j) {
   return i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 2 && !g.adv_on;
 }
 
-// Tensor (D11, D22, D12) of node (i, j) of this level.
-EQF_HD void tensor_at(const LevelGeom& g, int i, int j, double& d11, double& d22, double& d12) {
+// Tensor (D11, D22, D12) of node (i, j) of this level, in the stencil's arithmetic
+// (FP32 stencils read the FP32 copy; the host reads its own FP64 copy).
+template <class T>
+EQF_HD void tensor_at(const LevelGeom& g, int i, int j, T& d11, T& d22, T& d12) {
+  const long long k = (long long)i * g.P + j;
 #ifdef __CUDA_ARCH__
+  if (sizeof(T) == sizeof(float)) {
+    const float* t = g.tensf;
+    d11 = (T)t[k];
+    d22 = (T)t[k + g.tstride];
+    d12 = (T)t[k + 2 * g.tstride];
+    return;
+  }
   const double* t = g.tens;
 #else
   const double* t = g.htens;
 #endif
-  const long long k = (long long)i * g.P + j;
-  d11 = t[k];
-  d22 = t[k + g.tstride];
-  d12 = t[k + 2 * g.tstride];
+  d11 = (T)t[k];
+  d22 = (T)t[k + g.tstride];
+  d12 = (T)t[k + 2 * g.tstride];
 }
 
 // One triangle's stiffness beta * area * grad(phi_a) . A grad(phi_b), A the mean of its
 // vertex tensors, added to the node's row: gn the node's gradient, (gb[q], cb[q]) the
 // other two vertices' gradients and the stencil entries they go to.
 template <class T>
-EQF_HD void aniso_tri(T beta_area, const double (&m)[3], T gnx, T gny, T gbx0, T gby0,
+EQF_HD void aniso_tri(T beta_area, const T (&m)[3], T gnx, T gny, T gbx0, T gby0,
                       T& cb0, T gbx1, T gby1, T& cb1, T& cc) {
-  const T a11 = T(m[0]), a22 = T(m[1]), a12 = T(m[2]);
+  const T a11 = m[0], a22 = m[1], a12 = m[2];
   auto form = [&](T ux, T uy, T vx, T vy) {
     return ux * (a11 * vx + a12 * vy) + uy * (a12 * vx + a22 * vy);
   };
@@ -142,16 +156,16 @@ template <class T>
 EQF_HD void aniso_stiffness(const LevelGeom& g, int i, int j, T hxl, T hxr, T hyd, T hyu,
                             Sten<T>& s) {
   const T beta = lens<T>(g).beta, half = T(0.5), third = T(1.0 / 3.0);
-  double t0[3];
-  tensor_at(g, i, j, t0[0], t0[1], t0[2]);
-  auto mean3 = [&](int i1, int j1, int i2, int j2, double (&m)[3]) {
-    double u[3], v[3];
-    tensor_at(g, i1, j1, u[0], u[1], u[2]);
-    tensor_at(g, i2, j2, v[0], v[1], v[2]);
-    for (int q = 0; q < 3; ++q) m[q] = (double)(third * (T)(t0[q] + u[q] + v[q]));
+  T t0[3];
+  tensor_at<T>(g, i, j, t0[0], t0[1], t0[2]);
+  auto mean3 = [&](int i1, int j1, int i2, int j2, T (&m)[3]) {
+    T u[3], v[3];
+    tensor_at<T>(g, i1, j1, u[0], u[1], u[2]);
+    tensor_at<T>(g, i2, j2, v[0], v[1], v[2]);
+    for (int q = 0; q < 3; ++q) m[q] = third * (t0[q] + u[q] + v[q]);
   };
   T zero = T(0);
-  double m[3];
+  T m[3];
   if (hxr > T(0) && hyu > T(0)) {
     const T ba = beta * half * hxr * hyu, ix = T(1) / hxr, iy = T(1) / hyu;
     mean3(i, j + 1, i + 1, j + 1, m);  // (node, E, NE)
@@ -179,11 +193,13 @@ EQF_HD void aniso_stiffness(const LevelGeom& g, int i, int j, T hxl, T hxr, T hy
 }
 
 // Full stencil of node (i, j) from the surrounding cell sizes, in arithmetic T.
+// ANISO = false leaves out the anisotropic branch (for device callers that never see
+// a tensor: anisotropic levels read their stencils built once by k_aniso_coefs).
 // Mass (scaled by alpha): each triangle of area A adds A/6 on the diagonal and
 // A/12 per edge.  Stiffness (scaled by beta): right triangles couple only along
 // their legs, -cot/2 = -(other leg)/(2*this leg); hypotenuses carry no stiffness.
 // Advection (c2): dt * int v_y d(phi_b)/dy phi_a over each triangle with a P1 v_y.
-template <class T>
+template <class T, bool ANISO = true>
 EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
   const Lens<T>& L = lens<T>(g);
   const T hxl = j > 0 ? (j == g.nx ? L.hxl : L.hx) : T(0);
@@ -198,7 +214,7 @@ EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
   const T sy = hyd + hyu, sx = hxl + hxr;
   const T a24 = a * T(1.0 / 24.0), a12 = a * T(1.0 / 12.0);
   Sten<T> s;
-  if (g.tens) {
+  if (ANISO && g.tens) {
     // mass as below; stiffness per incident triangle with the mean of the vertex
     // tensors (the P1 tensor integrates exactly to area x mean)
     s.e = a24 * hxr * sy;

@@ -268,7 +268,15 @@ __device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&
     for (int q = 0; q < 8; ++q) c[q] = T(0);
     return;
   }
-  const Sten<T> s = stencil_general<T>(g, i, j);
+  const T* pre = sizeof(T) == sizeof(float) ? (const T*)(const void*)g.coef_f
+                                            : (const T*)(const void*)g.coef_d;
+  if (pre) {  // an anisotropic level: the stencils built once (k_aniso_coefs)
+    const T* q = pre + 8 * ((long long)i * g.P + j);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) c[e] = q[e];
+    return;
+  }
+  const Sten<T> s = stencil_general<T, false>(g, i, j);  // advective rows
   c[0] = s.c;
   c[1] = s.e;
   c[2] = s.w;
@@ -278,11 +286,41 @@ __device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&
   c[6] = s.sw;
   c[7] = T(1) / s.c;
 }
+// The stencil of a general-path node: an anisotropic level reads the stencil built
+// once (k_aniso_coefs) inline; other general rows (advection) compute it out of line.
+template <class T>
+__device__ __forceinline__ void coef_node(const LevelGeom& g, int i, int j, T (&c)[8]) {
+  const T* pre = sizeof(T) == sizeof(float) ? (const T*)(const void*)g.coef_f
+                                            : (const T*)(const void*)g.coef_d;
+  if (pre && j >= 0 && j <= g.nx && i >= 0 && i <= g.ny) {
+    const T* q = pre + 8 * ((long long)i * g.P + j);
+    if (sizeof(T) == sizeof(float)) {  // one node's 8 values are two aligned 16-byte vectors
+      const float4 lo = __ldg(reinterpret_cast<const float4*>(q));
+      const float4 hi = __ldg(reinterpret_cast<const float4*>(q) + 1);
+      c[0] = (T)lo.x;
+      c[1] = (T)lo.y;
+      c[2] = (T)lo.z;
+      c[3] = (T)lo.w;
+      c[4] = (T)hi.x;
+      c[5] = (T)hi.y;
+      c[6] = (T)hi.z;
+      c[7] = (T)hi.w;
+      return;
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) c[e] = __ldg(q + e);
+    return;
+  }
+  T t[8];
+  coef_general<T>(g, i, j, t);
+#pragma unroll
+  for (int e = 0; e < 8; ++e) c[e] = t[e];
+}
 template <class T, class X>
 __device__ __forceinline__ T apply_general(const LevelGeom& g, const X& x, int k, int i, int j,
                                            T& idiag) {
   T c[8];
-  coef_general<T>(g, i, j, c);
+  coef_node<T>(g, i, j, c);
   idiag = c[7];
   const int P = g.P;
   return st_table(c, x[k], x[k + 1], x[k - 1], x[k + P], x[k - P], x[k + P + 1], x[k - P - 1]);
@@ -290,8 +328,36 @@ __device__ __forceinline__ T apply_general(const LevelGeom& g, const X& x, int k
 template <class T>
 __device__ __forceinline__ T inv_diag_general(const LevelGeom& g, int i, int j) {
   T c[8];
-  coef_general<T>(g, i, j, c);
+  coef_node<T>(g, i, j, c);
   return c[7];
+}
+
+// The per-node stencils of an anisotropic level: FP64 stencil_general (the same rows
+// the host bounds use), kept in FP64 and rounded to FP32.
+__global__ void k_aniso_coefs(const LevelGeom g, float* __restrict__ cf,
+                              double* __restrict__ cd) {
+  const long long n = (long long)g.P * (g.ny + 1);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / g.P), j = (int)(k - (long long)i * g.P);
+    double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (j <= g.nx) {
+      const Sten<double> s = stencil_general<double>(g, i, j);
+      c[0] = s.c;
+      c[1] = s.e;
+      c[2] = s.w;
+      c[3] = s.n;
+      c[4] = s.s;
+      c[5] = s.ne;
+      c[6] = s.sw;
+      c[7] = 1.0 / s.c;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      cd[8 * k + q] = c[q];
+      cf[8 * k + q] = (float)c[q];
+    }
+  }
 }
 
 // (A x)_k and 1/diagonal of node (i, j).  Every neighbour index must be readable
@@ -511,8 +577,8 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
       const T w = e == 0 ? xw : xc.v[e - 1];
       const T ee = e == 3 ? xe : xc.v[e + 1];
       if (g.adv_on) {
-        T c[8];  // filled out of line (local memory): advective traps only
-        coef_general<T>(g, i, j, c);
+        T c[8];  // general rows, out of line (an inline fetch spills the isotropic
+        coef_general<T>(g, i, j, c);  // quad path): advective or anisotropic traps only
         ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
         id.v[e] = c[7];
       } else {

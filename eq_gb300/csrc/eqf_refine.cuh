@@ -138,7 +138,7 @@ __device__ __forceinline__ DF df_apply(const LevelGeom& g, const float2* __restr
   DF c[7];
   if (general) {
     double cg[8];
-    coef_general<double>(g, i, j, cg);
+    coef_node<double>(g, i, j, cg);
 #pragma unroll
     for (int m = 0; m < 7; ++m) c[m] = df_split(cg[m]);
   } else {

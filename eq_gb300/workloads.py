@@ -65,6 +65,8 @@ class Trap:
     # wall conditions / flow channels (eqf_set_boundaries): {"walls": {side: (kind,
     # value, rate)}, "channel": {...}}; None = the walls bitfield above
     bc: Optional[dict] = None
+    # anisotropic tensor (eqf_set_tensor): (D11, D22, D12) per node in grid order
+    tensor: Optional[tuple] = None
 
     @property
     def n_nodes(self) -> int:
@@ -313,3 +315,16 @@ def rotated_tensor(theta: np.ndarray, Dx: float, Dy: float):
     c, s = np.cos(theta), np.sin(theta)
     cos2t, sin2t, sincost = c * c, s * s, s * c
     return Dx * cos2t + Dy * sin2t, Dx * sin2t + Dy * cos2t, (Dx - Dy) * sincost
+
+
+def batched_anisotropic(seed: int = 3, n_traps: int = 512, Dx: float = 2.0,
+                        Dy: float = 0.5) -> List[Trap]:
+    """The batched_uneven traps with a smoothly turning anisotropic tensor: diag(Dx, Dy)
+    rotated by theta(x, y) = 0.7 sin(2 pi x / W) + 0.5 y / H."""
+    traps = batched_uneven(seed=seed, n_traps=n_traps)
+    for t in traps:
+        y, x = np.meshgrid(np.linspace(0, t.H, t.ny + 1), np.linspace(0, t.W, t.nx + 1),
+                           indexing="ij")
+        theta = 0.7 * np.sin(2 * np.pi * x / t.W) + 0.5 * y / t.H
+        t.tensor = tuple(v.ravel() for v in rotated_tensor(theta, Dx, Dy))
+    return traps

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _worker(args):
-    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s, bc) = args
+    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s, bc, tensor) = args
     if ROOT not in sys.path:
         sys.path.insert(0, ROOT)
     from oracle import channel, hsld
@@ -30,7 +30,8 @@ def _worker(args):
     done = 0
     for _ in range(steps):
         if bc is None:
-            o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls)
+            t3 = tensor if tensor is not None else (None, None, None)
+            o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls, D11=t3[0], D22=t3[1], D12=t3[2])
             u = o.step(u, F)
         else:  # walls and channels re-assembled every step, as the reference does
             o = channel.MicrofluidicTrap(W, H, nx, ny, D, dt, g, bc["walls"], bc.get("channel"))
@@ -49,7 +50,8 @@ def reference_rate(traps, idx, steps_per_trap: int, budget_s: float, timeout_s: 
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     jobs = [(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls, t.cell_xy, t.cell_s,
-             steps_per_trap, budget_s, getattr(t, "bc", None)) for t in (traps[i] for i in idx)]
+             steps_per_trap, budget_s, getattr(t, "bc", None), getattr(t, "tensor", None))
+            for t in (traps[i] for i in idx)]
     procs = min(cores, len(jobs))
     t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(processes=procs) as pool:
