@@ -1415,6 +1415,7 @@ void Batch::setup_walls() {
         d.alloc(std::max<size_t>(1, h_.size()));
         if (!h_.empty()) d.upload(h_.data(), h_.size(), stream);
       };
+      for (double& v : b) v = 1.0 / v;  // the kernel multiplies by the reciprocal
       up(ch->k1, k1);
       up(ch->k2, k2);
       up(ch->bfin, b);
@@ -1464,7 +1465,11 @@ void Batch::setup_walls() {
   if (!hc.empty()) {
     d_chans.upload(hc.data(), hc.size(), stream);
     // the attribute belongs to the kernel, not to this batch: always the largest size
-    EQF_CK(cudaFuncSetAttribute(k_channel_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    EQF_CK(cudaFuncSetAttribute(k_channel_step<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)chan_smem_bytes(kChanMaxNodes)));
+    EQF_CK(cudaFuncSetAttribute(k_channel_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)chan_smem_bytes(kChanMaxNodes)));
+    EQF_CK(cudaFuncSetAttribute(k_channel_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)chan_smem_bytes(kChanMaxNodes)));
   }
   // the load vector restarts from the point cells alone (rims included)
@@ -1513,10 +1518,13 @@ void Batch::enqueue_walls() {
 // their sub-steps.
 void Batch::enqueue_channels() {
   if (chans.empty()) return;
+  // nodes per thread of the longest channel: the prefetching sweep up to 2 (more
+  // would hold so many registers that fewer channels share an SM)
+  const int npt = (chan_n_max + kChanThreads - 1) / kChanThreads;
+  auto kern = npt == 1 ? k_channel_step<1> : npt == 2 ? k_channel_step<2> : k_channel_step<0>;
   EQF_RUN(*this, KC_SCALAR,
-          (k_channel_step<<<dim3((unsigned)chans.size(), 2), kChanThreads,
-                            chan_smem_bytes(chan_n_max), stream>>>(
-              d_chans.p, L[0].dgeom.p, U[1 - cur].p, d_frozen.p)));
+          (kern<<<dim3((unsigned)chans.size(), 2), kChanThreads, chan_smem_bytes(chan_n_max),
+                  stream>>>(d_chans.p, L[0].dgeom.p, U[1 - cur].p, d_frozen.p)));
 }
 
 // ---------------------------------------------------------------------------

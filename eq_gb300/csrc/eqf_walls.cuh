@@ -128,7 +128,7 @@ struct ChanDev {  // the channels of one trap
   double well;    // well_scaling
   const double* k1;   // PCR multipliers [level * n + i]
   const double* k2;
-  const double* bfin;  // diagonal after the last level
+  const double* bfin;  // 1 / the diagonal after the last level
   const double* bl;    // explicit part: sub-, main and super-diagonal of the right side
   const double* bd;
   const double* bu;
@@ -139,8 +139,71 @@ constexpr int kChanThreads = 512;
 constexpr int kChanMaxNodes = 4097;
 __host__ __device__ constexpr size_t chan_smem_bytes(int n) { return (size_t)4 * n * sizeof(double); }
 
+// One reduction sweep of a sub-step, NPT nodes per thread (i = t + q*blockDim): the
+// multipliers of level lv+PD are loaded while level lv is reduced, so their L2
+// latency is paid once per sweep instead of once per level.  NPT = 0: the plain loop.
+// (FP64 throughput bounds the sweep on this part: two FP64 lanes per clock per SM.)
+template <int NPT>
+__device__ __forceinline__ double* chan_reduce(const ChanDev& ch, double* a, double* b) {
+  const int n = ch.n;
+  if (NPT == 0) {
+    for (int lv = 0, s = 1; lv < ch.levels; ++lv, s <<= 1) {
+      const double* K1 = ch.k1 + (size_t)lv * n;
+      const double* K2 = ch.k2 + (size_t)lv * n;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = a[i];
+        if (i - s >= 0) v -= K1[i] * a[i - s];
+        if (i + s < n) v -= K2[i] * a[i + s];
+        b[i] = v;
+      }
+      __syncthreads();
+      double* t = a;
+      a = b;
+      b = t;
+    }
+    return a;
+  }
+  constexpr int PD = 4, MAXLV = 13;
+  double r1[PD][NPT > 0 ? NPT : 1], r2[PD][NPT > 0 ? NPT : 1];
+#pragma unroll
+  for (int p = 0; p < PD; ++p)
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int i = threadIdx.x + q * blockDim.x;
+      const bool ok = p < ch.levels && i < n;
+      r1[p][q] = ok ? ch.k1[(size_t)p * n + i] : 0.0;
+      r2[p][q] = ok ? ch.k2[(size_t)p * n + i] : 0.0;
+    }
+#pragma unroll
+  for (int lv = 0; lv < MAXLV; ++lv) {
+    if (lv >= ch.levels) break;
+    const int s = 1 << lv;
+    const int slot = lv % PD;
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int i = threadIdx.x + q * blockDim.x;
+      if (i < n) {
+        double v = a[i];
+        if (i - s >= 0) v -= r1[slot][q] * a[i - s];
+        if (i + s < n) v -= r2[slot][q] * a[i + s];
+        b[i] = v;
+      }
+      const int nl = lv + PD;  // refill this slot with level lv + PD
+      const bool ok = nl < ch.levels && i < n;
+      r1[slot][q] = ok ? ch.k1[(size_t)nl * n + i] : 0.0;
+      r2[slot][q] = ok ? ch.k2[(size_t)nl * n + i] : 0.0;
+    }
+    __syncthreads();
+    double* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
 // One channel (blockIdx.x = trap, blockIdx.y = 0 bottom / 1 top) through one step:
 // the flux of the new trap field u, then `substeps` Crank-Nicolson sub-steps.
+template <int NPT>
 __global__ void __launch_bounds__(kChanThreads)
     k_channel_step(const ChanDev* __restrict__ chans, const LevelGeom* __restrict__ G,
                    const double* __restrict__ U, const int* __restrict__ frozen) {
@@ -160,15 +223,16 @@ __global__ void __launch_bounds__(kChanThreads)
   const int r0 = blockIdx.y == 0 ? 0 : g.ny, r1 = blockIdx.y == 0 ? 1 : g.ny - 1;
   // computeBoundaryFlux: gradc = (u[row next to the wall] - u[wall row]) / h;
   // flux = ds * (dt * D * gradc) / wellScaling with ds = h
+  // each sub-step adds flux / substeps: the same share every time, formed once
+  const double parts = (double)ch.substeps;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const double gradc = (u[(long long)r1 * P + j] - u[(long long)r0 * P + j]) / ch.h;
-    flux[j] = ch.h * (ch.dtD * gradc) / ch.well;
+    flux[j] = ch.h * (ch.dtD * gradc) / ch.well / parts;
     cc[j] = c[j];
   }
   __syncthreads();
-  const double parts = (double)ch.substeps;
   for (int sub = 0; sub < ch.substeps; ++sub) {
-    for (int j = threadIdx.x; j < n; j += blockDim.x) cc[j] += flux[j] / parts;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) cc[j] += flux[j];
     __syncthreads();
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
       double v = ch.bd[j] * cc[j];
@@ -177,23 +241,8 @@ __global__ void __launch_bounds__(kChanThreads)
       d0[j] = v;
     }
     __syncthreads();
-    double* a = d0;
-    double* b = d1;
-    for (int lv = 0, s = 1; lv < ch.levels; ++lv, s <<= 1) {
-      const double* K1 = ch.k1 + (size_t)lv * n;
-      const double* K2 = ch.k2 + (size_t)lv * n;
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = a[i];
-        if (i - s >= 0) v -= K1[i] * a[i - s];
-        if (i + s < n) v -= K2[i] * a[i + s];
-        b[i] = v;
-      }
-      __syncthreads();
-      double* t = a;
-      a = b;
-      b = t;
-    }
-    for (int j = threadIdx.x; j < n; j += blockDim.x) cc[j] = a[j] / ch.bfin[j];
+    const double* a = chan_reduce<NPT>(ch, d0, d1);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) cc[j] = a[j] * ch.bfin[j];
     __syncthreads();
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) c[j] = cc[j];
