@@ -78,34 +78,25 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const int na = padded_len(g);
   const View<T> xv = sg.add_guarded(x + g.off, qhalo_lo(g, tile), qhalo_hi(g, tile), na);
   const View<T> wv = sg.add(w + g.off, tile.k0, tile.k1, na);
-  const T* stab = stage_table<T>(sg, tab, ci);
-  if (!sg.run()) return;
+  const TableStage<T> tst = stage_table<T>(sg, tab, ci);
+  const T* stab = tst.s;
+  if (!sg.run(tst)) return;
   T* ys = y + g.off;
   const int P = g.P;
-  const QuadGeom qg(g, tile);
   T a0 = T(0), a1 = T(0);
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (QuadWalk q(g, tile.k0 >> 2); 4 * q.q < tile.k1; q.next()) {
-      const int k = 4 * q.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-      Q4<T> xc, id;
-      const Q4<T> ax =
-          apply_quad<T, PM>(g, ci, stab, xv, k, P, q.i, q.j, qg.interior(k, q.i, q.j), xc, id);
-      const Q4<T> wq = full ? wv.quad(k) : quad_masked<T>(wv, k, tile.k0, tile.k1);
+  // tiles are whole rows: every quad lies inside the tile
+  for_quads(g, QuadBlock{tile.r0, tile.r1, 0, P >> 2}, [&](int i, int cq, auto inner_) {
+    constexpr bool INNER = decltype(inner_)::value;
+    const int j = 4 * cq, k = i * P + j;
+    Q4<T> xc, id;
+    const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, k, P, i, j, INNER, xc, id);
+    const Q4<T> wq = wv.quad(k);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const bool in = full || (k + e >= tile.k0 && k + e < tile.k1);
-        if (in) {
-          a0 += wq.v[e] * ax.v[e];
-          if (NDOT == 2) a1 += ax.v[e] * ax.v[e];
-        }
-      }
-      if (full)
-        vst4<T>(ys + k, ax);
-      else
-        store_masked<T>(ys, ax, k, tile.k0, tile.k1);
+    for (int e = 0; e < 4; ++e) {
+      a0 += wq.v[e] * ax.v[e];
+      if (NDOT == 2) a1 += ax.v[e] * ax.v[e];
     }
+    vst4<T>(ys + k, ax);
   });
   const double t0 = block_sum(double(a0));
   const double t1 = NDOT == 2 ? block_sum(double(a1)) : 0.0;

@@ -87,25 +87,29 @@ struct RowStage {
     if (r < 0 || r >= nrows || b <= a) return 0u;
     return (uint32_t)(b - a) * (uint32_t)sizeof(T);
   }
+  // Only the guard parts are touched: whole rows outside the grid, and in grid rows
+  // the columns left of 0 and right of the pitch (none for an interior tile).
   __device__ __forceinline__ void zero_guards() const {
     const int S = w.S();
     const int a = w.ca > 0 ? w.ca : 0, b = w.cb < P ? w.cb : P;
+    const int lw = b > a ? a - w.ca : S;  // guard columns on the left (all: empty range)
+    const int rw = b > a ? w.cb - b : 0;  // and on the right
+    if (lw == 0 && rw == 0 && w.ra >= 0 && w.rb <= nrows) return;
     for (int r = w.ra + (int)(threadIdx.x >> 5); r < w.rb; r += (int)(blockDim.x >> 5)) {
       T* row = dst + (r - w.ra) * S;
-      const bool in = r >= 0 && r < nrows && b > a;
-      for (int c = (int)(threadIdx.x & 31); c < S; c += 32) {
-        const int col = w.ca + c;
-        if (!in || col < a || col >= b) row[c] = T(0);
+      if (r < 0 || r >= nrows) {
+        for (int c = (int)(threadIdx.x & 31); c < S; c += 32) row[c] = T(0);
+      } else {
+        for (int c = (int)(threadIdx.x & 31); c < lw; c += 32) row[c] = T(0);
+        for (int c = (int)(threadIdx.x & 31); c < rw; c += 32) row[S - rw + c] = T(0);
       }
     }
   }
-  __device__ __forceinline__ uint32_t total() const {
-    uint32_t t = 0;
-    for (int r = w.ra; r < w.rb; ++r) {
-      int a, b;
-      t += row_bytes(r, a, b);
-    }
-    return t;
+  __device__ __forceinline__ uint32_t total() const {  // in-grid rows x in-grid columns
+    const int a = w.ca > 0 ? w.ca : 0, b = w.cb < P ? w.cb : P;
+    const int r0 = w.ra > 0 ? w.ra : 0, r1 = w.rb < nrows ? w.rb : nrows;
+    if (b <= a || r1 <= r0) return 0u;
+    return (uint32_t)(r1 - r0) * (uint32_t)(b - a) * (uint32_t)sizeof(T);
   }
   __device__ __forceinline__ void issue(uint64_t* bar) const {  // warp 0
     for (int r = w.ra + (int)threadIdx.x; r < w.rb; r += 32) {
@@ -117,12 +121,13 @@ struct RowStage {
   }
 };
 
-// Stages the windows on one mbarrier; returns false, uniformly for the CTA, if the
-// bounded wait gave up (device error flag set).
-template <class T, int N>
-__device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st)[N]) {
-#pragma unroll
-  for (int q = 0; q < N; ++q) st[q].zero_guards();
+// Stages the windows on one mbarrier: warp 0 issues the row copies, then every
+// thread runs `fill` (the class table: its global loads overlap the copies) and
+// zero-fills the guards.  Returns false, uniformly for the CTA, if the bounded wait
+// gave up (device error flag set).
+template <class T, int N, class F>
+__device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st)[N],
+                                           const F& fill) {
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     uint32_t tot = 0;
@@ -135,6 +140,9 @@ __device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st
 #pragma unroll
     for (int q = 0; q < N; ++q) st[q].issue(bar);
   }
+  fill();
+#pragma unroll
+  for (int q = 0; q < N; ++q) st[q].zero_guards();
   bool ok = true;
   if (threadIdx.x == 0) {
     ok = false;
@@ -161,9 +169,9 @@ struct WinQuads {
   }
 };
 
-// The quad's nodes are all uniform-interior nodes.
-__device__ __forceinline__ bool quad_interior(const LevelGeom& g, int i, int j) {
-  return !g.adv_on && i >= 2 && i <= g.ny - 2 && j >= 2 && j <= g.nx - 5;
+// The quads of a window, for for_quads.
+__device__ __forceinline__ QuadBlock win_quads(const Win& w) {
+  return QuadBlock{w.ra, w.rb, w.ca, w.S() >> 2};
 }
 
 // 1 / diagonal of the quad's nodes (the same values every stencil path uses).
@@ -222,59 +230,50 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   T* bp = carve<T>(st, w1.count());
   T* x1p = carve<T>(st, w1.count());
   T* x2p = carve<T>(st, w2.count());
-  const T* stab = stage_table<T>(st, tab, ci);
+  const TableStage<T> tst = stage_table<T>(st, tab, ci);
+  const T* stab = tst.s;
   const RowStage<T> rs[1] = {{b + g.off, bp, w1, P, g.ny + 1}};
-  if (!stage_rows<T, 1>(st.bar, rs)) return;
+  if (!stage_rows<T, 1>(st.bar, rs, tst)) return;
   const int S1 = w1.S(), S2 = w2.S();
   // step 1 from zero (pointwise) on W1
-  {
-    const WinQuads wq(w1);
-    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
-      int row, cq;
-      wq.at(q, row, cq);
-      const int i = w1.ra + row, j = w1.ca + 4 * cq, kl = row * S1 + 4 * cq;
-      const Q4<T> bq = vld4<T>(bp + kl);
-      const Q4<T> id = inv_diag_quad<T>(g, ci, stab, i, j, quad_interior(g, i, j));
-      Q4<T> d;
+  for_quads(g, win_quads(w1), [&](int i, int cq, auto inner_) {
+    constexpr bool INNER = decltype(inner_)::value;
+    const int j = w1.ca + 4 * cq, kl = (i - w1.ra) * S1 + 4 * cq;
+    const Q4<T> bq = vld4<T>(bp + kl);
+    const Q4<T> id = inv_diag_quad<T>(g, ci, stab, i, j, INNER);
+    Q4<T> d;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) d.v[e] = (T(c0.c_res) * bq.v[e]) * id.v[e];
-      vst4<T>(x1p + kl, d);
-    }
-  }
+    for (int e = 0; e < 4; ++e) d.v[e] = (T(c0.c_res) * bq.v[e]) * id.v[e];
+    vst4<T>(x1p + kl, d);
+  });
   __syncthreads();
   // step 2 on W2 (d1 = x1)
   {
-    const WinQuads wq(w2);
     const View<T> x1v{x1p, 0};
-    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
-      int row, cq;
-      wq.at(q, row, cq);
-      const int i = w2.ra + row, j = w2.ca + 4 * cq;
+    for_quads(g, win_quads(w2), [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = w2.ca + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w1, i, j), S1, i, j,
-                                        quad_interior(g, i, j), xc, id);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w1, i, j), S1, i, j, INNER, xc, id);
       const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
         xn.v[e] = xc.v[e] + cheb_dir<T, false>(c1, bq.v[e], ax.v[e], id.v[e], xc.v[e]);
-      vst4<T>(x2p + row * S2 + 4 * cq, xn);
-    }
+      vst4<T>(x2p + (i - w2.ra) * S2 + 4 * cq, xn);
+    });
   }
   __syncthreads();
   // residual on the tile; store x2 and t
   {
-    const WinQuads wq(wt);
     const View<T> x2v{x2p, 0};
     T* xs = x + g.off;
     T* ts = t + g.off;
-    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
-      int row, cq;
-      wq.at(q, row, cq);
-      const int i = tile.r0 + row, j = tile.c0 + 4 * cq;
+    for_quads(g, win_quads(wt), [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = tile.c0 + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x2v, wl(w2, i, j), S2, i, j,
-                                        quad_interior(g, i, j), xc, id);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x2v, wl(w2, i, j), S2, i, j, INNER, xc, id);
       const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> r;
 #pragma unroll
@@ -282,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       const size_t k = (size_t)i * P + j;
       vst4<T>(xs + k, xc);
       vst4<T>(ts + k, r);
-    }
+    });
   }
 }
 
@@ -317,72 +316,81 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   T* bp = carve<T>(st, w2.count());
   T* cp = carve<T>(st, wc.count());
   T* x1p = carve<T>(st, w2.count());
-  const T* stab = stage_table<T>(st, tab, ci);
+  const TableStage<T> tst = stage_table<T>(st, tab, ci);
+  const T* stab = tst.s;
   const RowStage<T> rs[3] = {{xin + g.off, xp, w1, P, g.ny + 1},
                              {b + g.off, bp, w2, P, g.ny + 1},
                              {xc + c.off, cp, wc, c.P, c.ny + 1}};
-  if (!stage_rows<T, 3>(st.bar, rs)) return;
+  if (!stage_rows<T, 3>(st.bar, rs, tst)) return;
   const int S1 = w1.S(), S2 = w2.S(), SC = wc.S();
-  // x0 = x + P x_c on the in-grid nodes of W1 (in place)
+  // x0 = x + P x_c on the in-grid nodes of W1 (in place), one window quad per
+  // thread.  Fine node (i, j) lies between coarse nodes (i0, j0) and (i1, j1) along
+  // the cut's diagonal (i0 = i1 and/or j0 = j1 where it coincides with a coarse row,
+  // column or node), and takes 0.5 (c[i0][j0] + c[i1][j1]): the coarse value itself,
+  // an edge midpoint or a diagonal midpoint, bit for bit (0.5 (a + a) = a).
   {
-    const int n1 = w1.count();
-    const float inv1 = 1.0f / (float)S1;
-    for (int e = threadIdx.x; e < n1; e += blockDim.x) {
-      int row, col;
-      div_pitch(e, S1, inv1, row, col);
-      const int i = w1.ra + row, j = w1.ca + col;
-      if (i < 0 || i > g.ny || j < 0 || j > g.nx) continue;
-      int i0, i1, j0, j1;
-      fine_to_coarse(i, g.ny, c.cy, i0, i1);
-      fine_to_coarse(j, g.nx, c.cx, j0, j1);
+    const WinQuads wq(w1);
+    const int nx = g.nx, ny = g.ny;
+    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
+      int row, cq;
+      wq.at(q, row, cq);
+      const int i = w1.ra + row, j = w1.ca + 4 * cq;  // j: a multiple of 4
+      if (i < 0 || i > ny || j < 0 || j > nx) continue;  // j < 0 means j + 3 < 0
+      int i0, i1;
+      fine_to_coarse(i, ny, c.cy, i0, i1);
       const T* cr0 = cp + (i0 - wc.ra) * SC - wc.ca;
       const T* cr1 = cp + (i1 - wc.ra) * SC - wc.ca;
-      T v;
-      if (i0 == i1 && j0 == j1)
-        v = cr0[j0];
-      else if (i0 == i1)
-        v = T(0.5) * (cr0[j0] + cr0[j1]);
-      else if (j0 == j1)
-        v = T(0.5) * (cr0[j0] + cr1[j0]);
-      else
-        v = T(0.5) * (cr0[j0] + cr1[j1]);  // on the coarse diagonal
-      xp[e] += v;
+      int j0[4], j1[4];
+      if (c.cx) {  // columns j, j+1, j+2, j+3 -> (J,J), (J,J+1), (J+1,J+1), (J+1,J+2);
+        const int J = j >> 1;  // an odd last column nx coincides with coarse node (nx+1)/2
+        j0[0] = J;
+        j1[0] = J;
+        j0[1] = j + 1 == nx ? J + 1 : J;
+        j1[1] = J + 1;
+        j0[2] = J + 1;
+        j1[2] = J + 1;
+        j0[3] = j + 3 == nx ? J + 2 : J + 1;
+        j1[3] = J + 2;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) j0[e] = j1[e] = j + e;
+      }
+      T* xq = xp + row * S1 + 4 * cq;
+      Q4<T> xv = vld4<T>(xq);
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (j + e <= nx) xv.v[e] += T(0.5) * (cr0[j0[e]] + cr1[j1[e]]);
+      vst4<T>(xq, xv);
     }
   }
   __syncthreads();
   // first step (no previous direction) on W2
   {
-    const WinQuads wq(w2);
     const View<T> xv{xp, 0};
-    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
-      int row, cq;
-      wq.at(q, row, cq);
-      const int i = w2.ra + row, j = w2.ca + 4 * cq;
+    for_quads(g, win_quads(w2), [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = w2.ca + 4 * cq, kl = (i - w2.ra) * S2 + 4 * cq;
       Q4<T> x0q, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, wl(w1, i, j), S1, i, j,
-                                        quad_interior(g, i, j), x0q, id);
-      const Q4<T> bq = vld4<T>(bp + row * S2 + 4 * cq);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, wl(w1, i, j), S1, i, j, INNER, x0q, id);
+      const Q4<T> bq = vld4<T>(bp + kl);
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
         xn.v[e] = x0q.v[e] + cheb_dir<T, true>(c0, bq.v[e], ax.v[e], id.v[e], T(0));
-      vst4<T>(x1p + row * S2 + 4 * cq, xn);
-    }
+      vst4<T>(x1p + kl, xn);
+    });
   }
   __syncthreads();
   // second step on the tile, d1 = x1 - x0
   T acc = T(0);
   {
-    const WinQuads wq(wt);
     const View<T> x1v{x1p, 0};
     T* xo = xout + g.off;
-    for (int q = threadIdx.x; q < wq.n; q += blockDim.x) {
-      int row, cq;
-      wq.at(q, row, cq);
-      const int i = tile.r0 + row, j = tile.c0 + 4 * cq;
+    for_quads(g, win_quads(wt), [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = tile.c0 + 4 * cq;
       Q4<T> x1q, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w2, i, j), S2, i, j,
-                                        quad_interior(g, i, j), x1q, id);
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w2, i, j), S2, i, j, INNER, x1q, id);
       const Q4<T> bq = vld4<T>(bp + wl(w2, i, j));
       const Q4<T> x0q = vld4<T>(xp + wl(w1, i, j));
       Q4<T> xn;
@@ -393,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
         if (DOT) acc += bq.v[e] * xn.v[e];
       }
       vst4<T>(xo + (size_t)i * P + j, xn);
-    }
+    });
   }
   if (DOT) {
     const double s = block_sum(double(acc));

@@ -140,10 +140,20 @@ struct Stager {
   __device__ __forceinline__ View<T> add(const T* base, int ka, int kb, int nalloc) {
     return add_guarded<T>(base, ka, kb, nalloc);
   }
-  // Zero the guards, issue the copies and wait for them (bounded).  Returns
-  // false, uniformly for the CTA, if the wait gave up (device error flag set).
-  __device__ __forceinline__ bool run() {
-    if (threadIdx.x == 0) mbar_init(bar, 1);
+  // Issue the copies, run `fill` (other shared-memory staging that overlaps the
+  // copies in flight: it must not touch the staged ranges), zero the guards and
+  // wait for the copies (bounded).  Returns false, uniformly for the CTA, if the
+  // wait gave up (device error flag set).
+  template <class F>
+  __device__ __forceinline__ bool run(const F& fill) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      mbar_expect_tx(bar, total);
+#pragma unroll
+      for (int q = 0; q < kMaxStaged; ++q)
+        if (q < n && bytes[q]) bulk_copy_g2s(dst[q], src[q], bytes[q], bar);
+    }
+    fill();
 #pragma unroll
     for (int q = 0; q < 2 * kMaxStaged; ++q) {
       if (q < 2 * n && gbytes[q]) {
@@ -151,13 +161,6 @@ struct Stager {
         for (uint32_t e = threadIdx.x; e < gbytes[q] / 16u; e += blockDim.x)
           z[e] = make_uint4(0u, 0u, 0u, 0u);
       }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      mbar_expect_tx(bar, total);
-#pragma unroll
-      for (int q = 0; q < kMaxStaged; ++q)
-        if (q < n && bytes[q]) bulk_copy_g2s(dst[q], src[q], bytes[q], bar);
     }
     // One thread waits on the mbarrier (the others sleep in the barrier below
     // instead of spinning); the barrier then publishes the copied data CTA-wide.
@@ -172,6 +175,9 @@ struct Stager {
       }
     }
     return __syncthreads_and(ok ? 1 : 0) != 0;
+  }
+  __device__ __forceinline__ bool run() {
+    return run([] {});
   }
 };
 
@@ -294,7 +300,7 @@ __device__ __forceinline__ void coef_node(const LevelGeom& g, int i, int j, T (&
                                             : (const T*)(const void*)g.coef_d;
   if (pre && j >= 0 && j <= g.nx && i >= 0 && i <= g.ny) {
     const T* q = pre + 8 * ((long long)i * g.P + j);
-    if (sizeof(T) == sizeof(float)) {  // one node's 8 values are two aligned 16-byte vectors
+    if constexpr (sizeof(T) == sizeof(float)) {  // two aligned 16-byte vectors per node
       const float4 lo = __ldg(reinterpret_cast<const float4*>(q));
       const float4 hi = __ldg(reinterpret_cast<const float4*>(q) + 1);
       c[0] = (T)lo.x;
@@ -305,10 +311,10 @@ __device__ __forceinline__ void coef_node(const LevelGeom& g, int i, int j, T (&
       c[5] = (T)hi.y;
       c[6] = (T)hi.z;
       c[7] = (T)hi.w;
-      return;
-    }
+    } else {
 #pragma unroll
-    for (int e = 0; e < 8; ++e) c[e] = __ldg(q + e);
+      for (int e = 0; e < 8; ++e) c[e] = __ldg(q + e);
+    }
     return;
   }
   T t[8];
@@ -454,52 +460,71 @@ __device__ __forceinline__ void View<T>::row(int k0, T (&out)[5]) const {
   Row5<M, T>::load(*this, k0, out);
 }
 
-// Runs f(std::integral_constant<int, P mod 4>), the row misalignment of the quad
-// loops.  Device rows are padded to a multiple of 4 nodes, so it is always 0; the
-// parameter keeps the row loads generic over the pitch.
+// A block of quads: grid rows [ra, rb), QW quads per row, quad cq covering columns
+// ca + 4 cq .. ca + 4 cq + 3 (a row tile: ca = 0, QW = P / 4; a fused kernel's
+// window: its own rows and columns).
+struct QuadBlock {
+  int ra, rb, ca, QW;
+};
+
+// Visits every quad of a block once, in two passes: first the rectangle of quads
+// whose four nodes are all uniform-interior nodes (f(i, cq, true_type): every lane
+// of a warp takes the interior path), then the rest (f(i, cq, false_type): the
+// table path), so that no warp runs both paths with lanes masked off.
 template <class F>
-__device__ __forceinline__ void pitch_dispatch(int P, F&& f) {
-  (void)P;
-  f(std::integral_constant<int, 0>{});
-}
-
-
-// Walks the quads q = q0 + tid, q0 + tid + bd, ... of a tile, keeping
-// (i, j) of the quad's first node 4q with one division per thread.
-struct QuadWalk {
-  int q, i, j, qi, qj, P;
-  __device__ __forceinline__ QuadWalk(const LevelGeom& g, int q0) {
-    P = g.P;
-    q = q0 + threadIdx.x;
-    div_pitch(4 * q, P, g.inv_pitch, i, j);
-    div_pitch(4 * (int)blockDim.x, P, g.inv_pitch, qi, qj);
+__device__ __forceinline__ void for_quads(const LevelGeom& g, const QuadBlock& b, F&& f) {
+  // interior rows [2, ny - 2]; columns j = ca + 4 cq with 2 <= j and j + 3 <= nx - 2
+  int ia = b.ra > 2 ? b.ra : 2, ib = b.rb - 1 < g.ny - 2 ? b.rb - 1 : g.ny - 2;
+  int qa = 2 - b.ca > 0 ? (2 - b.ca + 3) >> 2 : 0;
+  int qb = g.nx - 5 - b.ca >= 0 ? (g.nx - 5 - b.ca) >> 2 : -1;
+  qb = qb < b.QW - 1 ? qb : b.QW - 1;
+  if (g.adv_on || ib < ia || qb < qa) {  // no interior rectangle
+    ia = b.ra;
+    ib = b.ra - 1;
+    qa = 0;
+    qb = -1;
   }
-  __device__ __forceinline__ void next() {
-    q += blockDim.x;
-    i += qi;
-    j += qj;
-    if (j >= P) {
-      j -= P;
-      ++i;
+  const int RW = qb - qa + 1, RH = ib - ia + 1;
+  if (RH > 0) {
+    const float inv = 1.0f / (float)RW;
+    int r, c, dr, dc;
+    div_pitch((int)threadIdx.x, RW, inv, r, c);
+    div_pitch((int)blockDim.x, RW, inv, dr, dc);
+    for (; r < RH;) {
+      f(ia + r, qa + c, std::true_type{});
+      r += dr;
+      c += dc;
+      if (c >= RW) {
+        c -= RW;
+        ++r;
+      }
     }
   }
-};
-
-// Geometry scalars a quad loop needs, held in registers.
-struct QuadGeom {
-  int k0, k1, ilo, ihi, jhi;  // tile range; interior rows [2, ny-2]; last interior quad start
-  __device__ __forceinline__ QuadGeom(const LevelGeom& g, const Tile& t) {
-    k0 = t.k0;
-    k1 = t.k1;
-    ilo = 2;
-    ihi = g.adv_on ? -1 : g.ny - 2;  // advection: no uniform interior
-    jhi = g.nx - 5;
+  // the rest: rows above the rectangle, the side quads of its rows, rows below it
+  const int top = (RH > 0 ? ia - b.ra : b.rb - b.ra) * b.QW;
+  const int nb = b.QW - (RH > 0 ? RW : 0);
+  const int mid = RH > 0 ? RH * nb : 0;
+  const int bot = RH > 0 ? (b.rb - 1 - ib) * b.QW : 0;
+  const int n = top + mid + bot;
+  if (n == 0) return;
+  const float invq = 1.0f / (float)b.QW, invb = nb > 0 ? 1.0f / (float)nb : 0.0f;
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    int r, c;
+    if (idx < top) {
+      div_pitch(idx, b.QW, invq, r, c);
+      r += b.ra;
+    } else if (idx < top + mid) {
+      int m;
+      div_pitch(idx - top, nb, invb, r, m);
+      r += ia;
+      c = m < qa ? m : m + RW;
+    } else {
+      div_pitch(idx - top - mid, b.QW, invq, r, c);
+      r += ib + 1;
+    }
+    f(r, c, std::false_type{});
   }
-  // The quad lies inside the tile and all four nodes are uniform-interior nodes.
-  __device__ __forceinline__ bool interior(int k, int i, int j) const {
-    return k >= k0 && k + 4 <= k1 && i >= ilo && i <= ihi && j >= 2 && j <= jhi;
-  }
-};
+}
 
 // Node (i, j) of node kk = 4q + e, from the quad's first node (i0, j0).
 // Rows are padded to a multiple of 4 nodes, so a quad never leaves its row.
@@ -518,21 +543,30 @@ __device__ __forceinline__ int node_class_clamped(const LevelGeom& g, int i, int
 
 // The trap's class table in shared memory, with the interior class replaced by
 // the interior weights, so that a node of the interior class evaluates to the same
-// bits through the table as through the interior constants.  Call before
-// Stager::run (whose barrier publishes it).
+// bits through the table as through the interior constants.  stage_table carves
+// the region; the returned filler runs inside Stager::run / stage_rows, after the
+// bulk copies are issued, so the table's global loads overlap them.
 template <class T>
-__device__ __forceinline__ const T* stage_table(Stager& st, const T* __restrict__ tab,
-                                                const Interior<T>& ci) {
+struct TableStage {
+  T* s;
+  const T* tab;
+  Interior<T> ci;
+  __device__ __forceinline__ void operator()() const {
+    for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) {
+      T v = tab[e];
+      const int q = e - 12 * kTabStride;
+      if (q >= 0 && q < kTabStride)
+        v = q == 0 ? ci.c : (q <= 2 ? ci.e : (q <= 4 ? ci.n : (q <= 6 ? ci.d : ci.ic)));
+      s[e] = v;
+    }
+  }
+};
+template <class T>
+__device__ __forceinline__ TableStage<T> stage_table(Stager& st, const T* __restrict__ tab,
+                                                     const Interior<T>& ci) {
   T* s = reinterpret_cast<T*>(st.cur);
   st.cur += kTabPerTrap * sizeof(T);
-  for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) {
-    T v = tab[e];
-    const int q = e - 12 * kTabStride;
-    if (q >= 0 && q < kTabStride)
-      v = q == 0 ? ci.c : (q <= 2 ? ci.e : (q <= 4 ? ci.n : (q <= 6 ? ci.d : ci.ic)));
-    s[e] = v;
-  }
-  return s;
+  return TableStage<T>{s, tab, ci};
 }
 
 // Quad halo window: one row and nine nodes each side, so that every vector load of
@@ -549,7 +583,8 @@ __device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
 // vector, two row ends, five above, five below); only the weights differ:
 // interior quads use the interior constants, the others (walls, row ends, ragged
 // last cells, advection traps) take per-node weights from the staged class table.
-// PM = P mod 4 (pitch_dispatch); x's base index is a multiple of 4.
+// PM = P mod 4, the row misalignment of the neighbour rows (0: device rows are
+// padded to a multiple of 4 nodes); x's base index is a multiple of 4.
 template <class T, int PM, class X>
 __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T>& ci,
                                             const T* __restrict__ stab, const X& x, int k,
@@ -591,21 +626,6 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
     }
   }
   return ax;
-}
-
-// A quad's nodes that lie in [k0, k1): masked loads of a tile-range view.
-template <class T>
-__device__ __forceinline__ Q4<T> quad_masked(const View<T>& v, int k, int k0, int k1) {
-  Q4<T> r;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) r.v[e] = (k + e >= k0 && k + e < k1) ? v[k + e] : T(0);
-  return r;
-}
-template <class T>
-__device__ __forceinline__ void store_masked(T* p, const Q4<T>& q, int k, int k0, int k1) {
-#pragma unroll
-  for (int e = 0; e < 4; ++e)
-    if (k + e >= k0 && k + e < k1) p[k + e] = q.v[e];
 }
 
 __device__ __forceinline__ double block_sum(double v) {
@@ -681,25 +701,21 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   T* xo = xout + g.off;
   T* ds = d + g.off;
   const int P = g.P;
-  const QuadGeom qg(g, tile);
   T acc = T(0);
+  // tiles are whole rows: every quad lies inside the tile
+  const QuadBlock qb{tile.r0, tile.r1, 0, P >> 2};
   if (ZERO) {
-    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-      const int k = 4 * w.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-      const Q4<T> bq = full ? vld4<T>(bs + k) : quad_masked<T>(View<T>{bs, 0}, k, tile.k0, tile.k1);
+    for_quads(g, qb, [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int k = i * P + 4 * cq;
+      const Q4<T> bq = vld4<T>(bs + k);
       Q4<T> id;
-      if (qg.interior(k, w.i, w.j)) {
+      if (INNER) {
 #pragma unroll
         for (int e = 0; e < 4; ++e) id.v[e] = ci.ic;
       } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          int i, j;
-          quad_node(P, w.i, w.j, e, i, j);
-          i = i > g.ny ? g.ny : i;
-          id.v[e] = inv_diag_tab<T>(g, ci, tab, i, j);
-        }
+        for (int e = 0; e < 4; ++e) id.v[e] = inv_diag_tab<T>(g, ci, tab, i, 4 * cq + e);
       }
       Q4<T> dn;
 #pragma unroll
@@ -707,14 +723,9 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
         dn.v[e] = (T(cc.c_res) * bq.v[e]) * id.v[e];
         if (DOT) acc += bq.v[e] * dn.v[e];
       }
-      if (full) {
-        vst4<T>(xo + k, dn);
-        vst4<T>(ds + k, dn);
-      } else {
-        store_masked<T>(xo, dn, k, tile.k0, tile.k1);
-        store_masked<T>(ds, dn, k, tile.k0, tile.k1);
-      }
-    }
+      vst4<T>(xo + k, dn);
+      vst4<T>(ds + k, dn);
+    });
   } else {
     Stager st(eqf_smem);
     const int na = padded_len(g);
@@ -722,40 +733,25 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     const View<T> bv = st.add(bs, tile.k0, tile.k1, na);
     View<T> dv = bv;
     if (!FIRST) dv = st.add(static_cast<const T*>(ds), tile.k0, tile.k1, na);
-    const T* stab = stage_table<T>(st, tab, ci);
-    if (!st.run()) return;
-    pitch_dispatch(P, [&](auto pm_) {
-      constexpr int PM = decltype(pm_)::value;
-      for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-        const int k = 4 * w.q;
-        const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-        Q4<T> xc, id;
-        const Q4<T> ax = apply_quad<T, PM>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j),
-                                       xc, id);
-        Q4<T> bq, dq;
-        if (full) {
-          bq = bv.quad(k);
-          if (!FIRST) dq = dv.quad(k);
-        } else {
-          bq = quad_masked<T>(bv, k, tile.k0, tile.k1);
-          if (!FIRST) dq = quad_masked<T>(dv, k, tile.k0, tile.k1);
-        }
-        if (FIRST) dq = bq;
-        Q4<T> dn, xn;
+    const TableStage<T> tst = stage_table<T>(st, tab, ci);
+    const T* stab = tst.s;
+    if (!st.run(tst)) return;
+    for_quads(g, qb, [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = 4 * cq, k = i * P + j;
+      Q4<T> xc, id;
+      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, k, P, i, j, INNER, xc, id);
+      const Q4<T> bq = bv.quad(k);
+      const Q4<T> dq = FIRST ? bq : dv.quad(k);
+      Q4<T> dn, xn;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          dn.v[e] = cheb_dir<T, FIRST>(cc, bq.v[e], ax.v[e], id.v[e], dq.v[e]);
-          xn.v[e] = xc.v[e] + dn.v[e];
-          if (DOT) acc += bq.v[e] * xn.v[e];
-        }
-        if (full) {
-          vst4<T>(xo + k, xn);
-          vst4<T>(ds + k, dn);
-        } else {
-          store_masked<T>(xo, xn, k, tile.k0, tile.k1);
-          store_masked<T>(ds, dn, k, tile.k0, tile.k1);
-        }
+      for (int e = 0; e < 4; ++e) {
+        dn.v[e] = cheb_dir<T, FIRST>(cc, bq.v[e], ax.v[e], id.v[e], dq.v[e]);
+        xn.v[e] = xc.v[e] + dn.v[e];
+        if (DOT) acc += bq.v[e] * xn.v[e];
       }
+      vst4<T>(xo + k, xn);
+      vst4<T>(ds + k, dn);
     });
   }
   if (DOT) {
@@ -780,28 +776,22 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const int na = padded_len(g);
   const View<T> xv = st.add_guarded(x + g.off, qhalo_lo(g, tile), qhalo_hi(g, tile), na);
   const View<T> bv = st.add(b + g.off, tile.k0, tile.k1, na);
-  const T* stab = stage_table<T>(st, tab, ci);
-  if (!st.run()) return;
+  const TableStage<T> tst = stage_table<T>(st, tab, ci);
+  const T* stab = tst.s;
+  if (!st.run(tst)) return;
   T* ts = t + g.off;
   const int P = g.P;
-  const QuadGeom qg(g, tile);
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-      const int k = 4 * w.q;
-      const bool full = k >= tile.k0 && k + 4 <= tile.k1;
-      Q4<T> xc, id;
-      const Q4<T> ax =
-          apply_quad<T, PM>(g, ci, stab, xv, k, P, w.i, w.j, qg.interior(k, w.i, w.j), xc, id);
-      const Q4<T> bq = full ? bv.quad(k) : quad_masked<T>(bv, k, tile.k0, tile.k1);
-      Q4<T> r;
+  // tiles are whole rows: every quad lies inside the tile
+  for_quads(g, QuadBlock{tile.r0, tile.r1, 0, P >> 2}, [&](int i, int cq, auto inner_) {
+    constexpr bool INNER = decltype(inner_)::value;
+    const int j = 4 * cq, k = i * P + j;
+    Q4<T> xc, id;
+    const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, k, P, i, j, INNER, xc, id);
+    const Q4<T> bq = bv.quad(k);
+    Q4<T> r;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
-      if (full)
-        vst4<T>(ts + k, r);
-      else
-        store_masked<T>(ts, r, k, tile.k0, tile.k1);
-    }
+    for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
+    vst4<T>(ts + k, r);
   });
 }
 
@@ -1015,34 +1005,24 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   if (!FIRST) pv = sg.add_guarded(pin + g.off, ka, kb, na);
   const T* tab = tabs + (size_t)g.trap * kTabPerTrap;
   const Interior<T> ci = interior<T>(g);
-  const T* stab = stage_table<T>(sg, tab, ci);
-  if (!sg.run()) return;
+  const TableStage<T> tst = stage_table<T>(sg, tab, ci);
+  const T* stab = tst.s;
+  if (!sg.run(tst)) return;
   const PNew<T, FIRST> pnew{zv, pv, beta};
   T* po = pout + g.off;
   T* qs = q + g.off;
   const int P = g.P;
-  const QuadGeom qg(g, tile);
   T acc = T(0);
-  pitch_dispatch(P, [&](auto pm_) {
-    constexpr int PM = decltype(pm_)::value;
-    for (QuadWalk w(g, tile.k0 >> 2); 4 * w.q < tile.k1; w.next()) {
-      const int k = 4 * w.q;
-      Q4<T> pc, id;
-      const Q4<T> a =
-          apply_quad<T, PM>(g, ci, stab, pnew, k, P, w.i, w.j, qg.interior(k, w.i, w.j), pc, id);
-      if (k >= tile.k0 && k + 4 <= tile.k1) {
+  // tiles are whole rows: every quad lies inside the tile
+  for_quads(g, QuadBlock{tile.r0, tile.r1, 0, P >> 2}, [&](int i, int cq, auto inner_) {
+    constexpr bool INNER = decltype(inner_)::value;
+    const int j = 4 * cq, k = i * P + j;
+    Q4<T> pc, id;
+    const Q4<T> a = apply_quad<T, 0>(g, ci, stab, pnew, k, P, i, j, INNER, pc, id);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
-        vst4<T>(po + k, pc);
-        vst4<T>(qs + k, a);
-      } else {
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (k + e >= tile.k0 && k + e < tile.k1) acc += pc.v[e] * a.v[e];
-        store_masked<T>(po, pc, k, tile.k0, tile.k1);
-        store_masked<T>(qs, a, k, tile.k0, tile.k1);
-      }
-    }
+    for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
+    vst4<T>(po + k, pc);
+    vst4<T>(qs + k, a);
   });
   const double t = block_sum(double(acc));
   if (threadIdx.x == 0) part[blockIdx.x] = t;
