@@ -402,6 +402,9 @@ class Batch {
   // cells
   std::vector<std::vector<double>> cell_xy, cell_s;  // per trap (host copies)
   bool cells_dirty = false;
+  // d_cell_s holds rates the host copies lack (eqf_set_cell_rates_all leaves the host
+  // copies to pull_cell_s, so the per-step rate upload costs no host-side copy)
+  bool cell_s_stale = false;
   int ncells = 0, nseg = 0;
   DevBuf<CellGeom> dcg;
   DevBuf<int> d_cell_trap, d_ent_node, d_perm, d_seg_start;
@@ -501,6 +504,7 @@ class Batch {
   void step(int n);
   void run_step();
   void rebuild_cells();
+  void pull_cell_s();
   void refresh_load();
   void build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& perm,
                       DevBuf<int>& seg_start, int& nseg_out, const double* xy, const double* s,
@@ -1807,7 +1811,21 @@ void Batch::build_segments(int nent, int* d_node, int* d_counts, DevBuf<int>& pe
   nseg_out = ns;
 }
 
+// Brings the host copies of the per-cell rates up to date with d_cell_s.
+void Batch::pull_cell_s() {
+  if (!cell_s_stale) return;
+  cell_s_stale = false;
+  if (ncells == 0) return;
+  std::vector<double> sv(ncells);
+  EQF_CK(cudaMemcpyAsync(sv.data(), d_cell_s.p, ncells * sizeof(double), cudaMemcpyDeviceToHost,
+                         stream));
+  sync();
+  for (int t = 0; t < ntraps; ++t)
+    std::copy(sv.begin() + cell_first[t], sv.begin() + cell_first[t + 1], cell_s[t].begin());
+}
+
 void Batch::rebuild_cells() {
+  pull_cell_s();
   cells_dirty = false;
   ncp = 0;
   drop_graphs();
@@ -2133,6 +2151,7 @@ int eqf_set_cells(eqf_batch* b, int32_t trap, int64_t n, const double* xy, const
                       xy[2 * i + 1] <= p.height,
                   "cell outside the trap");
     }
+    b->impl->pull_cell_s();
     b->impl->cell_xy[trap].assign(xy, xy + 2 * n);
     b->impl->cell_s[trap].assign(s, s + n);
     b->impl->cells_dirty = true;
@@ -2253,6 +2272,7 @@ int eqf_couple_species(eqf_batch* b, int32_t trap1, int32_t trap2, const int32_t
                 "bad coupling law");
     const size_t n = B.cell_s[trap1].size();
     EQF_REQUIRE(n == 0 || sender, "null sender flags");
+    B.pull_cell_s();
     Batch::Coupling c{trap1, trap2, eqf::CouplingLaw{vmax, K, uptake}, {}};
     c.sender.assign(sender, sender + n);
     B.cell_xy[trap2] = B.cell_xy[trap1];
@@ -2269,6 +2289,7 @@ int eqf_set_cell_rates(eqf_batch* b, int32_t trap, int64_t n, const double* s) {
     Batch& B = *b->impl;
     EQF_REQUIRE(n == (int64_t)B.cell_s[trap].size() && (n == 0 || s), "rate count mismatch");
     for (int64_t i = 0; i < n; ++i) EQF_REQUIRE(std::isfinite(s[i]), "non-finite cell rate");
+    B.pull_cell_s();
     B.cell_s[trap].assign(s, s + n);
     if (B.cells_dirty) return;  // the rebuild will pick the rates up
     if (n == 0) return;
@@ -2432,9 +2453,7 @@ int eqf_set_cell_rates_all(eqf_batch* b, int64_t n, const double* s) {
     EQF_CK(cudaMemcpyAsync(B.d_cell_s.p, s, n * sizeof(double), cudaMemcpyHostToDevice,
                            B.stream));
     B.refresh_load();
-    // keep the host copies consistent for later rebuilds
-    for (int t = 0; t < B.ntraps; ++t)
-      std::copy(s + B.cell_first[t], s + B.cell_first[t + 1], B.cell_s[t].begin());
+    B.cell_s_stale = true;  // the host copies follow on demand (pull_cell_s)
   });
 }
 

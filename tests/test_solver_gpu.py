@@ -114,6 +114,30 @@ def test_batch_wide_cell_io_matches_per_trap(lib):
         assert np.array_equal(allc, per)
 
 
+def test_batch_wide_rates_survive_a_cell_rebuild(lib):
+    """Batch-wide rates live on the device until a rebuild needs them: replacing one
+    trap's cells afterwards keeps the other traps' batch-wide rates."""
+    traps = wl.batched_uneven(4, 3)
+    new = [t.cell_s * (2.0 + i) for i, t in enumerate(traps)]
+    moved = wl.batched_uneven(5, 3)[1]
+    res = []
+    for via_all in (True, False):
+        with F.TrapBatch([tparams(t) for t in traps], F.default_opts(F.FP64)) as b:
+            for i, t in enumerate(traps):
+                b.set_cells(i, t.cell_xy, t.cell_s)
+            b.step(1)
+            if via_all:
+                b.set_cell_rates_all(np.concatenate(new))
+            else:
+                for i in range(3):
+                    b.set_cell_rates(i, new[i])
+            xy = np.clip(moved.cell_xy, 0, [traps[1].W, traps[1].H])
+            b.set_cells(1, xy, moved.cell_s)  # rebuild: traps 0 and 2 keep `new`
+            b.step(2)
+            res.append(np.concatenate([b.read_nodal(i) for i in range(3)]))
+    assert np.array_equal(res[0], res[1])
+
+
 def test_reference_step_semantics_through_the_mirror(lib):
     """FieldSolver: deposits added into solution_vector, then stepDiffusion (as the
     reference's controller/worker exchange does), against the oracle."""
