@@ -160,6 +160,119 @@ __device__ __forceinline__ DF df_apply(const LevelGeom& g, const float2* __restr
   return acc.result();
 }
 
+// A x on the quad of nodes k .. k+3 (row i, columns j .. j+3) from a pair window x
+// (node k at x[k - a], k - a even, so four pairs are two aligned 16-byte loads) of a
+// class-table trap.  The interior quads (INNER) take the interior weights `ci`, the
+// others per-node weights from the table.  Every node accumulates its seven products
+// in df_apply's order, so both paths give df_apply's bits.  (General-path traps take
+// df_residual_general: their stencil fetch would cost this path its registers.)
+template <bool INNER>
+__device__ __forceinline__ void df_apply_quad(const LevelGeom& g, const float2* __restrict__ stab,
+                                              const DF (&ci)[7], const float2* x, int a, int k,
+                                              int i, int j, DF (&out)[4]) {
+  const int P = g.P;
+  const float2* xc = x + (k - a);
+  auto ld2 = [](const float2* p, float2& u, float2& v) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    u = make_float2(q.x, q.y);
+    v = make_float2(q.z, q.w);
+  };
+  // two nodes at a time (fewer values live): x[k+2h-1 .. k+2h+2], x[k+2h+P .. +2],
+  // x[k+2h-P-1 .. k+2h-P+1]
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float2* xh = xc + 2 * h;
+    float2 r0[4], rn[3], rs[3];
+    r0[0] = xh[-1];
+    ld2(xh, r0[1], r0[2]);
+    r0[3] = xh[2];
+    ld2(xh + P, rn[0], rn[1]);
+    rn[2] = xh[P + 2];
+    rs[0] = xh[-P - 1];
+    ld2(xh - P, rs[1], rs[2]);
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const int e = 2 * h + f;
+      DF c[7];
+      if (INNER) {
+#pragma unroll
+        for (int m = 0; m < 7; ++m) c[m] = ci[m];
+      } else {
+        const float2* t = stab + node_class(g, i, j + e) * kTabStride;
+#pragma unroll
+        for (int m = 0; m < 7; ++m) c[m] = DF{t[m].x, t[m].y};
+      }
+      const float2 v[7] = {r0[f + 1], r0[f + 2], r0[f], rn[f], rs[f + 1], rn[f + 1], rs[f]};
+      DFAcc acc;
+      acc.first(c[0], DF{v[0].x, v[0].y});
+#pragma unroll
+      for (int m = 1; m < 7; ++m) acc.add(c[m], DF{v[m].x, v[m].y});
+      out[e] = acc.result();
+    }
+  }
+}
+
+// The interior weights (class 12) of a staged pair table.
+__device__ __forceinline__ void df_interior(const float2* stab, DF (&ci)[7]) {
+  const float2* t = stab + 12 * kTabStride;
+#pragma unroll
+  for (int m = 0; m < 7; ++m) ci[m] = DF{t[m].x, t[m].y};
+}
+
+// r = b - A x on a quad (Dirichlet rows: 0, or b - x with wall values), stored when
+// STORE; |r|^2 accumulated in `arr`.
+template <bool INNER>
+__device__ __forceinline__ void df_residual_quad(const LevelGeom& g, const float2* __restrict__ sA,
+                                                 const DF (&ca)[7], const float2* x, int a, int k,
+                                                 int i, int j, const float2* __restrict__ bs,
+                                                 float* __restrict__ rs, SqAcc& arr, bool store) {
+  DF ax[4];
+  df_apply_quad<INNER>(g, sA, ca, x, a, k, i, j, ax);
+  const float4 b01 = reinterpret_cast<const float4*>(bs + k)[0];
+  const float4 b23 = reinterpret_cast<const float4*>(bs + k)[1];
+  const DF bv[4] = {DF{b01.x, b01.y}, DF{b01.z, b01.w}, DF{b23.x, b23.y}, DF{b23.z, b23.w}};
+  float rk[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const bool dir = !INNER && g.walls && is_dirichlet(g, i, j + e);
+    rk[e] = 0.f;
+    if (!dir) {
+      const DF res = df_add(bv[e], df_neg(ax[e]));
+      rk[e] = __fadd_rn(res.h, res.l);
+    } else if (g.dvals) {
+      const float2 xv = x[k + e - a];
+      const DF res = df_add(bv[e], df_neg(DF{xv.x, xv.y}));
+      rk[e] = __fadd_rn(res.h, res.l);
+    }
+    arr.add(rk[e]);
+  }
+  if (store) *reinterpret_cast<float4*>(rs + k) = make_float4(rk[0], rk[1], rk[2], rk[3]);
+}
+
+// The same residual node by node for a general-path trap (advection, anisotropic
+// tensor), whose stencils come from coef_node.
+__device__ __forceinline__ void df_residual_general(const LevelGeom& g, const Tile& tile,
+                                                    const float2* x, int a,
+                                                    const float2* __restrict__ bs,
+                                                    float* __restrict__ rs, SqAcc& arr,
+                                                    bool store) {
+  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
+    const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
+    float rk = 0.f;
+    if (!dir) {
+      const float2 b = bs[w.k];
+      const DF res = df_add(DF{b.x, b.y}, df_neg(df_apply(g, nullptr, true, x, a, w.k, w.i, w.j)));
+      rk = __fadd_rn(res.h, res.l);
+    } else if (g.dvals) {
+      const float2 b = bs[w.k], xv = x[w.k - a];
+      const DF res = df_add(DF{b.x, b.y}, df_neg(DF{xv.x, xv.y}));
+      rk = __fadd_rn(res.h, res.l);
+    }
+    if (store) rs[w.k] = rk;
+    arr.add(rk);
+  }
+}
+
 // Converts the staged doubles of window [ka, kb) to pairs in place (same 8 bytes).
 __device__ __forceinline__ void window_to_pairs(const View<double>& v, int ka, int kb) {
   double* p = const_cast<double*>(v.p);
@@ -202,16 +315,36 @@ __global__ void __launch_bounds__(kThreads)
   const double* Fs = F + g.off;
   float2* bs = b2 + g.off;
   SqAcc abb, arr;
-  // b = F + M u_in
-  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-    const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
-    DF bk{0.f, 0.f};
-    if (!dir)
-      bk = df_add(df_split(Fs[w.k]), df_apply(g, sM, false, xw, xa, w.k, w.i, w.j));
-    else if (g.dvals)  // the identity row with the wall value held in F
-      bk = df_split(Fs[w.k]);
-    bs[w.k] = make_float2(bk.h, bk.l);
-    abb.add(bk.h);
+  const int P = g.P;
+  // tiles are whole rows: every quad lies inside the tile
+  const QuadBlock qb{tile.r0, tile.r1, 0, P >> 2};
+  // b = F + M u_in (the mass operator: its interior weights from class 12 too)
+  {
+    DF cm[7];
+    df_interior(sM, cm);
+    for_quads(g, qb, [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = 4 * cq, k = i * P + j;
+      DF mu[4];
+      df_apply_quad<INNER>(g, sM, cm, xw, xa, k, i, j, mu);
+      const double2 f01 = *reinterpret_cast<const double2*>(Fs + k);
+      const double2 f23 = *reinterpret_cast<const double2*>(Fs + k + 2);
+      const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
+      float2 bo[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const bool dir = !INNER && g.walls && is_dirichlet(g, i, j + e);
+        DF bk{0.f, 0.f};
+        if (!dir)
+          bk = df_add(df_split(fv[e]), mu[e]);
+        else if (g.dvals)  // the identity row with the wall value held in F
+          bk = df_split(fv[e]);
+        bo[e] = make_float2(bk.h, bk.l);
+        abb.add(bk.h);
+      }
+      reinterpret_cast<float4*>(bs + k)[0] = make_float4(bo[0].x, bo[0].y, bo[1].x, bo[1].y);
+      reinterpret_cast<float4*>(bs + k)[1] = make_float4(bo[2].x, bo[2].y, bo[3].x, bo[3].y);
+    });
   }
   __syncthreads();  // every read of u_in done: the window becomes u0 in place
   {
@@ -233,22 +366,17 @@ __global__ void __launch_bounds__(kThreads)
     }
   }
   __syncthreads();
-  const bool general = g.adv_on != 0;
   float* rs = r + g.off;
-  for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-    const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
-    float rk = 0.f;
-    if (!dir) {
-      const float2 b = bs[w.k];
-      const DF res = df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, xa, w.k, w.i, w.j)));
-      rk = __fadd_rn(res.h, res.l);
-    } else if (g.dvals) {
-      const float2 b = bs[w.k], x = xw[w.k - xa];
-      const DF res = df_add(DF{b.x, b.y}, df_neg(DF{x.x, x.y}));
-      rk = __fadd_rn(res.h, res.l);
-    }
-    rs[w.k] = rk;
-    arr.add(rk);
+  if (g.adv_on) {
+    df_residual_general(g, tile, xw, xa, bs, rs, arr, true);
+  } else {
+    DF ca[7];
+    df_interior(sA, ca);
+    for_quads(g, qb, [&](int i, int cq, auto inner_) {
+      constexpr bool INNER = decltype(inner_)::value;
+      const int j = 4 * cq, k = i * P + j;
+      df_residual_quad<INNER>(g, sA, ca, xw, xa, k, i, j, bs, rs, arr, true);
+    });
   }
   const double tb = block_sum(abb.total());
   const double tr = block_sum(arr.total());
@@ -262,7 +390,7 @@ __global__ void __launch_bounds__(kThreads)
 // With FINAL the residual is only measured and every trap also reports |d|^2
 // (partial [2]) for the next step's extrapolation factor.
 template <bool FINAL>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     k_irf_residual(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                    const float2* __restrict__ tabA, const int* __restrict__ skip,
                    const float2* __restrict__ b2, const double* __restrict__ u,
@@ -291,24 +419,20 @@ __global__ void __launch_bounds__(kThreads)
     window_to_pairs(uv, ka, kb);
     __syncthreads();
     const float2* xw = reinterpret_cast<const float2*>(uv.p);
-    const bool general = g.adv_on != 0;
     const float2* bs = b2 + g.off;
     float* rs = r + g.off;
-    for (NodeWalk w(g, tile.k0); w.k < tile.k1; w.next()) {
-      const bool dir = g.walls && is_dirichlet(g, w.i, w.j);
-      float rk = 0.f;
-      if (!dir) {
-        const float2 b = bs[w.k];
-        const DF res =
-            df_add(DF{b.x, b.y}, df_neg(df_apply(g, sA, general, xw, uv.a, w.k, w.i, w.j)));
-        rk = __fadd_rn(res.h, res.l);
-      } else if (g.dvals) {
-        const float2 b = bs[w.k], x = xw[w.k - uv.a];
-        const DF res = df_add(DF{b.x, b.y}, df_neg(DF{x.x, x.y}));
-        rk = __fadd_rn(res.h, res.l);
-      }
-      if (!FINAL) rs[w.k] = rk;
-      arr.add(rk);
+    const int P = g.P;
+    if (g.adv_on) {
+      df_residual_general(g, tile, xw, uv.a, bs, rs, arr, !FINAL);
+    } else {
+      DF ca[7];
+      df_interior(sA, ca);
+      // tiles are whole rows: every quad lies inside the tile
+      for_quads(g, QuadBlock{tile.r0, tile.r1, 0, P >> 2}, [&](int i, int cq, auto inner_) {
+        constexpr bool INNER = decltype(inner_)::value;
+        const int j = 4 * cq, k = i * P + j;
+        df_residual_quad<INNER>(g, sA, ca, xw, uv.a, k, i, j, bs, rs, arr, !FINAL);
+      });
     }
   }
   const double tr = block_sum(arr.total());
