@@ -1014,6 +1014,25 @@ Work<T>::Work(Batch& b) : B(b) {
 }
 
 // Launch wrapper: profiler marks around one kernel launch.
+// Launch of a solver kernel with programmatic stream serialization: its CTAs may be
+// scheduled while the previous kernel's last CTAs run (each solver kernel starts
+// with grid_dep_sync, which holds it until that grid has completed).
+template <class... KArgs, class... Args>
+static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  EQF_CK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+}
+
 #define EQF_RUN(B_, cls_, launch_)                     \
   do {                                                 \
     unsigned long long* W = (B_).prof_begin(cls_);     \
@@ -1033,24 +1052,24 @@ static void cheb_step(Batch& B, cudaStream_t s, int lev, int nt, const LevelGeom
   const size_t sm = zero ? 0 : B.L[lev].sm_cheb;
   if (zero) {
     if (dot)
-      EQF_RUN(B, cls, (k_cheb<T, true, true, true><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, true, true>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
     else
-      EQF_RUN(B, cls, (k_cheb<T, true, true, false><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, true, false>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
   } else if (first) {
     if (dot)
-      EQF_RUN(B, cls, (k_cheb<T, true, false, true><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, false, true>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
     else
-      EQF_RUN(B, cls, (k_cheb<T, true, false, false><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, false, false>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
   } else {
     if (dot)
-      EQF_RUN(B, cls, (k_cheb<T, false, false, true><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, false, false, true>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, st, b, xin, xout, d, part, W)));
     else
-      EQF_RUN(B, cls, (k_cheb<T, false, false, false><<<nt, kThreads, sm, s>>>(
+      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, false, false, false>, nt, kThreads, sm, s, 
                            G, tl, tab, skip, st, b, xin, xout, d, part, W)));
   }
 }
@@ -1087,7 +1106,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   if (coarsest && Lv_.sm_coarse && !dot) {
     // the whole coarsest solve in one CTA per trap
     EQF_RUN(B, KC_COARSE,
-            (k_coarse_solve<T><<<B.ntraps, kThreads, Lv_.sm_coarse, s>>>(G, tab, skip, deg_pre,
+            (launch_pdl(k_coarse_solve<T>, B.ntraps, kThreads, Lv_.sm_coarse, s, G, tab, skip, deg_pre,
                                                                           bl, cur)));
     return cur;
   }
@@ -1097,20 +1116,20 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
     // prolongation + post-smoothing
     const int nt2 = (int)Lv_.tiles2.size();
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_DOWN0,
-            (k_down<T><<<nt2, kThreads, Lv_.sm_down, s>>>(G, Lv_.dtiles2.p, tab, skip, bl, cur,
+            (launch_pdl(k_down<T>, nt2, kThreads, Lv_.sm_down, s, G, Lv_.dtiles2.p, tab, skip, bl, cur,
                                                            v.t.p, W)));
     const Level& Lc = B.L[lev + 1];
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
-            (k_restrict<T><<<Lc.ntiles(), kThreads, Lc.sm_restrict, s>>>(
+            (launch_pdl(k_restrict<T>, Lc.ntiles(), kThreads, Lc.sm_restrict, s, 
                 Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
     T* xc = vcycle(s, lev + 1, false);
     if (dot)
       EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
-              (k_up<T, true><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
+              (launch_pdl(k_up<T, true>, nt2, kThreads, Lv_.sm_up, s, G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
                                                              skip, xc, bl, cur, oth, part, W)));
     else
       EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
-              (k_up<T, false><<<nt2, kThreads, Lv_.sm_up, s>>>(G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
+              (launch_pdl(k_up<T, false>, nt2, kThreads, Lv_.sm_up, s, G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
                                                               skip, xc, bl, cur, oth, part, W)));
     return oth;
   }
@@ -1126,15 +1145,15 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   // residual, restriction, coarse correction, prolongation
   const int c0 = lev > 0 ? KC_COARSE : KC_RESID0;
   EQF_RUN(B, c0,
-          (k_resid<T><<<nt, kThreads, Lv_.sm_resid, s>>>(G, tl, tab, skip, bl, cur, v.t.p,
+          (launch_pdl(k_resid<T>, nt, kThreads, Lv_.sm_resid, s, G, tl, tab, skip, bl, cur, v.t.p,
                                                           W)));
   const Level& Lc = B.L[lev + 1];
   EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
-          (k_restrict<T><<<Lc.ntiles(), kThreads, Lc.sm_restrict, s>>>(
+          (launch_pdl(k_restrict<T>, Lc.ntiles(), kThreads, Lc.sm_restrict, s, 
               Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
   T* xc = vcycle(s, lev + 1, false);
   EQF_RUN(B, lev > 0 ? KC_COARSE : KC_PROLONG0,
-          (k_prolong<T><<<nt, kThreads, Lv_.sm_prolong, s>>>(G, Lc.dgeom.p, tl, skip, xc, cur,
+          (launch_pdl(k_prolong<T>, nt, kThreads, Lv_.sm_prolong, s, G, Lc.dgeom.p, tl, skip, xc, cur,
                                                               W)));
   // post-smoothing from the corrected iterate
   const int deg_post = B.opts.cheb_post;
@@ -1170,32 +1189,32 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
     float2* b2 = reinterpret_cast<float2*>(B.b64.p);
     if (first)
       EQF_RUN(B, KC_IR_RESID_FIRST,
-              (k_irf_first<<<nt, kThreads, L0.sm_irf1, s>>>(
+              (launch_pdl(k_irf_first, nt, kThreads, L0.sm_irf1, s, 
                   G, tl, B.tabA2.p, B.tabM2.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
                   b2, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
     else
       EQF_RUN(B, KC_IR_RESID,
-              (k_irf_residual<false><<<nt, kThreads, L0.sm_irf, s>>>(
+              (launch_pdl(k_irf_residual<false>, nt, kThreads, L0.sm_irf, s, 
                   G, tl, B.tabA2.p, B.d_ir_done.p, b2, u_out, d_out, r, part, nt, W)));
   } else {
     if (first)
       EQF_RUN(B, KC_IR_RESID_FIRST,
-              (k_ir_first<T><<<nt, kThreads, L0.sm_ir, s>>>(
+              (launch_pdl(k_ir_first<T>, nt, kThreads, L0.sm_ir, s, 
                   G, tl, L0.tabd.p, B.tabM0.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
                   B.b64.p, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
     else
       EQF_RUN(B, KC_IR_RESID,
-              (k_ir_residual<T, false><<<nt, kThreads, L0.sm_ir, s>>>(
+              (launch_pdl(k_ir_residual<T, false>, nt, kThreads, L0.sm_ir, s, 
                   G, tl, L0.tabd.p, B.d_ir_done.p, B.b64.p, u_out, d_out, r, part, nt, W)));
   }
   EQF_RUN(B, KC_SCALAR,
-          (k_s_ir<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
+          (launch_pdl(k_s_ir, nb, 128, 0, s, B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
                                      B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p, B.d_frozen.p)));
   EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs);
     EQF_RUN(B, KC_IR_UPDATE,
-            (k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, u_out, d_out,
+            (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out, d_out,
                                                     W)));
     return;
   }
@@ -1204,28 +1223,28 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   for (int it = 0; it < B.opts.max_iters; ++it) {
     T* z = vcycle(s, 0, true);
     EQF_RUN(B, KC_SCALAR,
-            (k_s_rz<<<nb, 128, 0, s>>>(B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
+            (launch_pdl(k_s_rz, nb, 128, 0, s, B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
                                        B.dstate.p, B.d_cg_skip.p)));
     if (it == 0)
       EQF_RUN(B, KC_CG_DIR,
-              (k_cg_dir<T, true><<<nt, kThreads, L0.sm_cgdir, s>>>(
+              (launch_pdl(k_cg_dir<T, true>, nt, kThreads, L0.sm_cgdir, s, 
                   G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
     else
       EQF_RUN(B, KC_CG_DIR,
-              (k_cg_dir<T, false><<<nt, kThreads, L0.sm_cgdir, s>>>(
+              (launch_pdl(k_cg_dir<T, false>, nt, kThreads, L0.sm_cgdir, s, 
                   G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_pq<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
+            (launch_pdl(k_s_pq, nb, 128, 0, s, B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
     EQF_RUN(B, KC_CG_UPDATE,
-            (k_cg_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p,
+            (launch_pdl(k_cg_update<T>, nt, kThreads, 0, s, G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p,
                                                     xs.p, r, part, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_rr<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
+            (launch_pdl(k_s_rr, nb, 128, 0, s, B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
                                        B.d_cg_skip.p)));
     std::swap(pin, pout);
   }
   EQF_RUN(B, KC_IR_UPDATE,
-          (k_ir_update<T><<<nt, kThreads, 0, s>>>(G, tl, B.d_ir_done.p, xs.p, u_out, d_out, W)));
+          (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out, d_out, W)));
 }
 
 // Right-preconditioned BiCGSTAB on the correction x (xs) from residual r (the
@@ -1249,37 +1268,37 @@ void Work<T>::bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs) {
   for (int it = 0; it < iters; ++it) {
     if (it == 0) {
       EQF_RUN(B, KC_CG_UPDATE,
-              (k_bs_dir<T, true><<<nt, kThreads, 0, s>>>(G, tl, skip, st, r, v, p, rh.p, part,
+              (launch_pdl(k_bs_dir<T, true>, nt, kThreads, 0, s, G, tl, skip, st, r, v, p, rh.p, part,
                                                          W)));
       EQF_RUN(B, KC_SCALAR,
-              (k_s_bs_rho0<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, st, skip)));
+              (launch_pdl(k_s_bs_rho0, nb, 128, 0, s, B.ntraps, B.drange.p, part, st, skip)));
     } else {
       EQF_RUN(B, KC_CG_UPDATE,
-              (k_bs_dir<T, false><<<nt, kThreads, 0, s>>>(G, tl, skip, st, r, v, p, rh.p, part,
+              (launch_pdl(k_bs_dir<T, false>, nt, kThreads, 0, s, G, tl, skip, st, r, v, p, rh.p, part,
                                                           W)));
     }
     const T* ph = vcycle(s, 0, false, p);
     EQF_RUN(B, KC_CG_DIR,
-            (k_apply_dot<T, 1><<<nt, kThreads, L0.sm_resid, s>>>(G, tl, tab, skip, ph, rh.p, v,
+            (launch_pdl(k_apply_dot<T, 1>, nt, kThreads, L0.sm_resid, s, G, tl, tab, skip, ph, rh.p, v,
                                                                   part, nt, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_bs_alpha<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, st, skip)));
+            (launch_pdl(k_s_bs_alpha, nb, 128, 0, s, B.ntraps, B.drange.p, part, st, skip)));
     EQF_RUN(B, KC_CG_UPDATE,
-            (k_bs_half<T><<<nt, kThreads, 0, s>>>(G, tl, skip, st, ph, v, xs.p, r, part, W)));
+            (launch_pdl(k_bs_half<T>, nt, kThreads, 0, s, G, tl, skip, st, ph, v, xs.p, r, part, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_bs_half<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, tol_rel, tol_abs, st,
+            (launch_pdl(k_s_bs_half, nb, 128, 0, s, B.ntraps, B.drange.p, part, tol_rel, tol_abs, st,
                                             skip)));
     const T* sh = vcycle(s, 0, false, r);
     EQF_RUN(B, KC_CG_DIR,
-            (k_apply_dot<T, 2><<<nt, kThreads, L0.sm_resid, s>>>(G, tl, tab, skip, sh, r, t,
+            (launch_pdl(k_apply_dot<T, 2>, nt, kThreads, L0.sm_resid, s, G, tl, tab, skip, sh, r, t,
                                                                   part, nt, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_bs_omega<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, st, skip)));
+            (launch_pdl(k_s_bs_omega, nb, 128, 0, s, B.ntraps, B.drange.p, part, nt, st, skip)));
     EQF_RUN(B, KC_CG_UPDATE,
-            (k_bs_full<T><<<nt, kThreads, 0, s>>>(G, tl, skip, st, sh, t, rh.p, xs.p, r, part,
+            (launch_pdl(k_bs_full<T>, nt, kThreads, 0, s, G, tl, skip, st, sh, t, rh.p, xs.p, r, part,
                                                   nt, W)));
     EQF_RUN(B, KC_SCALAR,
-            (k_s_bs_rho<<<nb, 128, 0, s>>>(B.ntraps, B.drange.p, part, nt, tol_rel, tol_abs, st,
+            (launch_pdl(k_s_bs_rho, nb, 128, 0, s, B.ntraps, B.drange.p, part, nt, tol_rel, tol_abs, st,
                                            skip)));
   }
 }
@@ -1292,17 +1311,17 @@ void Work<T>::enqueue_check(cudaStream_t s, bool update_gamma) {
   const int nt = L0.ntiles();
   if constexpr (std::is_same<T, float>::value)
     EQF_RUN(B, KC_IR_RESID,
-            (k_irf_residual<true><<<nt, kThreads, L0.sm_irf, s>>>(
+            (launch_pdl(k_irf_residual<true>, nt, kThreads, L0.sm_irf, s, 
                 L0.dgeom.p, L0.dtiles.p, B.tabA2.p, B.d_ir_done.p,
                 reinterpret_cast<const float2*>(B.b64.p), B.U[1 - B.cur].p, B.Dd[1 - B.cur].p,
                 lv[0].b.p, B.dpart.p, nt, W)));
   else
     EQF_RUN(B, KC_IR_RESID,
-            (k_ir_residual<T, true><<<nt, kThreads, L0.sm_ir, s>>>(
+            (launch_pdl(k_ir_residual<T, true>, nt, kThreads, L0.sm_ir, s, 
                 L0.dgeom.p, L0.dtiles.p, L0.tabd.p, B.d_ir_done.p, B.b64.p, B.U[1 - B.cur].p,
                 B.Dd[1 - B.cur].p, lv[0].b.p, B.dpart.p, nt, W)));
   EQF_RUN(B, KC_SCALAR,
-          (k_s_final<<<(B.ntraps + 127) / 128, 128, 0, s>>>(B.ntraps, B.drange.p, B.dpart.p, nt,
+          (launch_pdl(k_s_final, (B.ntraps + 127) / 128, 128, 0, s, B.ntraps, B.drange.p, B.dpart.p, nt,
                                                              B.opts.rtol, B.dstate.p,
                                                              B.d_ir_done.p, B.d_fail.p,
                                                              update_gamma ? 1 : 0)));

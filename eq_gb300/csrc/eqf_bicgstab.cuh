@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(kThreads)
              const int* __restrict__ skip, const CgState* __restrict__ st,
              const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p,
              T* __restrict__ rhat, double* __restrict__ part, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
@@ -49,7 +50,7 @@ __global__ void __launch_bounds__(kThreads)
     }
   }
   if (FIRST) {
-    const double t = block_sum(double(acc));
+    const double t = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
   }
 }
@@ -62,6 +63,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
                 const T* __restrict__ tabs, const int* __restrict__ skip,
                 const T* __restrict__ x, const T* __restrict__ w, T* __restrict__ y,
                 double* __restrict__ part, int ntiles, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
@@ -98,8 +100,8 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     }
     vst4<T>(ys + k, ax);
   });
-  const double t0 = block_sum(double(a0));
-  const double t1 = NDOT == 2 ? block_sum(double(a1)) : 0.0;
+  const double t0 = block_sum(a0);
+  const double t1 = NDOT == 2 ? block_sum(a1) : 0.0;
   if (threadIdx.x == 0) {
     part[blockIdx.x] = t0;
     if (NDOT == 2) part[ntiles + blockIdx.x] = t1;
@@ -113,6 +115,7 @@ __global__ void __launch_bounds__(kThreads)
               const int* __restrict__ skip, const CgState* __restrict__ st,
               const T* __restrict__ ph, const T* __restrict__ v, T* __restrict__ x,
               T* __restrict__ r, double* __restrict__ part, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(kThreads)
     r[o + k] = sk;
     acc += sk * sk;
   }
-  const double t = block_sum(double(acc));
+  const double t = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
@@ -141,6 +144,7 @@ __global__ void __launch_bounds__(kThreads)
               const T* __restrict__ sh, const T* __restrict__ t, const T* __restrict__ rhat,
               T* __restrict__ x, T* __restrict__ r, double* __restrict__ part, int ntiles,
               unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
@@ -161,8 +165,8 @@ __global__ void __launch_bounds__(kThreads)
     a0 += rk * rk;
     a1 += rhat[o + k] * rk;
   }
-  const double t0 = block_sum(double(a0));
-  const double t1 = block_sum(double(a1));
+  const double t0 = block_sum(a0);
+  const double t1 = block_sum(a1);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = t0;
     part[ntiles + blockIdx.x] = t1;
@@ -174,6 +178,7 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void k_s_bs_rho0(int ntraps, const TileRange* __restrict__ range,
                             const double* __restrict__ part, CgState* __restrict__ st,
                             const int* __restrict__ skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || skip[t]) return;
   st[t].rz = trap_sum(part, range[t]);
@@ -184,6 +189,7 @@ __global__ void k_s_bs_rho0(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_bs_alpha(int ntraps, const TileRange* __restrict__ range,
                              const double* __restrict__ part, CgState* __restrict__ st,
                              int* __restrict__ skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || skip[t]) return;
   CgState s = st[t];
@@ -201,6 +207,7 @@ __global__ void k_s_bs_alpha(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_bs_half(int ntraps, const TileRange* __restrict__ range,
                             const double* __restrict__ part, double tol_rel, double rtol_abs,
                             CgState* __restrict__ st, int* __restrict__ skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || skip[t]) return;
   CgState s = st[t];
@@ -217,6 +224,7 @@ __global__ void k_s_bs_half(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_bs_omega(int ntraps, const TileRange* __restrict__ range,
                              const double* __restrict__ part, int ntiles,
                              CgState* __restrict__ st, int* __restrict__ skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || skip[t]) return;
   const double ts = trap_sum(part, range[t]);
@@ -233,6 +241,7 @@ __global__ void k_s_bs_omega(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_bs_rho(int ntraps, const TileRange* __restrict__ range,
                            const double* __restrict__ part, int ntiles, double tol_rel,
                            double rtol_abs, CgState* __restrict__ st, int* __restrict__ skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || skip[t]) return;
   CgState s = st[t];

@@ -162,7 +162,7 @@ struct WinQuads {
   __device__ __forceinline__ explicit WinQuads(const Win& w) {
     QW = w.S() >> 2;
     n = (w.rb - w.ra) * QW;
-    inv = 1.0f / (float)QW;
+    inv = __fdividef(1.0f, (float)QW);  // div_pitch corrects the floor by one
   }
   __device__ __forceinline__ void at(int q, int& row, int& cq) const {
     div_pitch(q, QW, inv, row, cq);
@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
            T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+  grid_dep_sync();
   const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
          const int* __restrict__ skip, const T* __restrict__ xc, const T* __restrict__ b,
          const T* __restrict__ xin, T* __restrict__ xout, double* __restrict__ part,
          unsigned long long* work) {
+  grid_dep_sync();
   const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     });
   }
   if (DOT) {
-    const double s = block_sum(double(acc));
+    const double s = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
   }
 }

@@ -37,6 +37,17 @@ extern __shared__ __align__(16) char eqf_smem[];
 // Device-side error flag: set when a bounded wait gives up (never expected).
 __device__ int g_eqf_device_error = 0;
 
+// Programmatic dependent launch.  The solver's kernels are launched with programmatic
+// stream serialization, so a kernel's CTAs may be scheduled while its predecessor's
+// last CTAs still run.  Every solver kernel calls this first: it returns once the
+// predecessor grid has completed and its writes are visible (the hardware holds the
+// CTA; no spinning), then allows the successor grid to be scheduled.  For a kernel
+// launched without the attribute both instructions are no-ops.
+__device__ __forceinline__ void grid_dep_sync() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Bulk-copy staging (global -> shared) completed on one mbarrier.
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -342,6 +353,7 @@ __device__ __forceinline__ T inv_diag_general(const LevelGeom& g, int i, int j) 
 // the host bounds use), kept in FP64 and rounded to FP32.
 __global__ void k_aniso_coefs(const LevelGeom g, float* __restrict__ cf,
                               double* __restrict__ cd) {
+  grid_dep_sync();
   const long long n = (long long)g.P * (g.ny + 1);
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
        k += (long long)gridDim.x * blockDim.x) {
@@ -486,7 +498,7 @@ __device__ __forceinline__ void for_quads(const LevelGeom& g, const QuadBlock& b
   }
   const int RW = qb - qa + 1, RH = ib - ia + 1;
   if (RH > 0) {
-    const float inv = 1.0f / (float)RW;
+    const float inv = __fdividef(1.0f, (float)RW);  // div_pitch corrects the floor by one
     int r, c, dr, dc;
     div_pitch((int)threadIdx.x, RW, inv, r, c);
     div_pitch((int)blockDim.x, RW, inv, dr, dc);
@@ -507,7 +519,8 @@ __device__ __forceinline__ void for_quads(const LevelGeom& g, const QuadBlock& b
   const int bot = RH > 0 ? (b.rb - 1 - ib) * b.QW : 0;
   const int n = top + mid + bot;
   if (n == 0) return;
-  const float invq = 1.0f / (float)b.QW, invb = nb > 0 ? 1.0f / (float)nb : 0.0f;
+  const float invq = __fdividef(1.0f, (float)b.QW);
+  const float invb = nb > 0 ? __fdividef(1.0f, (float)nb) : 0.0f;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     int r, c;
     if (idx < top) {
@@ -628,19 +641,31 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
   return ax;
 }
 
-__device__ __forceinline__ double block_sum(double v) {
+// Sum over the CTA of the warps' sums (lane 0 of each warp holds one): FP64 in
+// warp 0, a shuffle tree over the warps present.  Valid in thread 0.
+__device__ __forceinline__ double warps_sum(double v) {
   __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
   if (lane == 0) red[w] = v;
   __syncthreads();
   double t = 0.0;
   if (w == 0) {
-    t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-  }
+    t = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1)
+      if (o < nw) t += __shfl_down_sync(0xffffffffu, t, o);  // (adding the zeros beyond
+  }                                                           //  nw would change nothing)
   __syncthreads();
-  return t;  // valid in thread 0
+  return t;
+}
+__device__ __forceinline__ double block_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return warps_sum(v);
+}
+// FP32 partials: the warp stage in FP32 (five dependent FP64 adds would cost several
+// hundred cycles on this part's narrow FP64 pipe), the warps' sums in FP64.
+__device__ __forceinline__ double block_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return warps_sum((double)v);
 }
 
 // Optional profiling counter: nodes actually processed by a launch (tiles of
@@ -687,6 +712,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
            const T* __restrict__ tabs, const int* __restrict__ skip, int step,
            const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
            T* __restrict__ d, double* __restrict__ part, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
@@ -755,7 +781,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     });
   }
   if (DOT) {
-    const double t = block_sum(double(acc));
+    const double t = block_sum(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
   }
 }
@@ -766,6 +792,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_resid(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
             const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
             const T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
@@ -825,6 +852,7 @@ __global__ void __launch_bounds__(kThreads)
     k_restrict(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                const int* __restrict__ skip, const T* __restrict__ tf, T* __restrict__ bc,
                unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
@@ -868,6 +896,7 @@ __global__ void __launch_bounds__(kThreads)
     k_prolong(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
               const Tile* __restrict__ tiles, const int* __restrict__ skip,
               const T* __restrict__ xc, T* __restrict__ xf, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
@@ -907,6 +936,7 @@ __global__ void __launch_bounds__(kThreads)
     k_coarse_solve(const LevelGeom* __restrict__ G, const T* __restrict__ tabs,
                    const int* __restrict__ skip, int deg, const T* __restrict__ b,
                    T* __restrict__ xout) {
+  grid_dep_sync();
   const LevelGeom& g = G[blockIdx.x];
   if (skip && skip[g.trap]) return;
   const int n = g.P * (g.ny + 1);
@@ -989,6 +1019,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
              const CgState* __restrict__ st, const T* __restrict__ z, const T* __restrict__ pin,
              T* __restrict__ pout, T* __restrict__ q, double* __restrict__ part,
              unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
@@ -1024,7 +1055,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     vst4<T>(po + k, pc);
     vst4<T>(qs + k, a);
   });
-  const double t = block_sum(double(acc));
+  const double t = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
@@ -1035,6 +1066,7 @@ __global__ void __launch_bounds__(kThreads)
                 const int* __restrict__ skip, const CgState* __restrict__ st,
                 const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
                 T* __restrict__ r, double* __restrict__ part, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
@@ -1069,7 +1101,7 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
   }
-  const double t = block_sum(double(acc));
+  const double t = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
@@ -1091,6 +1123,7 @@ __global__ void __launch_bounds__(kThreads)
                double* __restrict__ b64, double* __restrict__ u_out, float* __restrict__ d_out,
                T* __restrict__ r, double* __restrict__ part, int ntiles,
                const int* __restrict__ frozen, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (frozen[g.trap]) {
@@ -1155,6 +1188,7 @@ __global__ void __launch_bounds__(kThreads)
                   const double* __restrict__ b64, const double* __restrict__ u,
                   const float* __restrict__ dcur, T* __restrict__ r, double* __restrict__ part,
                   int ntiles, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   const bool skipped = skip && skip[g.trap];
@@ -1214,6 +1248,7 @@ __global__ void __launch_bounds__(kThreads)
     k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                 const int* __restrict__ skip, const T* __restrict__ x, double* __restrict__ u,
                 float* __restrict__ d, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
@@ -1261,6 +1296,7 @@ __global__ void k_s_ir(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, int ntiles, int first_sweep, double rtol,
                        CgState* __restrict__ st, int* __restrict__ ir_done,
                        int* __restrict__ cg_skip, const int* __restrict__ frozen) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps) return;
   if (frozen[t]) {  // inactive trap: nothing to solve
@@ -1294,6 +1330,7 @@ __global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
                           const double* __restrict__ part, int ntiles, double rtol,
                           CgState* __restrict__ st, int* __restrict__ ir_done,
                           int* __restrict__ fail, int update_gamma) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps) return;
   CgState s = st[t];
@@ -1320,6 +1357,7 @@ __global__ void k_s_final(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_rz(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, CgState* __restrict__ st,
                        const int* __restrict__ cg_skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || cg_skip[t]) return;
   const double rz = trap_sum(part, range[t]);
@@ -1333,6 +1371,7 @@ __global__ void k_s_rz(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_pq(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, CgState* __restrict__ st,
                        const int* __restrict__ cg_skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || cg_skip[t]) return;
   const double pq = trap_sum(part, range[t]);
@@ -1346,6 +1385,7 @@ __global__ void k_s_pq(int ntraps, const TileRange* __restrict__ range,
 __global__ void k_s_rr(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, double tol_rel, double rtol_abs,
                        CgState* __restrict__ st, int* __restrict__ cg_skip) {
+  grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || cg_skip[t]) return;
   CgState s = st[t];

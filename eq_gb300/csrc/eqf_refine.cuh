@@ -120,6 +120,16 @@ struct SqAcc {
     return f2d(big) + f2d(tiny) * 2.9387358770557188e-39;  // 2^-128
   }
 };
+// CTA sum of the threads' sums of squares: both accumulators summed over the warp in
+// FP32, the warps' totals in FP64.  Valid in thread 0.
+__device__ __forceinline__ double block_sum(const SqAcc& a) {
+  SqAcc w = a;
+  for (int o = 16; o > 0; o >>= 1) {
+    w.big += __shfl_down_sync(0xffffffffu, w.big, o);
+    w.tiny += __shfl_down_sync(0xffffffffu, w.tiny, o);
+  }
+  return warps_sum(w.total());
+}
 
 // Per-trap pair tables: 25 classes x 8 pairs (c, e, w, n, s, ne, sw, unused), the
 // interior class holding the interior weights (same layout as the FP64 tables).
@@ -293,6 +303,7 @@ __global__ void __launch_bounds__(kThreads)
                 float2* __restrict__ b2, double* __restrict__ u_out, float* __restrict__ d_out,
                 float* __restrict__ r, double* __restrict__ part, int ntiles,
                 const int* __restrict__ frozen, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (frozen[g.trap]) {  // inactive trap: its field is left as it is
@@ -378,8 +389,8 @@ __global__ void __launch_bounds__(kThreads)
       df_residual_quad<INNER>(g, sA, ca, xw, xa, k, i, j, bs, rs, arr, true);
     });
   }
-  const double tb = block_sum(abb.total());
-  const double tr = block_sum(arr.total());
+  const double tb = block_sum(abb);
+  const double tr = block_sum(arr);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = tb;
     part[ntiles + blockIdx.x] = tr;
@@ -396,6 +407,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                    const float2* __restrict__ b2, const double* __restrict__ u,
                    const float* __restrict__ dcur, float* __restrict__ r,
                    double* __restrict__ part, int ntiles, unsigned long long* work) {
+  grid_dep_sync();
   const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   const bool skipped = skip && skip[g.trap];
@@ -435,8 +447,8 @@ __global__ void __launch_bounds__(kThreads, 4)
       });
     }
   }
-  const double tr = block_sum(arr.total());
-  const double td = FINAL ? block_sum(add.total()) : 0.0;
+  const double tr = block_sum(arr);
+  const double td = FINAL ? block_sum(add) : 0.0;
   if (threadIdx.x == 0) {
     part[ntiles + blockIdx.x] = tr;
     if (FINAL) part[2 * ntiles + blockIdx.x] = td;
