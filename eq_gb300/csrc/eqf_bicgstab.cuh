@@ -27,8 +27,9 @@ __global__ void __launch_bounds__(kThreads)
              const int* __restrict__ skip, const CgState* __restrict__ st,
              const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p,
              T* __restrict__ rhat, double* __restrict__ part, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
     if (FIRST && threadIdx.x == 0) part[blockIdx.x] = 0.0;
@@ -63,8 +64,9 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
                 const T* __restrict__ tabs, const int* __restrict__ skip,
                 const T* __restrict__ x, const T* __restrict__ w, T* __restrict__ y,
                 double* __restrict__ part, int ntiles, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
     if (threadIdx.x == 0) {
@@ -115,8 +117,9 @@ __global__ void __launch_bounds__(kThreads)
               const int* __restrict__ skip, const CgState* __restrict__ st,
               const T* __restrict__ ph, const T* __restrict__ v, T* __restrict__ x,
               T* __restrict__ r, double* __restrict__ part, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
     if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
@@ -144,8 +147,9 @@ __global__ void __launch_bounds__(kThreads)
               const T* __restrict__ sh, const T* __restrict__ t, const T* __restrict__ rhat,
               T* __restrict__ x, T* __restrict__ r, double* __restrict__ part, int ntiles,
               unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip[g.trap]) {
     if (threadIdx.x == 0) {

@@ -215,8 +215,9 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
            T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+  const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   if (work && threadIdx.x == 0)
@@ -296,8 +297,9 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
          const int* __restrict__ skip, const T* __restrict__ xc, const T* __restrict__ b,
          const T* __restrict__ xin, T* __restrict__ xout, double* __restrict__ part,
          unsigned long long* work) {
+  const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile2 tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
     if (DOT && threadIdx.x == 0) part[blockIdx.x] = 0.0;

@@ -48,6 +48,16 @@ __device__ __forceinline__ void grid_dep_sync() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Before grid_dep_sync a kernel may only read what no kernel of a step writes: its
+// tile descriptor and the level geometry.  This pulls the geometry into L1 while the
+// predecessor finishes.
+template <class G>
+__device__ __forceinline__ void prefetch_l1(const G* p) {
+  const char* c = reinterpret_cast<const char*>(p);
+  for (int o = (int)threadIdx.x * 128; o < (int)sizeof(G); o += (int)blockDim.x * 128)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(c + o));
+}
+
 // ---------------------------------------------------------------------------
 // Bulk-copy staging (global -> shared) completed on one mbarrier.
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -712,8 +722,9 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
            const T* __restrict__ tabs, const int* __restrict__ skip, int step,
            const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
            T* __restrict__ d, double* __restrict__ part, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
     if (DOT && threadIdx.x == 0) part[blockIdx.x] = 0.0;
@@ -792,8 +803,9 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_resid(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
             const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
             const T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
@@ -852,8 +864,9 @@ __global__ void __launch_bounds__(kThreads)
     k_restrict(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                const int* __restrict__ skip, const T* __restrict__ tf, T* __restrict__ bc,
                unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
@@ -896,8 +909,9 @@ __global__ void __launch_bounds__(kThreads)
     k_prolong(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
               const Tile* __restrict__ tiles, const int* __restrict__ skip,
               const T* __restrict__ xc, T* __restrict__ xf, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
@@ -1019,8 +1033,9 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
              const CgState* __restrict__ st, const T* __restrict__ z, const T* __restrict__ pin,
              T* __restrict__ pout, T* __restrict__ q, double* __restrict__ part,
              unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
     if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
@@ -1066,8 +1081,9 @@ __global__ void __launch_bounds__(kThreads)
                 const int* __restrict__ skip, const CgState* __restrict__ st,
                 const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
                 T* __restrict__ r, double* __restrict__ part, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
     if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
@@ -1123,8 +1139,9 @@ __global__ void __launch_bounds__(kThreads)
                double* __restrict__ b64, double* __restrict__ u_out, float* __restrict__ d_out,
                T* __restrict__ r, double* __restrict__ part, int ntiles,
                const int* __restrict__ frozen, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (frozen[g.trap]) {
     if (threadIdx.x == 0) part[blockIdx.x] = part[ntiles + blockIdx.x] = 0.0;
@@ -1188,8 +1205,9 @@ __global__ void __launch_bounds__(kThreads)
                   const double* __restrict__ b64, const double* __restrict__ u,
                   const float* __restrict__ dcur, T* __restrict__ r, double* __restrict__ part,
                   int ntiles, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   const bool skipped = skip && skip[g.trap];
   if (skipped && !FINAL) {
@@ -1248,8 +1266,9 @@ __global__ void __launch_bounds__(kThreads)
     k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                 const int* __restrict__ skip, const T* __restrict__ x, double* __restrict__ u,
                 float* __restrict__ d, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);

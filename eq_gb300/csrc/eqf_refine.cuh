@@ -133,11 +133,19 @@ __device__ __forceinline__ double block_sum(const SqAcc& a) {
 
 // Per-trap pair tables: 25 classes x 8 pairs (c, e, w, n, s, ne, sw, unused), the
 // interior class holding the interior weights (same layout as the FP64 tables).
-__device__ __forceinline__ const float2* stage_pair_table(Stager& st, const float2* tab) {
+// stage_pair_table carves the region; the returned filler runs inside Stager::run,
+// after the bulk copies are issued.
+struct PairTableStage {
+  float2* s;
+  const float2* tab;
+  __device__ __forceinline__ void operator()() const {
+    for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) s[e] = tab[e];
+  }
+};
+__device__ __forceinline__ PairTableStage stage_pair_table(Stager& st, const float2* tab) {
   float2* s = reinterpret_cast<float2*>(st.cur);
   st.cur += kTabPerTrap * sizeof(float2);
-  for (int e = threadIdx.x; e < kTabPerTrap; e += blockDim.x) s[e] = tab[e];
-  return s;
+  return PairTableStage{s, tab};
 }
 
 // (A x)_k for node (i, j) from a pair window x (node k at x[k - a]).
@@ -303,8 +311,9 @@ __global__ void __launch_bounds__(kThreads)
                 float2* __restrict__ b2, double* __restrict__ u_out, float* __restrict__ d_out,
                 float* __restrict__ r, double* __restrict__ part, int ntiles,
                 const int* __restrict__ frozen, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   if (frozen[g.trap]) {  // inactive trap: its field is left as it is
     if (threadIdx.x == 0) part[blockIdx.x] = part[ntiles + blockIdx.x] = 0.0;
@@ -316,9 +325,15 @@ __global__ void __launch_bounds__(kThreads)
   const int ka = halo_lo(g, tile), kb = halo_hi(g, tile);
   const View<double> uv = sg.add_guarded(u_in + g.off, ka, kb, na);
   const View<float> dv = sg.add_guarded(d_in + g.off, ka, kb, na);
-  const float2* sA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
-  const float2* sM = stage_pair_table(sg, tabM + (size_t)g.trap * kTabPerTrap);
-  if (!sg.run()) return;
+  const PairTableStage tA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
+  const PairTableStage tM = stage_pair_table(sg, tabM + (size_t)g.trap * kTabPerTrap);
+  const float2* sA = tA.s;
+  const float2* sM = tM.s;
+  if (!sg.run([&] {
+        tA();
+        tM();
+      }))
+    return;
   window_to_pairs(uv, ka, kb);
   __syncthreads();
   const float2* xw = reinterpret_cast<const float2*>(uv.p);
@@ -407,8 +422,9 @@ __global__ void __launch_bounds__(kThreads, 4)
                    const float2* __restrict__ b2, const double* __restrict__ u,
                    const float* __restrict__ dcur, float* __restrict__ r,
                    double* __restrict__ part, int ntiles, unsigned long long* work) {
+  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+  prefetch_l1(G + tile.geom);
   grid_dep_sync();
-  const Tile tile = tiles[blockIdx.x];
   const LevelGeom& g = G[tile.geom];
   const bool skipped = skip && skip[g.trap];
   if (skipped && !FINAL) {
@@ -416,18 +432,33 @@ __global__ void __launch_bounds__(kThreads, 4)
     return;
   }
   SqAcc arr, add;
-  if (FINAL) {
-    const float* ds = dcur + g.off;
-    for (int k = tile.k0 + threadIdx.x; k < tile.k1; k += blockDim.x) add.add(ds[k]);
-  }
+  // |d|^2 of the tile (tiles are whole rows of 16-byte-aligned quads)
+  auto dnorm = [&] {
+    if (FINAL) {
+      const float4* ds = reinterpret_cast<const float4*>(dcur + g.off);
+      for (int q = (tile.k0 >> 2) + (int)threadIdx.x; q < (tile.k1 >> 2); q += blockDim.x) {
+        const float4 v = ds[q];
+        add.add(v.x);
+        add.add(v.y);
+        add.add(v.z);
+        add.add(v.w);
+      }
+    }
+  };
+  if (skipped) dnorm();
   if (!skipped) {
     count_work(work, tile);
     Stager sg(eqf_smem);
     const int na = padded_len(g);
     const int ka = halo_lo(g, tile), kb = halo_hi(g, tile);
     const View<double> uv = sg.add_guarded(u + g.off, ka, kb, na);
-    const float2* sA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
-    if (!sg.run()) return;
+    const PairTableStage tA = stage_pair_table(sg, tabA + (size_t)g.trap * kTabPerTrap);
+    const float2* sA = tA.s;
+    if (!sg.run([&] {
+          tA();
+          dnorm();
+        }))
+      return;
     window_to_pairs(uv, ka, kb);
     __syncthreads();
     const float2* xw = reinterpret_cast<const float2*>(uv.p);
