@@ -710,7 +710,8 @@ def run_ncu_target(args):
         return
     traps = make_workload(args.workload, args.seed, args.traps)
     b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1,
-                                                          tile_nodes=args.tile_nodes))
+                                                          tile_nodes=args.tile_nodes,
+                                                          fuse_levels=0 if args.no_fuse else 1))
     load_traps(b, traps)
     b.step(args.warmup + args.steps)
     b.sync()
