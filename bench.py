@@ -210,7 +210,7 @@ def run_ours(args, rank, world, local_rank):
     ncells = sum(t.n_cells for t in traps)
 
     opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, tile_nodes=args.tile_nodes,
-                          fuse_levels=0 if args.no_fuse else 1)
+                          fuse_levels=0 if args.no_fuse else args.fuse_levels)
     # the autotuner picks the row tile target and smoother degrees per size bucket
     table = None
     if args.tune_budget > 0 and args.tile_nodes == 0:
@@ -711,7 +711,8 @@ def run_ncu_target(args):
     traps = make_workload(args.workload, args.seed, args.traps)
     b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1,
                                                           tile_nodes=args.tile_nodes,
-                                                          fuse_levels=0 if args.no_fuse else 1))
+                                                          fuse_levels=0 if args.no_fuse
+                                                          else args.fuse_levels))
     load_traps(b, traps)
     b.step(args.warmup + args.steps)
     b.sync()
@@ -745,6 +746,9 @@ def main():
                     help="serving: CPU seconds for the oracle audit")
     ap.add_argument("--no-fuse", action="store_true",
                     help="step-by-step level kernels instead of the temporally blocked ones")
+    ap.add_argument("--fuse-levels", type=int, default=1, choices=[1, 2],
+                    help="1: temporally blocked level kernels (default); 2: also the "
+                         "small bottom levels in one kernel per trap")
     ap.add_argument("--tune-budget", type=float, default=20.0,
                     help="seconds for the autotuner before the timed run (0: no tuning)")
     ap.add_argument("--tile-nodes", type=int, default=0,

@@ -351,6 +351,9 @@ class Batch {
  public:
   int ntraps = 0;
   int nlev = 0;
+  // the V-cycle below level bottom_lb runs in k_bottom, one CTA per trap (-1: not used)
+  int bottom_lb = -1;
+  size_t sm_bottom = 0;
   eqf_solver_opts opts{};
   std::vector<eqf_trap_params> params;
   std::vector<Level> L;
@@ -933,6 +936,28 @@ void Batch::build_levels() {
     }
     Lc.sm_coarse = (nlev > 1 && need <= kMaxDynSmem) ? need : 0;
   }
+  // the shallowest bottom level (>= 2) whose levels down to the coarsest fit one CTA's
+  // shared memory for every trap (fused level path only: the step-by-step path stays
+  // launch by launch)
+  bottom_lb = -1;
+  sm_bottom = 0;
+  if (opts.fuse_levels >= 2 && opts.cheb_pre == 2 && opts.cheb_post == 2 &&
+      L[nlev - 1].sm_coarse > 0) {
+    for (int lb = std::max(2, nlev - kMaxBottom); lb <= nlev - 2; ++lb) {
+      size_t need = 0;
+      for (int t = 0; t < ntraps; ++t) {
+        size_t b = kSmemHeader + 32;
+        for (int l = lb; l < nlev; ++l)
+          b += bottom_level_bytes(L[l].geom[t].P, L[l].geom[t].ny, tsz) + 96;
+        need = std::max(need, b);
+      }
+      if (need <= kMaxDynSmem) {
+        bottom_lb = lb;
+        sm_bottom = need;
+        break;
+      }
+    }
+  }
   range.assign(ntraps, TileRange{0, 0});
   for (int i = 0; i < L[0].ntiles(); ++i) {
     const int t = L[0].tiles[i].geom;
@@ -985,6 +1010,7 @@ static void allow_dyn_smem() {
   smem_attrs(k_apply_dot<T, 2>, mx);
   smem_attrs(k_irf_residual<true>, mx);
   smem_attrs(k_irf_residual<false>, mx);
+  smem_attrs(k_bottom<T>, mx);
 }
 
 template <class T>
@@ -1103,6 +1129,20 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   T* oth = v.y.p;
   const bool coarsest = lev == B.nlev - 1;
   const int deg_pre = coarsest ? B.opts.cheb_coarse : B.opts.cheb_pre;
+  if (lev == B.bottom_lb && !dot) {
+    // levels lev .. coarsest in one CTA per trap
+    BottomArgs<T> a{};
+    a.nlev = B.nlev - lev;
+    for (int m = 0; m < a.nlev; ++m) {
+      a.G[m] = B.L[lev + m].dgeom.p;
+      a.tabs[m] = level_tab<T>(B.L[lev + m]);
+    }
+    a.deg_pre = B.opts.cheb_pre;
+    a.deg_coarse = B.opts.cheb_coarse;
+    EQF_RUN(B, KC_COARSE,
+            (launch_pdl(k_bottom<T>, B.ntraps, kBottomThreads, B.sm_bottom, s, a, skip, bl, cur)));
+    return cur;
+  }
   if (coarsest && Lv_.sm_coarse && !dot) {
     // the whole coarsest solve in one CTA per trap
     EQF_RUN(B, KC_COARSE,

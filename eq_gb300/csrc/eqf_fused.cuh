@@ -198,12 +198,6 @@ __device__ __forceinline__ Q4<T> inv_diag_quad(const LevelGeom& g, const Interio
   return id;
 }
 
-template <class T>
-__device__ __forceinline__ T* carve(Stager& st, int count) {
-  T* p = reinterpret_cast<T*>(st.cur);
-  st.cur += (((uint32_t)count * sizeof(T) + 15u) & ~15u) + 16u;
-  return p;
-}
 // Local index of node (i, j) in window w.
 __device__ __forceinline__ int wl(const Win& w, int i, int j) {
   return (i - w.ra) * w.S() + (j - w.ca);
@@ -380,7 +374,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       Q4<T> xn;
 #pragma unroll
       for (int e = 0; e < 4; ++e)
-        xn.v[e] = x0q.v[e] + cheb_dir<T, true>(c0, bq.v[e], ax.v[e], id.v[e], T(0));
+        xn.v[e] = add_(x0q.v[e], cheb_dir<T, true>(c0, bq.v[e], ax.v[e], id.v[e], T(0)));
       vst4<T>(x1p + kl, xn);
     });
   }

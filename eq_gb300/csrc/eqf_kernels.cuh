@@ -271,6 +271,10 @@ __device__ __forceinline__ Interior<double> interior<double>(const LevelGeom& g)
 // weights (c, e, w, n, s, ne, sw) are applied in that order.
 __device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+// A sum the compiler may not fuse with the product that produced an operand (kernels
+// that must give the same bits write it out where the product also has other uses).
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
 
 template <class T>
 __device__ __forceinline__ T st_table(const T* c, T x0, T xe, T xw, T xn, T xs, T xne, T xsw) {
@@ -590,6 +594,15 @@ __device__ __forceinline__ TableStage<T> stage_table(Stager& st, const T* __rest
   T* s = reinterpret_cast<T*>(st.cur);
   st.cur += kTabPerTrap * sizeof(T);
   return TableStage<T>{s, tab, ci};
+}
+
+// A region of `count` elements of shared memory after the staged ranges (16-byte
+// aligned, with the 16-byte pad every region keeps after it).
+template <class T>
+__device__ __forceinline__ T* carve(Stager& st, int count) {
+  T* p = reinterpret_cast<T*>(st.cur);
+  st.cur += (((uint32_t)count * sizeof(T) + 15u) & ~15u) + 16u;
+  return p;
 }
 
 // Quad halo window: one row and nine nodes each side, so that every vector load of
@@ -974,16 +987,222 @@ __global__ void __launch_bounds__(kThreads)
     for (NodeWalk w(g, 0); w.k < n; w.next()) {
       T id;
       const T ax = apply_tab<T>(g, ci, tab, xi, w.k, w.i, w.j, id);
-      T dn = T(cc.c_res) * (bv[w.k] - ax) * id;
-      if (it > 0) dn += T(cc.c_old) * dd[w.k];
+      T dn = (T(cc.c_res) * (bv[w.k] - ax)) * id;
+      if (it > 0) dn = fma_(T(cc.c_old), dd[w.k], dn);
       dd[w.k] = dn;
-      xo[w.k] = xi[w.k] + dn;
+      xo[w.k] = add_(xi[w.k], dn);
     }
     __syncthreads();
   }
   const T* xf = (deg & 1) ? xb : xa;
   T* out = xout + g.off;
   for (int k = threadIdx.x; k < n; k += blockDim.x) out[k] = xf[k];
+}
+
+// ---------------------------------------------------------------------------
+// The bottom of the V-cycle in one CTA per trap: levels lb .. coarsest of one trap
+// live in shared memory, and the kernel runs what the fused V(2,2) path does there
+// (k_down's two pre-smoothing steps from zero and residual, k_restrict, k_coarse_solve,
+// k_up's prolongation and two post-smoothing steps), node by node with the same
+// expressions on the same operands, so its results are bit-identical to that path and
+// the small levels cost one launch instead of seven, with no HBM round trips.
+constexpr int kMaxBottom = 4;      // levels in the bottom kernel
+constexpr int kBottomThreads = 512;
+template <class T>
+struct BottomArgs {
+  const LevelGeom* G[kMaxBottom];  // per level lb + m: the level's geometry array (by trap)
+  const T* tabs[kMaxBottom];       // and its class tables
+  int nlev;                        // levels lb .. lb + nlev - 1 (the last the coarsest)
+  int deg_pre, deg_coarse;  // (two post-smoothing steps, as k_up)
+};
+// Shared-memory bytes of one level: rhs b and direction d, iterates x and y with
+// zero guards of gpad >= P + 1 nodes each side.
+EQF_HD size_t bottom_level_bytes(int P, int ny, int tsize) {
+  const long long na = (((long long)P * (ny + 1)) + 31) & ~31ll;
+  const long long gp = ((P + 1 + 7) / 8) * 8;
+  return (size_t)((4 * na + 4 * gp) * tsize);
+}
+
+template <class T>
+struct BottomLevel {
+  T *b, *x, *y, *d;  // x and y point at node 0 (guards before and after)
+  int n, na, gp;
+};
+
+template <class T>
+__device__ __forceinline__ void bottom_sweep(const LevelGeom& g, const Interior<T>& ci,
+                                             const T* __restrict__ tab, const ChebCoef& cc,
+                                             bool first, const T* b, const T* x, T* xo, T* d,
+                                             int n) {
+  const View<T> xv{x, 0};
+  for (NodeWalk w(g, 0); w.k < n; w.next()) {
+    T id;
+    const T ax = apply_tab<T>(g, ci, tab, xv, w.k, w.i, w.j, id);
+    const T dn = first ? (T(cc.c_res) * (b[w.k] - ax)) * id
+                       : cheb_dir<T, false>(cc, b[w.k], ax, id, d[w.k]);
+    d[w.k] = dn;
+    xo[w.k] = add_(x[w.k], dn);
+  }
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBottomThreads, 1)
+    k_bottom(const BottomArgs<T> a, const int* __restrict__ skip, const T* __restrict__ b0,
+             T* __restrict__ x0) {
+  grid_dep_sync();
+  const int trap = blockIdx.x;
+  if (skip && skip[trap]) return;
+  BottomLevel<T> lv[kMaxBottom];
+  Stager st(eqf_smem);
+  const LevelGeom& g0 = a.G[0][trap];
+  const int n0 = g0.P * (g0.ny + 1);
+  const View<T> b0v = st.add(b0 + g0.off, 0, n0, padded_len(g0));  // level lb's rhs
+  lv[0].b = const_cast<T*>(b0v.p);
+  for (int m = 0; m < a.nlev; ++m) {
+    const LevelGeom& g = a.G[m][trap];
+    BottomLevel<T>& L = lv[m];
+    L.n = g.P * (g.ny + 1);
+    L.na = padded_len(g);
+    L.gp = ((g.P + 1 + 7) / 8) * 8;
+    if (m > 0) L.b = carve<T>(st, L.na);
+    T* xg = carve<T>(st, 2 * (L.na + 2 * L.gp));  // x and y with their guards
+    L.x = xg + L.gp;
+    L.y = L.x + L.na + 2 * L.gp;
+    L.d = carve<T>(st, L.na);
+  }
+  // zero the iterates and their guards (disjoint from the staged rhs) while it lands
+  if (!st.run([&] {
+        for (int m = 0; m < a.nlev; ++m) {
+          T* xg = lv[m].x - lv[m].gp;
+          for (int e = threadIdx.x; e < 2 * (lv[m].na + 2 * lv[m].gp); e += blockDim.x)
+            xg[e] = T(0);
+        }
+      }))
+    return;
+  const int mc = a.nlev - 1;
+  // down: pre-smoothing from zero, residual (into y), restriction
+  for (int m = 0; m < mc; ++m) {
+    const LevelGeom& g = a.G[m][trap];
+    const T* tab = a.tabs[m] + (size_t)trap * kTabPerTrap;
+    const Interior<T> ci = interior<T>(g);
+    BottomLevel<T>& L = lv[m];
+    {
+      const ChebCoef cc = cheb_at(g, 0);
+      for (NodeWalk w(g, 0); w.k < L.n; w.next()) {
+        const T dn = (T(cc.c_res) * L.b[w.k]) * inv_diag_tab<T>(g, ci, tab, w.i, w.j);
+        L.x[w.k] = dn;
+        L.d[w.k] = dn;
+      }
+      __syncthreads();
+    }
+    for (int s = 1; s < a.deg_pre; ++s) {
+      bottom_sweep<T>(g, ci, tab, cheb_at(g, s), false, L.b, L.x, L.y, L.d, L.n);
+      T* t = L.x;
+      L.x = L.y;
+      L.y = t;
+    }
+    {
+      const View<T> xv{L.x, 0};
+      for (NodeWalk w(g, 0); w.k < L.n; w.next()) {
+        T id;
+        L.y[w.k] = L.b[w.k] - apply_tab<T>(g, ci, tab, xv, w.k, w.i, w.j, id);
+      }
+      __syncthreads();
+    }
+    // b_c = P^T t on the coarse level (k_restrict's gather)
+    const LevelGeom& gc = a.G[m + 1][trap];
+    const BottomLevel<T>& C = lv[m + 1];
+    const T* t = L.y;
+    const int nfx = gc.fine_nx, nfy = gc.fine_ny, PF = gc.fine_P;
+    for (NodeWalk w(gc, 0); w.k < C.n; w.next()) {
+      if (w.j > gc.nx || (gc.walls && is_dirichlet(gc, w.i, w.j))) {
+        C.b[w.k] = T(0);
+        continue;
+      }
+      const int fi = coarse_to_fine(w.i, nfy, gc.cy), fj = coarse_to_fine(w.j, nfx, gc.cx);
+      const int kf = fj + fi * PF;
+      T half = T(0);
+      const bool mE = fj + 1 <= nfx && is_mid(fj + 1, nfx, gc.cx);
+      const bool mW = fj - 1 >= 0 && is_mid(fj - 1, nfx, gc.cx);
+      const bool mN = fi + 1 <= nfy && is_mid(fi + 1, nfy, gc.cy);
+      const bool mS = fi - 1 >= 0 && is_mid(fi - 1, nfy, gc.cy);
+      if (mE) half += t[kf + 1];
+      if (mW) half += t[kf - 1];
+      if (mN) half += t[kf + PF];
+      if (mS) half += t[kf - PF];
+      if (mE && mN) half += t[kf + PF + 1];
+      if (mW && mS) half += t[kf - PF - 1];
+      C.b[w.k] = t[kf] + T(0.5) * half;
+    }
+    __syncthreads();
+  }
+  // the coarsest level: deg_coarse Chebyshev iterations from zero (k_coarse_solve's)
+  {
+    const LevelGeom& g = a.G[mc][trap];
+    const T* tab = a.tabs[mc] + (size_t)trap * kTabPerTrap;
+    const Interior<T> ci = interior<T>(g);
+    BottomLevel<T>& L = lv[mc];
+    for (int it = 0; it < a.deg_coarse; ++it) {
+      const ChebCoef cc = cheb_at(g, it);
+      const View<T> xi{L.x, 0};
+      for (NodeWalk w(g, 0); w.k < L.n; w.next()) {
+        T id;
+        const T ax = apply_tab<T>(g, ci, tab, xi, w.k, w.i, w.j, id);
+        T dn = (T(cc.c_res) * (L.b[w.k] - ax)) * id;
+        if (it > 0) dn = fma_(T(cc.c_old), L.d[w.k], dn);
+        L.d[w.k] = dn;
+        L.y[w.k] = add_(L.x[w.k], dn);
+      }
+      __syncthreads();
+      T* t = L.x;
+      L.x = L.y;
+      L.y = t;
+    }
+  }
+  // up: prolongation (k_prolong's), post-smoothing
+  for (int m = mc - 1; m >= 0; --m) {
+    const LevelGeom& g = a.G[m][trap];
+    const LevelGeom& gc = a.G[m + 1][trap];
+    const T* tab = a.tabs[m] + (size_t)trap * kTabPerTrap;
+    const Interior<T> ci = interior<T>(g);
+    BottomLevel<T>& L = lv[m];
+    const T* xc = lv[m + 1].x;
+    const int PC = gc.P;
+    for (NodeWalk w(g, 0); w.k < L.n; w.next()) {
+      if (w.j > g.nx) continue;  // pad column stays zero
+      int i0, i1, j0, j1;
+      fine_to_coarse(w.i, g.ny, gc.cy, i0, i1);
+      fine_to_coarse(w.j, g.nx, gc.cx, j0, j1);
+      T v;
+      if (i0 == i1 && j0 == j1)
+        v = xc[j0 + i0 * PC];
+      else if (i0 == i1)
+        v = T(0.5) * (xc[j0 + i0 * PC] + xc[j1 + i0 * PC]);
+      else if (j0 == j1)
+        v = T(0.5) * (xc[j0 + i0 * PC] + xc[j0 + i1 * PC]);
+      else
+        v = T(0.5) * (xc[j0 + i0 * PC] + xc[j1 + i1 * PC]);  // on the coarse diagonal
+      L.x[w.k] += v;
+    }
+    __syncthreads();
+    // post-smoothing as k_up does it: x1 = x0 + c0 D^-1 (b - A x0), then
+    // x2 = x1 + c_old (x1 - x0) + c1 D^-1 (b - A x1), the direction recomputed as x1 - x0
+    bottom_sweep<T>(g, ci, tab, cheb_at(g, 0), true, L.b, L.x, L.y, L.d, L.n);
+    {
+      const ChebCoef cc = cheb_at(g, 1);
+      const View<T> x1v{L.y, 0};
+      for (NodeWalk w(g, 0); w.k < L.n; w.next()) {
+        T id;
+        const T ax = apply_tab<T>(g, ci, tab, x1v, w.k, w.i, w.j, id);
+        const T x1 = L.y[w.k], x0 = L.x[w.k];
+        L.x[w.k] = x1 + cheb_dir<T, false>(cc, L.b[w.k], ax, id, x1 - x0);  // own node only
+      }
+      __syncthreads();
+    }
+  }
+  T* out = x0 + g0.off;
+  for (int k = threadIdx.x; k < lv[0].n; k += blockDim.x) out[k] = lv[0].x[k];
 }
 
 // ---------------------------------------------------------------------------

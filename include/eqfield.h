@@ -86,7 +86,12 @@ typedef struct eqf_solver_opts {
   int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
   int32_t tile_nodes; /* target nodes per row tile of the finest level (0: default) */
   int32_t krylov;     /* EQF_KRYLOV_*: AUTO = BiCGSTAB iff some trap has advection */
-  int32_t fuse_levels; /* temporally blocked V(2,2) level kernels where they fit (1) */
+  int32_t fuse_levels; /* 0: step-by-step V-cycle kernels; 1 (default): temporally
+                        * blocked V(2,2) level kernels where they fit; 2: also the levels
+                        * from the first whose grids fit one CTA's shared memory down to
+                        * the coarsest in one kernel, one CTA per trap (bit-identical to
+                        * 1; slower on large uneven batches, where the largest trap's
+                        * CTA sets the time) */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;

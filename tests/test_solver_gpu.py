@@ -233,12 +233,13 @@ def test_batched_sample_against_oracle(lib):
 
 @pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
 def test_fused_and_unfused_level_kernels_agree(lib, precision):
-    """The temporally blocked level kernels (default) and the step-by-step kernels
-    solve the same systems: both meet the oracle's tolerance and agree closely."""
+    """The one-kernel bottom levels, the temporally blocked level kernels (default)
+    and the step-by-step kernels solve the same systems: all meet the oracle's
+    tolerance and agree closely."""
     t = wl.scaled(wl.single_large(1), 256, 128, n_cells=2000)
     ref = hsld.run_trap(t, steps=12)
     out = []
-    for fuse in (1, 0):
+    for fuse in (2, 1, 0):
         with F.TrapBatch([tparams(t)], F.default_opts(precision, use_graph=1,
                                                       fuse_levels=fuse)) as b:
             b.set_cells(0, t.cell_xy, t.cell_s)
@@ -246,4 +247,38 @@ def test_fused_and_unfused_level_kernels_agree(lib, precision):
             u = b.read_nodal(0)
             assert rel(u, ref["u"][0]) <= TOL[precision]
             out.append(u)
-    assert rel(out[0], out[1]) <= TOL[precision]
+    assert rel(out[0], out[2]) <= TOL[precision]
+    assert rel(out[1], out[2]) <= TOL[precision]
+
+
+def test_bottom_levels_kernel_on_uneven_traps(lib):
+    """Uneven traps of a batch share the level count; the one-kernel bottom levels
+    (per trap, in shared memory) give the step-by-step path's solution."""
+    traps = wl.batched_uneven(6, 6)
+    res = []
+    for fuse in (2, 0):
+        with F.TrapBatch([tparams(t) for t in traps],
+                         F.default_opts(F.FP32_IR, use_graph=1, fuse_levels=fuse)) as b:
+            for i, t in enumerate(traps):
+                b.set_cells(i, t.cell_xy, t.cell_s)
+            b.step(5)
+            res.append([b.read_nodal(i) for i in range(len(traps))])
+    for a, c in zip(res[0], res[1]):
+        assert rel(a, c) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
+def test_bottom_levels_kernel_is_bit_identical_to_level_kernels(lib, precision):
+    """The one-kernel bottom levels evaluate the fused level kernels' expressions on
+    the same operands: the same bits whichever level the batch starts it at."""
+    traps = wl.batched_uneven(3, 4)
+    res = []
+    for fuse in (2, 1):
+        with F.TrapBatch([tparams(t) for t in traps],
+                         F.default_opts(precision, use_graph=1, fuse_levels=fuse)) as b:
+            for i, t in enumerate(traps):
+                b.set_cells(i, t.cell_xy, t.cell_s)
+            b.step(4)
+            res.append([b.read_nodal(i) for i in range(len(traps))])
+    for a, c in zip(res[0], res[1]):
+        assert np.array_equal(a, c)
