@@ -262,6 +262,7 @@ struct Level {
   size_t sm_cheb = 0, sm_resid = 0, sm_cgdir = 0, sm_ir = 0;
   size_t sm_irf1 = 0, sm_irf = 0;  // pair-arithmetic refinement residuals (FP32 form)
   size_t sm_down = 0, sm_up = 0;   // fused level kernels (0: not built for this level)
+  int ntiles2_cls = 0;  // tiles2[0, ntiles2_cls): class-table traps; the rest general-path
 
   size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
   size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
@@ -776,6 +777,7 @@ void Batch::build_levels() {
       opts.tile_nodes > 0 ? opts.tile_nodes : (tsz == 4 ? kTileNodes : kTileNodes / 2);
   for (int l = 0; l < nlev; ++l) {
     long long off = 0;
+    std::vector<Tile2> gen2;  // 2-D tiles of general-path traps: after the others
     for (int t = 0; t < ntraps; ++t) {
       LevelGeom& g = L[l].geom[t];
       g.off = off;
@@ -797,10 +799,13 @@ void Batch::build_levels() {
       const int R2 = (int)std::max<long long>(2, tgt / CW);
       for (int r0 = 0; r0 <= g.ny; r0 += R2)
         for (int c0 = 0; c0 < P; c0 += CW)
-          L[l].tiles2.push_back(Tile2{t, r0, std::min(g.ny + 1, r0 + R2), c0,
-                                      (int)std::min<long long>(P, c0 + CW)});
+          (g.adv_on ? gen2 : L[l].tiles2)
+              .push_back(Tile2{t, r0, std::min(g.ny + 1, r0 + R2), c0,
+                               (int)std::min<long long>(P, c0 + CW)});
       off = align_up(off + n, 32);
     }
+    L[l].ntiles2_cls = (int)L[l].tiles2.size();
+    L[l].tiles2.insert(L[l].tiles2.end(), gen2.begin(), gen2.end());
     L[l].nodes = off;
     if (off >= (1ll << 31)) throw Error(EQF_ERR_INVALID, "batch too large for 32-bit node indices");
     L[l].dgeom.alloc(ntraps);
@@ -1003,9 +1008,12 @@ static void allow_dyn_smem() {
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
   smem_attrs(k_irf_first, mx);
-  smem_attrs(k_down<T>, mx);
-  smem_attrs(k_up<T, true>, mx);
-  smem_attrs(k_up<T, false>, mx);
+  smem_attrs(k_down<T, false>, mx);
+  smem_attrs(k_down<T, true>, mx);
+  smem_attrs(k_up<T, true, false>, mx);
+  smem_attrs(k_up<T, false, false>, mx);
+  smem_attrs(k_up<T, true, true>, mx);
+  smem_attrs(k_up<T, false, true>, mx);
   smem_attrs(k_apply_dot<T, 1>, mx);
   smem_attrs(k_apply_dot<T, 2>, mx);
   smem_attrs(k_irf_residual<true>, mx);
@@ -1154,23 +1162,38 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
       Lv_.sm_down > 0) {
     // temporally blocked: pre-smoothing + residual, restriction, coarse correction,
     // prolongation + post-smoothing
-    const int nt2 = (int)Lv_.tiles2.size();
-    EQF_RUN(B, lev > 0 ? KC_COARSE : KC_DOWN0,
-            (launch_pdl(k_down<T>, nt2, kThreads, Lv_.sm_down, s, G, Lv_.dtiles2.p, tab, skip, bl, cur,
-                                                           v.t.p, W)));
+    // class-table traps' tiles first, general-path traps' tiles after: one kernel each
+    const int nc2 = Lv_.ntiles2_cls, ng2 = (int)Lv_.tiles2.size() - nc2;
+    const Tile2* tc2 = Lv_.dtiles2.p;
+    const Tile2* tg2 = Lv_.dtiles2.p + nc2;
+    const int cd = lev > 0 ? KC_COARSE : KC_DOWN0, cu = lev > 0 ? KC_COARSE : KC_UP0;
+    if (nc2 > 0)
+      EQF_RUN(B, cd, (launch_pdl(k_down<T, false>, nc2, kThreads, Lv_.sm_down, s, G, tc2, tab,
+                                 skip, bl, cur, v.t.p, W)));
+    if (ng2 > 0)
+      EQF_RUN(B, cd, (launch_pdl(k_down<T, true>, ng2, kThreads, Lv_.sm_down, s, G, tg2, tab,
+                                 skip, bl, cur, v.t.p, W)));
     const Level& Lc = B.L[lev + 1];
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
-            (launch_pdl(k_restrict<T>, Lc.ntiles(), kThreads, Lc.sm_restrict, s, 
-                Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
+            (launch_pdl(k_restrict<T>, Lc.ntiles(), kThreads, Lc.sm_restrict, s,
+                        Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
     T* xc = vcycle(s, lev + 1, false);
-    if (dot)
-      EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
-              (launch_pdl(k_up<T, true>, nt2, kThreads, Lv_.sm_up, s, G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
-                                                             skip, xc, bl, cur, oth, part, W)));
-    else
-      EQF_RUN(B, lev > 0 ? KC_COARSE : KC_UP0,
-              (launch_pdl(k_up<T, false>, nt2, kThreads, Lv_.sm_up, s, G, Lc.dgeom.p, Lv_.dtiles2.p, tab,
-                                                              skip, xc, bl, cur, oth, part, W)));
+    // the dot partials of a tile go to part[its index in tiles2]
+    if (dot) {
+      if (nc2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, true, false>, nc2, kThreads, Lv_.sm_up, s, G,
+                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, true, true>, ng2, kThreads, Lv_.sm_up, s, G,
+                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2, W)));
+    } else {
+      if (nc2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, false, false>, nc2, kThreads, Lv_.sm_up, s, G,
+                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, false, true>, ng2, kThreads, Lv_.sm_up, s, G,
+                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2, W)));
+    }
     return oth;
   }
   // pre-smoothing (or the coarsest-level solve) from zero

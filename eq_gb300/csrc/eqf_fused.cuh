@@ -27,6 +27,12 @@
 
 namespace eqf {
 
+// GEN: the kernel runs on the tiles of general-path traps (advection, anisotropic
+// tensor: per-node weights fetched inline); otherwise on the tiles of class-table traps
+// only, so the class-table kernels carry no general path at all.
+template <bool GEN>
+constexpr int kGM = GEN ? 2 : 1;  // apply_quad's border weights for a GEN kernel
+
 // Resident CTAs per SM the fused kernels are compiled for.
 template <class T>
 constexpr int kFusedCtas = sizeof(T) == 4 ? 3 : 2;
@@ -175,7 +181,7 @@ __device__ __forceinline__ QuadBlock win_quads(const Win& w) {
 }
 
 // 1 / diagonal of the quad's nodes (the same values every stencil path uses).
-template <class T>
+template <class T, int GM>
 __device__ __forceinline__ Q4<T> inv_diag_quad(const LevelGeom& g, const Interior<T>& ci,
                                                const T* __restrict__ stab, int i, int j0,
                                                bool inner) {
@@ -186,9 +192,12 @@ __device__ __forceinline__ Q4<T> inv_diag_quad(const LevelGeom& g, const Interio
   } else {
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      if (g.adv_on) {
+      if (GM == 2 || (GM == 0 && g.adv_on)) {
         T c[8];
-        coef_general<T>(g, i, j0 + e, c);
+        if (GM == 2)
+          coef_node<T>(g, i, j0 + e, c);
+        else
+          coef_general<T>(g, i, j0 + e, c);
         id.v[e] = c[7];
       } else {
         id.v[e] = stab[node_class_clamped(g, i, j0 + e) * kTabStride + 7];
@@ -204,7 +213,7 @@ __device__ __forceinline__ int wl(const Win& w, int i, int j) {
 }
 
 // Pre-smoothing (two steps from zero) and residual of one tile.
-template <class T>
+template <class T, bool GEN>
 __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
@@ -236,7 +245,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     constexpr bool INNER = decltype(inner_)::value;
     const int j = w1.ca + 4 * cq, kl = (i - w1.ra) * S1 + 4 * cq;
     const Q4<T> bq = vld4<T>(bp + kl);
-    const Q4<T> id = inv_diag_quad<T>(g, ci, stab, i, j, INNER);
+    const Q4<T> id = inv_diag_quad<T, kGM<GEN>>(g, ci, stab, i, j, INNER);
     Q4<T> d;
 #pragma unroll
     for (int e = 0; e < 4; ++e) d.v[e] = (T(c0.c_res) * bq.v[e]) * id.v[e];
@@ -250,7 +259,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       constexpr bool INNER = decltype(inner_)::value;
       const int j = w2.ca + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w1, i, j), S1, i, j, INNER, xc, id);
+      const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, x1v,
+          wl(w1, i, j), S1, i, j, INNER, xc, id);
       const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> xn;
 #pragma unroll
@@ -269,7 +279,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       constexpr bool INNER = decltype(inner_)::value;
       const int j = tile.c0 + 4 * cq;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x2v, wl(w2, i, j), S2, i, j, INNER, xc, id);
+      const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, x2v,
+          wl(w2, i, j), S2, i, j, INNER, xc, id);
       const Q4<T> bq = vld4<T>(bp + wl(w1, i, j));
       Q4<T> r;
 #pragma unroll
@@ -284,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
 // Prolongation and post-smoothing (two steps) of one tile: reads x (xin) and the
 // coarse correction, writes x2 to xout (another buffer: neighbouring tiles still
 // stage xin).  DOT adds a partial of b.x2 (r.z of the Krylov iteration).
-template <class T, bool DOT>
+template <class T, bool DOT, bool GEN>
 __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_up(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
          const Tile2* __restrict__ tiles, const T* __restrict__ tabs,
@@ -369,7 +380,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       constexpr bool INNER = decltype(inner_)::value;
       const int j = w2.ca + 4 * cq, kl = (i - w2.ra) * S2 + 4 * cq;
       Q4<T> x0q, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, wl(w1, i, j), S1, i, j, INNER, x0q, id);
+      const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, xv,
+          wl(w1, i, j), S1, i, j, INNER, x0q, id);
       const Q4<T> bq = vld4<T>(bp + kl);
       Q4<T> xn;
 #pragma unroll
@@ -388,7 +400,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       constexpr bool INNER = decltype(inner_)::value;
       const int j = tile.c0 + 4 * cq;
       Q4<T> x1q, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, x1v, wl(w2, i, j), S2, i, j, INNER, x1q, id);
+      const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, x1v,
+          wl(w2, i, j), S2, i, j, INNER, x1q, id);
       const Q4<T> bq = vld4<T>(bp + wl(w2, i, j));
       const Q4<T> x0q = vld4<T>(xp + wl(w1, i, j));
       Q4<T> xn;

@@ -621,7 +621,12 @@ __device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
 // last cells, advection traps) take per-node weights from the staged class table.
 // PM = P mod 4, the row misalignment of the neighbour rows (0: device rows are
 // padded to a multiple of 4 nodes); x's base index is a multiple of 4.
-template <class T, int PM, class X>
+// GM selects the border path's weights: 0 the general path when the trap has one
+// (g.adv_on), else the class table; 1 the class table only (kernels launched on the
+// tiles of class-table traps); 2 the general path only, fetched inline (kernels
+// launched on the tiles of general-path traps: the fetch's registers stay out of the
+// class-table kernels).
+template <class T, int PM, class X, int GM = 0>
 __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T>& ci,
                                             const T* __restrict__ stab, const X& x, int k,
                                             int P, int i0, int j0, bool inner, Q4<T>& xc,
@@ -647,9 +652,12 @@ __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T
       quad_node(P, i0, j0, e, i, j);
       const T w = e == 0 ? xw : xc.v[e - 1];
       const T ee = e == 3 ? xe : xc.v[e + 1];
-      if (g.adv_on) {
-        T c[8];  // general rows, out of line (an inline fetch spills the isotropic
-        coef_general<T>(g, i, j, c);  // quad path): advective or anisotropic traps only
+      if (GM == 2 || (GM == 0 && g.adv_on)) {
+        T c[8];  // general rows: out of line in shared kernels (an inline fetch spills
+        if (GM == 2)  // the class-table path), inline in the general-path kernels
+          coef_node<T>(g, i, j, c);
+        else
+          coef_general<T>(g, i, j, c);
         ax.v[e] = st_table(c, xc.v[e], ee, w, nr[e], sr[e + 1], nr[e + 1], sr[e]);
         id.v[e] = c[7];
       } else {
