@@ -263,6 +263,7 @@ struct Level {
   size_t sm_irf1 = 0, sm_irf = 0;  // pair-arithmetic refinement residuals (FP32 form)
   size_t sm_down = 0, sm_up = 0;   // fused level kernels (0: not built for this level)
   int ntiles2_cls = 0;  // tiles2[0, ntiles2_cls): class-table traps; the rest general-path
+  int ntiles_cls = 0;   // the same split of the row tiles
 
   size_t sm_restrict = 0;  // restriction into this level (tiles of this level)
   size_t sm_prolong = 0;   // prolongation from the next coarser level (tiles of this level)
@@ -777,6 +778,7 @@ void Batch::build_levels() {
       opts.tile_nodes > 0 ? opts.tile_nodes : (tsz == 4 ? kTileNodes : kTileNodes / 2);
   for (int l = 0; l < nlev; ++l) {
     long long off = 0;
+    std::vector<Tile> gen1;   // row tiles of general-path traps: after the others
     std::vector<Tile2> gen2;  // 2-D tiles of general-path traps: after the others
     for (int t = 0; t < ntraps; ++t) {
       LevelGeom& g = L[l].geom[t];
@@ -792,7 +794,7 @@ void Batch::build_levels() {
       const int R = (int)std::max<long long>(1, tgt / P);
       for (int r0 = 0; r0 <= g.ny; r0 += R) {
         const int r1 = std::min(g.ny + 1, r0 + R);
-        L[l].tiles.push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
+        (g.adv_on ? gen1 : L[l].tiles).push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
       }
       // 2-D tiles of the fused kernels: column blocks of at most 128 nodes
       const int CW = (int)std::min<long long>(128, P);
@@ -804,6 +806,8 @@ void Batch::build_levels() {
                                (int)std::min<long long>(P, c0 + CW)});
       off = align_up(off + n, 32);
     }
+    L[l].ntiles_cls = (int)L[l].tiles.size();
+    L[l].tiles.insert(L[l].tiles.end(), gen1.begin(), gen1.end());
     L[l].ntiles2_cls = (int)L[l].tiles2.size();
     L[l].tiles2.insert(L[l].tiles2.end(), gen2.begin(), gen2.end());
     L[l].nodes = off;
@@ -1002,8 +1006,10 @@ static void allow_dyn_smem() {
   smem_attrs(k_restrict<T>, mx);
   smem_attrs(k_prolong<T>, mx);
   smem_attrs(k_coarse_solve<T>, mx);
-  smem_attrs(k_cg_dir<T, true>, mx);
-  smem_attrs(k_cg_dir<T, false>, mx);
+  smem_attrs(k_cg_dir<T, true, false>, mx);
+  smem_attrs(k_cg_dir<T, false, false>, mx);
+  smem_attrs(k_cg_dir<T, true, true>, mx);
+  smem_attrs(k_cg_dir<T, false, true>, mx);
   smem_attrs(k_ir_first<T>, mx);
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
@@ -1288,14 +1294,29 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
     EQF_RUN(B, KC_SCALAR,
             (launch_pdl(k_s_rz, nb, 128, 0, s, B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
                                        B.dstate.p, B.d_cg_skip.p)));
-    if (it == 0)
-      EQF_RUN(B, KC_CG_DIR,
-              (launch_pdl(k_cg_dir<T, true>, nt, kThreads, L0.sm_cgdir, s, 
-                  G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
-    else
-      EQF_RUN(B, KC_CG_DIR,
-              (launch_pdl(k_cg_dir<T, false>, nt, kThreads, L0.sm_cgdir, s, 
-                  G, tl, tab, B.d_cg_skip.p, B.dstate.p, z, pin, pout, q.p, part, W)));
+    {  // class-table traps' row tiles, then general-path traps' (part by tile index)
+      const int nc = L0.ntiles_cls, ng = nt - nc;
+      int* sk = B.d_cg_skip.p;
+      CgState* cs = B.dstate.p;
+      if (it == 0) {
+        if (nc > 0)
+          EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, true, false>, nc, kThreads, L0.sm_cgdir,
+                                            s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, W)));
+        if (ng > 0)
+          EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, true, true>, ng, kThreads, L0.sm_cgdir, s,
+                                            G, tl + nc, tab, sk, cs, z, pin, pout, q.p,
+                                            part + nc, W)));
+      } else {
+        if (nc > 0)
+          EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, false, false>, nc, kThreads,
+                                            L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout,
+                                            q.p, part, W)));
+        if (ng > 0)
+          EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, false, true>, ng, kThreads,
+                                            L0.sm_cgdir, s, G, tl + nc, tab, sk, cs, z, pin,
+                                            pout, q.p, part + nc, W)));
+      }
+    }
     EQF_RUN(B, KC_SCALAR,
             (launch_pdl(k_s_pq, nb, 128, 0, s, B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
     EQF_RUN(B, KC_CG_UPDATE,

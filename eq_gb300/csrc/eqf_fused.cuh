@@ -30,9 +30,6 @@ namespace eqf {
 // GEN: the kernel runs on the tiles of general-path traps (advection, anisotropic
 // tensor: per-node weights fetched inline); otherwise on the tiles of class-table traps
 // only, so the class-table kernels carry no general path at all.
-template <bool GEN>
-constexpr int kGM = GEN ? 2 : 1;  // apply_quad's border weights for a GEN kernel
-
 // Resident CTAs per SM the fused kernels are compiled for.
 template <class T>
 constexpr int kFusedCtas = sizeof(T) == 4 ? 3 : 2;

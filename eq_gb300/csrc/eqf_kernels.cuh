@@ -626,6 +626,8 @@ __device__ __forceinline__ int qhalo_hi(const LevelGeom& g, const Tile& t) {
 // tiles of class-table traps); 2 the general path only, fetched inline (kernels
 // launched on the tiles of general-path traps: the fetch's registers stay out of the
 // class-table kernels).
+template <bool GEN>
+constexpr int kGM = GEN ? 2 : 1;  // apply_quad's border weights for a GEN kernel
 template <class T, int PM, class X, int GM = 0>
 __device__ __forceinline__ Q4<T> apply_quad(const LevelGeom& g, const Interior<T>& ci,
                                             const T* __restrict__ stab, const X& x, int k,
@@ -1253,7 +1255,9 @@ struct PNew {  // p_out = z + beta p_in evaluated on the fly from the staged z, 
   }
 };
 
-template <class T, bool FIRST>
+// GEN: launched on the tiles of general-path traps (inline stencil fetch), else on
+// the tiles of class-table traps only (see apply_quad).
+template <class T, bool FIRST, bool GEN>
 __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_cg_dir(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
              const T* __restrict__ tabs, const int* __restrict__ skip,
@@ -1291,7 +1295,8 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     constexpr bool INNER = decltype(inner_)::value;
     const int j = 4 * cq, k = i * P + j;
     Q4<T> pc, id;
-    const Q4<T> a = apply_quad<T, 0>(g, ci, stab, pnew, k, P, i, j, INNER, pc, id);
+    const Q4<T> a =
+        apply_quad<T, 0, PNew<T, FIRST>, kGM<GEN>>(g, ci, stab, pnew, k, P, i, j, INNER, pc, id);
 #pragma unroll
     for (int e = 0; e < 4; ++e) acc += pc.v[e] * a.v[e];
     vst4<T>(po + k, pc);
