@@ -998,10 +998,14 @@ static void smem_attrs(K kernel, int mx) {
 template <class T>
 static void allow_dyn_smem() {
   const int mx = (int)kMaxDynSmem;
-  smem_attrs(k_cheb<T, true, false, true>, mx);
-  smem_attrs(k_cheb<T, true, false, false>, mx);
-  smem_attrs(k_cheb<T, false, false, true>, mx);
-  smem_attrs(k_cheb<T, false, false, false>, mx);
+  smem_attrs(k_cheb<T, true, false, true, false>, mx);
+  smem_attrs(k_cheb<T, true, false, false, false>, mx);
+  smem_attrs(k_cheb<T, false, false, true, false>, mx);
+  smem_attrs(k_cheb<T, false, false, false, false>, mx);
+  smem_attrs(k_cheb<T, true, false, true, true>, mx);
+  smem_attrs(k_cheb<T, true, false, false, true>, mx);
+  smem_attrs(k_cheb<T, false, false, true, true>, mx);
+  smem_attrs(k_cheb<T, false, false, false, true>, mx);
   smem_attrs(k_resid<T>, mx);
   smem_attrs(k_restrict<T>, mx);
   smem_attrs(k_prolong<T>, mx);
@@ -1090,27 +1094,31 @@ static void cheb_step(Batch& B, cudaStream_t s, int lev, int nt, const LevelGeom
                       double* part) {
   const int cls = lev > 0 ? KC_COARSE : (zero ? KC_SMOOTH0_FIRST : KC_SMOOTH0);
   const size_t sm = zero ? 0 : B.L[lev].sm_cheb;
+  // class-table traps' row tiles, then general-path traps' (part by tile index)
+  const int nc = B.L[lev].ntiles_cls, ng = nt - nc;
+  auto run = [&](auto kc, auto kg, int step) {
+    if (nc > 0)
+      EQF_RUN(B, cls, (launch_pdl(kc, nc, kThreads, sm, s, G, tl, tab, skip, step, b, xin, xout,
+                                  d, part, W)));
+    if (ng > 0)
+      EQF_RUN(B, cls, (launch_pdl(kg, ng, kThreads, sm, s, G, tl + nc, tab, skip, step, b, xin,
+                                  xout, d, part + nc, W)));
+  };
   if (zero) {
     if (dot)
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, true, true>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
+      run(k_cheb<T, true, true, true, false>, k_cheb<T, true, true, true, true>, 0);
     else
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, true, false>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
+      run(k_cheb<T, true, true, false, false>, k_cheb<T, true, true, false, true>, 0);
   } else if (first) {
     if (dot)
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, false, true>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
+      run(k_cheb<T, true, false, true, false>, k_cheb<T, true, false, true, true>, 0);
     else
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, true, false, false>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, 0, b, xin, xout, d, part, W)));
+      run(k_cheb<T, true, false, false, false>, k_cheb<T, true, false, false, true>, 0);
   } else {
     if (dot)
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, false, false, true>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, st, b, xin, xout, d, part, W)));
+      run(k_cheb<T, false, false, true, false>, k_cheb<T, false, false, true, true>, st);
     else
-      EQF_RUN(B, cls, (launch_pdl(k_cheb<T, false, false, false>, nt, kThreads, sm, s, 
-                           G, tl, tab, skip, st, b, xin, xout, d, part, W)));
+      run(k_cheb<T, false, false, false, false>, k_cheb<T, false, false, false, true>, st);
   }
 }
 

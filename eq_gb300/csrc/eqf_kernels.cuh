@@ -412,10 +412,11 @@ __device__ __forceinline__ T apply_tab(const LevelGeom& g, const Interior<T>& ci
   return st_table(c, x0, xe, xw, xn, xs, xne, xsw);
 }
 
-template <class T>
+// GM as apply_quad's: 0 general path when the trap has one, 1 table only, 2 general only.
+template <class T, int GM = 0>
 __device__ __forceinline__ T inv_diag_tab(const LevelGeom& g, const Interior<T>& ci,
                                           const T* __restrict__ tab, int i, int j) {
-  if (g.adv_on) return inv_diag_general<T>(g, i, j);
+  if (GM == 2 || (GM == 0 && g.adv_on)) return inv_diag_general<T>(g, i, j);
   return is_uniform_interior(g, i, j) ? ci.ic : tab[node_class(g, i, j) * kTabStride + 7];
 }
 
@@ -739,7 +740,8 @@ __device__ __forceinline__ T cheb_dir(const ChebCoef& cc, T bk, T ax, T id, T do
 //   otherwise:       d = c_old d + c_res D^-1 (b - A x_in); x_out = x_in + d
 // The coefficients come from the level's Chebyshev table (the smoothing interval,
 // or the full interval on the coarsest level).  DOT adds a partial of b.x_out.
-template <class T, bool FIRST, bool ZERO, bool DOT>
+// GEN as k_cg_dir's: the launch covers general-path traps' tiles or class-table ones.
+template <class T, bool FIRST, bool ZERO, bool DOT, bool GEN>
 __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     k_cheb(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, int step,
@@ -775,7 +777,8 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
         for (int e = 0; e < 4; ++e) id.v[e] = ci.ic;
       } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) id.v[e] = inv_diag_tab<T>(g, ci, tab, i, 4 * cq + e);
+        for (int e = 0; e < 4; ++e)
+          id.v[e] = inv_diag_tab<T, kGM<GEN>>(g, ci, tab, i, 4 * cq + e);
       }
       Q4<T> dn;
 #pragma unroll
@@ -800,7 +803,8 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
       constexpr bool INNER = decltype(inner_)::value;
       const int j = 4 * cq, k = i * P + j;
       Q4<T> xc, id;
-      const Q4<T> ax = apply_quad<T, 0>(g, ci, stab, xv, k, P, i, j, INNER, xc, id);
+      const Q4<T> ax =
+          apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, xv, k, P, i, j, INNER, xc, id);
       const Q4<T> bq = bv.quad(k);
       const Q4<T> dq = FIRST ? bq : dv.quad(k);
       Q4<T> dn, xn;
