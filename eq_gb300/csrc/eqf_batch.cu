@@ -1815,15 +1815,13 @@ void Batch::run_step() {
 }
 
 void Batch::check_fail() {
-  int derr = 0;
+  int derr = 0, f = 0;  // both flags in one round trip
   EQF_CK(cudaMemcpyFromSymbolAsync(&derr, g_eqf_device_error, sizeof(int), 0,
                                    cudaMemcpyDeviceToHost, stream));
+  EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
   sync();
   if (derr)
     throw Error(EQF_ERR_CUDA, "a device-side bounded wait gave up (staging copy never landed)");
-  int f = 0;
-  EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  sync();
   if (f > 0) {
     EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
     throw Error(EQF_ERR_NOT_CONVERGED,
