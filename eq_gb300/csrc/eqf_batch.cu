@@ -272,6 +272,9 @@ struct Level {
 };
 
 constexpr size_t kSmemHeader = 16;              // mbarrier
+// Krylov iterations of a refinement sweep the host adds after a step missed rtol (the
+// graph's sweeps run opts.max_iters): such a sweep corrects a small residual.
+constexpr int kExtraSweepIters = 6;
 constexpr size_t kMaxDynSmem = 200 * 1024;      // per CTA budget for staged kernels
 
 // ---------------------------------------------------------------------------
@@ -327,7 +330,8 @@ struct Prof {
 
 struct WorkBase {
   virtual ~WorkBase() = default;
-  virtual void enqueue_sweep(cudaStream_t s, bool first) = 0;
+  // one refinement sweep of `iters` preconditioned Krylov iterations
+  virtual void enqueue_sweep(cudaStream_t s, bool first, int iters) = 0;
   virtual void enqueue_check(cudaStream_t s, bool update_gamma) = 0;
 };
 
@@ -343,10 +347,10 @@ struct Work : WorkBase {
   DevBuf<T> xs, p0, p1, q;  // fine CG: correction, directions, A p
   DevBuf<T> rh;             // BiCGSTAB shadow residual (only when BiCGSTAB is used)
   explicit Work(Batch& b);
-  void enqueue_sweep(cudaStream_t s, bool first) override;
+  void enqueue_sweep(cudaStream_t s, bool first, int iters) override;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
   T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr);
-  void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs);
+  void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs, int max_iters);
 };
 
 class Batch {
@@ -1245,7 +1249,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
 // One refinement sweep: FP64 residual, preconditioned CG on the correction,
 // update.  The step reads U[cur] and writes U[1 - cur].
 template <class T>
-void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
+void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
   const int nb = (B.ntraps + 127) / 128;
@@ -1289,7 +1293,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
                                      B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p, B.d_frozen.p)));
   EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   if (B.use_bicgstab) {
-    bicgstab(s, r, tol_rel, tol_abs);
+    bicgstab(s, r, tol_rel, tol_abs, iters);
     EQF_RUN(B, KC_IR_UPDATE,
             (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out, d_out,
                                                     W)));
@@ -1297,7 +1301,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
   }
   T* pin = p0.p;
   T* pout = p1.p;
-  for (int it = 0; it < B.opts.max_iters; ++it) {
+  for (int it = 0; it < iters; ++it) {
     T* z = vcycle(s, 0, true);
     EQF_RUN(B, KC_SCALAR,
             (launch_pdl(k_s_rz, nb, 128, 0, s, B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
@@ -1343,7 +1347,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first) {
 // V-cycle is the preconditioner); ceil(max_iters / 2) iterations of two
 // preconditioner applications each.
 template <class T>
-void Work<T>::bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs) {
+void Work<T>::bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs, int max_iters) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
   const int nb = (B.ntraps + 127) / 128;
@@ -1356,7 +1360,7 @@ void Work<T>::bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs) {
   T* p = p0.p;
   T* v = p1.p;
   T* t = q.p;
-  const int iters = (B.opts.max_iters + 1) / 2;
+  const int iters = (max_iters + 1) / 2;
   for (int it = 0; it < iters; ++it) {
     if (it == 0) {
       EQF_RUN(B, KC_CG_UPDATE,
@@ -1810,7 +1814,8 @@ void Batch::run_step() {
   enqueue_rods();
   enqueue_coupling();
   enqueue_walls();
-  for (int sw = 0; sw < opts.max_sweeps; ++sw) work->enqueue_sweep(stream, sw == 0);
+  for (int sw = 0; sw < opts.max_sweeps; ++sw)
+    work->enqueue_sweep(stream, sw == 0, opts.max_iters);
   work->enqueue_check(stream, true);
 }
 
@@ -1855,7 +1860,7 @@ void Batch::step(int n) {
         sync();
         if (f == 0) break;
         EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
-        work->enqueue_sweep(stream, false);
+        work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters));
         work->enqueue_check(stream, false);
       }
       if (f != 0) {
