@@ -131,7 +131,8 @@ class GpuFieldSolver EQFIELD_BASE {
 #endif
 
   // The reference writes DOLFIN .pvd files; this writes the nodal field in grid
-  // order as a JSON frame like the driver's externalHSL record (src/main.cpp:148-162).
+  // order as a JSON frame like the reference main program's externalHSL record
+  // (src/main.cpp:148-162).
   void writeDiffusionFiles(double timestamp) EQFIELD_OVERRIDE {
     if (filePath_.empty()) return;
     std::ofstream f(filePath_ + "_" + std::to_string(timestamp) + ".json");

@@ -1577,7 +1577,7 @@ __global__ void k_s_ir(int ntraps, const TileRange* __restrict__ range,
   st[t] = s;
 }
 
-// After the final check: convergence verdict and the next extrapolation factor
+// After the final check: the convergence outcome and the next extrapolation factor
 // gamma = |d_n| / |d_{n-1}| (clamped), from the increments of the last two steps.
 // update_gamma is 0 for the extra checks of adaptive sweeps: the factor belongs to
 // the step, so a trap's guess never depends on what the other traps needed.

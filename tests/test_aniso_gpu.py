@@ -91,3 +91,34 @@ def test_tensor_argument_errors(lib):
             b.set_tensor(0, np.ones(n), np.ones(n), np.full(n, 2.0))
         # all three fields or none
         assert b._lib.eqf_set_tensor(b._h, 0, F._dp(np.ones(n)), None, None) == -1
+
+
+@pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
+def test_mixed_batch_is_bit_identical_to_each_trap_alone(lib, precision):
+    """Class-table and general-path traps run as separate launches of the same level
+    kernels: a mixed batch gives every trap the bits it gets alone."""
+    base = wl.batched_uneven(7, 4)
+    traps = [wl.scaled(t, t.nx // 4 * 2, t.ny // 4 * 2, n_cells=60) for t in base]
+    tens = {1: smooth_field(traps[1].nx, traps[1].ny, traps[1].W, traps[1].H),
+            3: smooth_field(traps[3].nx, traps[3].ny, traps[3].W, traps[3].H, 0.5, 2.0)}
+    o = F.default_opts(precision, use_graph=1)
+
+    def tp(t):
+        return F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls)
+
+    alone = []
+    for i, t in enumerate(traps):
+        with F.TrapBatch([tp(t)], o) as b:
+            b.set_cells(0, t.cell_xy, t.cell_s)
+            if i in tens:
+                b.set_tensor(0, *tens[i])
+            b.step(4)
+            alone.append(b.read_nodal(0))
+    with F.TrapBatch([tp(t) for t in traps], o) as b:
+        for i, t in enumerate(traps):
+            b.set_cells(i, t.cell_xy, t.cell_s)
+            if i in tens:
+                b.set_tensor(i, *tens[i])
+        b.step(4)
+        for i in range(len(traps)):
+            assert np.array_equal(b.read_nodal(i), alone[i])
