@@ -442,6 +442,8 @@ class Batch {
     DevBuf<RodLawDev> dlaw;
     DevBuf<int> fp_off, fp_node, ent_cell, wave_cells, wave_off;
     DevBuf<int> cover, start, cursor, flag;  // wave analysis scratch
+    // more scratch, kept between analyses (grow-only: a cudaFree would synchronise)
+    DevBuf<int> sc_count, sc_perm, sc_pred, sc_succ, sc_wave, sc_wcount, sc_wstart;
     DevBuf<int4> winfo;     // wave order: (cell, footprint offset, size)
     DevBuf<double> cellk;   // per cell: volume constants
     DevBuf<double> ihsl, prod, ehsl;
@@ -538,6 +540,11 @@ class Batch {
   void sync() { EQF_CK(cudaStreamSynchronize(stream)); }
   void check_fail();
   void scan(int n, const int* in, int* out);
+  DevBuf<int> scan_sums;  // scan's block sums (grow-only)
+  template <class U>
+  static void grow(DevBuf<U>& b, size_t n) {
+    if (b.n < n) b.alloc(n + n / 4 + 64);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -1659,8 +1666,8 @@ Batch::RodSet* Batch::rod_set_of(int layer0) {
 void Batch::rod_analyse(RodSet& rs) {
   const int n = rs.n, bs = 256;
   rs.grid = std::max(1, std::min((n * 32 + bs - 1) / bs, num_sms * 16));
-  DevBuf<int> count;
-  count.alloc(n);
+  grow(rs.sc_count, n);
+  DevBuf<int>& count = rs.sc_count;
   k_rod_footprint<false><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, count.p, nullptr,
                                                      nullptr, nullptr);
   EQF_LAUNCH_CHECK();
@@ -1695,12 +1702,17 @@ void Batch::rod_analyse(RodSet& rs) {
     // bucket the entries by node, each bucket in cell order; wave = longest chain
     scan((int)rs.span, rs.cover.p, rs.start.p);
     EQF_CK(cudaMemsetAsync(rs.cursor.p, 0, rs.span * sizeof(int), stream));
-    DevBuf<int> perm, pred, succ, wave, wcount, wstart;
-    perm.alloc(nent);
-    pred.alloc(nent);
-    succ.alloc(nent);
-    wave.alloc(n);
-    wcount.alloc(n);
+    grow(rs.sc_perm, nent);
+    grow(rs.sc_pred, nent);
+    grow(rs.sc_succ, nent);
+    grow(rs.sc_wave, n);
+    grow(rs.sc_wcount, n);
+    DevBuf<int>& perm = rs.sc_perm;
+    DevBuf<int>& pred = rs.sc_pred;
+    DevBuf<int>& succ = rs.sc_succ;
+    DevBuf<int>& wave = rs.sc_wave;
+    DevBuf<int>& wcount = rs.sc_wcount;
+    DevBuf<int>& wstart = rs.sc_wstart;
     k_rod_place<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cursor.p, perm.p);
     EQF_LAUNCH_CHECK();
     k_rod_bucket_order<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cover.p,
@@ -1710,25 +1722,21 @@ void Batch::rod_analyse(RodSet& rs) {
                                        pred.p, succ.p);
     EQF_LAUNCH_CHECK();
     EQF_CK(cudaMemsetAsync(wave.p, 0, n * sizeof(int), stream));
-    for (int it = 0;; ++it) {
-      if (it > n) throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
-      int changed = 0;
-      EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
-      k_rod_relax<<<ge, bs, 0, stream>>>(nent, pred.p, succ.p, wave.p, rs.flag.p);
-      EQF_LAUNCH_CHECK();
-      EQF_CK(cudaMemcpyAsync(&changed, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-      sync();
-      if (!changed) break;
-    }
+    // the whole relaxation in one CTA (no host round trip per pass); flag[1] reports a
+    // relaxation that did not settle within its bound
+    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, 2 * sizeof(int), stream));
+    k_rod_relax_all<<<1, 1024, 0, stream>>>(nent, n, pred.p, succ.p, wave.p, rs.flag.p + 1);
+    EQF_LAUNCH_CHECK();
     EQF_CK(cudaMemsetAsync(wcount.p, 0, n * sizeof(int), stream));
-    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
     k_rod_wave_count<<<gc, bs, 0, stream>>>(n, wave.p, wcount.p, rs.flag.p);
     EQF_LAUNCH_CHECK();
-    int wmax = 0;
-    EQF_CK(cudaMemcpyAsync(&wmax, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    int fl[2] = {0, 0};  // highest wave, unsettled
+    EQF_CK(cudaMemcpyAsync(fl, rs.flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     sync();
+    if (fl[1]) throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
+    const int wmax = fl[0];
     const int waves = wmax + 1;
-    wstart.alloc(waves + 1);
+    grow(wstart, waves + 1);
     scan(waves, wcount.p, wstart.p);
     EQF_CK(cudaMemsetAsync(wcount.p, 0, waves * sizeof(int), stream));
     k_rod_wave_place<<<gc, bs, 0, stream>>>(n, wave.p, wstart.p, wcount.p, rs.wave_cells.p);
@@ -1882,15 +1890,13 @@ void Batch::step(int n) {
 void Batch::scan(int n, const int* in, int* out) {
   if (n <= 0) return;
   const int nb = (n + kScanTile - 1) / kScanTile;
-  DevBuf<int> sums;
-  sums.alloc(nb);
-  k_scan_sums<<<nb, kScanBlock, 0, stream>>>(n, in, sums.p);
+  grow(scan_sums, nb);  // stream-ordered reuse; callers sync before reading on the host
+  k_scan_sums<<<nb, kScanBlock, 0, stream>>>(n, in, scan_sums.p);
   EQF_LAUNCH_CHECK();
-  k_scan_top<<<1, kScanBlock, 0, stream>>>(nb, sums.p);
+  k_scan_top<<<1, kScanBlock, 0, stream>>>(nb, scan_sums.p);
   EQF_LAUNCH_CHECK();
-  k_scan_apply<<<nb, kScanBlock, 0, stream>>>(n, in, sums.p, out);
+  k_scan_apply<<<nb, kScanBlock, 0, stream>>>(n, in, scan_sums.p, out);
   EQF_LAUNCH_CHECK();
-  sync();
 }
 
 // Deterministic sort of entries by node: counting sort, then each bucket ordered
@@ -2879,7 +2885,7 @@ int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eq
     rs->cover.alloc(rs->span);
     rs->start.alloc(rs->span + 1);
     rs->cursor.alloc(rs->span);
-    rs->flag.alloc(1);
+    rs->flag.alloc(2);
     rs->ihsl.alloc(n4);
     rs->prod.alloc(n4);
     rs->ehsl.alloc(n4);

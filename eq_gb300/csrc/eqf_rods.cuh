@@ -235,16 +235,29 @@ __global__ void k_rod_preds(int nent, const int* __restrict__ node, long long ke
   pred[p] = start[key] == p ? -1 : ent_cell[perm[p - 1]];
 }
 
-// One relaxation of wave[c] = max over its predecessors of wave[pred] + 1.
-__global__ void k_rod_relax(int nent, const int* __restrict__ pred, const int* __restrict__ succ,
-                            int* __restrict__ wave, int* __restrict__ changed) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nent) return;
-  const int a = pred[p];
-  if (a < 0) return;
-  const int w = wave[a] + 1;
-  const int c = succ[p];
-  if (w > wave[c] && atomicMax(&wave[c], w) < w) *changed = 1;
+// The waves of one rod set in one CTA: passes of wave[c] = max over c's predecessors
+// of wave[pred] + 1, separated by CTA barriers, until a pass changes nothing.  A chain of n cells settles within n
+// passes; past that bound the kernel stops and sets *unsettled (never expected).
+__global__ void __launch_bounds__(1024)
+    k_rod_relax_all(int nent, int n, const int* __restrict__ pred, const int* __restrict__ succ,
+                    int* __restrict__ wave, int* __restrict__ unsettled) {
+  __shared__ int changed;
+  for (int pass = 0; pass <= n + 1; ++pass) {
+    if (threadIdx.x == 0) changed = 0;
+    __syncthreads();
+    for (int p = threadIdx.x; p < nent; p += blockDim.x) {
+      const int a = pred[p];
+      if (a < 0) continue;
+      // L2 reads: the other threads' updates are atomics performed there
+      const int w = __ldcg(&wave[a]) + 1;
+      const int c = succ[p];
+      if (w > __ldcg(&wave[c]) && atomicMax(&wave[c], w) < w) changed = 1;
+    }
+    __syncthreads();  // this pass's waves are visible to the whole CTA
+    if (!changed) return;
+    __syncthreads();  // every thread has read `changed` before it is reset
+  }
+  if (threadIdx.x == 0) *unsettled = 1;
 }
 
 // wave sizes and the highest wave
