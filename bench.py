@@ -457,7 +457,7 @@ def run_rods(args, rank, world, local_rank):
     b.close()
     # e2e through the public API: every step the host re-sends every rod's geometry
     # (the agent-based model moved them; footprints and waves are recomputed), steps,
-    # and reads every cell's intracellular and gathered HSL back
+    # and reads every cell's intracellular and gathered HSL back, all sets per call
     b = colony_batch(cols, opts)
     b.step(args.warmup)
     b.sync()
@@ -465,16 +465,11 @@ def run_rods(args, rank, world, local_rank):
     t0 = time.perf_counter()
     ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ee0.record(stream)
+    all_rods = np.concatenate([c.rods for c in cols])  # the colonies' sets in layer order
     for _ in range(args.steps):
-        t = 0
-        for c in cols:
-            b.update_rods(t, c.rods)
-            t += c.n_layers
+        b.update_rods_all(all_rods)
         b.step(1)
-        t = 0
-        for c in cols:
-            b.read_rods(t)
-            t += c.n_layers
+        b.read_rods_all()
     ee1.record(stream)
     b.sync()
     e2e_ms = max(ee0.elapsed_time(ee1), (time.perf_counter() - t0) * 1e3)

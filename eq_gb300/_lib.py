@@ -34,6 +34,7 @@ EXPORTS = (
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
     "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
+    "eqf_update_rods_all", "eqf_read_rods_all",
     "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels", "eqf_set_well",
     "eqf_read_well", "eqf_set_tensor", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
     "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
@@ -163,6 +164,8 @@ def load() -> C.CDLL:
                                    C.c_void_p, dp, dp, P(C.c_uint8)]),
         "eqf_update_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, dp]),
         "eqf_read_rods": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp, dp, P(C.c_int32)]),
+        "eqf_update_rods_all": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, dp]),
+        "eqf_read_rods_all": (C.c_int, [C.c_void_p, C.c_int64, dp, dp, P(C.c_int32)]),
         "eqf_exchange_rods": (C.c_int, [C.c_void_p]),
         "eqf_set_boundaries": (C.c_int, [C.c_void_p, C.c_int32, P(Boundaries)]),
         "eqf_read_channels": (C.c_int, [C.c_void_p, C.c_int32, dp, dp]),

@@ -82,6 +82,29 @@ struct DevBuf {
   }
 };
 
+// Page-locked host memory, grow-only: asynchronous copies from and to it do not
+// synchronise the stream the way pageable copies do.
+template <class T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void grow(size_t count) {
+    if (count <= n) return;
+    if (p) cudaFreeHost(p);  // (waits for nothing: callers sync before growing)
+    p = nullptr;
+    n = 0;
+    const size_t cap = count + count / 4 + 64;
+    EQF_CK(cudaMallocHost(&p, cap * sizeof(T)));
+    n = cap;
+  }
+};
+
 constexpr int kTileNodes = 4096;
 constexpr int kMaxLevels = 16;
 
@@ -498,6 +521,12 @@ class Batch {
   int rod_launches = 0, rod_grid = 0;  // wave launches and blocks per set, as captured
   RodSet* rod_set_of(int layer0);
   void rod_analyse(RodSet& rs);
+  // footprints and waves of several sets, phase by phase over all of them (one host
+  // round trip per phase for the lot)
+  void rod_analyse_sets(const std::vector<RodSet*>& sets);
+  PinnedBuf<int> rod_hflags;  // per set: footprint size, shared flag, highest wave, unsettled
+  PinnedBuf<int> rod_hwoff;   // per set: wave offsets
+  PinnedBuf<unsigned char> rod_hstage;  // rods / production / readbacks of the batch calls
   void rod_publish();
   void enqueue_rods();
   void drop_graphs() {
@@ -1663,43 +1692,58 @@ Batch::RodSet* Batch::rod_set_of(int layer0) {
   return nullptr;
 }
 
-void Batch::rod_analyse(RodSet& rs) {
-  const int n = rs.n, bs = 256;
-  rs.grid = std::max(1, std::min((n * 32 + bs - 1) / bs, num_sms * 16));
-  grow(rs.sc_count, n);
-  DevBuf<int>& count = rs.sc_count;
-  k_rod_footprint<false><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, count.p, nullptr,
-                                                     nullptr, nullptr);
-  EQF_LAUNCH_CHECK();
-  scan(n, count.p, rs.fp_off.p);
-  int nent = 0;
-  EQF_CK(cudaMemcpyAsync(&nent, rs.fp_off.p + n, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  sync();
-  if ((size_t)nent > rs.fp_node.n) {
-    const size_t cap = (size_t)nent + (size_t)nent / 4 + 64;
-    rs.fp_node.alloc(cap);
-    rs.ent_cell.alloc(cap);
-  }
-  rs.nent = nent;
-  k_rod_footprint<true><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, nullptr,
-                                                    rs.fp_off.p, rs.fp_node.p, rs.ent_cell.p);
-  EQF_LAUNCH_CHECK();
-  // does any node lie in two footprints?
-  const int ge = (nent + bs - 1) / bs, gc = (n + bs - 1) / bs;
-  EQF_CK(cudaMemsetAsync(rs.cover.p, 0, rs.span * sizeof(int), stream));
-  EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
-  k_rod_cover<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.cover.p, rs.flag.p);
-  EQF_LAUNCH_CHECK();
-  int shared = 0;
-  EQF_CK(cudaMemcpyAsync(&shared, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  sync();
-  std::vector<int> woff;
-  if (!shared) {
-    k_rod_iota<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p);
+void Batch::rod_analyse(RodSet& rs) { rod_analyse_sets({&rs}); }
+
+// Footprints (sizes, then nodes), the shared-node test, the waves of the sets with
+// shared nodes and the wave offsets: each phase is queued for every set, then one
+// round trip brings the sizes the next phase needs.
+void Batch::rod_analyse_sets(const std::vector<RodSet*>& sets) {
+  const int bs = 256, ns = (int)sets.size();
+  if (ns == 0) return;
+  rod_hflags.grow(4 * (size_t)ns);  // per set: footprint size, shared, highest wave, unsettled
+  int* hf = rod_hflags.p;
+  for (int q = 0; q < ns; ++q) {
+    RodSet& rs = *sets[q];
+    const int n = rs.n;
+    rs.grid = std::max(1, std::min((n * 32 + bs - 1) / bs, num_sms * 16));
+    grow(rs.sc_count, n);
+    k_rod_footprint<false><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, rs.sc_count.p,
+                                                       nullptr, nullptr, nullptr);
     EQF_LAUNCH_CHECK();
-    woff = {0, n};
-  } else {
-    // bucket the entries by node, each bucket in cell order; wave = longest chain
+    scan(n, rs.sc_count.p, rs.fp_off.p);
+    EQF_CK(cudaMemcpyAsync(hf + 4 * q, rs.fp_off.p + n, sizeof(int), cudaMemcpyDeviceToHost,
+                           stream));
+  }
+  sync();
+  for (int q = 0; q < ns; ++q) {  // the footprints; does any node lie in two of them?
+    RodSet& rs = *sets[q];
+    const int n = rs.n, nent = hf[4 * q];
+    if ((size_t)nent > rs.fp_node.n) {
+      const size_t cap = (size_t)nent + (size_t)nent / 4 + 64;
+      rs.fp_node.alloc(cap);
+      rs.ent_cell.alloc(cap);
+    }
+    rs.nent = nent;
+    k_rod_footprint<true><<<rs.grid, bs, 0, stream>>>(n, rs.rods.p, rs.dlaw.p, nullptr,
+                                                      rs.fp_off.p, rs.fp_node.p, rs.ent_cell.p);
+    EQF_LAUNCH_CHECK();
+    const int ge = (nent + bs - 1) / bs;
+    EQF_CK(cudaMemsetAsync(rs.cover.p, 0, rs.span * sizeof(int), stream));
+    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
+    k_rod_cover<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.cover.p, rs.flag.p);
+    EQF_LAUNCH_CHECK();
+    EQF_CK(cudaMemcpyAsync(hf + 4 * q + 1, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost,
+                           stream));
+  }
+  sync();
+  bool any = false;
+  for (int q = 0; q < ns; ++q) {  // waves: bucket the entries by node, each bucket in
+    RodSet& rs = *sets[q];        // cell order; a cell's wave = its longest chain
+    hf[4 * q + 2] = hf[4 * q + 3] = 0;
+    if (!hf[4 * q + 1]) continue;
+    any = true;
+    const int n = rs.n, nent = rs.nent;
+    const int ge = (nent + bs - 1) / bs, gc = (n + bs - 1) / bs;
     scan((int)rs.span, rs.cover.p, rs.start.p);
     EQF_CK(cudaMemsetAsync(rs.cursor.p, 0, rs.span * sizeof(int), stream));
     grow(rs.sc_perm, nent);
@@ -1707,57 +1751,74 @@ void Batch::rod_analyse(RodSet& rs) {
     grow(rs.sc_succ, nent);
     grow(rs.sc_wave, n);
     grow(rs.sc_wcount, n);
-    DevBuf<int>& perm = rs.sc_perm;
-    DevBuf<int>& pred = rs.sc_pred;
-    DevBuf<int>& succ = rs.sc_succ;
-    DevBuf<int>& wave = rs.sc_wave;
-    DevBuf<int>& wcount = rs.sc_wcount;
-    DevBuf<int>& wstart = rs.sc_wstart;
-    k_rod_place<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cursor.p, perm.p);
+    k_rod_place<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cursor.p,
+                                       rs.sc_perm.p);
     EQF_LAUNCH_CHECK();
     k_rod_bucket_order<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.cover.p,
-                                              perm.p);
+                                              rs.sc_perm.p);
     EQF_LAUNCH_CHECK();
-    k_rod_preds<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, perm.p, rs.ent_cell.p,
-                                       pred.p, succ.p);
+    k_rod_preds<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.start.p, rs.sc_perm.p,
+                                       rs.ent_cell.p, rs.sc_pred.p, rs.sc_succ.p);
     EQF_LAUNCH_CHECK();
-    EQF_CK(cudaMemsetAsync(wave.p, 0, n * sizeof(int), stream));
+    EQF_CK(cudaMemsetAsync(rs.sc_wave.p, 0, n * sizeof(int), stream));
     // the whole relaxation in one CTA (no host round trip per pass); flag[1] reports a
     // relaxation that did not settle within its bound
     EQF_CK(cudaMemsetAsync(rs.flag.p, 0, 2 * sizeof(int), stream));
-    k_rod_relax_all<<<1, 1024, 0, stream>>>(nent, n, pred.p, succ.p, wave.p, rs.flag.p + 1);
+    k_rod_relax_all<<<1, 1024, 0, stream>>>(nent, n, rs.sc_pred.p, rs.sc_succ.p, rs.sc_wave.p,
+                                            rs.flag.p + 1);
     EQF_LAUNCH_CHECK();
-    EQF_CK(cudaMemsetAsync(wcount.p, 0, n * sizeof(int), stream));
-    k_rod_wave_count<<<gc, bs, 0, stream>>>(n, wave.p, wcount.p, rs.flag.p);
+    EQF_CK(cudaMemsetAsync(rs.sc_wcount.p, 0, n * sizeof(int), stream));
+    k_rod_wave_count<<<gc, bs, 0, stream>>>(n, rs.sc_wave.p, rs.sc_wcount.p, rs.flag.p);
     EQF_LAUNCH_CHECK();
-    int fl[2] = {0, 0};  // highest wave, unsettled
-    EQF_CK(cudaMemcpyAsync(fl, rs.flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-    sync();
-    if (fl[1]) throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
-    const int wmax = fl[0];
-    const int waves = wmax + 1;
-    grow(wstart, waves + 1);
-    scan(waves, wcount.p, wstart.p);
-    EQF_CK(cudaMemsetAsync(wcount.p, 0, waves * sizeof(int), stream));
-    k_rod_wave_place<<<gc, bs, 0, stream>>>(n, wave.p, wstart.p, wcount.p, rs.wave_cells.p);
-    EQF_LAUNCH_CHECK();
-    woff.resize(waves + 1);
-    EQF_CK(cudaMemcpyAsync(woff.data(), wstart.p, (waves + 1) * sizeof(int),
-                           cudaMemcpyDeviceToHost, stream));
-    sync();
+    EQF_CK(cudaMemcpyAsync(hf + 4 * q + 2, rs.flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                           stream));
   }
-  k_rod_cell_info<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p, rs.fp_off.p, rs.rods.p, rs.dlaw.p,
-                                         rs.winfo.p, rs.cellk.p);
-  EQF_LAUNCH_CHECK();
-  rs.waves = (int)woff.size() - 1;
-  if (rs.wave_off.n < woff.size()) rs.wave_off.alloc(woff.size() + 8);
-  EQF_CK(cudaMemcpyAsync(rs.wave_off.p, woff.data(), woff.size() * sizeof(int),
-                         cudaMemcpyHostToDevice, stream));
-  sync();
+  if (any) sync();
+  // wave offsets: {0, n} when no node is shared, else the scan of the wave sizes
+  std::vector<size_t> wo(ns + 1, 0);
+  for (int q = 0; q < ns; ++q) {
+    if (hf[4 * q + 1] && hf[4 * q + 3])
+      throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
+    wo[q + 1] = wo[q] + (hf[4 * q + 1] ? (size_t)hf[4 * q + 2] + 2 : 2);
+  }
+  rod_hwoff.grow(wo[ns]);
+  int* hw = rod_hwoff.p;
+  for (int q = 0; q < ns; ++q) {
+    RodSet& rs = *sets[q];
+    const int n = rs.n, gc = (n + bs - 1) / bs;
+    if (!hf[4 * q + 1]) {
+      k_rod_iota<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p);
+      EQF_LAUNCH_CHECK();
+      hw[wo[q]] = 0;
+      hw[wo[q] + 1] = n;
+    } else {
+      const int waves = hf[4 * q + 2] + 1;
+      grow(rs.sc_wstart, waves + 1);
+      scan(waves, rs.sc_wcount.p, rs.sc_wstart.p);
+      EQF_CK(cudaMemsetAsync(rs.sc_wcount.p, 0, waves * sizeof(int), stream));
+      k_rod_wave_place<<<gc, bs, 0, stream>>>(n, rs.sc_wave.p, rs.sc_wstart.p, rs.sc_wcount.p,
+                                              rs.wave_cells.p);
+      EQF_LAUNCH_CHECK();
+      EQF_CK(cudaMemcpyAsync(hw + wo[q], rs.sc_wstart.p, (waves + 1) * sizeof(int),
+                             cudaMemcpyDeviceToHost, stream));
+    }
+  }
+  if (any) sync();
+  for (int q = 0; q < ns; ++q) {
+    RodSet& rs = *sets[q];
+    const int n = rs.n, gc = (n + bs - 1) / bs;
+    k_rod_cell_info<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p, rs.fp_off.p, rs.rods.p,
+                                           rs.dlaw.p, rs.winfo.p, rs.cellk.p);
+    EQF_LAUNCH_CHECK();
+    const size_t len = wo[q + 1] - wo[q];
+    rs.waves = (int)len - 1;
+    if (rs.wave_off.n < len) rs.wave_off.alloc(len + 8);
+    EQF_CK(cudaMemcpyAsync(rs.wave_off.p, hw + wo[q], len * sizeof(int), cudaMemcpyHostToDevice,
+                           stream));
+  }
+  sync();  // the pinned staging is reused by the next analysis
 }
 
-// Device descriptors of every rod set.  A captured step holds only the descriptor
-// array, the launch count and the grid: it is re-captured when one of those changes.
 void Batch::rod_publish() {
   std::vector<RodSetDev> h;
   int waves = 0, grid = 1;
@@ -2966,6 +3027,116 @@ int eqf_read_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, double* ihsl, d
         if (ehsl) ehsl[c * nl + l] = he[c * eqf::kRodLayers + l];
       }
       if (points) points[c] = off[c + 1] - off[c];
+    }
+  });
+}
+
+// The batch's rod sets in increasing order of their first layer.
+static std::vector<Batch::RodSet*> rod_sets_by_layer(Batch& B) {
+  std::vector<Batch::RodSet*> v;
+  for (auto& up : B.rod_sets) v.push_back(up.get());
+  std::sort(v.begin(), v.end(), [](const Batch::RodSet* a, const Batch::RodSet* b) {
+    return a->layers[0] < b->layers[0];
+  });
+  return v;
+}
+
+int eqf_update_rods_all(eqf_batch* b, int64_t n_total, const eqf_rod* rods,
+                        const double* production) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    const std::vector<Batch::RodSet*> sets = rod_sets_by_layer(B);
+    int64_t tot = 0, totp = 0;
+    for (const Batch::RodSet* rs : sets) {
+      tot += rs->n;
+      totp += (int64_t)rs->n * (int64_t)rs->layers.size();
+    }
+    EQF_REQUIRE(n_total == tot && (n_total == 0 || rods), "rod count mismatch");
+    if (production)
+      for (int64_t i = 0; i < totp; ++i)
+        EQF_REQUIRE(std::isfinite(production[i]), "non-finite production");
+    // stage the rods and the productions (in the device's kRodLayers layout) in pinned
+    // memory, so the uploads are asynchronous
+    size_t prod4 = 0;
+    for (const Batch::RodSet* rs : sets) prod4 += (size_t)rs->n * eqf::kRodLayers;
+    const size_t rbytes = (size_t)tot * sizeof(eqf_rod);
+    B.rod_hstage.grow(rbytes + (production ? prod4 * sizeof(double) : 0) + 16);
+    unsigned char* st = B.rod_hstage.p;
+    double* hp = reinterpret_cast<double*>(st + ((rbytes + 15) & ~size_t(15)));
+    int64_t c0 = 0, p0 = 0;
+    size_t q0 = 0;
+    for (Batch::RodSet* rs : sets) {
+      const int nl = (int)rs->layers.size();
+      const size_t n = (size_t)rs->n;
+      check_rods(B.params[rs->layers[0]], rods + c0, rs->n);
+      std::memcpy(st + (size_t)c0 * sizeof(eqf_rod), rods + c0, n * sizeof(eqf_rod));
+      EQF_CK(cudaMemcpyAsync(rs->rods.p, st + (size_t)c0 * sizeof(eqf_rod),
+                             n * sizeof(eqf_rod), cudaMemcpyHostToDevice, B.stream));
+      if (production) {
+        double* q = hp + q0;
+        std::fill(q, q + n * eqf::kRodLayers, 0.0);
+        for (size_t c = 0; c < n; ++c)
+          for (int l = 0; l < nl; ++l) q[c * eqf::kRodLayers + l] = production[p0 + c * nl + l];
+        EQF_CK(cudaMemcpyAsync(rs->prod.p, q, n * eqf::kRodLayers * sizeof(double),
+                               cudaMemcpyHostToDevice, B.stream));
+      }
+      c0 += rs->n;
+      p0 += (int64_t)rs->n * nl;
+      q0 += n * eqf::kRodLayers;
+    }
+    B.rod_analyse_sets(sets);  // ends with a sync: the staging may be reused
+    B.rod_publish();
+  });
+}
+
+int eqf_read_rods_all(eqf_batch* b, int64_t n_total, double* ihsl, double* ehsl,
+                      int32_t* points) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    const std::vector<Batch::RodSet*> sets = rod_sets_by_layer(B);
+    int64_t tot = 0;
+    size_t n4 = 0;
+    for (const Batch::RodSet* rs : sets) {
+      tot += rs->n;
+      n4 += (size_t)rs->n * eqf::kRodLayers;
+    }
+    EQF_REQUIRE(n_total == tot, "rod count mismatch");
+    const size_t dbytes = n4 * sizeof(double);
+    B.rod_hstage.grow(2 * dbytes + ((size_t)tot + sets.size()) * sizeof(int) + 16);
+    double* hi = reinterpret_cast<double*>(B.rod_hstage.p);
+    double* he = hi + n4;
+    int* ho = reinterpret_cast<int*>(he + n4);
+    size_t q0 = 0, o0 = 0;
+    for (const Batch::RodSet* rs : sets) {
+      const size_t n = (size_t)rs->n, m = n * eqf::kRodLayers;
+      EQF_CK(cudaMemcpyAsync(hi + q0, rs->ihsl.p, m * sizeof(double), cudaMemcpyDeviceToHost,
+                             B.stream));
+      EQF_CK(cudaMemcpyAsync(he + q0, rs->ehsl.p, m * sizeof(double), cudaMemcpyDeviceToHost,
+                             B.stream));
+      EQF_CK(cudaMemcpyAsync(ho + o0, rs->fp_off.p, (n + 1) * sizeof(int),
+                             cudaMemcpyDeviceToHost, B.stream));
+      q0 += m;
+      o0 += n + 1;
+    }
+    B.sync();
+    q0 = o0 = 0;
+    int64_t c0 = 0, p0 = 0;
+    for (const Batch::RodSet* rs : sets) {
+      const int nl = (int)rs->layers.size();
+      const size_t n = (size_t)rs->n;
+      for (size_t c = 0; c < n; ++c) {
+        for (int l = 0; l < nl; ++l) {
+          if (ihsl) ihsl[p0 + c * nl + l] = hi[q0 + c * eqf::kRodLayers + l];
+          if (ehsl) ehsl[p0 + c * nl + l] = he[q0 + c * eqf::kRodLayers + l];
+        }
+        if (points) points[c0 + c] = ho[o0 + c + 1] - ho[o0 + c];
+      }
+      q0 += n * eqf::kRodLayers;
+      o0 += n + 1;
+      c0 += rs->n;
+      p0 += (int64_t)rs->n * nl;
     }
   });
 }

@@ -281,6 +281,40 @@ class TrapBatch:
                                          pts.ctypes.data_as(C.POINTER(C.c_int32))))
         return ih, eh, pts
 
+    def _rod_sets(self):
+        """(first layer, cells, layers) of every rod set, in increasing first layer."""
+        return [(l0, n, nl) for l0, (n, nl) in sorted(getattr(self, "_rods", {}).items())
+                if n > 0]
+
+    def update_rods_all(self, rods: np.ndarray, production: Optional[np.ndarray] = None):
+        """update_rods for every rod set in one call: the sets' cells in turn, in
+        increasing order of their first layer (production: each set's block laid out
+        as for update_rods)."""
+        rods = np.ascontiguousarray(rods, dtype=_lib.rod_dtype())
+        pr = None
+        if production is not None:
+            pr = _dp(np.ascontiguousarray(production, dtype=np.float64).ravel())
+        self._ck(self._lib.eqf_update_rods_all(self._h, len(rods), rods.ctypes.data, pr))
+
+    def read_rods_all(self):
+        """read_rods for every rod set in one call: lists of each set's (ihsl, ehsl,
+        points), in increasing order of the sets' first layer."""
+        sets = self._rod_sets()
+        tot = sum(n for _, n, _ in sets)
+        totp = sum(n * nl for _, n, nl in sets)
+        ih = np.empty(totp)
+        eh = np.empty(totp)
+        pts = np.empty(tot, dtype=np.int32)
+        self._ck(self._lib.eqf_read_rods_all(self._h, tot, _dp(ih), _dp(eh),
+                                             pts.ctypes.data_as(C.POINTER(C.c_int32))))
+        out, c0, p0 = [], 0, 0
+        for _, n, nl in sets:
+            out.append((ih[p0:p0 + n * nl].reshape(n, nl), eh[p0:p0 + n * nl].reshape(n, nl),
+                        pts[c0:c0 + n]))
+            c0 += n
+            p0 += n * nl
+        return out
+
     def exchange_rods(self):
         """One pass of the cell loop without a solve."""
         self._ck(self._lib.eqf_exchange_rods(self._h))

@@ -421,6 +421,17 @@ int eqf_update_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, const eqf_rod
  * the first), and per cell the number of footprint nodes.  Any pointer may be NULL. */
 int eqf_read_rods(eqf_batch* b, int32_t layer0, int64_t n_cells, double* ihsl, double* ehsl,
                   int32_t* points);
+/* eqf_update_rods and eqf_read_rods for every rod set of the batch in one call (no
+ * reference counterpart: a controller driving several simulations on one GPU).  The
+ * sets are taken in increasing order of their first layer; rods, production, ihsl,
+ * ehsl and points hold each set's block in turn, laid out as for the per-set calls;
+ * n_total is the number of cells of all sets.  The result is the same as one per-set
+ * call per set, with a few host round trips for the whole batch instead of several
+ * per set. */
+int eqf_update_rods_all(eqf_batch* b, int64_t n_total, const eqf_rod* rods,
+                        const double* production);
+int eqf_read_rods_all(eqf_batch* b, int64_t n_total, double* ihsl, double* ehsl,
+                      int32_t* points);
 /* Runs the exchange once now, without a solve (the reference's updateCells alone). */
 int eqf_exchange_rods(eqf_batch* b);
 /* Number of sequential waves the exchange of the current rod cells takes (1 when

@@ -275,3 +275,50 @@ def test_several_rod_sets_in_one_batch_bitwise(lib):
             for l in range(c.n_layers):
                 assert np.array_equal(b.read_nodal(t + l), f[l].ravel())
             t += c.n_layers
+
+
+def test_batch_wide_rod_update_and_read_match_per_set_calls(lib):
+    """update_rods_all / read_rods_all: the same bits as one update_rods / read_rods per
+    set (sets taken in increasing order of their first layer)."""
+    spec = [(24.0, 12.0, 2.0, 40), (20.0, 10.0, 4.0, 150), (16.0, 8.0, 2.0, 5)]
+    cols = [wl.rod_colony(seed=40 + k, W=W, H=H, npm=npm, n_cells=n)
+            for k, (W, H, npm, n) in enumerate(spec)]
+    moved = [wl.rod_colony(seed=50 + k, W=W, H=H, npm=npm, n_cells=n)
+             for k, (W, H, npm, n) in enumerate(spec)]
+    rng = np.random.Generator(np.random.PCG64(9))
+    params, fields = [], []
+    for c in cols:
+        params += layer_params(c.W, c.H, c.npm, c.n_layers)
+        fields.append([rng.uniform(0, 30, (c.ny + 1, c.nx + 1)) for _ in range(c.n_layers)])
+    prods = [rng.uniform(0, 5, (c.n_cells, c.n_layers)) for c in cols]
+    out = []
+    for batch_wide in (False, True):
+        with F.TrapBatch(params, F.default_opts(F.FP64)) as b:
+            t, firsts = 0, []
+            for c, f in zip(cols, fields):
+                for l in range(c.n_layers):
+                    b.set_nodal(t + l, f[l].ravel())
+                b.set_rods(list(range(t, t + c.n_layers)), c.rods, c.ihsl, c.prod, c.mode,
+                           c.npm, c.dt, c.km)
+                firsts.append(t)
+                t += c.n_layers
+            b.exchange_rods()
+            if batch_wide:
+                b.update_rods_all(np.concatenate([m.rods for m in moved]),
+                                  np.concatenate([p.ravel() for p in prods]))
+            else:
+                for t0, m, p in zip(firsts, moved, prods):
+                    b.update_rods(t0, m.rods, p)
+            b.exchange_rods()
+            b.step(2)
+            reads = (b.read_rods_all() if batch_wide
+                     else [b.read_rods(t0) for t0 in firsts])
+            nod = [b.read_nodal(k) for k in range(len(params))]
+            out.append((reads, nod, b.rod_waves()))
+    (ra, na, wa), (rb, nb, wb) = out
+    assert wa == wb
+    for x, y in zip(ra, rb):
+        for u, v in zip(x, y):
+            assert np.array_equal(u, v)
+    for u, v in zip(na, nb):
+        assert np.array_equal(u, v)
