@@ -122,3 +122,24 @@ def test_mixed_batch_is_bit_identical_to_each_trap_alone(lib, precision):
         b.step(4)
         for i in range(len(traps)):
             assert np.array_equal(b.read_nodal(i), alone[i])
+
+
+def test_bottom_levels_kernel_with_general_path_traps(lib):
+    """The one-kernel bottom levels fetch a general-path trap's stencils as the level
+    kernels do: fuse_levels 2 and 1 give the same bits on a mixed batch."""
+    base = wl.batched_uneven(8, 3)
+    traps = [wl.scaled(t, t.nx // 4 * 2, t.ny // 4 * 2, n_cells=60) for t in base]
+    tens = {0: smooth_field(traps[0].nx, traps[0].ny, traps[0].W, traps[0].H)}
+    res = []
+    for fuse in (2, 1):
+        with F.TrapBatch([F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls)
+                          for t in traps],
+                         F.default_opts(F.FP32_IR, use_graph=1, fuse_levels=fuse)) as b:
+            for i, t in enumerate(traps):
+                b.set_cells(i, t.cell_xy, t.cell_s)
+                if i in tens:
+                    b.set_tensor(i, *tens[i])
+            b.step(3)
+            res.append([b.read_nodal(i) for i in range(len(traps))])
+    for a, c in zip(res[0], res[1]):
+        assert np.array_equal(a, c)
