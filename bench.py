@@ -141,19 +141,31 @@ def trap_params_of(traps):
     return [F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls) for t in traps]
 
 
-def sample_indices(traps, k: int, seed: int = 11):
+def sample_indices(traps, k: int):
     """k traps stratified by node count (deterministic)."""
-    order = np.argsort([t.n_nodes for t in traps], kind="stable")
-    if k >= len(traps):
-        return list(order)
-    pos = np.linspace(0, len(traps) - 1, k).round().astype(int)
-    return [int(order[p]) for p in pos]
+    from eq_gb300 import workloads as wl
+    return wl.stratified_sample(traps, k)
 
 
 # ------------------------------------------------------------- CPU baselines
 def cpu_reference_rate(traps, idx, steps_per_trap: int, budget_s: float):
     from oracle import cpu_baseline
     return cpu_baseline.reference_rate(traps, idx, steps_per_trap, budget_s)
+
+
+def launch_traffic(tc, d):
+    """DRAM traffic per launch of a kernel class: the ncu capture's read+write bytes
+    per processed node times the nodes an average launch of this run processed (the
+    profiler counts them; tiles of converged traps are skipped), beside the
+    algorithmic bytes per node."""
+    if not tc or d["launches"] == 0 or d["nodes"] == 0:
+        return {"traffic": None}
+    nodes = d["nodes"] / d["launches"]
+    return {"traffic": tc["bytes_per_node"] * nodes, "nodes_per_launch": nodes,
+            "traffic_bytes_per_node": tc["bytes_per_node"],
+            "algorithmic_bytes_per_node": d["bytes"] / d["nodes"],
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per node "
+                              "(profiles/traffic.json) x nodes per launch of this run"}
 
 
 def profiled_roofline(b, stream, prof_steps: int, workload: str):
@@ -184,17 +196,93 @@ def profiled_roofline(b, stream, prof_steps: int, workload: str):
             tj = json.load(f)
         if tj.get("workload") == workload:
             tclasses = tj.get("classes", {})
-    traffic = tclasses.get(dom, {}).get("bytes_per_launch")
     roofline = {"bound": "hbm", "kernel_class": dom, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": traffic, "peak_source": peak_kind,
+                "peak_source": peak_kind,
                 "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
                 "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
+    roofline.update(launch_traffic(tclasses.get(dom), d))
     if dom in ("down0", "up0"):
         roofline["note"] = ("temporally blocked level kernel: several smoothing steps per HBM "
                             "pass, bytes counted once (compute-bound by design)")
     return prof, prof_total, launches_per_step, roofline, tclasses
+
+
+# ------------------------------------------------------------ oracle checks
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_checks(precisions=None):
+    """The solver workloads at their stated sizes against the FP64 oracle's committed
+    fixtures (tests/golden, made by tests/golden/make_config_golden.py): the 1024x512
+    trap over 500 steps (relL2 of the cells after every 50 steps, of the nodal field
+    after 50, 250, 500) and the stratified 8-trap sample of the uneven batch over 200
+    steps, with the FP64 mass-balance drift of every step; for each precision, the
+    device time of those steps."""
+    import torch
+    from eq_gb300 import field as F
+    from eq_gb300 import workloads as wl
+    gdir = os.path.join(ROOT, "tests", "golden")
+    precisions = precisions or [("fp32_ir", F.FP32_IR), ("fp64", F.FP64)]
+    out = {}
+
+    def timed(b, n):
+        s = torch.cuda.ExternalStream(b.stream_handle())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        b.step(n)
+        e1.record(s)
+        b.sync()
+        return e0.elapsed_time(e1)
+
+    g = np.load(os.path.join(gdir, "single_large_oracle.npz"))
+    t = wl.single_large(1)
+    res = {}
+    for name, prec in precisions:
+        with F.TrapBatch(trap_params_of([t]), F.default_opts(prec, use_graph=1, adaptive=1)) as b:
+            b.set_cells(0, t.cell_xy, t.cell_s)
+            b.mass_balance(True)
+            cells, nodal, ms, done = {}, {}, 0.0, 0
+            for n in g["cell_steps"]:
+                ms += timed(b, int(n) - done)
+                done = int(n)
+                cells[int(n)] = rel(b.read_cells(0), g[f"c0_{n}"])
+                if n in g["nodal_steps"]:
+                    nodal[int(n)] = rel(b.read_nodal(0), g[f"u0_{n}"])
+            bal = b.read_balance(0)
+        res[name] = {"cells_relL2": cells, "nodal_relL2": nodal,
+                     "dof_steps_per_s": t.n_nodes * done / (ms / 1e3),
+                     "mass_balance": {"drift_rel_max": bal["drift_rel_max"],
+                                      "drift_sum_over_load_sum": bal["drift_sum"] / bal["load_sum"],
+                                      "load_sum": bal["load_sum"], "mass_final": bal["mass"],
+                                      "wall_outflow_last_step": bal["wall_outflow"]}}
+    out["single_large"] = {"config": "100x40 um, 1024x512 squares (525,825 nodes), 20,000 cells, "
+                                     "dt 0.05, 500 steps", **res}
+    g = np.load(os.path.join(gdir, "batched_sample_oracle.npz"))
+    traps = wl.batched_uneven(int(g["seed"]), int(g["n_traps"]))
+    idx = [int(i) for i in g["traps"]]
+    sub = [traps[i] for i in idx]
+    res = {}
+    for name, prec in precisions:
+        with F.TrapBatch(trap_params_of(sub), F.default_opts(prec, use_graph=1, adaptive=1)) as b:
+            load_traps(b, sub)
+            b.mass_balance(True)
+            worst, done = {}, 0
+            for n in g["cell_steps"]:
+                b.step(int(n) - done)
+                done = int(n)
+                worst[int(n)] = max(rel(b.read_cells(k), g[f"t{i}_c0_{n}"])
+                                    for k, i in enumerate(idx))
+            nod = max(rel(b.read_nodal(k), g[f"t{i}_u0_200"]) for k, i in enumerate(idx))
+            drift = max(b.read_balance(k)["drift_rel_max"] for k in range(len(sub)))
+        res[name] = {"cells_relL2_max_over_traps": worst, "nodal_relL2_max_step200": nod,
+                     "mass_drift_rel_max": drift}
+    out["batched_sample"] = {"config": f"traps {idx} of the 512-trap uneven batch (seed "
+                                       f"{int(g['seed'])}), 200 steps", **res}
+    out["fixtures"] = "tests/golden/*_oracle.npz (FP64 hslD assembly + SuperLU)"
+    return out
 
 
 # -------------------------------------------------------------------- our arm
@@ -224,6 +312,7 @@ def run_ours(args, rank, world, local_rank):
     # warm-up (graph capture happens on the first steps)
     b.step(args.warmup)
     b.sync()
+    b.mass_balance(True)  # every timed step closes its FP64 mass balance on the device
     probe = sample_indices(traps, 8)
     st0 = [b.stats(i) for i in probe]
 
@@ -242,6 +331,13 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    bals = [b.read_balance(i) for i in range(len(traps))]
+    balance = {"traps": len(bals), "steps": int(bals[0]["steps"]),
+               "drift_rel_max": max(x["drift_rel_max"] for x in bals),
+               "drift_sum_over_load_sum": sum(x["drift_sum"] for x in bals) /
+                                          sum(x["load_sum"] for x in bals),
+               "note": "per step and trap: mass - mass_prev - load + decay + wall outflow, "
+                       "FP64 on the device, relative to the step's largest term"}
     st1 = [b.stats(i) for i in probe]
     sweeps_ps = sum(a["sweeps"] - z["sweeps"] for a, z in zip(st1, st0)) / len(probe) / args.steps
     iters_ps = sum(a["iters"] - z["iters"] for a, z in zip(st1, st0)) / len(probe) / args.steps
@@ -283,6 +379,7 @@ def run_ours(args, rank, world, local_rank):
     prof, prof_total, launches_per_step, roofline, tclasses = profiled_roofline(
         b, stream, prof_steps, args.workload)
     peak, peak_kind = measured_peaks()
+    step_bytes = sum(v["bytes"] for v in prof.values()) / prof_steps
 
     # ---- the operator kernel alone: the step-by-step smoothing step (k_cheb on the
     #      finest level) in a short profiled pass of an unfused batch
@@ -303,10 +400,11 @@ def run_ours(args, rank, world, local_rank):
                          "achieved": round(op_ach, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(op_ach / peak, 4), "peak_source": peak_kind,
                          "bytes_per_node": 20, "launches": so["launches"],
-                         "avg_launch_us": so["ms"] * 1e3 / max(so["launches"], 1),
-                         "traffic": tclasses.get("smooth0", {}).get("bytes_per_launch")}
+                         "avg_launch_us": so["ms"] * 1e3 / max(so["launches"], 1)}
+    operator_roofline.update(launch_traffic(tclasses.get("smooth0"), so))
 
     b.close()
+    checks = oracle_checks() if rank == 0 and not args.no_oracle else None
 
     # ---- e2e through the host API: a fresh batch taken through the same warm-up, then
     #      the same steps as the timed loop, each with the pinned per-cell rates copied
@@ -364,8 +462,16 @@ def run_ours(args, rank, world, local_rank):
                                        "speedup_of_batched_fp32ir": value / world / fp64_rate},
             "solver": {"sweeps_per_step": sweeps_ps, "iters_per_step": iters_ps,
                        "sample": f"{len(probe)} traps stratified by size, timed steps"},
+            "mass_balance": balance,
+            "oracle_checks": checks,
             "roofline": roofline,
             "operator_roofline": operator_roofline,
+            "step_effective_bandwidth": {
+                "algorithmic_bytes_per_step": step_bytes,
+                "GBps_timed": step_bytes / (total_ms / args.steps / 1e3) / 1e9,
+                "frac_of_peak": step_bytes / (total_ms / args.steps / 1e3) / 1e9 / peak,
+                "note": "all kernel classes' algorithmic bytes of a step (profiled pass) over "
+                        "the timed ms per step"},
             "profile": {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                             "GBps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else 0}
                         for k, v in prof.items()},
@@ -732,6 +838,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the full-size checks against the oracle's fixtures")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: requests/s")
     ap.add_argument("--duration", type=float, default=10.0, help="serving: arrival window, s")
     ap.add_argument("--drain-limit", type=float, default=20.0,

@@ -38,7 +38,8 @@ EXPORTS = (
     "eqf_set_boundaries", "eqf_read_channels", "eqf_set_channels", "eqf_set_well",
     "eqf_read_well", "eqf_set_tensor", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
     "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
-    "eqf_vtk_write_host", "eqf_vtk_close",
+    "eqf_vtk_write_host", "eqf_vtk_close", "eqf_mass_balance", "eqf_read_balance",
+    "eqf_rod_relax_passes",
 )
 
 # wall conditions (eqf_set_boundaries)
@@ -46,11 +47,18 @@ EQF_SIDE_BOTTOM, EQF_SIDE_TOP, EQF_SIDE_LEFT, EQF_SIDE_RIGHT = 0, 1, 2, 3
 EQF_BC_NEUMANN, EQF_BC_DIRICHLET, EQF_BC_ROBIN, EQF_BC_CHANNEL, EQF_BC_WELL = 0, 1, 2, 3, 4
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
-                "down0", "up0", "rod_exchange")
+                "down0", "up0", "rod_exchange", "balance")
 
 # rod cells (eqf_set_rods): per cell and layer modes, and the eqf_rod record
 EQF_MAX_ROD_LAYERS = 4
 EQF_ROD_HELD, EQF_ROD_CIRCUIT, EQF_ROD_INERT = 0, 1, 2
+
+
+class Balance(C.Structure):
+    """eqf_balance: the last step's FP64 mass-balance terms and the sums since enabled."""
+    _fields_ = [(n, C.c_double) for n in (
+        "mass", "mass_prev", "load", "decay", "operator_loss", "wall_outflow", "drift",
+        "drift_sum", "drift_abs_sum", "load_sum", "drift_rel_max")] + [("steps", C.c_int64)]
 
 
 class TrapParams(C.Structure):
@@ -189,6 +197,9 @@ def load() -> C.CDLL:
         "eqf_vtk_close": (C.c_int, [C.c_void_p]),
         "eqf_read_well": (C.c_int, [C.c_void_p, C.c_int32, dp, i64p]),
         "eqf_rod_waves": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "eqf_rod_relax_passes": (C.c_int, [C.c_void_p, P(C.c_int32)]),
+        "eqf_mass_balance": (C.c_int, [C.c_void_p, C.c_int32]),
+        "eqf_read_balance": (C.c_int, [C.c_void_p, C.c_int32, P(Balance)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

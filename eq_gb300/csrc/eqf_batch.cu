@@ -26,6 +26,7 @@
 #include "eqf_fused.cuh"
 #include "eqf_rods.cuh"
 #include "eqf_walls.cuh"
+#include "eqf_balance.cuh"
 
 namespace eqf {
 
@@ -319,6 +320,7 @@ enum KClass : int {
   KC_DOWN0,           // finest level, fused pre-smoothing + residual
   KC_UP0,             // finest level, fused prolongation + post-smoothing
   KC_ROD,             // rod-cell exchange waves (gather, membrane exchange, deposit)
+  KC_BALANCE,         // per-step FP64 mass balance (eqf_mass_balance)
   KC_COUNT
 };
 static_assert(KC_COUNT == EQF_PROF_CLASSES, "profiler class count");
@@ -460,6 +462,7 @@ class Batch {
     eqf_rod_law law{};
     RodLawDev dev{};
     int n = 0, nent = 0, waves = 0, grid = 0;
+    int relax_passes = 0;  // passes the last wave relaxation took (0: no shared node)
     long long span = 0;  // lattice nodes of the layers' trap in device layout
     DevBuf<eqf_rod> rods;
     DevBuf<RodLawDev> dlaw;
@@ -487,6 +490,14 @@ class Batch {
   DevBuf<ChanDev> d_chans;
   int chan_n_max = 0;
   void setup_walls();
+  DevBuf<int> d_wall_of;  // per trap: its index in d_walls, -1 for none
+  // per-step FP64 mass balance (eqf_mass_balance): per trap record, tile partials
+  bool bal_on = false;
+  // the last balance's mass (of the field the next step starts from) and load still
+  // hold: the next balance carries them over instead of summing c and F again
+  bool bal_prev_ok = false, bal_load_ok = false;
+  DevBuf<double> d_bal, bal_part, bal_rpart;
+  void enqueue_balance();
   bool ops_dirty = false;  // walls or tensors changed: operators rebuilt before the next use
   void ensure_ops() {
     if (!ops_dirty) return;
@@ -635,6 +646,11 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
   d_well_under.alloc(ntraps);
   EQF_CK(cudaMemsetAsync(d_well_c.p, 0, ntraps * sizeof(double), stream));
   EQF_CK(cudaMemsetAsync(d_well_under.p, 0, ntraps * sizeof(long long), stream));
+  d_wall_of.alloc(ntraps);
+  {
+    const std::vector<int> none(ntraps, -1);
+    d_wall_of.upload(none.data(), ntraps, stream);
+  }
   sync();
 }
 
@@ -1591,6 +1607,11 @@ void Batch::setup_walls() {
   walls_active = !hwalls.empty();
   d_walls.alloc(hwalls.size());
   if (walls_active) d_walls.upload(hwalls.data(), hwalls.size(), stream);
+  {
+    std::vector<int> of(ntraps, -1);
+    for (size_t w = 0; w < hwalls.size(); ++w) of[hwalls[w].trap] = (int)w;
+    d_wall_of.upload(of.data(), ntraps, stream);
+  }
   d_fbase.alloc(std::max(rim_total, 1));
   EQF_CK(cudaMemsetAsync(d_fbase.p, 0, d_fbase.n * sizeof(double), stream));
   std::vector<ChanDev> hc;
@@ -1628,6 +1649,7 @@ void Batch::setup_walls() {
                                 (int)chan_smem_bytes(kChanMaxNodes)));
   }
   // the load vector restarts from the point cells alone (rims included)
+  bal_load_ok = false;
   if (!cells_dirty) {
     EQF_CK(cudaMemsetAsync(F.p, 0, L[0].nodes * sizeof(double), stream));
     refresh_load();
@@ -1662,6 +1684,41 @@ void Batch::enqueue_wells() {
               d_wells.p, L[0].dgeom.p, U[1 - cur].p, d_frozen.p)));
 }
 
+// After the solve (and any extra sweeps): the step's FP64 balance from the new field
+// U[1 - cur], the field the step started from U[cur] and the step's load F.
+void Batch::enqueue_balance() {
+  if (!bal_on) return;
+  const int nt = L[0].ntiles();
+  int longest = 1;  // outer ring, or the two-node rim of a trap with wall values
+  for (int t = 0; t < ntraps; ++t) {
+    const LevelGeom& g = L[0].geom[t];
+    longest = std::max(longest, 2 * (g.nx + 1) + 2 * (g.ny - 1));
+    if (g.nx >= 3 && g.ny >= 3) longest = std::max(longest, rim_count(g.nx, g.ny));
+  }
+  const int rim_blocks = std::min((longest + kThreads - 1) / kThreads, 64);
+  grow(bal_part, (size_t)nt * kBalTileParts);
+  grow(bal_rpart, (size_t)ntraps * rim_blocks * kBalRimParts);
+  // the field a step starts from is the last step's result unless the host or the rod
+  // exchange changed it; the load stays unless the cells' rates, the coupling or the
+  // wall values rebuilt it
+  const bool old = !bal_prev_ok || !rod_sets.empty();
+  const bool load = !bal_load_ok || ncp > 0 || walls_active;
+  auto tiles = old ? (load ? k_balance_tiles<true, true> : k_balance_tiles<true, false>)
+                   : (load ? k_balance_tiles<false, true> : k_balance_tiles<false, false>);
+  EQF_RUN(*this, KC_BALANCE,
+          (tiles<<<nt, kThreads, 0, stream>>>(L[0].dgeom.p, L[0].dtiles.p, U[1 - cur].p, U[cur].p,
+                                              F.p, d_frozen.p, bal_part.p)));
+  EQF_RUN(*this, KC_BALANCE,
+          (k_balance_rim<<<dim3(rim_blocks, ntraps), kThreads, 0, stream>>>(
+              L[0].dgeom.p, U[1 - cur].p, U[cur].p, F.p, d_wall_of.p, d_walls.p, d_fbase.p,
+              d_frozen.p, old ? 1 : 0, load ? 1 : 0, bal_rpart.p)));
+  EQF_RUN(*this, KC_BALANCE,
+          (k_balance_finish<<<(ntraps + 3) / 4, 128, 0, stream>>>(
+              L[0].dgeom.p, drange.p, bal_part.p, bal_rpart.p, rim_blocks, d_frozen.p, ntraps,
+              old ? 1 : 0, load ? 1 : 0, d_bal.p)));
+  bal_prev_ok = bal_load_ok = true;
+}
+
 void Batch::enqueue_walls() {
   if (!walls_active) return;
   const dim3 grid((rim_max + 255) / 256, (unsigned)hwalls.size());
@@ -1694,13 +1751,16 @@ Batch::RodSet* Batch::rod_set_of(int layer0) {
 
 void Batch::rod_analyse(RodSet& rs) { rod_analyse_sets({&rs}); }
 
+constexpr int kRodFlags = 5;  // per set in rod_hflags
+
 // Footprints (sizes, then nodes), the shared-node test, the waves of the sets with
 // shared nodes and the wave offsets: each phase is queued for every set, then one
 // round trip brings the sizes the next phase needs.
 void Batch::rod_analyse_sets(const std::vector<RodSet*>& sets) {
   const int bs = 256, ns = (int)sets.size();
   if (ns == 0) return;
-  rod_hflags.grow(4 * (size_t)ns);  // per set: footprint size, shared, highest wave, unsettled
+  // per set: footprint size, shared, highest wave, unsettled, relaxation passes
+  rod_hflags.grow(kRodFlags * (size_t)ns);
   int* hf = rod_hflags.p;
   for (int q = 0; q < ns; ++q) {
     RodSet& rs = *sets[q];
@@ -1711,13 +1771,13 @@ void Batch::rod_analyse_sets(const std::vector<RodSet*>& sets) {
                                                        nullptr, nullptr, nullptr);
     EQF_LAUNCH_CHECK();
     scan(n, rs.sc_count.p, rs.fp_off.p);
-    EQF_CK(cudaMemcpyAsync(hf + 4 * q, rs.fp_off.p + n, sizeof(int), cudaMemcpyDeviceToHost,
+    EQF_CK(cudaMemcpyAsync(hf + kRodFlags * q, rs.fp_off.p + n, sizeof(int), cudaMemcpyDeviceToHost,
                            stream));
   }
   sync();
   for (int q = 0; q < ns; ++q) {  // the footprints; does any node lie in two of them?
     RodSet& rs = *sets[q];
-    const int n = rs.n, nent = hf[4 * q];
+    const int n = rs.n, nent = hf[kRodFlags * q];
     if ((size_t)nent > rs.fp_node.n) {
       const size_t cap = (size_t)nent + (size_t)nent / 4 + 64;
       rs.fp_node.alloc(cap);
@@ -1732,15 +1792,15 @@ void Batch::rod_analyse_sets(const std::vector<RodSet*>& sets) {
     EQF_CK(cudaMemsetAsync(rs.flag.p, 0, sizeof(int), stream));
     k_rod_cover<<<ge, bs, 0, stream>>>(nent, rs.fp_node.p, 0, rs.cover.p, rs.flag.p);
     EQF_LAUNCH_CHECK();
-    EQF_CK(cudaMemcpyAsync(hf + 4 * q + 1, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost,
+    EQF_CK(cudaMemcpyAsync(hf + kRodFlags * q + 1, rs.flag.p, sizeof(int), cudaMemcpyDeviceToHost,
                            stream));
   }
   sync();
   bool any = false;
   for (int q = 0; q < ns; ++q) {  // waves: bucket the entries by node, each bucket in
     RodSet& rs = *sets[q];        // cell order; a cell's wave = its longest chain
-    hf[4 * q + 2] = hf[4 * q + 3] = 0;
-    if (!hf[4 * q + 1]) continue;
+    hf[kRodFlags * q + 2] = hf[kRodFlags * q + 3] = hf[kRodFlags * q + 4] = 0;
+    if (!hf[kRodFlags * q + 1]) continue;
     any = true;
     const int n = rs.n, nent = rs.nent;
     const int ge = (nent + bs - 1) / bs, gc = (n + bs - 1) / bs;
@@ -1762,37 +1822,38 @@ void Batch::rod_analyse_sets(const std::vector<RodSet*>& sets) {
     EQF_LAUNCH_CHECK();
     EQF_CK(cudaMemsetAsync(rs.sc_wave.p, 0, n * sizeof(int), stream));
     // the whole relaxation in one CTA (no host round trip per pass); flag[1] reports a
-    // relaxation that did not settle within its bound
-    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, 2 * sizeof(int), stream));
+    // relaxation that did not settle within its bound, flag[2] the passes it took
+    EQF_CK(cudaMemsetAsync(rs.flag.p, 0, 3 * sizeof(int), stream));
     k_rod_relax_all<<<1, 1024, 0, stream>>>(nent, n, rs.sc_pred.p, rs.sc_succ.p, rs.sc_wave.p,
-                                            rs.flag.p + 1);
+                                            rs.flag.p + 1, rs.flag.p + 2);
     EQF_LAUNCH_CHECK();
     EQF_CK(cudaMemsetAsync(rs.sc_wcount.p, 0, n * sizeof(int), stream));
     k_rod_wave_count<<<gc, bs, 0, stream>>>(n, rs.sc_wave.p, rs.sc_wcount.p, rs.flag.p);
     EQF_LAUNCH_CHECK();
-    EQF_CK(cudaMemcpyAsync(hf + 4 * q + 2, rs.flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+    EQF_CK(cudaMemcpyAsync(hf + kRodFlags * q + 2, rs.flag.p, 3 * sizeof(int), cudaMemcpyDeviceToHost,
                            stream));
   }
   if (any) sync();
   // wave offsets: {0, n} when no node is shared, else the scan of the wave sizes
   std::vector<size_t> wo(ns + 1, 0);
   for (int q = 0; q < ns; ++q) {
-    if (hf[4 * q + 1] && hf[4 * q + 3])
+    if (hf[kRodFlags * q + 1] && hf[kRodFlags * q + 3])
       throw Error(EQF_ERR_CUDA, "rod wave analysis did not settle");
-    wo[q + 1] = wo[q] + (hf[4 * q + 1] ? (size_t)hf[4 * q + 2] + 2 : 2);
+    wo[q + 1] = wo[q] + (hf[kRodFlags * q + 1] ? (size_t)hf[kRodFlags * q + 2] + 2 : 2);
+    sets[q]->relax_passes = hf[kRodFlags * q + 4];
   }
   rod_hwoff.grow(wo[ns]);
   int* hw = rod_hwoff.p;
   for (int q = 0; q < ns; ++q) {
     RodSet& rs = *sets[q];
     const int n = rs.n, gc = (n + bs - 1) / bs;
-    if (!hf[4 * q + 1]) {
+    if (!hf[kRodFlags * q + 1]) {
       k_rod_iota<<<gc, bs, 0, stream>>>(n, rs.wave_cells.p);
       EQF_LAUNCH_CHECK();
       hw[wo[q]] = 0;
       hw[wo[q] + 1] = n;
     } else {
-      const int waves = hf[4 * q + 2] + 1;
+      const int waves = hf[kRodFlags * q + 2] + 1;
       grow(rs.sc_wstart, waves + 1);
       scan(waves, rs.sc_wcount.p, rs.sc_wstart.p);
       EQF_CK(cudaMemsetAsync(rs.sc_wcount.p, 0, waves * sizeof(int), stream));
@@ -1937,9 +1998,11 @@ void Batch::step(int n) {
         enqueue_channels();
         enqueue_wells();
         cur = 1 - cur;
+        bal_prev_ok = false;
         throw Error(EQF_ERR_NOT_CONVERGED, "trap(s) missed rtol after extra refinement sweeps");
       }
     }
+    enqueue_balance();  // before the channels move the wall values of the next step
     enqueue_channels();
     enqueue_wells();
     cur = 1 - cur;
@@ -2013,6 +2076,7 @@ void Batch::rebuild_cells() {
   cell_first.assign(ntraps + 1, 0);
   for (int t = 0; t < ntraps; ++t) cell_first[t + 1] = cell_first[t] + (int)cell_s[t].size();
   ncells = cell_first[ntraps];
+  bal_load_ok = false;
   EQF_CK(cudaMemsetAsync(F.p, 0, L[0].nodes * sizeof(double), stream));
   if (ncells == 0) {
     nseg = 0;
@@ -2098,6 +2162,7 @@ void Batch::rebuild_cells() {
 
 // F = dt * sum_i s_i phi(x_i) from the current rates (segments fixed)
 void Batch::refresh_load() {
+  bal_load_ok = false;
   if (ncells == 0) return;
   const dim3 rim_grid((rim_max + 255) / 256, (unsigned)hwalls.size());
   if (walls_active)  // the rim takes the point cells' load alone, then is kept apart
@@ -2488,6 +2553,7 @@ int eqf_set_nodal(eqf_batch* b, int32_t trap, const double* c) {
     EQF_REQUIRE(c != nullptr, "null field");
     Batch& B = *b->impl;
     const long long off = B.L[0].geom[trap].off;
+    B.bal_prev_ok = false;
     B.copy_field_to_device(B.u_cur() + off, c, trap, B.stream);
     // a new field invalidates the increment history of the initial guess
     EQF_CK(cudaMemsetAsync(B.Dd[B.cur].p + off, 0, B.fine_span(trap) * sizeof(float), B.stream));
@@ -2506,6 +2572,7 @@ int eqf_add_nodal(eqf_batch* b, int32_t trap, int64_t n, const int64_t* node,
     EQF_REQUIRE(n >= 0 && (n == 0 || (node && delta)), "bad nodal arrays");
     if (n == 0) return;
     Batch& B = *b->impl;
+    B.bal_prev_ok = false;
     const int64_t nn = B.fine_nodes(trap);
     for (int64_t i = 0; i < n; ++i)
       EQF_REQUIRE(node[i] >= 0 && node[i] < nn && std::isfinite(delta[i]),
@@ -2605,6 +2672,47 @@ int eqf_total_mass(eqf_batch* b, int32_t trap, double* mass) {
     EQF_TRAP_CHECK(b, trap);
     EQF_REQUIRE(mass != nullptr, "null output");
     *mass = trap_reduce(*b->impl, trap, 0);
+  });
+}
+
+int eqf_mass_balance(eqf_batch* b, int32_t enable) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    Batch& B = *b->impl;
+    EQF_REQUIRE(enable == 0 || enable == 1, "enable must be 0 or 1");
+    B.bal_on = enable != 0;
+    B.bal_prev_ok = B.bal_load_ok = false;
+    if (!B.bal_on) return;
+    const size_t n = (size_t)B.ntraps * eqf::kBalFields;
+    if (B.d_bal.n != n) B.d_bal.alloc(n);
+    EQF_CK(cudaMemsetAsync(B.d_bal.p, 0, n * sizeof(double), B.stream));
+    B.sync();
+  });
+}
+
+int eqf_read_balance(eqf_batch* b, int32_t trap, eqf_balance* out) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(out != nullptr, "null output");
+    Batch& B = *b->impl;
+    EQF_REQUIRE(B.d_bal.n > 0, "the mass balance was never enabled (eqf_mass_balance)");
+    double r[eqf::kBalFields];
+    EQF_CK(cudaMemcpyAsync(r, B.d_bal.p + (size_t)trap * eqf::kBalFields, sizeof(r),
+                           cudaMemcpyDeviceToHost, B.stream));
+    B.sync();
+    out->mass = r[eqf::BAL_MASS];
+    out->mass_prev = r[eqf::BAL_MASS_PREV];
+    out->load = r[eqf::BAL_LOAD];
+    out->decay = r[eqf::BAL_DECAY];
+    out->operator_loss = r[eqf::BAL_OPERATOR];
+    out->wall_outflow = r[eqf::BAL_WALL];
+    out->drift = r[eqf::BAL_DRIFT];
+    out->drift_sum = r[eqf::BAL_DRIFT_SUM];
+    out->drift_abs_sum = r[eqf::BAL_DRIFT_ABS_SUM];
+    out->load_sum = r[eqf::BAL_LOAD_SUM];
+    out->drift_rel_max = r[eqf::BAL_DRIFT_REL_MAX];
+    out->steps = (int64_t)r[eqf::BAL_STEPS];
   });
 }
 
@@ -2946,7 +3054,7 @@ int eqf_set_rods(eqf_batch* b, int32_t n_layers, const int32_t* layers, const eq
     rs->cover.alloc(rs->span);
     rs->start.alloc(rs->span + 1);
     rs->cursor.alloc(rs->span);
-    rs->flag.alloc(2);
+    rs->flag.alloc(3);
     rs->ihsl.alloc(n4);
     rs->prod.alloc(n4);
     rs->ehsl.alloc(n4);
@@ -3056,6 +3164,15 @@ int eqf_update_rods_all(eqf_batch* b, int64_t n_total, const eqf_rod* rods,
     if (production)
       for (int64_t i = 0; i < totp; ++i)
         EQF_REQUIRE(std::isfinite(production[i]), "non-finite production");
+    // every set's rods are checked before anything is uploaded: a bad set leaves all
+    // sets (device rods, footprints, waves) as they were
+    {
+      int64_t c = 0;
+      for (const Batch::RodSet* rs : sets) {
+        check_rods(B.params[rs->layers[0]], rods + c, rs->n);
+        c += rs->n;
+      }
+    }
     // stage the rods and the productions (in the device's kRodLayers layout) in pinned
     // memory, so the uploads are asynchronous
     size_t prod4 = 0;
@@ -3066,26 +3183,32 @@ int eqf_update_rods_all(eqf_batch* b, int64_t n_total, const eqf_rod* rods,
     double* hp = reinterpret_cast<double*>(st + ((rbytes + 15) & ~size_t(15)));
     int64_t c0 = 0, p0 = 0;
     size_t q0 = 0;
-    for (Batch::RodSet* rs : sets) {
-      const int nl = (int)rs->layers.size();
-      const size_t n = (size_t)rs->n;
-      check_rods(B.params[rs->layers[0]], rods + c0, rs->n);
-      std::memcpy(st + (size_t)c0 * sizeof(eqf_rod), rods + c0, n * sizeof(eqf_rod));
-      EQF_CK(cudaMemcpyAsync(rs->rods.p, st + (size_t)c0 * sizeof(eqf_rod),
-                             n * sizeof(eqf_rod), cudaMemcpyHostToDevice, B.stream));
-      if (production) {
-        double* q = hp + q0;
-        std::fill(q, q + n * eqf::kRodLayers, 0.0);
-        for (size_t c = 0; c < n; ++c)
-          for (int l = 0; l < nl; ++l) q[c * eqf::kRodLayers + l] = production[p0 + c * nl + l];
-        EQF_CK(cudaMemcpyAsync(rs->prod.p, q, n * eqf::kRodLayers * sizeof(double),
-                               cudaMemcpyHostToDevice, B.stream));
+    try {
+      for (Batch::RodSet* rs : sets) {
+        const int nl = (int)rs->layers.size();
+        const size_t n = (size_t)rs->n;
+        std::memcpy(st + (size_t)c0 * sizeof(eqf_rod), rods + c0, n * sizeof(eqf_rod));
+        EQF_CK(cudaMemcpyAsync(rs->rods.p, st + (size_t)c0 * sizeof(eqf_rod),
+                               n * sizeof(eqf_rod), cudaMemcpyHostToDevice, B.stream));
+        if (production) {
+          double* q = hp + q0;
+          std::fill(q, q + n * eqf::kRodLayers, 0.0);
+          for (size_t c = 0; c < n; ++c)
+            for (int l = 0; l < nl; ++l) q[c * eqf::kRodLayers + l] = production[p0 + c * nl + l];
+          EQF_CK(cudaMemcpyAsync(rs->prod.p, q, n * eqf::kRodLayers * sizeof(double),
+                                 cudaMemcpyHostToDevice, B.stream));
+        }
+        c0 += rs->n;
+        p0 += (int64_t)rs->n * nl;
+        q0 += n * eqf::kRodLayers;
       }
-      c0 += rs->n;
-      p0 += (int64_t)rs->n * nl;
-      q0 += n * eqf::kRodLayers;
+      B.rod_analyse_sets(sets);  // ends with a sync: the staging may be reused
+    } catch (...) {
+      // copies may still read the pinned staging: let them finish before the next
+      // call writes it
+      cudaStreamSynchronize(B.stream);
+      throw;
     }
-    B.rod_analyse_sets(sets);  // ends with a sync: the staging may be reused
     B.rod_publish();
   });
 }
@@ -3155,6 +3278,14 @@ int eqf_rod_waves(eqf_batch* b, int32_t* waves) {
   int w = 0;
   for (const auto& rs : b->impl->rod_sets) w = std::max(w, rs->waves);
   *waves = w;
+  return EQF_OK;
+}
+
+int eqf_rod_relax_passes(eqf_batch* b, int32_t* passes) {
+  if (!b || !passes) return EQF_ERR_INVALID;
+  int p = 0;
+  for (const auto& rs : b->impl->rod_sets) p = std::max(p, rs->relax_passes);
+  *passes = p;
   return EQF_OK;
 }
 

@@ -114,17 +114,25 @@ extern "C" int eqf_field_integral_noalloc(const double* d_field, int32_t nx, int
   if (!d_field || !out || nx < 1 || ny < 1 || !(width > 0.0) || !(height > 0.0) ||
       (what != 0 && what != 1))
     return EQF_ERR_INVALID;
-  const long long n = (long long)(nx + 1) * (long long)(ny + 1);
+  const long long n = ((long long)nx + 1) * ((long long)ny + 1);
   if (n > (long long)EQF_NOALLOC_MAX_NODES) return EQF_ERR_TOO_LARGE;
   double* scratch = nullptr;
   const int rc = scratch_for_current_device(&scratch);
   if (rc != EQF_OK) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int nblocks = (int)((n + kNoallocBlockNodes - 1) / kNoallocBlockNodes);
-  k_noalloc_partials<<<nblocks, kNoallocThreads, 0, s>>>(d_field, nx, ny, width / nx,
-                                                          height / ny, what, scratch);
-  k_noalloc_total<<<1, 32, 0, s>>>(scratch, nblocks, scale);
-  if (cudaGetLastError() != cudaSuccess) return EQF_ERR_CUDA;
+  int nblocks = (int)((n + kNoallocBlockNodes - 1) / kNoallocBlockNodes);
+  double hx = width / nx, hy = height / ny;
+  // each launch's status comes from its own cudaLaunchKernel call: a cudaGetLastError
+  // afterwards would also take (and clear) an error the caller had left pending
+  void* part_args[] = {(void*)&d_field, (void*)&nx, (void*)&ny, (void*)&hx, (void*)&hy,
+                       (void*)&what, (void*)&scratch};
+  if (cudaLaunchKernel((const void*)k_noalloc_partials, dim3(nblocks), dim3(kNoallocThreads),
+                       part_args, 0, s) != cudaSuccess)
+    return EQF_ERR_CUDA;
+  void* total_args[] = {(void*)&scratch, (void*)&nblocks, (void*)&scale};
+  if (cudaLaunchKernel((const void*)k_noalloc_total, dim3(1), dim3(32), total_args, 0, s) !=
+      cudaSuccess)
+    return EQF_ERR_CUDA;
   if (cudaMemcpyAsync(out, scratch + kNoallocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost,
                       s) != cudaSuccess)
     return EQF_ERR_CUDA;

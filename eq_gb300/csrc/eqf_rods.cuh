@@ -238,9 +238,13 @@ __global__ void k_rod_preds(int nent, const int* __restrict__ node, long long ke
 // The waves of one rod set in one CTA: passes of wave[c] = max over c's predecessors
 // of wave[pred] + 1, separated by CTA barriers, until a pass changes nothing.  A chain of n cells settles within n
 // passes; past that bound the kernel stops and sets *unsettled (never expected).
+// *passes receives the number of passes run (the last one changing nothing): each
+// costs one sweep over all nent entries on this one CTA, so the relaxation's time
+// grows with nent times the longest dependency chain.
 __global__ void __launch_bounds__(1024)
     k_rod_relax_all(int nent, int n, const int* __restrict__ pred, const int* __restrict__ succ,
-                    int* __restrict__ wave, int* __restrict__ unsettled) {
+                    int* __restrict__ wave, int* __restrict__ unsettled,
+                    int* __restrict__ passes) {
   __shared__ int changed;
   for (int pass = 0; pass <= n + 1; ++pass) {
     if (threadIdx.x == 0) changed = 0;
@@ -254,10 +258,16 @@ __global__ void __launch_bounds__(1024)
       if (w > __ldcg(&wave[c]) && atomicMax(&wave[c], w) < w) changed = 1;
     }
     __syncthreads();  // this pass's waves are visible to the whole CTA
-    if (!changed) return;
+    if (!changed) {
+      if (threadIdx.x == 0) *passes = pass + 1;
+      return;
+    }
     __syncthreads();  // every thread has read `changed` before it is reset
   }
-  if (threadIdx.x == 0) *unsettled = 1;
+  if (threadIdx.x == 0) {
+    *unsettled = 1;
+    *passes = n + 2;
+  }
 }
 
 // wave sizes and the highest wave

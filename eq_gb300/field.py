@@ -324,6 +324,11 @@ class TrapBatch:
         self._ck(self._lib.eqf_rod_waves(self._h, C.byref(w)))
         return w.value
 
+    def rod_relax_passes(self) -> int:
+        p = C.c_int32()
+        self._ck(self._lib.eqf_rod_relax_passes(self._h, C.byref(p)))
+        return p.value
+
     def read_nodal(self, trap: int, out: Optional[np.ndarray] = None) -> np.ndarray:
         if out is None:
             out = np.empty(self.num_nodes(trap))
@@ -346,6 +351,21 @@ class TrapBatch:
         v = C.c_double()
         self._ck(self._lib.eqf_total_mass(self._h, trap, C.byref(v)))
         return v.value
+
+    def set_active(self, trap: int, active: bool):
+        """Freezes (False) or resumes (True) a trap (eqf_set_active)."""
+        self._ck(self._lib.eqf_set_active(self._h, int(trap), 1 if active else 0))
+
+    def mass_balance(self, enable: bool = True):
+        """Per-step FP64 mass balance of every trap (eqf_mass_balance); enabling zeroes
+        the sums."""
+        self._ck(self._lib.eqf_mass_balance(self._h, 1 if enable else 0))
+
+    def read_balance(self, trap: int) -> Dict[str, float]:
+        """The last step's balance terms of a trap and the sums since enabled."""
+        out = _lib.Balance()
+        self._ck(self._lib.eqf_read_balance(self._h, trap, C.byref(out)))
+        return {name: getattr(out, name) for name, _ in _lib.Balance._fields_}
 
     def stats(self, trap: int) -> Dict[str, float]:
         st, sw, it = C.c_int64(), C.c_int64(), C.c_int64()

@@ -136,6 +136,16 @@ def batched_uneven(seed: int = 3, n_traps: int = 512, h: float = 0.25,
     return traps
 
 
+def stratified_sample(traps: List[Trap], k: int) -> List[int]:
+    """Indices of k traps spread evenly over the batch sorted by node count (the
+    smallest and the largest included); deterministic."""
+    order = np.argsort([t.n_nodes for t in traps], kind="stable")
+    if k >= len(traps):
+        return [int(i) for i in order]
+    pos = np.linspace(0, len(traps) - 1, k).round().astype(int)
+    return [int(order[p]) for p in pos]
+
+
 def scaled(trap: Trap, nx: int, ny: int, n_cells: Optional[int] = None,
            seed: int = 7) -> Trap:
     """Same physics and domain as ``trap`` on a coarser mesh with fresh cells."""

@@ -200,6 +200,33 @@ int eqf_boundary_flux(eqf_batch* b, int32_t trap, double* flux);
 /* Total amount 1^T M c (FP64), for the mass-balance check. */
 int eqf_total_mass(eqf_batch* b, int32_t trap, double* mass);
 
+/* FP64 total-HSL mass balance of every step (no reference counterpart: the
+ * reference keeps only the facet flux functional of the new field,
+ * fenics/boundary.ufl:9-12, src/fHSL.cpp:156-160, and the boundary well built on it,
+ * src/simulation.cpp:581-604).  While enabled, every step ends with an FP64
+ * reduction over each trap (one extra pass over the old and new fields and the load)
+ * that closes the step's discrete balance
+ *   mass - mass_prev = load - decay - operator_loss - wall_outflow + drift
+ * where mass = 1^T M c^{n+1}; mass_prev = 1^T M c^n, the field the step started from
+ * (after any deposit into it); load = the sum of the step's load F (point cells,
+ * Robin walls); decay = dt*g*mass; operator_loss = 1^T (dt C + R) c^{n+1} (advective
+ * and Robin outflow); wall_outflow = the consistent flux through the Dirichlet walls
+ * (minus the full operator's residual summed over the Dirichlet rows); drift = the
+ * solver's residual summed over the free rows, zero up to the step's tolerance.
+ * Enabling (again) zeroes the sums; eqf_read_balance returns the last step's terms
+ * and the sums since then. */
+typedef struct eqf_balance {
+  double mass, mass_prev, load, decay, operator_loss, wall_outflow, drift;
+  double drift_sum;     /* sum of drift over the steps since enabled */
+  double drift_abs_sum; /* sum of |drift| */
+  double load_sum;      /* sum of load */
+  double drift_rel_max; /* max over steps of |drift| / max(|mass|, |mass_prev|, |load|,
+                           |wall_outflow|) */
+  int64_t steps;        /* steps since enabled (frozen traps' steps not counted) */
+} eqf_balance;
+int eqf_mass_balance(eqf_batch* b, int32_t enable);
+int eqf_read_balance(eqf_batch* b, int32_t trap, eqf_balance* out);
+
 /* Solver statistics of a trap since creation: steps, refinement sweeps and
  * Krylov iterations, and the last step's relative FP64 residual. */
 int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64_t* iters,
@@ -437,6 +464,11 @@ int eqf_exchange_rods(eqf_batch* b);
 /* Number of sequential waves the exchange of the current rod cells takes (1 when
  * no two cells share a footprint node). */
 int eqf_rod_waves(eqf_batch* b, int32_t* waves);
+/* Passes the last wave analysis of any rod set took to settle (0 when no set has a
+ * shared node).  The analysis relaxes every footprint entry once per pass in one CTA,
+ * so its device time grows with the entries times this count (the longest chain of
+ * cells sharing nodes, plus one). */
+int eqf_rod_relax_passes(eqf_batch* b, int32_t* passes);
 
 /* Built-in profiler (no counterpart in the reference, which only keeps MPI_Wtime
  * accumulators, src/simulation.h:512-521).  While enabled, steps run without CUDA
@@ -449,12 +481,13 @@ int eqf_rod_waves(eqf_batch* b, int32_t* waves);
  * finest level, coarser levels, CG direction (q = A p), CG update, refinement
  * residual (first of a step), refinement residual, refinement update, per-trap
  * scalar phases, finest-level fused pre-smoothing + residual, finest-level fused
- * prolongation + post-smoothing, rod-cell exchange (eqf_set_rods). */
+ * prolongation + post-smoothing, rod-cell exchange (eqf_set_rods), mass balance
+ * (eqf_mass_balance). */
 /* The CUDA stream (cudaStream_t) all work of the batch is queued on, for callers
  * that time the batch with their own CUDA events or order their own work. */
 int eqf_stream(eqf_batch* b, void** stream);
 
-#define EQF_PROF_CLASSES 15
+#define EQF_PROF_CLASSES 16
 int eqf_profile(eqf_batch* b, int32_t enable);
 int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
                      int64_t* nodes, double* bytes);
@@ -473,8 +506,9 @@ int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launc
  * the library (about 32 KB per GPU, held until exit), sized for at most
  * EQF_NOALLOC_MAX_NODES nodes; larger fields return EQF_ERR_TOO_LARGE.  The first
  * call on each device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race, so serialise them. */
+ * make that first call before any stream capture.  Every call waits on `stream` for
+ * its result (cudaStreamSynchronize) and copies it into *out.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them. */
 #define EQF_NOALLOC_MAX_NODES 8388608
 int eqf_field_integral_noalloc(const double* d_field, int32_t nx, int32_t ny, double width,
                                double height, int32_t what, double scale, void* stream,

@@ -337,6 +337,7 @@ class HsldOracle:
             A = A + sp.coo_matrix((np.concatenate(Rv), (np.concatenate(Rr), np.concatenate(Rc))),
                                   shape=A.shape).tocsr()
         self.M = _assemble(m, tabulate_mass(m))
+        self.A_full = A  # before the Dirichlet rows are replaced (for the balance)
         self.dir = m.wall_nodes(self.walls)
         # DirichletBC.apply: zero the row, unit diagonal, rhs = wall value (0)
         Dm = sp.diags((~self.dir).astype(np.float64))
@@ -359,6 +360,24 @@ class HsldOracle:
         if self.lu is None:
             return spla.spsolve(self.A, b)
         return self.lu.solve(b)
+
+    def balance(self, u_new: np.ndarray, u_old: np.ndarray,
+                F: Optional[np.ndarray] = None) -> dict:
+        """Discrete balance of one step from the assembled matrices.  r = A_full u_new
+        - M u_old - F_full on every row (A_full without the Dirichlet replacement,
+        F_full the point load plus the Robin load); its sum over the Dirichlet rows is
+        minus the wall outflow, over the free rows the drift.  The decay and operator
+        terms split 1'A_full u_new - 1'M u_new (the stiffness sums to zero)."""
+        Ff = self.robin_load + (0.0 if F is None else F)
+        r = self.A_full @ u_new - self.M @ u_old - Ff
+        mass = float(np.sum(self.M @ u_new))
+        decay = self.dt * self.g * mass
+        total_op = float(np.sum(self.A_full @ u_new))
+        return {"mass": mass, "mass_prev": float(np.sum(self.M @ u_old)),
+                "load": float(np.sum(Ff)), "decay": decay,
+                "operator_loss": total_op - (1.0 + self.dt * self.g) * mass,
+                "wall_outflow": -float(np.sum(r[self.dir])),
+                "drift": float(np.sum(r[~self.dir]))}
 
     def total_mass(self, u: np.ndarray) -> float:
         return float(np.sum(self.M @ u))

@@ -31,7 +31,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(REF_DIR, "libhsld_ref2.so")
-REFERENCE = os.environ.get("EQ_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: EQ_REFERENCE_ROOT, else a "reference" directory beside the
+# repository
+REFERENCE = os.environ.get("EQ_REFERENCE_ROOT",
+                           os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 HSLD_CLASSES = ["hsld_cell_integral_0_otherwise", "hsld_exterior_facet_integral_0_1",
                 "hsld_exterior_facet_integral_0_2", "hsld_cell_integral_1_otherwise",

@@ -39,7 +39,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(REF_DIR, "librods_ref.so")
-REFERENCE = os.environ.get("EQ_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: EQ_REFERENCE_ROOT, else a "reference" directory beside the
+# repository
+REFERENCE = os.environ.get("EQ_REFERENCE_ROOT",
+                           os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 STUBS = r'''
 // Stand-ins for what the sliced reference code needs (not reference code).

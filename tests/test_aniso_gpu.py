@@ -130,7 +130,7 @@ def test_bottom_levels_kernel_with_general_path_traps(lib):
     base = wl.batched_uneven(8, 3)
     traps = [wl.scaled(t, t.nx // 4 * 2, t.ny // 4 * 2, n_cells=60) for t in base]
     tens = {0: smooth_field(traps[0].nx, traps[0].ny, traps[0].W, traps[0].H)}
-    res = []
+    res, launches = [], []
     for fuse in (2, 1):
         with F.TrapBatch([F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls)
                           for t in traps],
@@ -141,5 +141,11 @@ def test_bottom_levels_kernel_with_general_path_traps(lib):
                     b.set_tensor(i, *tens[i])
             b.step(3)
             res.append([b.read_nodal(i) for i in range(len(traps))])
+            b.profile(True)
+            b.step(1)
+            b.sync()
+            launches.append(b.profile_read()["coarse"]["launches"])
+            b.profile(False)
     for a, c in zip(res[0], res[1]):
         assert np.array_equal(a, c)
+    assert launches[0] < launches[1]  # the one-kernel bottom levels ran

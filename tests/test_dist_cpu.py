@@ -34,12 +34,16 @@ def _rank_main(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        traps = wl.batched_uneven(shard.rank_seed(3, rank), 16)  # weak scaling: own batch
-        mine = shard.balanced_shards([t.n_nodes for t in traps], world)[rank]
-        nodes = sum(traps[i].n_nodes for i in mine)
+        # weak scaling (bench.py's mode): every rank steps its own batch
+        own = wl.batched_uneven(shard.rank_seed(3, rank), 16)
+        nodes = sum(t.n_nodes for t in own)
+        # strong scaling: one shared workload split into per-rank shards of whole traps
+        common = wl.batched_uneven(3, 16)
+        mine = shard.balanced_shards([t.n_nodes for t in common], world)[rank]
         fake_ms = 10.0 + 5.0 * rank
         dist.barrier()
-        q.put((rank, shard.max_over_ranks(fake_ms), shard.sum_over_ranks(nodes), sorted(mine)))
+        q.put((rank, shard.max_over_ranks(fake_ms), shard.sum_over_ranks(nodes), sorted(mine),
+               [(t.nx, t.ny) for t in own], nodes))
     finally:
         dist.destroy_process_group()
 
@@ -58,5 +62,9 @@ def test_two_gloo_ranks_reduce_timing_and_place_traps():
         assert p.exitcode == 0
     res = sorted(q.get(timeout=10) for _ in range(2))
     assert res[0][1] == res[1][1] == 15.0  # max over ranks
-    assert res[0][2] == res[1][2]  # same global sum on both ranks
-    assert set(res[0][3]).isdisjoint(res[1][3]) or res[0][3] != res[1][3]
+    assert res[0][2] == res[1][2] == res[0][5] + res[1][5]  # global sum of the own batches
+    # strong-scaling shards: disjoint, together the whole workload
+    assert set(res[0][3]).isdisjoint(res[1][3])
+    assert sorted(res[0][3] + res[1][3]) == list(range(16))
+    # weak scaling: the ranks' batches are different draws
+    assert res[0][4] != res[1][4]

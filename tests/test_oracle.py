@@ -172,3 +172,47 @@ def test_odd_mesh_fixture_reproduces():
                        walls=walls, cell_xy=d["xy"], cell_s=d["s"])
         out = hsld.run_trap(trap, steps=8)
         assert _rel(out["u"][0], d[f"u_walls{walls}"]) < 1e-12
+
+
+def test_oracle_step_closes_its_mass_balance():
+    """The balance identity on the oracle's own direct solve: the drift (free rows'
+    residual sum) is rounding, the wall outflow is the consistent flux and agrees with
+    the reference's facet functional up to the discretisation."""
+    t = wl.single_small(0)
+    o = hsld.HsldOracle(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls)
+    Fl = hsld.point_load(o.mesh, t.cell_xy, t.cell_s, scale=t.dt)
+    u = np.zeros(o.mesh.n_nodes)
+    for _ in range(30):
+        un = o.step(u, Fl)
+        bal = o.balance(un, u, Fl)
+        u = un
+        assert abs(bal["drift"]) <= 1e-12 * bal["mass"]
+        lhs = bal["mass"] - bal["mass_prev"]
+        rhs = bal["load"] - bal["decay"] - bal["operator_loss"] - bal["wall_outflow"]
+        assert abs(lhs - rhs - bal["drift"]) <= 1e-12 * bal["mass"]
+    assert bal["operator_loss"] == pytest.approx(0.0, abs=1e-12 * bal["mass"])
+    assert abs(bal["load"] - t.dt * t.cell_s.sum()) <= 1e-12 * bal["load"]
+    flux = o.boundary_flux(u)
+    assert flux > 0 and abs(bal["wall_outflow"] - flux) <= 0.2 * flux
+
+
+@pytest.mark.parametrize("name", ["single_large_oracle.npz", "two_species_oracle.npz",
+                                  "batched_sample_oracle.npz"])
+def test_config_fixtures_are_self_consistent(name):
+    """The full-size fixtures: their cell values are the barycentric gather of their
+    nodal fields at the workload's cells, and the batched sample is the stratified one."""
+    g = np.load(os.path.join(GOLDEN, name))
+    if name == "single_large_oracle.npz":
+        t, pairs = wl.single_large(1), [("c0_500", "u0_500"), ("c0_50", "u0_50")]
+    elif name == "two_species_oracle.npz":
+        t, pairs = wl.two_species(2), [("c0_300", "u0_300"), ("c1_300", "u1_300")]
+    else:
+        traps = wl.batched_uneven(int(g["seed"]), int(g["n_traps"]))
+        idx = [int(i) for i in g["traps"]]
+        assert idx == wl.stratified_sample(traps, len(idx))
+        t, pairs = traps[idx[-1]], [(f"t{idx[-1]}_c0_200", f"t{idx[-1]}_u0_200")]
+    mesh = hsld.RightMesh(t.W, t.H, t.nx, t.ny)
+    for c, u in pairs:
+        assert g[u].shape == (t.n_nodes,)
+        assert np.allclose(hsld.gather(mesh, g[u], t.cell_xy), g[c], rtol=1e-13, atol=0)
+        assert np.all(np.isfinite(g[u])) and np.abs(g[u]).max() > 0

@@ -251,11 +251,22 @@ def test_fused_and_unfused_level_kernels_agree(lib, precision):
     assert rel(out[1], out[2]) <= TOL[precision]
 
 
+def coarse_launches(b):
+    """Launches of the coarse-level class in one profiled step: the one-kernel bottom
+    levels replace several launches per V-cycle, so fewer launches show that it ran."""
+    b.profile(True)
+    b.step(1)
+    b.sync()
+    n = b.profile_read()["coarse"]["launches"]
+    b.profile(False)
+    return n
+
+
 def test_bottom_levels_kernel_on_uneven_traps(lib):
     """Uneven traps of a batch share the level count; the one-kernel bottom levels
     (per trap, in shared memory) give the step-by-step path's solution."""
     traps = wl.batched_uneven(6, 6)
-    res = []
+    res, launches = [], []
     for fuse in (2, 0):
         with F.TrapBatch([tparams(t) for t in traps],
                          F.default_opts(F.FP32_IR, use_graph=1, fuse_levels=fuse)) as b:
@@ -263,8 +274,10 @@ def test_bottom_levels_kernel_on_uneven_traps(lib):
                 b.set_cells(i, t.cell_xy, t.cell_s)
             b.step(5)
             res.append([b.read_nodal(i) for i in range(len(traps))])
+            launches.append(coarse_launches(b))
     for a, c in zip(res[0], res[1]):
         assert rel(a, c) <= 1e-6
+    assert launches[0] < launches[1]
 
 
 @pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
@@ -272,7 +285,7 @@ def test_bottom_levels_kernel_is_bit_identical_to_level_kernels(lib, precision):
     """The one-kernel bottom levels evaluate the fused level kernels' expressions on
     the same operands: the same bits whichever level the batch starts it at."""
     traps = wl.batched_uneven(3, 4)
-    res = []
+    res, launches = [], []
     for fuse in (2, 1):
         with F.TrapBatch([tparams(t) for t in traps],
                          F.default_opts(precision, use_graph=1, fuse_levels=fuse)) as b:
@@ -280,5 +293,7 @@ def test_bottom_levels_kernel_is_bit_identical_to_level_kernels(lib, precision):
                 b.set_cells(i, t.cell_xy, t.cell_s)
             b.step(4)
             res.append([b.read_nodal(i) for i in range(len(traps))])
+            launches.append(coarse_launches(b))
     for a, c in zip(res[0], res[1]):
         assert np.array_equal(a, c)
+    assert launches[0] < launches[1]  # k_bottom ran
