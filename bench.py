@@ -354,6 +354,7 @@ def run_ours(args, rank, world, local_rank):
     c32 = {i: b.read_cells(i) for i in idx}
     rels, relc = [], []
     fp64_ms, fp64_dofs = 0.0, 0
+    ref64 = {}
     o64 = F.default_opts(F.FP64, use_graph=1, adaptive=1)
     for i in idx:
         with F.TrapBatch([tps[i]], o64) as b1:
@@ -370,9 +371,38 @@ def run_ours(args, rank, world, local_rank):
             fp64_dofs += traps[i].n_nodes * (total_steps - 1)
             u64 = b1.read_nodal(0)
             cc = b1.read_cells(0)
+        ref64[i] = (u64, cc)
         rels.append(float(np.linalg.norm(u32[i] - u64) / max(np.linalg.norm(u64), 1e-300)))
         relc.append(float(np.linalg.norm(c32[i] - cc) / max(np.linalg.norm(cc), 1e-300)))
     fp64_rate = fp64_dofs / (fp64_ms / 1e3)
+
+    # ---- the same form with its refinement residual in FP64 instead of float pairs
+    #      (eqf_solver_opts.residual64): the same timed steps, relL2 on the same sample
+    variant = None
+    if not args.no_variant:
+        vb = F.TrapBatch(tps, F.default_opts(F.FP32_IR, use_graph=1, adaptive=1,
+                                             tile_nodes=args.tile_nodes, residual64=1,
+                                             fuse_levels=opts.fuse_levels), tune=table)
+        load_traps(vb, traps)
+        vb.step(args.warmup)
+        vb.sync()
+        vb.mass_balance(True)  # as in the timed run
+        vs = torch.cuda.ExternalStream(vb.stream_handle())
+        v0, v1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        v0.record(vs)
+        for _ in range(args.steps):
+            vb.step(1)
+        v1.record(vs)
+        vb.sync()
+        vms = v0.elapsed_time(v1)
+        vrel = max(rel(vb.read_nodal(i), ref64[i][0]) for i in idx)
+        vrelc = max(rel(vb.read_cells(i), ref64[i][1]) for i in idx)
+        vb.close()
+        variant = {"residual": "FP64 (the plain form's refinement kernels)",
+                   "value": nodes * args.steps / (vms / 1e3), "ms_per_step": vms / args.steps,
+                   "relL2_vs_fp64": {"nodal_max": vrel, "cells_max": vrelc},
+                   "default_residual": "float pairs (~47 bits) on the FP32 pipe",
+                   "default_value": value / world}
 
     # ---- profiled pass (no graphs): per kernel class time / nodes / bytes
     prof_steps = max(2, min(args.steps, 5))
@@ -463,6 +493,7 @@ def run_ours(args, rank, world, local_rank):
             "solver": {"sweeps_per_step": sweeps_ps, "iters_per_step": iters_ps,
                        "sample": f"{len(probe)} traps stratified by size, timed steps"},
             "mass_balance": balance,
+            "fp64_residual_variant": variant,
             "oracle_checks": checks,
             "roofline": roofline,
             "operator_roofline": operator_roofline,
@@ -838,6 +869,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variant", action="store_true",
+                    help="skip the timed pass with the refinement residual in FP64")
     ap.add_argument("--no-oracle", action="store_true",
                     help="skip the full-size checks against the oracle's fixtures")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: requests/s")

@@ -39,6 +39,7 @@ EXPORTS = (
     "eqf_read_well", "eqf_set_tensor", "eqf_trap_info", "eqf_json_open", "eqf_json_frame", "eqf_json_frame_host",
     "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
     "eqf_vtk_write_host", "eqf_vtk_close", "eqf_mass_balance", "eqf_read_balance",
+    "eqf_read_nodal_dof", "eqf_set_nodal_dof", "eqf_set_well_concentration",
     "eqf_rod_relax_passes",
 )
 
@@ -72,7 +73,8 @@ class SolverOpts(C.Structure):
                 ("max_iters", C.c_int32), ("inner_tol", C.c_double), ("cheb_pre", C.c_int32),
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
                 ("use_graph", C.c_int32), ("adaptive", C.c_int32),
-                ("tile_nodes", C.c_int32), ("krylov", C.c_int32), ("fuse_levels", C.c_int32)]
+                ("tile_nodes", C.c_int32), ("krylov", C.c_int32), ("fuse_levels", C.c_int32),
+                ("residual64", C.c_int32)]
 
 
 class TuneBucket(C.Structure):
@@ -200,6 +202,9 @@ def load() -> C.CDLL:
         "eqf_rod_relax_passes": (C.c_int, [C.c_void_p, P(C.c_int32)]),
         "eqf_mass_balance": (C.c_int, [C.c_void_p, C.c_int32]),
         "eqf_read_balance": (C.c_int, [C.c_void_p, C.c_int32, P(Balance)]),
+        "eqf_read_nodal_dof": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32), dp]),
+        "eqf_set_nodal_dof": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32), dp]),
+        "eqf_set_well_concentration": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -1317,19 +1317,24 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   const double tol_abs = fp32 ? 0.3 * B.opts.rtol : B.opts.rtol;
   double* u_out = B.U[1 - B.cur].p;
   float* d_out = B.Dd[1 - B.cur].p;
+  bool pairs = false;
   if constexpr (std::is_same<T, float>::value) {
-    // FP32 form: residuals in float-pair arithmetic, rhs b kept as pairs
-    float2* b2 = reinterpret_cast<float2*>(B.b64.p);
-    if (first)
-      EQF_RUN(B, KC_IR_RESID_FIRST,
-              (launch_pdl(k_irf_first, nt, kThreads, L0.sm_irf1, s, 
-                  G, tl, B.tabA2.p, B.tabM2.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
-                  b2, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
-    else
-      EQF_RUN(B, KC_IR_RESID,
-              (launch_pdl(k_irf_residual<false>, nt, kThreads, L0.sm_irf, s, 
-                  G, tl, B.tabA2.p, B.d_ir_done.p, b2, u_out, d_out, r, part, nt, W)));
-  } else {
+    pairs = !B.opts.residual64;
+    if (pairs) {
+      // FP32 form: residuals in float-pair arithmetic, rhs b kept as pairs
+      float2* b2 = reinterpret_cast<float2*>(B.b64.p);
+      if (first)
+        EQF_RUN(B, KC_IR_RESID_FIRST,
+                (launch_pdl(k_irf_first, nt, kThreads, L0.sm_irf1, s,
+                    G, tl, B.tabA2.p, B.tabM2.p, B.dstate.p, B.F.p, B.U[B.cur].p, B.Dd[B.cur].p,
+                    b2, u_out, d_out, r, part, nt, B.d_frozen.p, W)));
+      else
+        EQF_RUN(B, KC_IR_RESID,
+                (launch_pdl(k_irf_residual<false>, nt, kThreads, L0.sm_irf, s,
+                    G, tl, B.tabA2.p, B.d_ir_done.p, b2, u_out, d_out, r, part, nt, W)));
+    }
+  }
+  if (!pairs) {  // FP64 residuals (the plain form; the FP32 form with residual64)
     if (first)
       EQF_RUN(B, KC_IR_RESID_FIRST,
               (launch_pdl(k_ir_first<T>, nt, kThreads, L0.sm_ir, s, 
@@ -1457,13 +1462,17 @@ template <class T>
 void Work<T>::enqueue_check(cudaStream_t s, bool update_gamma) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
-  if constexpr (std::is_same<T, float>::value)
-    EQF_RUN(B, KC_IR_RESID,
-            (launch_pdl(k_irf_residual<true>, nt, kThreads, L0.sm_irf, s, 
-                L0.dgeom.p, L0.dtiles.p, B.tabA2.p, B.d_ir_done.p,
-                reinterpret_cast<const float2*>(B.b64.p), B.U[1 - B.cur].p, B.Dd[1 - B.cur].p,
-                lv[0].b.p, B.dpart.p, nt, W)));
-  else
+  bool pairs = false;
+  if constexpr (std::is_same<T, float>::value) {
+    pairs = !B.opts.residual64;
+    if (pairs)
+      EQF_RUN(B, KC_IR_RESID,
+              (launch_pdl(k_irf_residual<true>, nt, kThreads, L0.sm_irf, s,
+                  L0.dgeom.p, L0.dtiles.p, B.tabA2.p, B.d_ir_done.p,
+                  reinterpret_cast<const float2*>(B.b64.p), B.U[1 - B.cur].p, B.Dd[1 - B.cur].p,
+                  lv[0].b.p, B.dpart.p, nt, W)));
+  }
+  if (!pairs)
     EQF_RUN(B, KC_IR_RESID,
             (launch_pdl(k_ir_residual<T, true>, nt, kThreads, L0.sm_ir, s, 
                 L0.dgeom.p, L0.dtiles.p, L0.tabd.p, B.d_ir_done.p, B.b64.p, B.U[1 - B.cur].p,
@@ -2620,6 +2629,51 @@ int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c) {
   });
 }
 
+namespace {
+// dof_from_vertex must be a permutation of 0 .. n-1
+void check_dof_map(const int32_t* dof, long long n) {
+  EQF_REQUIRE(dof != nullptr, "null DOF map");
+  std::vector<unsigned char> seen((size_t)n, 0);
+  for (long long v = 0; v < n; ++v) {
+    const int32_t d = dof[v];
+    EQF_REQUIRE(d >= 0 && d < n && !seen[(size_t)d], "the DOF map is not a permutation");
+    seen[(size_t)d] = 1;
+  }
+}
+}  // namespace
+
+int eqf_read_nodal_dof(eqf_batch* b, int32_t trap, const int32_t* dof_from_vertex, double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(c != nullptr, "null output");
+    Batch& B = *b->impl;
+    const long long n = B.fine_nodes(trap);
+    check_dof_map(dof_from_vertex, n);
+    std::vector<double> grid((size_t)n);
+    B.copy_field_to_host(grid.data(), B.u_cur() + B.L[0].geom[trap].off, trap, B.stream);
+    B.sync();
+    B.check_fail();
+    for (long long v = 0; v < n; ++v) c[dof_from_vertex[v]] = grid[(size_t)v];
+  });
+}
+
+int eqf_set_nodal_dof(eqf_batch* b, int32_t trap, const int32_t* dof_from_vertex,
+                      const double* c) {
+  if (!b) return EQF_ERR_INVALID;
+  std::vector<double> grid;
+  const int rc = guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(c != nullptr, "null field");
+    const long long n = b->impl->fine_nodes(trap);
+    check_dof_map(dof_from_vertex, n);
+    grid.resize((size_t)n);
+    for (long long v = 0; v < n; ++v) grid[(size_t)v] = c[dof_from_vertex[v]];
+  });
+  if (rc != EQF_OK) return rc;
+  return eqf_set_nodal(b, trap, grid.data());
+}
+
 int eqf_read_cells(eqf_batch* b, int32_t trap, int64_t n, double* c) {
   if (!b) return EQF_ERR_INVALID;
   return guarded(b, [&] {
@@ -2875,6 +2929,18 @@ int eqf_set_well(eqf_batch* b, int32_t trap, double well_scaling, double decay_r
     B.well[trap].scale = well_scaling;
     B.well[trap].decay = decay_rate;
     B.setup_wells();
+  });
+}
+
+int eqf_set_well_concentration(eqf_batch* b, int32_t trap, double concentration) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_TRAP_CHECK(b, trap);
+    EQF_REQUIRE(std::isfinite(concentration), "non-finite concentration");
+    Batch& B = *b->impl;
+    EQF_CK(cudaMemcpyAsync(B.d_well_c.p + trap, &concentration, sizeof(double),
+                           cudaMemcpyHostToDevice, B.stream));
+    B.sync();
   });
 }
 

@@ -335,6 +335,23 @@ class TrapBatch:
         self._ck(self._lib.eqf_read_nodal(self._h, trap, _dp(out)))
         return out
 
+    def read_nodal_dof(self, trap: int, dof_from_vertex: np.ndarray) -> np.ndarray:
+        """The nodal field in a DOF order: out[dof_from_vertex[v]] = field(v)."""
+        dof = np.ascontiguousarray(dof_from_vertex, dtype=np.int32)
+        out = np.empty(self.num_nodes(trap))
+        self._ck(self._lib.eqf_read_nodal_dof(self._h, trap,
+                                              dof.ctypes.data_as(C.POINTER(C.c_int32)), _dp(out)))
+        return out
+
+    def set_nodal_dof(self, trap: int, dof_from_vertex: np.ndarray, c: np.ndarray):
+        dof = np.ascontiguousarray(dof_from_vertex, dtype=np.int32)
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        self._ck(self._lib.eqf_set_nodal_dof(self._h, trap,
+                                             dof.ctypes.data_as(C.POINTER(C.c_int32)), _dp(c)))
+
+    def set_well_concentration(self, trap: int, c: float):
+        self._ck(self._lib.eqf_set_well_concentration(self._h, trap, float(c)))
+
     def read_cells(self, trap: int, out: Optional[np.ndarray] = None) -> np.ndarray:
         n = self._ncells[trap]
         if out is None:

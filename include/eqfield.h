@@ -92,6 +92,11 @@ typedef struct eqf_solver_opts {
                         * the coarsest in one kernel, one CTA per trap (bit-identical to
                         * 1; slower on large uneven batches, where the largest trap's
                         * CTA sets the time) */
+  int32_t residual64;  /* FP32 form: 0 (default) evaluates the refinement's right-hand
+                        * side b = F + M c^n and residual b - A c in float-pair arithmetic
+                        * on the FP32 pipe (~47 significant bits); 1 evaluates them in FP64
+                        * with the plain form's kernels (the FP64 pipe is ~1/64 of the
+                        * FP32 rate on this part).  Ignored by the FP64 form. */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;
@@ -188,6 +193,18 @@ int eqf_step(eqf_batch* b, int32_t n_steps);
 /* Reads the nodal field (grid order).  Replaces reading solution_vector after
  * stepDiffusion (src/fHSL.cpp:108; src/simulation.cpp:491-492). */
 int eqf_read_nodal(eqf_batch* b, int32_t trap, double* c);
+
+/* The nodal field in a caller's DOF order: dof_from_vertex[v] is the DOF index of
+ * vertex v = j + i*(nx+1) (grid order), a permutation of 0 .. n-1 (checked), such as
+ * DOLFIN's vertex_to_dof_map that fenicsShell::getVertexMappings exports
+ * (src/fHSL.h:82-87) and Simulation::create_HSLgrid turns into its lookup table
+ * (src/simulation.cpp:363-386).  eqf_read_nodal_dof writes c[dof_from_vertex[v]] =
+ * field(v) (solution_vector after stepDiffusion, src/fHSL.cpp:108); eqf_set_nodal_dof
+ * sets field(v) = c[dof_from_vertex[v]] (u0 before the solve, src/fHSL.cpp:104), as
+ * eqf_set_nodal does. */
+int eqf_read_nodal_dof(eqf_batch* b, int32_t trap, const int32_t* dof_from_vertex, double* c);
+int eqf_set_nodal_dof(eqf_batch* b, int32_t trap, const int32_t* dof_from_vertex,
+                      const double* c);
 
 /* Concentration at the cells set by eqf_set_cells, sampled on their triangles.
  * Replaces the gather readHSL (src/abm/eQabm.cpp:326-337) for point cells. */
@@ -337,6 +354,12 @@ int eqf_set_tensor(eqf_batch* b, int32_t trap, const double* D11, const double* 
  * the well off; it starts at 0. */
 int eqf_set_well(eqf_batch* b, int32_t trap, double well_scaling, double decay_rate);
 int eqf_read_well(eqf_batch* b, int32_t trap, double* concentration, int64_t* underflows);
+/* Sets the well concentration w that EQF_BC_WELL walls take as their value in the
+ * next step: fenicsInterface::setBoundaryValues (src/fHSL.cpp:601-604), called by
+ * Simulation::computeBoundaryWell with the host's own well model under
+ * DIRICHLET_UPDATE (src/simulation.cpp:581-604).  With the device's well model off
+ * (well_scaling 0) the value stays until set again. */
+int eqf_set_well_concentration(eqf_batch* b, int32_t trap, double concentration);
 
 /* ---------------------------------------------------------------------------
  * Output in the reference's formats (host-side writers; the reads from a batch are

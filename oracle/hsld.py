@@ -56,20 +56,34 @@ _QPHI = np.array([[2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0],
 
 
 class RightMesh:
-    """Structured "right" triangulation of [0, W] x [0, H] with nx x ny squares."""
+    """Structured triangulation of [0, W] x [0, H] with nx x ny squares.
 
-    def __init__(self, W: float, H: float, nx: int, ny: int):
+    diagonal "right" (the reference's RectangleMesh(..., "right"), src/fHSL.cpp:171)
+    cuts each square along (i, j)-(i+1, j+1); "left" along (i, j+1)-(i+1, j).  The
+    direction comes from DOLFIN, which is not part of the reference tree, so it is a
+    switch here; "right" is what the GPU library implements.
+    """
+
+    def __init__(self, W: float, H: float, nx: int, ny: int, diagonal: str = "right"):
+        if diagonal not in ("right", "left"):
+            raise ValueError(diagonal)
         self.W, self.H, self.nx, self.ny = float(W), float(H), int(nx), int(ny)
+        self.diagonal = diagonal
         self.hx, self.hy = self.W / nx, self.H / ny
         jj, ii = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1))
         self.coords = np.stack([jj.ravel() * self.hx, ii.ravel() * self.hy], axis=1)
         sj, si = np.meshgrid(np.arange(nx), np.arange(ny))
         v0 = (sj + si * (nx + 1)).ravel()
         v1, v2, v3 = v0 + 1, v0 + nx + 1, v0 + nx + 2
-        # cell order per square: lower-right (v0, v1, v3), then upper-left (v0, v2, v3)
         self.cells = np.empty((2 * nx * ny, 3), dtype=np.int64)
-        self.cells[0::2] = np.stack([v0, v1, v3], axis=1)
-        self.cells[1::2] = np.stack([v0, v2, v3], axis=1)
+        if diagonal == "right":
+            # per square: lower-right (v0, v1, v3), then upper-left (v0, v2, v3)
+            self.cells[0::2] = np.stack([v0, v1, v3], axis=1)
+            self.cells[1::2] = np.stack([v0, v2, v3], axis=1)
+        else:
+            # per square: lower-left (v0, v1, v2), then upper-right (v1, v2, v3)
+            self.cells[0::2] = np.stack([v0, v1, v2], axis=1)
+            self.cells[1::2] = np.stack([v1, v2, v3], axis=1)
 
     @property
     def n_nodes(self) -> int:
@@ -256,9 +270,19 @@ def point_weights(mesh: RightMesh, xy: np.ndarray) -> Tuple[np.ndarray, np.ndarr
     xi = X - j
     eta = Y - i
     v0 = j + i * (nx + 1)
-    lower = xi >= eta
     nodes = np.empty((len(xy), 3), dtype=np.int64)
     w = np.empty((len(xy), 3))
+    if getattr(mesh, "diagonal", "right") == "left":
+        # lower-left (v0, v1, v2) where xi + eta <= 1, else upper-right (v1, v2, v3)
+        low = xi + eta <= 1.0
+        nodes[:, 0] = np.where(low, v0, v0 + 1)
+        nodes[:, 1] = np.where(low, v0 + 1, v0 + nx + 1)
+        nodes[:, 2] = np.where(low, v0 + nx + 1, v0 + nx + 2)
+        w[:, 0] = np.where(low, 1.0 - xi - eta, 1.0 - eta)
+        w[:, 1] = np.where(low, xi, 1.0 - xi)
+        w[:, 2] = np.where(low, eta, xi + eta - 1.0)
+        return nodes, w
+    lower = xi >= eta
     nodes[:, 0] = v0
     nodes[:, 1] = np.where(lower, v0 + 1, v0 + nx + 1)
     nodes[:, 2] = v0 + nx + 2
@@ -291,6 +315,14 @@ def boundary_flux_integral(mesh: RightMesh, u: np.ndarray) -> float:
     nx, ny = mesh.nx, mesh.ny
     hx, hy = mesh.hx, mesh.hy
     U = u.reshape(ny + 1, nx + 1)
+    if getattr(mesh, "diagonal", "right") == "left":
+        # bottom and left edges bound the lower-left triangle (v0, v1, v2), top and
+        # right edges the upper-right one (v1, v2, v3)
+        fb = np.sum((U[1, :-1] - U[0, :-1]) / hy) * hx
+        ft = np.sum(-(U[ny, 1:] - U[ny - 1, 1:]) / hy) * hx
+        fl = np.sum((U[:-1, 1] - U[:-1, 0]) / hx) * hy
+        fr = np.sum(-(U[1:, nx] - U[1:, nx - 1]) / hx) * hy
+        return float(fb + ft + fl + fr)
     # bottom (n = (0,-1)): -du/dy on triangle (v0,v1,v3) = (u3 - u1)/hy
     fb = np.sum((U[1, 1:] - U[0, 1:]) / hy) * hx
     # top (n = (0,1)): -du/dy on (v0,v2,v3) = -(u2 - u0)/hy, u2 = U[ny, j], u0 = U[ny-1, j]
@@ -312,8 +344,8 @@ class HsldOracle:
     """
 
     def __init__(self, W, H, nx, ny, D, dt, g=0.0, walls=WALL_BOTTOM, D11=None, D22=None,
-                 D12=None, velocity=None, robin=None, factor=True):
-        self.mesh = RightMesh(W, H, nx, ny)
+                 D12=None, velocity=None, robin=None, factor=True, diagonal="right"):
+        self.mesh = RightMesh(W, H, nx, ny, diagonal)
         self.D, self.dt, self.g, self.walls = float(D), float(dt), float(g), int(walls)
         m = self.mesh
         Ae = tabulate_a(m, self.D, self.dt, D11, D22, D12, mass_scale=1.0 + self.dt * self.g)

@@ -216,3 +216,39 @@ def test_config_fixtures_are_self_consistent(name):
         assert g[u].shape == (t.n_nodes,)
         assert np.allclose(hsld.gather(mesh, g[u], t.cell_xy), g[c], rtol=1e-13, atol=0)
         assert np.all(np.isfinite(g[u])) and np.abs(g[u]).max() > 0
+
+
+def test_left_diagonal_mesh_is_the_mirror_of_the_right_one():
+    """The oracle's diagonal switch: the "left" triangulation is the "right" one mirrored
+    in x, so a trap solved on it equals the mirrored trap on the "right" mesh (cells
+    at W - x, left and right walls swapped, the tensor's D12 negated)."""
+    W, H, nx, ny = 6.0, 3.0, 24, 12
+    rng = np.random.Generator(np.random.PCG64(4))
+    xy = np.stack([rng.uniform(0.2, W - 0.2, 15), rng.uniform(0.2, H - 0.2, 15)], 1)
+    s = rng.uniform(0.5, 2.0, 15)
+    n = (nx + 1) * (ny + 1)
+    y, x = np.meshgrid(np.linspace(0, H, ny + 1), np.linspace(0, W, nx + 1), indexing="ij")
+    th = 0.5 * np.sin(x) + 0.3 * y
+    D11, D22, D12 = wl.rotated_tensor(th, 2.0, 0.5)
+    mir = lambda a: np.asarray(a).reshape(ny + 1, nx + 1)[:, ::-1].ravel()  # noqa: E731
+    walls = hsld.WALL_BOTTOM | hsld.WALL_LEFT
+    left = hsld.HsldOracle(W, H, nx, ny, 49.0, 0.1, 0.01, walls, D11=D11.ravel(), D22=D22.ravel(),
+                           D12=D12.ravel(), diagonal="left")
+    right = hsld.HsldOracle(W, H, nx, ny, 49.0, 0.1, 0.01, hsld.WALL_BOTTOM | hsld.WALL_RIGHT,
+                            D11=mir(D11), D22=mir(D22), D12=-mir(D12))
+    xm = np.stack([W - xy[:, 0], xy[:, 1]], 1)
+    Fl = hsld.point_load(left.mesh, xy, s, scale=0.1)
+    Fr = hsld.point_load(right.mesh, xm, s, scale=0.1)
+    ul, ur = np.zeros(n), np.zeros(n)
+    for _ in range(4):
+        ul, ur = left.step(ul, Fl), right.step(ur, Fr)
+    assert np.allclose(ul, mir(ur), rtol=1e-12, atol=1e-14 * np.abs(ur).max())
+    assert np.allclose(hsld.gather(left.mesh, ul, xy), hsld.gather(right.mesh, ur, xm), rtol=1e-12)
+    assert abs(left.boundary_flux(ul) - right.boundary_flux(ur)) <= 1e-12 * abs(right.boundary_flux(ur))
+    # and it is a different discretisation: the same trap on the two meshes differs
+    same = hsld.HsldOracle(W, H, nx, ny, 49.0, 0.1, 0.01, walls, D11=D11.ravel(),
+                           D22=D22.ravel(), D12=D12.ravel())
+    ur2 = np.zeros(n)
+    for _ in range(4):
+        ur2 = same.step(ur2, hsld.point_load(same.mesh, xy, s, scale=0.1))
+    assert np.linalg.norm(ur2 - ul) > 1e-6 * np.linalg.norm(ul)
