@@ -467,9 +467,18 @@ def run_ours(args, rank, world, local_rank):
     out = None
     if rank == 0:
         cpu = None
+        cpu_more = None
         if world == 1 and not args.no_cpu:
             cidx = sample_indices(traps, args.cpu_sample)
             cpu = cpu_reference_rate(traps, cidx, args.cpu_steps, args.cpu_budget)
+            if args.workload == "batched_uneven":
+                from oracle import cpu_baseline, gmg_cpu
+                cpu_more = {
+                    "assemble_lu_every_step": {"value": cpu["value"], "cores": cpu["cores"]},
+                    "lu_factor_once": cpu_baseline.factor_once_rate(traps, cidx, 20,
+                                                                    args.cpu_budget),
+                    "multigrid_pcg_openmp": gmg_cpu.rate(traps, sample_indices(traps, 32), 10,
+                                                         args.cpu_budget)}
         sm = sorted(step_ms)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -477,7 +486,8 @@ def run_ours(args, rank, world, local_rank):
             "p50_step_ms": float(np.percentile(sm, 50)), "p99_step_ms": float(np.percentile(sm, 99)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-ir",
             "data": "synthetic (seeded PCG64; the reference publishes no dataset)",
-            "autotune": ({"seconds": round(tune_s, 2), "buckets": F.tune_table_dict(table)}
+            "autotune": ({"seconds": round(tune_s, 2), "buckets": F.tune_table_dict(table),
+                          "candidates": getattr(table, "log", None)}
                          if table is not None else None),
             "config": {"workload": args.workload, "traps": len(traps), "nodes": nodes,
                        "cells": ncells, "seed": args.seed, "precision": "FP32 inner + FP64 refinement",
@@ -511,6 +521,7 @@ def run_ours(args, rank, world, local_rank):
             "e2e": e2e,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "cpu_baselines": cpu_more,
         }
     return out
 
@@ -760,17 +771,23 @@ def run_serving(args, rank, world, local_rank):
     t0 = time.perf_counter()
     clocks.start()
     k = 0
+    t_sub = t_prog = t_res = 0.0
     while k < n or len(results) < n:
         now = time.perf_counter() - t0
+        ta = time.perf_counter()
         while k < n and arrivals[k] <= now:
             t = serving_request(seed, k)
             sizes[k] = (t.n_nodes, t.n_species)
             ids[srv.submit(params(t), t.cell_xy, t.cell_s, t.steps, sender=t.cell_kind,
                            want_nodal=k in audit)] = k
             k += 1
+        tb = time.perf_counter()
         srv.progress()
+        tc = time.perf_counter()
         for rid in srv.take_done():
             results[ids[rid]] = srv.result(rid)
+        td = time.perf_counter()
+        t_sub, t_prog, t_res = t_sub + tb - ta, t_prog + tc - tb, t_res + td - tc
         if k >= n and now > args.duration + args.drain_limit:
             break
     wall = time.perf_counter() - t0
@@ -820,6 +837,10 @@ def run_serving(args, rank, world, local_rank):
         "admission_wait_s": {"p50": float(np.percentile(wait, 50)),
                              "p99": float(np.percentile(wait, 99))},
         "bytes_peak_gb": st["bytes_peak"] / (1 << 30),
+        "host_s": {"submit_python": round(t_sub, 2), "progress": round(t_prog, 2),
+                   "results_python": round(t_res, 2), "of_which_admit": round(st["admit_s"], 2),
+                   "of_which_launch": round(st["launch_s"], 2),
+                   "of_which_release": round(st["release_s"], 2)},
         "audit": {"sampled": len(audit), "completed": len(aud), "checked": checked,
                   "relL2_max": max(errs) if errs else None, "tolerance": 1e-6},
         "clocks": clk,
@@ -846,6 +867,7 @@ def run_ncu_target(args):
                                                           fuse_levels=0 if args.no_fuse
                                                           else args.fuse_levels))
     load_traps(b, traps)
+    b.mass_balance(True)  # as the timed run
     b.step(args.warmup + args.steps)
     b.sync()
     b.close()
@@ -885,7 +907,7 @@ def main():
     ap.add_argument("--fuse-levels", type=int, default=1, choices=[1, 2],
                     help="1: temporally blocked level kernels (default); 2: also the "
                          "small bottom levels in one kernel per trap")
-    ap.add_argument("--tune-budget", type=float, default=20.0,
+    ap.add_argument("--tune-budget", type=float, default=45.0,
                     help="seconds for the autotuner before the timed run (0: no tuning)")
     ap.add_argument("--tile-nodes", type=int, default=0,
                     help="target nodes per finest-level row tile (0: the library default)")

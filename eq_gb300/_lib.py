@@ -40,6 +40,7 @@ EXPORTS = (
     "eqf_json_close", "eqf_vtk_open", "eqf_vtk_write", "eqf_vtk_write_channel",
     "eqf_vtk_write_host", "eqf_vtk_close", "eqf_mass_balance", "eqf_read_balance",
     "eqf_read_nodal_dof", "eqf_set_nodal_dof", "eqf_set_well_concentration",
+    "eqf_autotune_log",
     "eqf_rod_relax_passes",
 )
 
@@ -74,12 +75,13 @@ class SolverOpts(C.Structure):
                 ("cheb_post", C.c_int32), ("cheb_coarse", C.c_int32), ("cheb_ratio", C.c_double),
                 ("use_graph", C.c_int32), ("adaptive", C.c_int32),
                 ("tile_nodes", C.c_int32), ("krylov", C.c_int32), ("fuse_levels", C.c_int32),
-                ("residual64", C.c_int32)]
+                ("residual64", C.c_int32), ("tile_cols", C.c_int32)]
 
 
 class TuneBucket(C.Structure):
     _fields_ = [("max_nodes", C.c_int64), ("tile_nodes", C.c_int32), ("cheb_pre", C.c_int32),
-                ("cheb_post", C.c_int32), ("dof_steps_per_s", C.c_double)]
+                ("cheb_post", C.c_int32), ("tile_cols", C.c_int32),
+                ("dof_steps_per_s", C.c_double)]
 
 
 EQF_TUNE_MAX_BUCKETS = 8
@@ -168,6 +170,8 @@ def load() -> C.CDLL:
                                        P(C.c_void_p)]),
         "eqf_autotune": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_double,
                                    P(TuneTable)]),
+        "eqf_autotune_log": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_double,
+                                       P(TuneTable), C.c_char_p, C.c_int64]),
         "eqf_footprint_estimate": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), C.c_int64,
                                              i64p]),
         "eqf_set_rods": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32), P(RodLaw), C.c_int64,

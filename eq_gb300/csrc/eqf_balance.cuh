@@ -126,11 +126,11 @@ __global__ void __launch_bounds__(kThreads)
   const double* b = uo + base;
   const double* f = F + base;
   const int qpr = P >> 2, nq = (tile.r1 - tile.r0) * qpr;
-  double sa = 0.0, sb = 0.0, sf = 0.0;
-#pragma unroll 4
-  for (int q = threadIdx.x; q < nq; q += kThreads) {
-    const int row = q / qpr, j0 = (q - row * qpr) * 4;
-    const int k = row * P + j0;
+  // 4-node vectors over the tile's rows, two quads per thread and pass in two
+  // independent accumulators
+  double sa0 = 0.0, sa1 = 0.0, sb0 = 0.0, sb1 = 0.0, sf0 = 0.0, sf1 = 0.0;
+  auto quad = [&](int q, double& xa, double& xb, double& xf) {
+    const int row = q / qpr, j0 = (q - row * qpr) * 4, k = row * P + j0;
     Q4<double> x = vld4<double>(a + k), y{}, z{};
     if (OLD) y = vld4<double>(b + k);
     if (LOAD) z = vld4<double>(f + k);
@@ -139,11 +139,15 @@ __global__ void __launch_bounds__(kThreads)
       for (int e = 0; e < 4; ++e)
         if (j0 + e > nx) x.v[e] = y.v[e] = z.v[e] = 0.0;
     }
-    sa += (x.v[0] + x.v[1]) + (x.v[2] + x.v[3]);
-    if (OLD) sb += (y.v[0] + y.v[1]) + (y.v[2] + y.v[3]);
-    if (LOAD) sf += (z.v[0] + z.v[1]) + (z.v[2] + z.v[3]);
+    xa += (x.v[0] + x.v[1]) + (x.v[2] + x.v[3]);
+    if (OLD) xb += (y.v[0] + y.v[1]) + (y.v[2] + y.v[3]);
+    if (LOAD) xf += (z.v[0] + z.v[1]) + (z.v[2] + z.v[3]);
+  };
+  for (int q = threadIdx.x; q < nq; q += 2 * kThreads) {
+    quad(q, sa0, sb0, sf0);
+    if (q + kThreads < nq) quad(q + kThreads, sa1, sb1, sf1);
   }
-  const double v[kBalTileParts] = {sa, sb, sf};
+  const double v[kBalTileParts] = {sa0 + sa1, sb0 + sb1, sf0 + sf1};
 #pragma unroll
   for (int p = 0; p < kBalTileParts; ++p) {
     const double t = block_sum(v[p]);
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(kThreads)
 // Robin column sums and, on Dirichlet rows, the full operator's residual; over the
 // two-node rim of a trap whose walls carry values or Robin loads, the load before
 // lifting minus the F the tile pass summed.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     k_balance_rim(const LevelGeom* __restrict__ G, const double* __restrict__ un,
                   const double* __restrict__ uo, const double* __restrict__ F,
                   const int* __restrict__ wall_of, const WallDev* __restrict__ walls,
@@ -203,9 +207,7 @@ __global__ void __launch_bounds__(kThreads)
           // the load before lifting
           const double fk = wi >= 0 ? rim_load(g, walls[wi], fbase, rim_index(i, j, nx, ny), i, j)
                                     : Fs[k];
-          LevelGeom fg = g;
-          fg.walls = 0;
-          const Sten<double> s = stencil_general<double>(fg, i, j);
+          const Sten<double> s = stencil_general<double, true, false>(g, i, j);
           const Sten<double> m = mass_stencil<double>(g, i, j);
           double res = s.c * an - m.c * ao - fk;
           if (j < nx) res += s.e * a[k + 1] - m.e * b[k + 1];

@@ -548,8 +548,10 @@ class Batch {
       }
   }
 
-  Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles = nullptr);
+  Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles = nullptr,
+        const int* cols = nullptr);
   std::vector<int> tile_target;  // per trap (0: opts.tile_nodes / the default)
+  std::vector<int> tile_width;   // per trap 2-D tile columns (0: opts.tile_cols / 128)
   ~Batch();
   void build_levels();
   void step(int n);
@@ -588,9 +590,11 @@ class Batch {
 };
 
 // ---------------------------------------------------------------------------
-Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles)
+Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles,
+             const int* cols)
     : ntraps(n), opts(o), params(p, p + n) {
   if (tiles) tile_target.assign(tiles, tiles + n);
+  if (cols) tile_width.assign(cols, cols + n);
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     throw Error(EQF_ERR_NO_DEVICE, "no CUDA device visible");
@@ -852,8 +856,11 @@ void Batch::build_levels() {
         const int r1 = std::min(g.ny + 1, r0 + R);
         (g.adv_on ? gen1 : L[l].tiles).push_back(Tile{t, (int)(r0 * P), (int)(r1 * P), r0, r1});
       }
-      // 2-D tiles of the fused kernels: column blocks of at most 128 nodes
-      const int CW = (int)std::min<long long>(128, P);
+      // 2-D tiles of the fused kernels: column blocks of at most tile_cols (128) nodes
+      const int cw = (!tile_width.empty() && tile_width[t] > 0) ? tile_width[t]
+                     : opts.tile_cols > 0                        ? opts.tile_cols
+                                                                 : 128;
+      const int CW = (int)std::min<long long>(cw, P);
       const int R2 = (int)std::max<long long>(2, tgt / CW);
       for (int r0 = 0; r0 <= g.ny; r0 += R2)
         for (int c0 = 0; c0 < P; c0 += CW)
@@ -1704,7 +1711,10 @@ void Batch::enqueue_balance() {
     longest = std::max(longest, 2 * (g.nx + 1) + 2 * (g.ny - 1));
     if (g.nx >= 3 && g.ny >= 3) longest = std::max(longest, rim_count(g.nx, g.ny));
   }
-  const int rim_blocks = std::min((longest + kThreads - 1) / kThreads, 64);
+  // one CTA per trap walks its ring (a few thousand nodes): more CTAs per trap only
+  // add waves of this register-heavy kernel
+  (void)longest;
+  const int rim_blocks = 1;
   grow(bal_part, (size_t)nt * kBalTileParts);
   grow(bal_rpart, (size_t)ntraps * rim_blocks * kBalRimParts);
   // the field a step starts from is the last step's result unless the host or the rod
@@ -2286,7 +2296,8 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
 }
 
 static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
-                       const eqf_solver_opts* opts, const int* tiles, eqf_batch** out) {
+                       const eqf_solver_opts* opts, const int* tiles, const int* cols,
+                       eqf_batch** out) {
   if (!out) return EQF_ERR_INVALID;
   *out = nullptr;
   auto* h = new (std::nothrow) eqf_batch();
@@ -2307,6 +2318,11 @@ static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
                     o.cheb_coarse <= eqf::kMaxChebSteps,
                 "Chebyshev degrees above 16");
     EQF_REQUIRE(o.tile_nodes >= 0 && o.tile_nodes <= 32768, "tile_nodes outside [0, 32768]");
+    auto width_ok = [](int c) { return c == 0 || (c >= 16 && c <= 512 && c % 4 == 0); };
+    EQF_REQUIRE(width_ok(o.tile_cols), "tile_cols not 0 or a multiple of 4 in [16, 512]");
+    if (cols)
+      for (int t = 0; t < n_traps; ++t)
+        EQF_REQUIRE(width_ok(cols[t]), "tile width not 0 or a multiple of 4 in [16, 512]");
     EQF_REQUIRE(o.krylov >= EQF_KRYLOV_AUTO && o.krylov <= EQF_KRYLOV_BICGSTAB,
                 "unknown Krylov method");
     for (int t = 0; t < n_traps; ++t) {
@@ -2318,7 +2334,7 @@ static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
     if (tiles)
       for (int t = 0; t < n_traps; ++t)
         EQF_REQUIRE(tiles[t] >= 0 && tiles[t] <= 32768, "tile target outside [0, 32768]");
-    h->impl.reset(new Batch(n_traps, traps, o, tiles));
+    h->impl.reset(new Batch(n_traps, traps, o, tiles, cols));
   });
   if (rc != EQF_OK) {
     g_create_err = h->err;
@@ -2331,7 +2347,7 @@ static int create_impl(int32_t n_traps, const eqf_trap_params* traps,
 
 int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
                eqf_batch** out) {
-  return create_impl(n_traps, traps, opts, nullptr, out);
+  return create_impl(n_traps, traps, opts, nullptr, nullptr, out);
 }
 
 // Bucket of a trap in a tuning table: the first whose max_nodes holds it (the last
@@ -2346,7 +2362,7 @@ int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_so
                      const eqf_tune_table* table, eqf_batch** out) {
   if (!out || !traps || n_traps < 1) return EQF_ERR_INVALID;
   if (!table || table->n < 1 || table->n > EQF_TUNE_MAX_BUCKETS)
-    return create_impl(n_traps, traps, opts, nullptr, out);
+    return create_impl(n_traps, traps, opts, nullptr, nullptr, out);
   eqf_solver_opts o;
   if (opts)
     o = *opts;
@@ -2354,18 +2370,19 @@ int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_so
     eqf_default_opts(EQF_PREC_FP64, &o);
   // tile target per trap from its bucket; smoother degrees from the bucket that
   // holds most of the batch's nodes
-  std::vector<int> tiles(n_traps);
+  std::vector<int> tiles(n_traps), cols(n_traps);
   std::vector<long long> mass(table->n, 0);
   for (int t = 0; t < n_traps; ++t) {
     const long long nodes = (long long)(traps[t].nx + 1) * (traps[t].ny + 1);
     const int k = tune_bucket(*table, nodes);
     tiles[t] = table->b[k].tile_nodes;
+    cols[t] = table->b[k].tile_cols;
     mass[k] += nodes;
   }
   const int kb = (int)(std::max_element(mass.begin(), mass.end()) - mass.begin());
   if (table->b[kb].cheb_pre > 0) o.cheb_pre = table->b[kb].cheb_pre;
   if (table->b[kb].cheb_post > 0) o.cheb_post = table->b[kb].cheb_post;
-  return create_impl(n_traps, traps, &o, tiles.data(), out);
+  return create_impl(n_traps, traps, &o, tiles.data(), cols.data(), out);
 }
 
 int eqf_destroy(eqf_batch* b) {

@@ -199,7 +199,8 @@ EQF_HD void aniso_stiffness(const LevelGeom& g, int i, int j, T hxl, T hxr, T hy
 // A/12 per edge.  Stiffness (scaled by beta): right triangles couple only along
 // their legs, -cot/2 = -(other leg)/(2*this leg); hypotenuses carry no stiffness.
 // Advection (c2): dt * int v_y d(phi_b)/dy phi_a over each triangle with a P1 v_y.
-template <class T, bool ANISO = true>
+// WALLS = false gives the full operator's row, without the Dirichlet reduction.
+template <class T, bool ANISO = true, bool WALLS = true>
 EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
   const Lens<T>& L = lens<T>(g);
   const T hxl = j > 0 ? (j == g.nx ? L.hxl : L.hx) : T(0);
@@ -305,7 +306,7 @@ EQF_HD Sten<T> stencil_general(const LevelGeom& g, int i, int j) {
     s.n += L.rob[3] * hyu * T(1.0 / 6.0);
     s.s += L.rob[3] * hyd * T(1.0 / 6.0);
   }
-  if (g.walls) {
+  if (WALLS && g.walls) {
     if (is_dirichlet(g, i, j)) {
       s.c = T(1);
       s.e = s.w = s.n = s.s = s.ne = s.sw = T(0);

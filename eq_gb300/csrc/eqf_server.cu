@@ -42,6 +42,7 @@ struct Req {
   bool done = false;
   bool taken = false;  // result handed out (the object lives until its cohort is released)
   int64_t klass = 0;   // cohort class: multigrid depth and symmetric / advective operator
+  bool picked = false; // taken into the cohort being formed
   int ntraps() const { return r.n_species; }
 };
 
@@ -61,6 +62,7 @@ struct Cohort {
   int64_t bytes = 0;
   int remaining = 0;
   int32_t fails_seen = 0;
+  bool retired = false;  // every request done; memory kept until it is needed
 };
 
 }  // namespace
@@ -223,34 +225,67 @@ void retire(eqs_server* s, Cohort& c) {
   }
 }
 
-// Forms one cohort from the head of the queue within the budget: the oldest request
-// and the following ones of its class, in arrival order.  Cohorts are class-pure
-// (same multigrid depth and Krylov method), so a request's result is the same bits
-// whichever requests share its cohort.
+// Frees the memory of retired cohorts (cudaFree waits for the whole device, so this
+// happens only when an admission needs the memory, or at shutdown).
+bool release_retired(eqs_server* s) {
+  const double t0 = s->now();
+  bool any = false;
+  for (auto& c : s->cohorts)
+    if (c->b && c->retired) {
+      release_cohort(s, *c);
+      for (Req* q : c->reqs)
+        if (q->taken) s->reqs.erase(q->id);
+      any = true;
+    }
+  s->cohorts.erase(std::remove_if(s->cohorts.begin(), s->cohorts.end(),
+                                  [](const std::unique_ptr<Cohort>& c) { return !c->b; }),
+                   s->cohorts.end());
+  s->st.release_s += s->now() - t0;
+  return any;
+}
+
+// Forms one cohort from the queue within the budget: the oldest request first, then
+// the waiting requests of its class with the nearest step counts (a cohort runs
+// until its longest request is done; requests of similar length keep its slots
+// busy), ties in arrival order.  Cohorts are class-pure (same multigrid depth and
+// Krylov method), so a request's result is the same bits whichever requests share
+// its cohort.
 bool admit(eqs_server* s) {
+  Req* head = s->pending.front();
+  const int64_t klass = head->klass;
+  // candidates: the oldest waiting requests of the head's class (a bounded window, so
+  // an admission costs the same however long the queue is)
+  constexpr size_t kWindow = 2048;
+  std::vector<Req*> cand;
+  for (Req* q : s->pending) {
+    if (cand.size() >= kWindow) break;
+    if (q != head && q->klass == klass) cand.push_back(q);
+  }
+  std::stable_sort(cand.begin(), cand.end(), [&](const Req* a, const Req* b) {
+    return std::abs(a->r.steps - head->r.steps) < std::abs(b->r.steps - head->r.steps);
+  });
+  cand.insert(cand.begin(), head);
   std::vector<Req*> take;
   int traps = 0;
-  const int64_t free_bytes = s->cfg.hbm_budget - s->st.bytes_in_use;
+  int64_t free_bytes = s->cfg.hbm_budget - s->st.bytes_in_use;
   int64_t bytes = 0;
-  const int64_t klass = s->pending.front()->klass;
-  for (auto it = s->pending.begin(); it != s->pending.end();) {
-    Req* q = *it;
-    if (q->klass != klass) {
-      ++it;
-      continue;
-    }
+  for (Req* q : cand) {
     if (traps + q->ntraps() > s->cfg.max_cohort_traps) break;
     take.push_back(q);
-    const int64_t b = estimate(s, take);
+    int64_t b = estimate(s, take);
+    if (b > free_bytes && release_retired(s)) free_bytes = s->cfg.hbm_budget - s->st.bytes_in_use;
     if (b > free_bytes) {
       take.pop_back();
       break;
     }
     bytes = b;
     traps += q->ntraps();
-    it = s->pending.erase(it);
   }
   if (take.empty()) return false;
+  for (Req* q : take) q->picked = true;
+  s->pending.erase(std::remove_if(s->pending.begin(), s->pending.end(),
+                                  [](const Req* q) { return q->picked; }),
+                   s->pending.end());
   std::unique_ptr<Cohort> c(new Cohort);
   c->id = s->next_cohort++;
   c->reqs = take;
@@ -266,7 +301,10 @@ bool admit(eqs_server* s) {
   if (rc != EQF_OK) {
     // put the requests back in arrival order and retry once memory frees up; with
     // nothing running no memory will free up: the oldest request fails
-    for (Req* q : take) s->pending.push_back(q);
+    for (Req* q : take) {
+      q->picked = false;
+      s->pending.push_back(q);
+    }
     std::sort(s->pending.begin(), s->pending.end(),
               [](const Req* a, const Req* b) { return a->id < b->id; });
     if ((rc == EQF_ERR_NOMEM || rc == EQF_ERR_CUDA) && !s->cohorts.empty()) return false;
@@ -312,33 +350,37 @@ bool admit(eqs_server* s) {
 void progress(eqs_server* s) {
   const double now = s->now();
   bool running = false;
-  for (auto& c : s->cohorts) running = running || c->b;
+  for (auto& c : s->cohorts) running = running || (c->b && !c->retired);
   if (running) s->st.busy_s += now - s->last_progress;
   s->last_progress = now;
-  // retire finished steps, release finished cohorts
+  // retire finished steps; a cohort whose requests are all done is retired (its
+  // device memory is released later, when an admission needs it)
   for (auto& c : s->cohorts) retire(s, *c);
   for (auto& c : s->cohorts)
-    if (c->b && c->remaining == 0 && c->inflight.empty()) {
-      const int rc = eqf_sync(c->b);
+    if (c->b && !c->retired && c->remaining == 0 && c->inflight.empty()) {
+      int idle = 0;
+      const int rc = eqf_poll(c->b, &idle);  // the steps are done: reports deferred errors
       if (rc == EQF_ERR_NOT_CONVERGED)
         for (Req* q : c->reqs) q->status = rc;
-      release_cohort(s, *c);
-      for (Req* q : c->reqs)
-        if (q->taken) s->reqs.erase(q->id);
+      c->retired = true;
     }
-  s->cohorts.erase(std::remove_if(s->cohorts.begin(), s->cohorts.end(),
-                                  [](const std::unique_ptr<Cohort>& c) { return !c->b; }),
-                   s->cohorts.end());
+  int live = 0;
+  for (auto& c : s->cohorts) live += c->b && !c->retired ? 1 : 0;
   // admit: an idle GPU, enough waiting requests, or a request waiting too long
-  while (!s->pending.empty() && (int)s->cohorts.size() < s->cfg.max_cohorts) {
-    const bool idle = s->cohorts.empty();
+  const double ta = s->now();
+  while (!s->pending.empty() && live < s->cfg.max_cohorts) {
+    const bool idle = live == 0;
     const bool enough = (int)s->pending.size() >= s->cfg.min_batch;
     const bool late = (now - s->pending.front()->t_submit) * 1e3 >= s->cfg.max_wait_ms;
     if (!(idle || enough || late)) break;
     if (!admit(s)) break;
+    ++live;
   }
+  const double tl = s->now();
+  s->st.admit_s += tl - ta;
   // keep every cohort's queue filled
   for (auto& c : s->cohorts) {
+    if (c->retired) continue;
     try {
       while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight)
         launch_step(s, *c);
@@ -347,8 +389,10 @@ void progress(eqs_server* s) {
       fail_cohort(s, *c, f.code);
     }
   }
+  s->st.launch_s += s->now() - tl;
   int64_t run = 0;
-  for (auto& c : s->cohorts) run += (int64_t)c->reqs.size();
+  for (auto& c : s->cohorts)
+    if (!c->retired) run += (int64_t)c->reqs.size();
   s->st.pending = (int64_t)s->pending.size();
   s->st.running = run;
 }
@@ -376,7 +420,7 @@ int eqs_default_config(eqs_config* c) {
   c->max_cohort_traps = 256;
   c->min_batch = 16;
   c->max_wait_ms = 20.0;
-  c->steps_in_flight = 2;
+  c->steps_in_flight = 4;
   return EQF_OK;
 }
 
@@ -517,7 +561,12 @@ int eqs_drain(eqs_server* s) {
   return guarded(s, [&] {
     for (;;) {
       progress(s);
-      if (s->pending.empty() && s->cohorts.empty()) break;
+      bool live = false;
+      for (auto& c : s->cohorts) live = live || (c->b && !c->retired);
+      if (s->pending.empty() && !live) {
+        release_retired(s);
+        break;
+      }
       bool any = false;
       for (auto& c : s->cohorts) any = any || !c->inflight.empty();
       if (any) {

@@ -13,8 +13,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
+#include <algorithm>
 
 #include "../../include/eqfield.h"
 
@@ -38,9 +41,11 @@ struct Rng {
 };
 
 // DOF-steps/s of one candidate (0 if it cannot run: e.g. rows too wide for the tile)
-double measure(const std::vector<eqf_trap_params>& traps, const eqf_solver_opts& o, int tile) {
+double measure(const std::vector<eqf_trap_params>& traps, const eqf_solver_opts& o, int tile,
+               int cols) {
   eqf_solver_opts c = o;
   c.tile_nodes = tile;
+  c.tile_cols = cols;
   c.use_graph = 1;
   c.adaptive = 1;
   eqf_batch* b = nullptr;
@@ -82,9 +87,11 @@ double measure(const std::vector<eqf_trap_params>& traps, const eqf_solver_opts&
 
 }  // namespace
 
-extern "C" int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps,
-                            const eqf_solver_opts* opts, double budget_s, eqf_tune_table* table) {
-  if (n_traps < 1 || !traps || !table || !(budget_s > 0)) return EQF_ERR_INVALID;
+extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
+                                const eqf_solver_opts* opts, double budget_s,
+                                eqf_tune_table* table, char* log, int64_t log_size) {
+  if (n_traps < 1 || !traps || !table || !(budget_s > 0) || (log && log_size < 1))
+    return EQF_ERR_INVALID;
   eqf_solver_opts o;
   if (opts)
     o = *opts;
@@ -94,14 +101,19 @@ extern "C" int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps,
   auto elapsed = [&] {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   };
+  std::string text;
   std::memset(table, 0, sizeof(*table));
   table->n = kBuckets;
-  const int tiles[] = {0, 2048, 8192};  // 0 = the library default
+  // stage 1: smoother degrees at the default tiles; stage 2: tile node targets x 2-D
+  // tile widths at the best degrees (0 = the library default)
   const int degs[][2] = {{0, 0}, {1, 1}, {3, 3}, {2, 1}};
+  const int tiles[] = {0, 2048, 6144};
+  const int widths[] = {0, 64, 256, 512};
   for (int k = 0; k < kBuckets; ++k) {
     eqf_tune_bucket& tb = table->b[k];
     tb.max_nodes = kBucketMax[k];
     tb.tile_nodes = 0;
+    tb.tile_cols = 0;
     tb.cheb_pre = o.cheb_pre;
     tb.cheb_post = o.cheb_post;
     std::vector<eqf_trap_params> sel;
@@ -120,24 +132,40 @@ extern "C" int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps,
       nodes += (long long)(p.nx + 1) * (p.ny + 1);
     }
     double best = 0.0;
-    for (const auto& d : degs) {
-      for (int tile : tiles) {
-        if (elapsed() > budget_s && best > 0.0) break;
-        eqf_solver_opts c = o;
-        if (d[0] > 0) {
-          c.cheb_pre = d[0];
-          c.cheb_post = d[1];
-        }
-        const double r = measure(batch, c, tile);
-        if (r > best) {
-          best = r;
-          tb.tile_nodes = tile;
-          tb.cheb_pre = c.cheb_pre;
-          tb.cheb_post = c.cheb_post;
-        }
+    auto trial = [&](int pre, int post, int tile, int cols) {
+      if (elapsed() > budget_s && best > 0.0) return;
+      eqf_solver_opts c = o;
+      c.cheb_pre = pre;
+      c.cheb_post = post;
+      const double r = measure(batch, c, tile, cols);
+      char line[160];
+      std::snprintf(line, sizeof(line), "%d %d %d %d %d %.6e\n", k, tile, cols, pre, post, r);
+      text += line;
+      if (r > best) {
+        best = r;
+        tb.tile_nodes = tile;
+        tb.tile_cols = cols;
+        tb.cheb_pre = pre;
+        tb.cheb_post = post;
       }
-    }
+    };
+    for (const auto& d : degs)
+      trial(d[0] > 0 ? d[0] : o.cheb_pre, d[0] > 0 ? d[1] : o.cheb_post, 0, 0);
+    const int pre = tb.cheb_pre, post = tb.cheb_post;
+    for (int tile : tiles)
+      for (int cols : widths)
+        if (tile != 0 || cols != 0) trial(pre, post, tile, cols);
     tb.dof_steps_per_s = best;
   }
+  if (log) {
+    const size_t n = std::min<size_t>(text.size(), (size_t)log_size - 1);
+    std::memcpy(log, text.data(), n);
+    log[n] = '\0';
+  }
   return EQF_OK;
+}
+
+extern "C" int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps,
+                            const eqf_solver_opts* opts, double budget_s, eqf_tune_table* table) {
+  return eqf_autotune_log(n_traps, traps, opts, budget_s, table, nullptr, 0);
 }

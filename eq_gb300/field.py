@@ -73,21 +73,27 @@ def trap_params(W, H, nx, ny, D, dt, decay=0.0, walls=WALL_BOTTOM, adv_u=0.0,
 
 def autotune(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
              budget_s: float = 20.0) -> _lib.TuneTable:
-    """Per size bucket, the fastest row tile target and Chebyshev degrees
-    (eqf_autotune; runs on the GPU for about budget_s seconds at most)."""
+    """Per size bucket, the fastest tile node target, 2-D tile width and Chebyshev
+    degrees (eqf_autotune_log; runs on the GPU for about budget_s seconds at most).
+    The returned table carries every measured candidate in .log."""
     lib = _lib.load()
     arr = (TrapParams * len(traps))(*traps)
     table = _lib.TuneTable()
-    rc = lib.eqf_autotune(len(traps), arr, C.byref(opts) if opts is not None else None,
-                          float(budget_s), C.byref(table))
+    buf = C.create_string_buffer(1 << 16)
+    rc = lib.eqf_autotune_log(len(traps), arr, C.byref(opts) if opts is not None else None,
+                              float(budget_s), C.byref(table), buf, len(buf))
     _check(lib, None, rc)
+    table.log = [dict(zip(("bucket", "tile_nodes", "tile_cols", "cheb_pre", "cheb_post",
+                           "dof_steps_per_s"), (float(x) for x in ln.split())))
+                 for ln in buf.value.decode().splitlines() if ln.strip()]
     return table
 
 
 def tune_table_dict(table: _lib.TuneTable) -> List[Dict[str, float]]:
     return [{"max_nodes": table.b[i].max_nodes, "tile_nodes": table.b[i].tile_nodes,
-             "cheb_pre": table.b[i].cheb_pre, "cheb_post": table.b[i].cheb_post,
-             "dof_steps_per_s": table.b[i].dof_steps_per_s} for i in range(table.n)]
+             "tile_cols": table.b[i].tile_cols, "cheb_pre": table.b[i].cheb_pre,
+             "cheb_post": table.b[i].cheb_post, "dof_steps_per_s": table.b[i].dof_steps_per_s}
+            for i in range(table.n)]
 
 
 class TrapBatch:

@@ -97,6 +97,9 @@ typedef struct eqf_solver_opts {
                         * on the FP32 pipe (~47 significant bits); 1 evaluates them in FP64
                         * with the plain form's kernels (the FP64 pipe is ~1/64 of the
                         * FP32 rate on this part).  Ignored by the FP64 form. */
+  int32_t tile_cols;   /* columns of the fused level kernels' 2-D tiles (a multiple of 4
+                        * in [16, 512]; 0: the default 128); their rows follow from the
+                        * tile node target */
 } eqf_solver_opts;
 
 typedef struct eqf_batch eqf_batch;
@@ -111,16 +114,17 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
                eqf_batch** out);
 
 /* Autotuning (no reference counterpart).  A tuning table maps trap size buckets
- * (node count <= max_nodes, ascending; the last bucket takes the rest) to the row
- * tile target of the finest level and the pre/post Chebyshev degrees that were
- * fastest for traps of that size (DOF-steps/s at the solver tolerance, measured by
- * eqf_autotune).  eqf_create_tuned creates a batch whose traps take the tile
- * target of their bucket and whose smoother takes the degrees of the bucket that
- * holds most of its nodes. */
+ * (node count <= max_nodes, ascending; the last bucket takes the rest) to the tile
+ * node target, the 2-D tile width of the fused level kernels and the pre/post
+ * Chebyshev degrees that were fastest for traps of that size (DOF-steps/s at the
+ * solver tolerance, measured by eqf_autotune).  eqf_create_tuned creates a batch
+ * whose traps take the tile target and width of their bucket and whose smoother
+ * takes the degrees of the bucket that holds most of its nodes. */
 #define EQF_TUNE_MAX_BUCKETS 8
 typedef struct eqf_tune_bucket {
   int64_t max_nodes;
   int32_t tile_nodes, cheb_pre, cheb_post;
+  int32_t tile_cols;      /* 2-D tile columns of the fused level kernels (0: default) */
   double dof_steps_per_s; /* measured rate of the chosen configuration */
 } eqf_tune_bucket;
 typedef struct eqf_tune_table {
@@ -131,13 +135,18 @@ typedef struct eqf_tune_table {
 int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
                      const eqf_tune_table* table, eqf_batch** out);
 
-/* Measures, for each size bucket, candidate tile targets and Chebyshev degrees on a
- * batch of the given traps that fall into the bucket (replicated up to a
- * GPU-filling node count), with random point cells, and writes the fastest into
- * *table.  Buckets: <= 32k, <= 128k, <= 512k nodes, and larger.  Takes about
- * budget_s seconds of GPU time at most (unexplored candidates keep the defaults). */
+/* Measures, for each size bucket, candidate Chebyshev degrees, then tile node
+ * targets x 2-D tile widths at the best degrees, on a batch of the given traps that
+ * fall into the bucket (replicated up to a GPU-filling node count), with random point
+ * cells, and writes the fastest into *table.  Buckets: <= 32k, <= 128k, <= 512k
+ * nodes, and larger.  Takes about budget_s seconds of GPU time at most (unexplored
+ * candidates keep the defaults).  When log is not NULL, one line per measured
+ * candidate ("bucket tile_nodes tile_cols cheb_pre cheb_post dof_steps_per_s") is
+ * written into it, at most log_size bytes including the terminating zero. */
 int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
                  double budget_s, eqf_tune_table* table);
+int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
+                     double budget_s, eqf_tune_table* table, char* log, int64_t log_size);
 
 /* Releases all device memory.  Replaces fenicsInterface::finalize / destructor
  * (src/fHSL.cpp:655-661). */

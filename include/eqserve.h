@@ -70,6 +70,9 @@ typedef struct eqs_stats {
   double step_ms_p50, step_ms_p99, step_ms_p999; /* cohort step latency (CUDA events) */
   int64_t step_samples;
   int64_t bytes_in_use, bytes_peak;
+  double admit_s;                   /* host seconds spent forming cohorts (incl. releases) */
+  double launch_s;                  /* host seconds spent queueing cohort steps */
+  double release_s;                 /* host seconds spent releasing retired cohorts */
 } eqs_stats;
 
 int eqs_default_config(eqs_config* cfg);

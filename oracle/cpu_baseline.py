@@ -69,6 +69,49 @@ def reference_rate(traps, idx, steps_per_trap: int, budget_s: float, timeout_s: 
             "dof_steps": int(dofs), "wall_s": round(wall, 3)}
 
 
+def _factor_once_worker(args):
+    (W, H, nx, ny, D, dt, g, walls, xy, s, steps, budget_s) = args
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    from oracle import hsld
+    t0 = time.perf_counter()
+    o = hsld.HsldOracle(W, H, nx, ny, D, dt, g, walls)  # assemble + LU factor, once
+    t_factor = time.perf_counter() - t0
+    F = hsld.point_load(o.mesh, xy, s, scale=dt)
+    u = np.zeros(o.mesh.n_nodes)
+    t1 = time.perf_counter()
+    done = 0
+    for _ in range(steps):
+        u = o.step(u, F)  # right-hand side + triangular solves
+        done += 1
+        if time.perf_counter() - t1 > budget_s:
+            break
+    return o.mesh.n_nodes * done, time.perf_counter() - t1, t_factor
+
+
+def factor_once_rate(traps, idx, steps_per_trap: int, budget_s: float,
+                     timeout_s: float = 600.0):
+    """DOF-steps/s of the same direct solve with the LU factor kept across steps (the
+    system matrix does not change between steps of a trap): per step only the
+    right-hand side and the two triangular solves; the one-time assembly + factor is
+    reported beside it.  One trap per process, serial SuperLU in each."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    jobs = [(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls, t.cell_xy, t.cell_s,
+             steps_per_trap, budget_s) for t in (traps[i] for i in idx)]
+    procs = min(cores, len(jobs))
+    with mp.get_context("spawn").Pool(processes=procs) as pool:
+        res = pool.map_async(_factor_once_worker, jobs).get(timeout=timeout_s)
+    dofs = sum(r[0] for r in res)
+    span = max(r[1] for r in res)
+    return {"value": dofs / max(span, 1e-9), "unit": "DOF-steps/s", "cores": procs,
+            "kind": "port",
+            "sample": f"{len(jobs)} traps stratified by size, up to {steps_per_trap} steps "
+                      f"each after one assembly + LU factor (scipy SuperLU), one trap per "
+                      f"process",
+            "factor_s_total": round(sum(r[2] for r in res), 3), "dof_steps": int(dofs)}
+
+
 def _rod_worker(args):
     (col, steps, budget_s) = args
     if ROOT not in sys.path:

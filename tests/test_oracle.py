@@ -252,3 +252,19 @@ def test_left_diagonal_mesh_is_the_mirror_of_the_right_one():
     for _ in range(4):
         ur2 = same.step(ur2, hsld.point_load(same.mesh, xy, s, scale=0.1))
     assert np.linalg.norm(ur2 - ul) > 1e-6 * np.linalg.norm(ul)
+
+
+def test_cpu_multigrid_baseline_solves_the_oracle_system():
+    """The C/OpenMP multigrid-PCG CPU baseline (oracle/csrc/gmg_cpu.c) reaches the
+    SuperLU solution of the same steps to the FP64 tolerance, on uneven traps with
+    ragged coarse cells and on every wall set."""
+    from oracle import gmg_cpu
+    traps = [wl.single_small(0), wl.scaled(wl.single_small(0), 37, 19, n_cells=40)]
+    for walls in (0, 13, 15):
+        traps.append(wl.Trap(W=9.25, H=4.75, nx=37, ny=19, D=[490.0], g=[0.01], dt=0.1, steps=6,
+                             walls=walls, cell_xy=traps[1].cell_xy, cell_s=traps[1].cell_s))
+    out, dofs, _, _, its, tsec = gmg_cpu.run(traps, 6)
+    assert dofs == 6 * sum(t.n_nodes for t in traps) and its > 0 and np.all(tsec > 0)
+    for t, u in zip(traps, out):
+        ref = hsld.run_trap(t, steps=6)["u"][0]
+        assert np.linalg.norm(u - ref) <= 1e-9 * np.linalg.norm(ref)

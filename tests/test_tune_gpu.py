@@ -27,10 +27,17 @@ def test_autotune_table_and_tuned_batch(lib):
     for k, r in enumerate(rows):
         if k in used:
             assert r["dof_steps_per_s"] > 0
-            assert r["tile_nodes"] in (0, 2048, 8192)
+            assert r["tile_nodes"] in (0, 2048, 6144)
+            assert r["tile_cols"] in (0, 64, 256, 512)
             assert 1 <= r["cheb_pre"] <= 3 and 1 <= r["cheb_post"] <= 3
         else:
             assert r["dof_steps_per_s"] == 0
+    # every measured candidate is logged, the chosen one with the bucket's best rate
+    log = table.log
+    assert log and {int(c["bucket"]) for c in log} == used
+    for k in used:
+        assert max(c["dof_steps_per_s"] for c in log if int(c["bucket"]) == k) == pytest.approx(
+            rows[k]["dof_steps_per_s"], rel=1e-6)
     refs = [hsld.run_trap(t, steps=6) for t in traps]
     with F.TrapBatch([tp(t) for t in traps], opts, tune=table) as b:
         for i, t in enumerate(traps):
@@ -39,3 +46,29 @@ def test_autotune_table_and_tuned_batch(lib):
         for i in range(2):
             assert rel(b.read_nodal(i), refs[i]["u"][0]) <= 1e-6
             assert rel(b.read_cells(i), refs[i]["cells"][0]) <= 1e-6
+
+
+@pytest.mark.parametrize("cols", [16, 64, 256, 512])
+def test_fused_tile_widths_solve_the_same_system(lib, cols):
+    """The fused level kernels on 2-D tiles of other widths (eqf_solver_opts.tile_cols):
+    the same solution within the chosen form's tolerance, on traps narrower and wider
+    than the tiles."""
+    traps = wl.batched_uneven(3, 512)
+    sub = [traps[i] for i in (int(np.argmin([t.n_nodes for t in traps])), 17, 301)]
+    refs = [hsld.run_trap(t, steps=8) for t in sub]
+    with F.TrapBatch([tp(t) for t in sub], F.default_opts(F.FP32_IR, tile_cols=cols,
+                                                          use_graph=1)) as b:
+        for i, t in enumerate(sub):
+            b.set_cells(i, t.cell_xy, t.cell_s)
+        b.step(8)
+        for i in range(len(sub)):
+            assert rel(b.read_nodal(i), refs[i]["u"][0]) <= 1e-6
+            assert rel(b.read_cells(i), refs[i]["cells"][0]) <= 1e-6
+
+
+def test_tile_width_is_checked(lib):
+    from eq_gb300._lib import EqfError
+    t = wl.single_small(0)
+    for bad in (8, 30, 1024):
+        with pytest.raises(EqfError):
+            F.TrapBatch([tp(t)], F.default_opts(F.FP32_IR, tile_cols=bad))
