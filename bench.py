@@ -840,7 +840,9 @@ def run_serving(args, rank, world, local_rank):
         "host_s": {"submit_python": round(t_sub, 2), "progress": round(t_prog, 2),
                    "results_python": round(t_res, 2), "of_which_admit": round(st["admit_s"], 2),
                    "of_which_launch": round(st["launch_s"], 2),
-                   "of_which_release": round(st["release_s"], 2)},
+                   "of_which_release": round(st["release_s"], 2),
+                   "of_which_first_steps": round(st["first_step_s"], 2),
+                   "of_which_readouts": round(st["readout_s"], 2)},
         "audit": {"sampled": len(audit), "completed": len(aud), "checked": checked,
                   "relL2_max": max(errs) if errs else None, "tolerance": 1e-6},
         "clocks": clk,

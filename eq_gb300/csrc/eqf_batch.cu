@@ -45,24 +45,42 @@ struct Error : std::runtime_error {
 
 #define EQF_LAUNCH_CHECK() EQF_CK(cudaGetLastError())
 
+// The stream that device buffers are allocated and freed on while a batch's call runs
+// (its own stream): cudaMallocAsync / cudaFreeAsync from the device's memory pool are
+// ordered on that stream alone, where cudaMalloc / cudaFree can wait for the whole
+// device, so batches created, grown or destroyed beside running ones (a server's
+// cohorts) do not stall them.  Unset (outside any batch call): plain cudaMalloc.
+thread_local cudaStream_t tl_alloc_stream = nullptr;
+struct AllocStream {
+  cudaStream_t prev;
+  explicit AllocStream(cudaStream_t s) : prev(tl_alloc_stream) { tl_alloc_stream = s; }
+  ~AllocStream() { tl_alloc_stream = prev; }
+  AllocStream(const AllocStream&) = delete;
+  AllocStream& operator=(const AllocStream&) = delete;
+};
+
 template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // allocated on this stream (stream-ordered free), or plain
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) {
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) {
     o.p = nullptr;
     o.n = 0;
+    o.s = nullptr;
   }
   DevBuf& operator=(DevBuf&& o) noexcept {
     if (this != &o) {
       release();
       p = o.p;
       n = o.n;
+      s = o.s;
       o.p = nullptr;
       o.n = 0;
+      o.s = nullptr;
     }
     return *this;
   }
@@ -70,13 +88,29 @@ struct DevBuf {
   void alloc(size_t count) {
     release();
     if (count == 0) return;
-    EQF_CK(cudaMalloc(&p, count * sizeof(T)));
+    if (tl_alloc_stream) {
+      EQF_CK(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), tl_alloc_stream));
+      s = tl_alloc_stream;
+    } else {
+      EQF_CK(cudaMalloc(&p, count * sizeof(T)));
+    }
     n = count;
+    // the staged kernels' bulk copies and vector loads rely on 256-byte bases
+    if (reinterpret_cast<uintptr_t>(p) & 255) {
+      release();
+      throw Error(EQF_ERR_CUDA, "device allocation not 256-byte aligned");
+    }
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s)
+        cudaFreeAsync(p, s);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    s = nullptr;
   }
   void upload(const T* h, size_t count, cudaStream_t s) {
     EQF_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
@@ -296,9 +330,29 @@ struct Level {
 };
 
 constexpr size_t kSmemHeader = 16;              // mbarrier
-// Krylov iterations of a refinement sweep the host adds after a step missed rtol (the
-// graph's sweeps run opts.max_iters): such a sweep corrects a small residual.
+// Krylov iterations of a refinement sweep added after a step missed rtol (the step's
+// own sweeps run opts.max_iters): such a sweep corrects a small residual.
 constexpr int kExtraSweepIters = 6;
+constexpr int kMaxExtraSweeps = 8;  // added sweeps per step before the step fails
+
+// Adaptive refinement without a host round trip: run once after a graph-captured
+// step's check (first = 1) and at the end of each added sweep, it sets the step graph's
+// conditional loop to run another sweep while some trap of this step missed rtol and
+// fewer than max_extra sweeps have run.  *fail counts failed trap-steps until the host
+// reads and clears it; st[0] holds the part of it from earlier steps (a sweep restarts
+// the count from there), st[1] the sweeps added in this step.
+__global__ void k_sweep_loop(cudaGraphConditionalHandle h, int* fail, int* st, int first,
+                             int max_extra) {
+  if (first) st[1] = 0;
+  const bool again = *fail > st[0] && st[1] < max_extra;
+  if (again) {
+    *fail = st[0];
+    st[1] += 1;
+  } else {
+    st[0] = *fail;  // this step's remaining failures stay counted
+  }
+  cudaGraphSetConditional(h, again ? 1u : 0u);
+}
 constexpr size_t kMaxDynSmem = 200 * 1024;      // per CTA budget for staged kernels
 
 // ---------------------------------------------------------------------------
@@ -380,6 +434,17 @@ struct Work : WorkBase {
 
 class Batch {
  public:
+  // Owns the batch's stream.  Declared first, so destroyed last: every buffer's
+  // stream-ordered free is queued on the stream before it goes.
+  struct StreamOwner {
+    cudaStream_t s = nullptr;
+    ~StreamOwner() {
+      if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+    }
+  } stream_owner;
   int ntraps = 0;
   int nlev = 0;
   // the V-cycle below level bottom_lb runs in k_bottom, one CTA per trap (-1: not used)
@@ -556,6 +621,16 @@ class Batch {
   void build_levels();
   void step(int n);
   void run_step();
+  // one step as a CUDA graph; with opts.adaptive the added refinement sweeps are a
+  // conditional loop node inside it (no host round trip per step)
+  void capture_step(cudaGraphExec_t& gx, bool device_loop);
+  bool device_loop_ok = true;  // conditional graph nodes available (else the host loop)
+  bool cond_failed = false;    // the last capture failed in a conditional-node call
+  DevBuf<int> d_loop;          // k_sweep_loop's state: earlier failures, added sweeps
+  void reset_fail() {
+    EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+    if (d_loop.n) EQF_CK(cudaMemsetAsync(d_loop.p, 0, 2 * sizeof(int), stream));
+  }
   void rebuild_cells();
   void pull_cell_s();
   void refresh_load();
@@ -599,6 +674,8 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     throw Error(EQF_ERR_NO_DEVICE, "no CUDA device visible");
   EQF_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  stream_owner.s = stream;
+  AllocStream scope(stream);
   {
     int dev = 0;
     EQF_CK(cudaGetDevice(&dev));
@@ -662,8 +739,7 @@ Batch::~Batch() {
   for (auto& gx : graph)
     if (gx) cudaGraphExecDestroy(gx);
   for (auto& e : prof.ev) cudaEventDestroy(e);
-  work.reset();
-  if (stream) cudaStreamDestroy(stream);
+  work.reset();  // (the stream goes with stream_owner, after the members' frees)
 }
 
 // Multigrid levels a trap needs: coarsen until the Fourier number beta/h^2 drops
@@ -1977,9 +2053,83 @@ void Batch::check_fail() {
   if (derr)
     throw Error(EQF_ERR_CUDA, "a device-side bounded wait gave up (staging copy never landed)");
   if (f > 0) {
-    EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+    reset_fail();
     throw Error(EQF_ERR_NOT_CONVERGED,
                 std::to_string(f) + " trap-step(s) missed rtol within the solver schedule");
+  }
+}
+
+// Captures run_step() (and, with device_loop, the adaptive sweeps as a WHILE node
+// whose body is one added sweep, its check and k_sweep_loop) and instantiates it.
+void Batch::capture_step(cudaGraphExec_t& gx, bool device_loop) {
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaGraph_t gr = nullptr;
+  bool capturing = false;
+  auto abandon = [&] {  // leave the stream out of capture mode on any error
+    if (capturing) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(stream, &g);
+      if (g) cudaGraphDestroy(g);
+    }
+    if (gr) cudaGraphDestroy(gr);
+    cudaGetLastError();
+  };
+  cond_failed = false;
+  // a failing conditional-node call marks the capture as one to redo without the loop
+#define EQF_COND_CK(call)   \
+  do {                      \
+    cond_failed = true;     \
+    EQF_CK(call);           \
+    cond_failed = false;    \
+  } while (0)
+  try {
+    cudaGraphConditionalHandle h{};
+    std::vector<cudaGraphNode_t> leaf;
+    if (device_loop && d_loop.n == 0) {
+      d_loop.alloc(2);
+      EQF_CK(cudaMemsetAsync(d_loop.p, 0, 2 * sizeof(int), stream));
+    }
+    EQF_CK(cudaStreamBeginCapture(stream, mode));
+    capturing = true;
+    run_step();
+    if (device_loop) {
+      cudaStreamCaptureStatus st;
+      cudaGraph_t cg = nullptr;
+      EQF_COND_CK(cudaStreamGetCaptureInfo(stream, &st, nullptr, &cg, nullptr, nullptr, nullptr));
+      EQF_COND_CK(cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+      k_sweep_loop<<<1, 1, 0, stream>>>(h, d_fail.p, d_loop.p, 1, kMaxExtraSweeps);
+      EQF_COND_CK(cudaGetLastError());
+      const cudaGraphNode_t* deps = nullptr;
+      size_t nd = 0;
+      EQF_COND_CK(cudaStreamGetCaptureInfo(stream, &st, nullptr, nullptr, &deps, nullptr, &nd));
+      leaf.assign(deps, deps + nd);
+    }
+    capturing = false;
+    EQF_CK(cudaStreamEndCapture(stream, &gr));
+    if (device_loop) {
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      EQF_COND_CK(cudaGraphAddNode(&node, gr, leaf.data(), nullptr, leaf.size(), &cp));
+      EQF_COND_CK(cudaStreamBeginCaptureToGraph(stream, cp.conditional.phGraph_out[0], nullptr,
+                                                nullptr, 0, mode));
+      capturing = true;
+      work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters));
+      work->enqueue_check(stream, false);
+      k_sweep_loop<<<1, 1, 0, stream>>>(h, d_fail.p, d_loop.p, 0, kMaxExtraSweeps);
+      EQF_COND_CK(cudaGetLastError());
+      cudaGraph_t body = nullptr;
+      capturing = false;
+      EQF_COND_CK(cudaStreamEndCapture(stream, &body));
+    }
+    EQF_COND_CK(cudaGraphInstantiate(&gx, gr, 0));
+    cudaGraphDestroy(gr);
+  } catch (...) {
+    abandon();
+    throw;
   }
 }
 
@@ -1987,33 +2137,40 @@ void Batch::step(int n) {
   ensure_ops();
   if (cells_dirty) rebuild_cells();
   for (int k = 0; k < n; ++k) {
+    bool looped = false;  // the added sweeps ran inside the step's graph
     if (opts.use_graph && !prof.on) {
       cudaGraphExec_t& gx = graph[cur];
       if (!gx) {
-        cudaGraph_t gr;
-        EQF_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        run_step();
-        EQF_CK(cudaStreamEndCapture(stream, &gr));
-        EQF_CK(cudaGraphInstantiate(&gx, gr, 0));
-        cudaGraphDestroy(gr);
+        if (opts.adaptive && device_loop_ok) {
+          try {
+            capture_step(gx, true);
+          } catch (const Error&) {
+            if (!cond_failed) throw;
+            // no conditional nodes here: the host adds the sweeps (below)
+            device_loop_ok = false;
+            drop_graphs();
+          }
+        }
+        if (!gx) capture_step(gx, false);
       }
       EQF_CK(cudaGraphLaunch(gx, stream));
+      looped = opts.adaptive && device_loop_ok;
     } else {
       run_step();
     }
-    if (opts.adaptive) {
+    if (opts.adaptive && !looped) {
       // add sweeps for traps that missed rtol (the others are skipped by ir_done)
       int f = 0;
-      for (int extra = 0; extra < 8; ++extra) {
+      for (int extra = 0; extra < kMaxExtraSweeps; ++extra) {
         EQF_CK(cudaMemcpyAsync(&f, d_fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         sync();
         if (f == 0) break;
-        EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        reset_fail();
         work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters));
         work->enqueue_check(stream, false);
       }
       if (f != 0) {
-        EQF_CK(cudaMemsetAsync(d_fail.p, 0, sizeof(int), stream));
+        reset_fail();
         enqueue_channels();
         enqueue_wells();
         cur = 1 - cur;
@@ -2246,6 +2403,7 @@ static thread_local std::string g_create_err;
 
 template <class F>
 static int guarded(eqf_batch* b, F&& f) {
+  eqf::AllocStream scope(b && b->impl ? b->impl->stream : nullptr);
   try {
     f();
     return EQF_OK;
@@ -2492,10 +2650,8 @@ int eqf_read_cells_async(eqf_batch* b, int32_t trap, int64_t n, double* c) {
     if (B.cells_dirty) B.rebuild_cells();
     EQF_REQUIRE(n == (int64_t)B.cell_s[trap].size() && (n == 0 || c), "cell count mismatch");
     if (n == 0) return;
-    if (B.d_cells_out.n < (size_t)B.ncells) {
-      B.sync();
-      B.d_cells_out.alloc(B.ncells);
-    }
+    // stream-ordered (re)allocation: no wait for the steps queued before it
+    if (B.d_cells_out.n < (size_t)B.ncells) B.d_cells_out.alloc(B.ncells);
     const int c0 = B.cell_first[trap];
     eqf::k_cells_gather<<<(int)((n + 255) / 256), 256, 0, B.stream>>>(
         (int)n, B.d_ent_node.p + 3 * (size_t)c0, B.d_ent_w.p + 3 * (size_t)c0, B.u_cur(),

@@ -52,6 +52,61 @@ struct StepMark {
   int32_t* fail = nullptr;  // pinned: the batch's failure counter after this step
 };
 
+// Page-locked host memory for the readouts, carved from large slabs and recycled by
+// power-of-two size class.  A cudaMallocHost / cudaFreeHost per request or per step
+// would stall the one host thread that keeps every cohort's queue filled.
+struct PinnedArena {
+  static constexpr size_t kSlab = (size_t)64 << 20;
+  std::vector<void*> slabs;
+  char* cur = nullptr;
+  size_t left = 0;
+  std::map<size_t, std::vector<void*>> free_by_class;
+  static size_t size_class(size_t n) {
+    size_t c = 256;
+    while (c < n) c <<= 1;
+    return c;
+  }
+  // nullptr when page-locked memory runs out
+  void* get(size_t n) {
+    const size_t c = size_class(n);
+    std::vector<void*>& fl = free_by_class[c];
+    if (!fl.empty()) {
+      void* p = fl.back();
+      fl.pop_back();
+      return p;
+    }
+    void* p = nullptr;
+    if (c > kSlab / 4) {  // large: a slab of its own
+      if (cudaMallocHost(&p, c) != cudaSuccess) return nullptr;
+      slabs.push_back(p);
+      return p;
+    }
+    if (left < c) {
+      if (cudaMallocHost(&p, kSlab) != cudaSuccess) return nullptr;
+      slabs.push_back(p);
+      cur = static_cast<char*>(p);
+      left = kSlab;
+    }
+    p = cur;
+    cur += c;
+    left -= c;
+    return p;
+  }
+  void put(void* p, size_t n) {
+    if (p) free_by_class[size_class(n)].push_back(p);
+  }
+  ~PinnedArena() {
+    for (void* p : slabs) cudaFreeHost(p);
+  }
+};
+
+size_t cells_bytes(const Req* q) {
+  return sizeof(double) * (size_t)std::max<int64_t>(1, q->r.n_cells * q->r.n_species);
+}
+size_t nodal_bytes(const Req* q) {
+  return sizeof(double) * (size_t)(q->n_nodes * q->r.n_species);
+}
+
 struct Cohort {
   int id = 0;
   eqf_batch* b = nullptr;
@@ -80,6 +135,11 @@ struct eqs_server {
   std::vector<int64_t> done_ids;
   std::vector<float> step_ms;
   eqs_stats st{};
+  PinnedArena pinned;  // destroyed after the cohorts' copies into it are done
+  // the device's memory pool keeps what released cohorts freed (up to the budget) for
+  // the next admissions; its previous release threshold is restored at destruction
+  cudaMemPool_t pool = nullptr;
+  uint64_t pool_threshold0 = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -138,7 +198,7 @@ void release_cohort(eqs_server* s, Cohort& c) {
   for (StepMark& m : c.inflight) {
     cudaEventDestroy(m.start);
     cudaEventDestroy(m.end);
-    cudaFreeHost(m.fail);
+    s->pinned.put(m.fail, sizeof(int32_t));
   }
   c.inflight.clear();
   if (c.b) eqf_destroy(c.b);
@@ -173,10 +233,12 @@ void launch_step(eqs_server* s, Cohort& c) {
   m.step = c.launched + 1;
   ckc(cudaEventCreate(&m.start), "cudaEventCreate");
   ckc(cudaEventCreate(&m.end), "cudaEventCreate");
-  ckc(cudaMallocHost(&m.fail, sizeof(int32_t)), "cudaMallocHost");
+  m.fail = static_cast<int32_t*>(s->pinned.get(sizeof(int32_t)));
+  if (!m.fail) throw Fail{EQF_ERR_NOMEM, "page-locked host memory exhausted"};
   *m.fail = 0;
   ckc(cudaEventRecord(m.start, c.stream), "cudaEventRecord");
   ckb(eqf_step(c.b, 1), c.b);
+  const double tr = s->now();
   for (Req* q : c.reqs) {
     if (q->r.steps != m.step) continue;
     for (int k = 0; k < q->r.n_species; ++k) {
@@ -188,6 +250,7 @@ void launch_step(eqs_server* s, Cohort& c) {
     }
   }
   ckb(eqf_fail_count_async(c.b, m.fail), c.b);
+  s->st.readout_s += s->now() - tr;
   ckc(cudaEventRecord(m.end, c.stream), "cudaEventRecord");
   c.inflight.push_back(m);
   c.launched = m.step;
@@ -220,7 +283,7 @@ void retire(eqs_server* s, Cohort& c) {
       }
     cudaEventDestroy(m.start);
     cudaEventDestroy(m.end);
-    cudaFreeHost(m.fail);
+    s->pinned.put(m.fail, sizeof(int32_t));
     c.inflight.pop_front();
   }
 }
@@ -295,7 +358,7 @@ bool admit(eqs_server* s) {
   int64_t cells = 0;
   trap_list(take, tp, cells);
   eqf_solver_opts o = s->cfg.opts;
-  o.adaptive = 0;
+  o.adaptive = 1;  // the added sweeps run inside the step's graph: no host round trip
   o.use_graph = 1;
   const int rc = eqf_create((int32_t)tp.size(), tp.data(), &o, &c->b);
   if (rc != EQF_OK) {
@@ -332,12 +395,10 @@ bool admit(eqs_server* s) {
                                q->r.uptake),
             c->b);
     }
-    ckc(cudaMallocHost(&q->h_cells, sizeof(double) * std::max<int64_t>(
-                                        1, q->r.n_cells * q->r.n_species)),
-        "cudaMallocHost");
-    if (q->r.want_nodal)
-      ckc(cudaMallocHost(&q->h_nodal, sizeof(double) * q->n_nodes * q->r.n_species),
-          "cudaMallocHost");
+    q->h_cells = static_cast<double*>(s->pinned.get(cells_bytes(q)));
+    if (q->r.want_nodal) q->h_nodal = static_cast<double*>(s->pinned.get(nodal_bytes(q)));
+    if (!q->h_cells || (q->r.want_nodal && !q->h_nodal))
+      throw Fail{EQF_ERR_NOMEM, "page-locked host memory exhausted"};
     c->steps_target = std::max(c->steps_target, q->r.steps);
     t += q->ntraps();
   }
@@ -382,8 +443,11 @@ void progress(eqs_server* s) {
   for (auto& c : s->cohorts) {
     if (c->retired) continue;
     try {
-      while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight)
+      while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight) {
+        const double t1 = c->launched == 0 ? s->now() : -1.0;
         launch_step(s, *c);
+        if (t1 >= 0) s->st.first_step_s += s->now() - t1;
+      }
     } catch (const Fail& f) {
       s->err = f.msg;
       fail_cohort(s, *c, f.code);
@@ -414,7 +478,6 @@ int eqs_default_config(eqs_config* c) {
   if (!c) return EQF_ERR_INVALID;
   std::memset(c, 0, sizeof(*c));
   eqf_default_opts(EQF_PREC_FP32_IR, &c->opts);
-  c->opts.max_sweeps = 3;  // no host round trip per step: one spare sweep instead
   c->hbm_budget = (int64_t)150 << 30;
   c->max_cohorts = 8;
   c->max_cohort_traps = 256;
@@ -434,6 +497,16 @@ int eqs_create(const eqs_config* cfg, eqs_server** out) {
   eqs_server* s = new (std::nothrow) eqs_server;
   if (!s) return EQF_ERR_NOMEM;
   s->cfg = *cfg;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&s->pool, dev) == cudaSuccess &&
+      cudaMemPoolGetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &s->pool_threshold0) ==
+          cudaSuccess) {
+    uint64_t keep = (uint64_t)cfg->hbm_budget;
+    if (keep > s->pool_threshold0)
+      cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    s->pool = nullptr;
+  }
   *out = s;
   return EQF_OK;
 }
@@ -445,11 +518,11 @@ int eqs_destroy(eqs_server* s) {
       eqf_sync(c->b);
       release_cohort(s, *c);
     }
-  for (auto& kv : s->reqs) {
-    if (kv.second->h_cells) cudaFreeHost(kv.second->h_cells);
-    if (kv.second->h_nodal) cudaFreeHost(kv.second->h_nodal);
+  if (s->pool) {
+    cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &s->pool_threshold0);
+    cudaMemPoolTrimTo(s->pool, 0);
   }
-  delete s;
+  delete s;  // the arena's slabs go with it (no copy into them is left in flight)
   return EQF_OK;
 }
 
@@ -534,8 +607,8 @@ int eqs_result(eqs_server* s, int64_t id, double* cells, double* nodal, eqs_resu
       info->cohort = q->cohort;
     }
     // no copy writes these buffers after the request finished
-    if (q->h_cells) cudaFreeHost(q->h_cells);
-    if (q->h_nodal) cudaFreeHost(q->h_nodal);
+    s->pinned.put(q->h_cells, cells_bytes(q));
+    s->pinned.put(q->h_nodal, nodal_bytes(q));
     q->h_cells = q->h_nodal = nullptr;
     q->taken = true;
     // the object itself stays while a live cohort still refers to it

@@ -42,7 +42,8 @@ class Stats(C.Structure):
                 ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
                 ("step_ms_p999", C.c_double), ("step_samples", C.c_int64),
                 ("bytes_in_use", C.c_int64), ("bytes_peak", C.c_int64),
-                ("admit_s", C.c_double), ("launch_s", C.c_double), ("release_s", C.c_double)]
+                ("admit_s", C.c_double), ("launch_s", C.c_double), ("release_s", C.c_double),
+                ("first_step_s", C.c_double), ("readout_s", C.c_double)]
 
 
 def _bind(lib):

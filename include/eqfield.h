@@ -83,7 +83,11 @@ typedef struct eqf_solver_opts {
   int32_t cheb_pre, cheb_post, cheb_coarse; /* Chebyshev degrees */
   double cheb_ratio;  /* smoothing interval [lmax/ratio, lmax] */
   int32_t use_graph;  /* capture steps as CUDA graphs */
-  int32_t adaptive;   /* after each step check convergence on the host and add sweeps */
+  int32_t adaptive;   /* after each step check convergence and add refinement sweeps
+                       * (up to 8) for the traps that missed rtol: with use_graph on
+                       * the device, as a conditional loop inside the step's graph (the
+                       * step does not wait; a trap still failing is reported by the
+                       * next eqf_sync or readout), else on the host after each step */
   int32_t tile_nodes; /* target nodes per row tile of the finest level (0: default) */
   int32_t krylov;     /* EQF_KRYLOV_*: AUTO = BiCGSTAB iff some trap has advection */
   int32_t fuse_levels; /* 0: step-by-step V-cycle kernels; 1 (default): temporally
@@ -262,8 +266,8 @@ int eqf_stats(eqf_batch* b, int32_t trap, int64_t* steps, int64_t* sweeps, int64
 int eqf_sync(eqf_batch* b);
 
 /* Asynchronous use (no reference counterpart; the serving loop of eqserve.h is
- * built on these).  With opts.adaptive = 0, eqf_step only queues the steps on the
- * batch's stream and returns.  eqf_poll sets *idle to 1 once all queued work has
+ * built on these).  With opts.adaptive = 0, or adaptive with use_graph, eqf_step
+ * only queues the steps on the batch's stream and returns.  eqf_poll sets *idle to 1 once all queued work has
  * finished (and then reports deferred errors, as eqf_sync), else 0, without
  * waiting.  eqf_read_cells_async / eqf_read_nodal_async queue the readout of a
  * trap's current state into host memory (pinned for the copy to overlap), valid

@@ -32,7 +32,7 @@ extern "C" {
 typedef struct eqs_server eqs_server;
 
 typedef struct eqs_config {
-  eqf_solver_opts opts;     /* cohort solver options (adaptive is forced off) */
+  eqf_solver_opts opts;     /* cohort solver options (graphs and adaptive sweeps forced on) */
   int64_t hbm_budget;       /* device bytes the server's cohorts may hold */
   int32_t max_cohorts;      /* cohorts stepping concurrently (one stream each) */
   int32_t max_cohort_traps; /* traps per cohort */
@@ -73,6 +73,10 @@ typedef struct eqs_stats {
   double admit_s;                   /* host seconds spent forming cohorts (incl. releases) */
   double launch_s;                  /* host seconds spent queueing cohort steps */
   double release_s;                 /* host seconds spent releasing retired cohorts */
+  double first_step_s;              /* of launch_s: queueing each cohort's first step
+                                       (its one-time set-up: cell index, graph capture) */
+  double readout_s;                 /* of launch_s: queueing finished requests' readouts
+                                       and freezes */
 } eqs_stats;
 
 int eqs_default_config(eqs_config* cfg);
