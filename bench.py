@@ -61,7 +61,7 @@ class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, index: int):
         self.index = index
@@ -91,7 +91,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
+        sm, mx, util, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -105,9 +105,17 @@ class ClockSampler:
             for n, v in zip(names, parts[3:7]):
                 if v.lower() == "active":
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+            if len(parts) > 7:
+                try:
+                    util.append(float(parts[7]))
+                except ValueError:
+                    pass
+        out = {"sm_mhz": statistics.median(sm) if sm else None,
+               "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if util:  # share of sample periods with a kernel running (nvidia-smi)
+            out["gpu_util_pct_mean"] = round(statistics.mean(util), 1)
+        return out
 
 
 # ------------------------------------------------------------------- workloads
@@ -795,6 +803,25 @@ def run_serving(args, rank, world, local_rank):
     st = srv.stats()
     srv.close()
     done = [r for r in results.values() if r.status == 0]
+    # cohorts: requests, work and live span (first admission to last completion)
+    coh = {}
+    for i, r in results.items():
+        if r.status != 0:
+            continue
+        nn, ns = sizes[i]
+        c = coh.setdefault(r.cohort, [0, 0.0, r.t_admit, r.t_done, 0])
+        c[0] += 1
+        c[1] += nn * ns * r.steps
+        c[2], c[3] = min(c[2], r.t_admit), max(c[3], r.t_done)
+        c[4] += ns
+    spans = [c[3] - c[2] for c in coh.values()]
+    cohort_summary = {
+        "count": len(coh),
+        "traps_mean": float(np.mean([c[4] for c in coh.values()])) if coh else 0.0,
+        "span_s_mean": float(np.mean(spans)) if spans else 0.0,
+        "live_mean": float(sum(spans) / max(wall, 1e-9)),
+        "dof_steps_per_s_per_cohort": float(np.mean([c[1] / max(c[3] - c[2], 1e-9)
+                                                     for c in coh.values()])) if coh else 0.0}
     lat = np.array([r.t_done - r.t_submit for r in done]) if done else np.zeros(1)
     wait = np.array([r.t_admit - r.t_submit for r in done]) if done else np.zeros(1)
     # audit: the seeded sample's completed requests against the FP64 oracle, as many
@@ -829,6 +856,7 @@ def run_serving(args, rank, world, local_rank):
                 "this measures saturation throughput plus admission and queueing latency",
         "completed": len(done), "failed": int(st["failed"]), "unfinished": n - len(results),
         "wall_s": wall, "busy_s": st["busy_s"], "cohorts": int(st["cohorts"]),
+        "cohort_summary": cohort_summary,
         "step_ms": {"p50": st["step_ms_p50"], "p99": st["step_ms_p99"],
                     "p99.9": st["step_ms_p999"], "samples": int(st["step_samples"])},
         "request_latency_s": {"p50": float(np.percentile(lat, 50)),

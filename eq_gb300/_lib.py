@@ -32,6 +32,7 @@ EXPORTS = (
     "eqf_sync", "eqf_set_cell_rates_all", "eqf_read_cells_all", "eqf_profile",
     "eqf_profile_read", "eqf_stream", "eqf_field_integral_noalloc", "eqf_couple_species",
     "eqf_poll", "eqf_read_cells_async", "eqf_read_nodal_async", "eqf_set_active",
+    "eqf_replace_trap", "eqf_replace_traps", "eqf_slot_fits",
     "eqf_footprint_estimate", "eqf_fail_count_async", "eqf_create_tuned", "eqf_autotune",
     "eqf_set_rods", "eqf_update_rods", "eqf_read_rods", "eqf_exchange_rods", "eqf_rod_waves",
     "eqf_update_rods_all", "eqf_read_rods_all",
@@ -165,6 +166,11 @@ def load() -> C.CDLL:
         "eqf_read_cells_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, dp]),
         "eqf_read_nodal_async": (C.c_int, [C.c_void_p, C.c_int32, dp]),
         "eqf_set_active": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "eqf_replace_trap": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(TrapParams)]),
+        "eqf_replace_traps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                        C.POINTER(TrapParams)]),
+        "eqf_slot_fits": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(TrapParams),
+                                    C.POINTER(C.c_int32)]),
         "eqf_fail_count_async": (C.c_int, [C.c_void_p, P(C.c_int32)]),
         "eqf_create_tuned": (C.c_int, [C.c_int32, P(TrapParams), P(SolverOpts), P(TuneTable),
                                        P(C.c_void_p)]),

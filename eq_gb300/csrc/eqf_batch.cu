@@ -13,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -244,6 +245,8 @@ static void interior_constants(LevelGeom& g) {
   q.tensf = nullptr;
   q.coef_f = nullptr;
   q.coef_d = nullptr;
+  q.rowc_f = nullptr;
+  q.rowc_d = nullptr;
   const Sten<double> s = stencil_general<double>(q, 500, 500);
   g.cC = s.c;
   g.cE = s.e;
@@ -412,6 +415,8 @@ struct WorkBase {
   // one refinement sweep of `iters` preconditioned Krylov iterations
   virtual void enqueue_sweep(cudaStream_t s, bool first, int iters) = 0;
   virtual void enqueue_check(cudaStream_t s, bool update_gamma) = 0;
+  // zeroes every work vector over nodes [off, off + n) of level `lev` (a reused slot)
+  virtual void clear_slot(cudaStream_t s, int lev, long long off, long long n) = 0;
 };
 
 class Batch;
@@ -428,9 +433,33 @@ struct Work : WorkBase {
   explicit Work(Batch& b);
   void enqueue_sweep(cudaStream_t s, bool first, int iters) override;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
+  void clear_slot(cudaStream_t s, int lev, long long off, long long n) override {
+    for (DevBuf<T>* v : {&lv[lev].b, &lv[lev].x, &lv[lev].y, &lv[lev].d, &lv[lev].t})
+      EQF_CK(cudaMemsetAsync(v->p + off, 0, n * sizeof(T), s));
+    if (lev == 0)
+      for (DevBuf<T>* v : {&xs, &p0, &p1, &q, &rh})
+        if (v->p) EQF_CK(cudaMemsetAsync(v->p + off, 0, n * sizeof(T), s));
+  }
   T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr);
   void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs, int max_iters);
 };
+
+// Executable graphs that are no longer used.  Destroying one that holds a conditional
+// node waits for the whole device, so they are kept here and destroyed in groups, a
+// wait per kRetiredGraphs batches instead of one each (the last group stays until the
+// process ends).
+constexpr size_t kRetiredGraphs = 64;
+static std::mutex g_retired_mu;
+static std::vector<cudaGraphExec_t> g_retired;
+static void retire_graph_exec(cudaGraphExec_t gx) {
+  std::vector<cudaGraphExec_t> doomed;
+  {
+    std::lock_guard<std::mutex> lk(g_retired_mu);
+    g_retired.push_back(gx);
+    if (g_retired.size() >= kRetiredGraphs) doomed.swap(g_retired);
+  }
+  for (cudaGraphExec_t g : doomed) cudaGraphExecDestroy(g);
+}
 
 class Batch {
  public:
@@ -453,6 +482,10 @@ class Batch {
   eqf_solver_opts opts{};
   std::vector<eqf_trap_params> params;
   std::vector<Level> L;
+  // per level and trap: the nodes reserved for the trap's slot (its grid at creation;
+  // eqf_replace_trap puts any grid that fits there), so replacing a trap moves no
+  // other trap and reallocates no vector.  Empty until the first build_levels.
+  std::vector<std::vector<long long>> slot_span;
   std::vector<TileRange> range;  // fine tiles per trap
   DevBuf<TileRange> drange;
   DevBuf<TileRange> drange2;     // fine 2-D tiles per trap (partials of the fused kernels)
@@ -569,7 +602,10 @@ class Batch {
     ops_dirty = false;
     build_levels();
     setup_walls();
+    grow(dpart, 3 * std::max((size_t)L[0].ntiles(), L[0].tiles2.size()));
   }
+  void check_replacement(int t, const eqf_trap_params& p) const;
+  void replace_trap(int t, const eqf_trap_params& p);
   void enqueue_walls();
   void enqueue_channels();
   // anisotropic tensors (eqf_set_tensor): per trap the caller's D11, D22, D12 in grid
@@ -580,6 +616,9 @@ class Batch {
   std::map<std::pair<int, int>, DevBuf<float>> dtensf;
   std::map<std::pair<int, int>, DevBuf<float>> dcoef_f;
   std::map<std::pair<int, int>, DevBuf<double>> dcoef_d;
+  // per (level, trap) of an advective trap: its rows' stencils (LevelGeom::rowc_*)
+  std::map<std::pair<int, int>, DevBuf<float>> drowc_f;
+  std::map<std::pair<int, int>, DevBuf<double>> drowc_d;
   void level_tensor(LevelGeom& g, int level, int t);
   // boundary wells (eqf_set_well)
   struct WellParams {
@@ -605,13 +644,11 @@ class Batch {
   PinnedBuf<unsigned char> rod_hstage;  // rods / production / readbacks of the batch calls
   void rod_publish();
   void enqueue_rods();
-  void drop_graphs() {
-    for (auto& gx : graph)
-      if (gx) {
-        cudaGraphExecDestroy(gx);
-        gx = nullptr;
-      }
-  }
+  // Marks the captured steps out of date: the next step of each parity recaptures it
+  // (updating a plain graph in place; the old executable graph of a conditional loop
+  // goes to the retired list, as destroying it would wait for the whole device).
+  bool graph_stale[2] = {false, false};
+  void drop_graphs() { graph_stale[0] = graph_stale[1] = true; }
 
   Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const int* tiles = nullptr,
         const int* cols = nullptr);
@@ -737,7 +774,7 @@ Batch::Batch(int n, const eqf_trap_params* p, const eqf_solver_opts& o, const in
 
 Batch::~Batch() {
   for (auto& gx : graph)
-    if (gx) cudaGraphExecDestroy(gx);
+    if (gx) retire_graph_exec(gx);
   for (auto& e : prof.ev) cudaEventDestroy(e);
   work.reset();  // (the stream goes with stream_owner, after the members' frees)
 }
@@ -840,6 +877,7 @@ void Batch::build_levels() {
   L.clear();
   int nl = 1;
   for (const auto& p : params) nl = std::max(nl, trap_levels(p));
+  if (!slot_span.empty()) nl = (int)slot_span.size();  // the depth is fixed at creation
   nlev = nl;
   L.resize(nlev);
   for (int l = 0; l < nlev; ++l) L[l].geom.resize(ntraps);
@@ -888,6 +926,8 @@ void Batch::build_levels() {
       g.tstride = 0;
       g.coef_f = nullptr;
       g.coef_d = nullptr;
+      g.rowc_f = nullptr;
+      g.rowc_d = nullptr;
       if (!tensor[t].empty()) level_tensor(g, l, t);
       interior_constants(g);
       if (g.tens) {
@@ -902,6 +942,30 @@ void Batch::build_levels() {
         EQF_LAUNCH_CHECK();
         g.coef_f = cf.p;
         g.coef_d = cd.p;
+      } else if (g.adv_on) {
+        // advection: the stencil depends on the row (v_y(y)) and the column class only
+        const size_t n = (size_t)(g.ny + 1) * 5 * 8;
+        std::vector<double> rd(n, 0.0);
+        std::vector<float> rf(n, 0.0f);
+        for (int i = 0; i <= g.ny; ++i)
+          for (int c = 0; c < 5; ++c) {
+            const int j = edge_rep(c, g.nx);
+            if (j < 0 || j > g.nx || edge_class(j, g.nx) != c) continue;  // absent class
+            const Sten<double> sd = stencil_general<double>(g, i, j);
+            const double v[8] = {sd.c, sd.e, sd.w, sd.n, sd.s, sd.ne, sd.sw, 1.0 / sd.c};
+            for (int q = 0; q < 8; ++q) {
+              rd[((size_t)i * 5 + c) * 8 + q] = v[q];
+              rf[((size_t)i * 5 + c) * 8 + q] = (float)v[q];
+            }
+          }
+        DevBuf<float>& bf = drowc_f[{l, t}];
+        DevBuf<double>& bd = drowc_d[{l, t}];
+        bf.alloc(n);
+        bf.upload(rf.data(), n, stream);
+        bd.alloc(n);
+        bd.upload(rd.data(), n, stream);
+        g.rowc_f = bf.p;
+        g.rowc_d = bd.p;
       }
       spectrum_bounds(g);
       cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
@@ -916,11 +980,16 @@ void Batch::build_levels() {
     long long off = 0;
     std::vector<Tile> gen1;   // row tiles of general-path traps: after the others
     std::vector<Tile2> gen2;  // 2-D tiles of general-path traps: after the others
+    if ((int)slot_span.size() < nlev) slot_span.resize(nlev);
+    std::vector<long long>& span = slot_span[l];
+    if ((int)span.size() < ntraps) span.resize(ntraps, -1);
     for (int t = 0; t < ntraps; ++t) {
       LevelGeom& g = L[l].geom[t];
       g.off = off;
       const long long P = g.P;
       const long long n = P * (g.ny + 1);
+      if (span[t] < 0) span[t] = n;
+      if (n > span[t]) throw Error(EQF_ERR_INVALID, "trap grid larger than its slot");
       if (l > 0) {
         g.fine_off = L[l - 1].geom[t].off;
         g.fine_P = L[l - 1].geom[t].P;
@@ -943,7 +1012,7 @@ void Batch::build_levels() {
           (g.adv_on ? gen2 : L[l].tiles2)
               .push_back(Tile2{t, r0, std::min(g.ny + 1, r0 + R2), c0,
                                (int)std::min<long long>(P, c0 + CW)});
-      off = align_up(off + n, 32);
+      off = align_up(off + span[t], 32);
     }
     L[l].ntiles_cls = (int)L[l].tiles.size();
     L[l].tiles.insert(L[l].tiles.end(), gen1.begin(), gen1.end());
@@ -2125,6 +2194,19 @@ void Batch::capture_step(cudaGraphExec_t& gx, bool device_loop) {
       capturing = false;
       EQF_COND_CK(cudaStreamEndCapture(stream, &body));
     }
+    if (gx) {
+      // an out-of-date step of this parity: a plain graph is updated in place when the
+      // topology allows; one with the conditional loop is replaced (its kernels name the
+      // loop's handle, which belongs to the graph it was created on)
+      cudaGraphExecUpdateResultInfo info{};
+      if (!device_loop && cudaGraphExecUpdate(gx, gr, &info) == cudaSuccess) {
+        cudaGraphDestroy(gr);
+        return;
+      }
+      cudaGetLastError();
+      retire_graph_exec(gx);
+      gx = nullptr;
+    }
     EQF_COND_CK(cudaGraphInstantiate(&gx, gr, 0));
     cudaGraphDestroy(gr);
   } catch (...) {
@@ -2140,10 +2222,12 @@ void Batch::step(int n) {
     bool looped = false;  // the added sweeps ran inside the step's graph
     if (opts.use_graph && !prof.on) {
       cudaGraphExec_t& gx = graph[cur];
-      if (!gx) {
+      if (!gx || graph_stale[cur]) {
+        bool done = false;
         if (opts.adaptive && device_loop_ok) {
           try {
             capture_step(gx, true);
+            done = true;
           } catch (const Error&) {
             if (!cond_failed) throw;
             // no conditional nodes here: the host adds the sweeps (below)
@@ -2151,7 +2235,8 @@ void Batch::step(int n) {
             drop_graphs();
           }
         }
-        if (!gx) capture_step(gx, false);
+        if (!done) capture_step(gx, false);
+        graph_stale[cur] = false;
       }
       EQF_CK(cudaGraphLaunch(gx, stream));
       looped = opts.adaptive && device_loop_ok;
@@ -2184,6 +2269,87 @@ void Batch::step(int n) {
     cur = 1 - cur;
     ++steps_done;
   }
+}
+
+// Slot reuse: trap t becomes a new trap p whose grid fits t's slot at every level
+// (the depth and the Krylov method of the batch stay; check_replacement first).  Its field, increments, solver
+// state, cells, couplings, walls (p.walls, no values), tensor and well start afresh;
+// the other traps keep their nodes and state.  Operators, tile lists and the cell
+// index are rebuilt, and the captured steps recaptured, before the next step.
+void Batch::check_replacement(int t, const eqf_trap_params& p) const {
+  if (!(p.nx >= 1 && p.ny >= 1 && p.width > 0 && p.height > 0 && p.dt > 0 && p.D >= 0 &&
+        p.decay >= 0 && (p.walls & ~15u) == 0))
+    throw Error(EQF_ERR_INVALID, "invalid trap parameters");
+  if (trap_levels(p) > nlev)
+    throw Error(EQF_ERR_INVALID, "trap needs more multigrid levels than its batch has");
+  const bool adv = p.adv_u != 0.0 && p.adv_len > 0.0;
+  if (adv && !use_bicgstab)
+    throw Error(EQF_ERR_INVALID, "advective trap in a batch that solves with CG");
+  for (const auto& rs : rod_sets)
+    for (int l : rs->layers)
+      if (l == t) throw Error(EQF_ERR_INVALID, "trap carries rod cells");
+  for (const auto& c : chans)
+    if (c->trap == t) throw Error(EQF_ERR_INVALID, "trap carries a flow channel");
+  {  // the grid of every level must fit the slot (build_levels' coarsening)
+    int nx = p.nx, ny = p.ny;
+    for (int l = 0; l < nlev; ++l) {
+      if (l > 0) {
+        const int cx = nx >= 4, cy = ny >= 4;
+        if (cx) nx = (nx + 1) / 2;
+        if (cy) ny = (ny + 1) / 2;
+      }
+      const long long P = (nx + 1 + 3) & ~3;
+      if (P * (ny + 1) > slot_span[l][t])
+        throw Error(EQF_ERR_INVALID, "trap grid larger than its slot");
+    }
+  }
+}
+
+void Batch::replace_trap(int t, const eqf_trap_params& p) {
+  // zero the slot at every level before anything reads it under the new layout (pad
+  // columns and rows must hold zeros)
+  for (int l = 0; l < nlev; ++l) work->clear_slot(stream, l, L[l].geom[t].off, slot_span[l][t]);
+  const long long off = L[0].geom[t].off, n0 = slot_span[0][t];
+  for (int q = 0; q < 2; ++q) {
+    EQF_CK(cudaMemsetAsync(U[q].p + off, 0, n0 * sizeof(double), stream));
+    EQF_CK(cudaMemsetAsync(Dd[q].p + off, 0, n0 * sizeof(float), stream));
+  }
+  EQF_CK(cudaMemsetAsync(F.p + off, 0, n0 * sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(b64.p + off, 0, n0 * sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(dstate.p + t, 0, sizeof(CgState), stream));
+  EQF_CK(cudaMemsetAsync(d_frozen.p + t, 0, sizeof(int), stream));
+  EQF_CK(cudaMemsetAsync(d_well_c.p + t, 0, sizeof(double), stream));
+  EQF_CK(cudaMemsetAsync(d_well_under.p + t, 0, sizeof(long long), stream));
+  params[t] = p;
+  eqf_boundaries& bc = bcs[t];
+  std::memset(&bc, 0, sizeof(bc));
+  const unsigned bits[4] = {WALL_BOTTOM, WALL_TOP, WALL_LEFT, WALL_RIGHT};
+  for (int w = 0; w < 4; ++w)
+    bc.wall[w].kind = (p.walls & bits[w]) ? EQF_BC_DIRICHLET : EQF_BC_NEUMANN;
+  bc.channel_substeps = 1;
+  bc.well_scaling = 1.0;
+  tensor[t].clear();
+  auto drop = [t](auto& m) {
+    for (auto it = m.begin(); it != m.end();) it = it->first.second == t ? m.erase(it) : std::next(it);
+  };
+  drop(htens);
+  drop(dtens);
+  drop(dtensf);
+  drop(dcoef_f);
+  drop(dcoef_d);
+  drop(drowc_f);
+  drop(drowc_d);
+  well[t] = WellParams{};
+  pull_cell_s();  // the other traps' rates as the device holds them
+  cell_xy[t].clear();
+  cell_s[t].clear();
+  couplings.erase(std::remove_if(couplings.begin(), couplings.end(),
+                                 [t](const Coupling& c) { return c.t1 == t || c.t2 == t; }),
+                  couplings.end());
+  cells_dirty = true;
+  ops_dirty = true;
+  bal_prev_ok = bal_load_ok = false;
+  drop_graphs();
 }
 
 // ---------------------------------------------------------------------------
@@ -2625,6 +2791,37 @@ int eqf_set_active(eqf_batch* b, int32_t trap, int32_t active) {
     // stream-ordered, no host memory involved: the call does not wait
     EQF_CK(cudaMemsetAsync(B.d_frozen.p + trap, active ? 0 : 1, sizeof(int), B.stream));
   });
+}
+
+int eqf_replace_traps(eqf_batch* b, int32_t n, const int32_t* traps,
+                      const eqf_trap_params* p) {
+  if (!b) return EQF_ERR_INVALID;
+  return guarded(b, [&] {
+    EQF_REQUIRE(n >= 0 && (n == 0 || (traps && p)), "bad replacement arrays");
+    Batch& B = *b->impl;
+    for (int32_t k = 0; k < n; ++k) {
+      EQF_TRAP_CHECK(b, traps[k]);
+      for (int32_t m = 0; m < k; ++m) EQF_REQUIRE(traps[m] != traps[k], "trap listed twice");
+    }
+    for (int32_t k = 0; k < n; ++k) B.check_replacement(traps[k], p[k]);  // all or none
+    for (int32_t k = 0; k < n; ++k) B.replace_trap(traps[k], p[k]);
+    if (n > 0) B.ensure_ops();  // the new geometry, for readouts before the next step
+  });
+}
+
+int eqf_replace_trap(eqf_batch* b, int32_t trap, const eqf_trap_params* p) {
+  return eqf_replace_traps(b, 1, &trap, p);
+}
+
+int eqf_slot_fits(const eqf_batch* b, int32_t trap, const eqf_trap_params* p, int32_t* fits) {
+  if (!b || !p || !fits || trap < 0 || trap >= b->impl->ntraps) return EQF_ERR_INVALID;
+  try {
+    b->impl->check_replacement(trap, *p);
+    *fits = 1;
+  } catch (const Error&) {
+    *fits = 0;
+  }
+  return EQF_OK;
 }
 
 int eqf_poll(eqf_batch* b, int32_t* idle) {

@@ -64,6 +64,11 @@ struct LevelGeom {
   // pitched), built once per tensor update: the general path reads them
   const float* coef_f;
   const double* coef_d;
+  // an advective level's stencils, which vary by row only (v_y depends on y): per row
+  // i and column class edge_class(j) (c, e, w, n, s, ne, sw, 1/c), built once from
+  // the FP64 rows (FP32: rounded); null = none
+  const float* rowc_f;
+  const double* rowc_d;
   Lens<double> ld;
   Lens<float> lf;
   // Uniform-interior stencil (nodes with 2 <= i <= ny-2 and 2 <= j <= nx-2).
@@ -100,6 +105,12 @@ template <class T>
 struct Sten {
   T c, e, w, n, s, ne, sw;
 };
+
+// Class of node index j on a grid of n cells along one axis: 0 and 1 (the first two
+// nodes), 2 (interior, 2 <= j <= n - 2), 3 (n - 1) and 4 (n); edge_rep is the node a
+// class's stencil is evaluated at (where edge_class(edge_rep(c)) == c).
+EQF_HD int edge_class(int j, int n) { return j < 2 ? j : (j > n - 2 ? 4 - (n - j) : 2); }
+EQF_HD int edge_rep(int c, int n) { return c < 2 ? c : (c == 2 ? 2 : (c == 3 ? n - 1 : n)); }
 
 EQF_HD bool is_dirichlet(const LevelGeom& g, int i, int j) {
   return ((g.walls & WALL_BOTTOM) && i == 0) || ((g.walls & WALL_TOP) && i == g.ny) ||

@@ -307,6 +307,14 @@ __device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&
     for (int e = 0; e < 8; ++e) c[e] = q[e];
     return;
   }
+  const T* row = sizeof(T) == sizeof(float) ? (const T*)(const void*)g.rowc_f
+                                            : (const T*)(const void*)g.rowc_d;
+  if (row) {  // an advective level: the row's stencils built once
+    const T* q = row + 8 * ((long long)i * 5 + edge_class(j, g.nx));
+#pragma unroll
+    for (int e = 0; e < 8; ++e) c[e] = q[e];
+    return;
+  }
   const Sten<T> s = stencil_general<T, false>(g, i, j);  // advective rows
   c[0] = s.c;
   c[1] = s.e;
@@ -318,13 +326,18 @@ __device__ __noinline__ void coef_general(const LevelGeom& g, int i, int j, T (&
   c[7] = T(1) / s.c;
 }
 // The stencil of a general-path node: an anisotropic level reads the stencil built
-// once (k_aniso_coefs) inline; other general rows (advection) compute it out of line.
+// once (k_aniso_coefs) inline, an advective level its row's (built once on the host);
+// other general rows compute it out of line.
 template <class T>
 __device__ __forceinline__ void coef_node(const LevelGeom& g, int i, int j, T (&c)[8]) {
   const T* pre = sizeof(T) == sizeof(float) ? (const T*)(const void*)g.coef_f
                                             : (const T*)(const void*)g.coef_d;
-  if (pre && j >= 0 && j <= g.nx && i >= 0 && i <= g.ny) {
-    const T* q = pre + 8 * ((long long)i * g.P + j);
+  const T* row = sizeof(T) == sizeof(float) ? (const T*)(const void*)g.rowc_f
+                                            : (const T*)(const void*)g.rowc_d;
+  if ((pre || row) && j >= 0 && j <= g.nx && i >= 0 && i <= g.ny) {
+    // anisotropic: per node; advective: per row and column class (L1-resident)
+    const T* q = pre ? pre + 8 * ((long long)i * g.P + j)
+                     : row + 8 * ((long long)i * 5 + edge_class(j, g.nx));
     if constexpr (sizeof(T) == sizeof(float)) {  // two aligned 16-byte vectors per node
       const float4 lo = __ldg(reinterpret_cast<const float4*>(q));
       const float4 hi = __ldg(reinterpret_cast<const float4*>(q) + 1);

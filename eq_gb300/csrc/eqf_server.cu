@@ -37,6 +37,8 @@ struct Req {
   int status = EQF_OK;
   int cohort = -1;
   int trap0 = -1;
+  int step0 = 0;  // cohort steps queued before the request's first step
+  int end_step() const { return step0 + r.steps; }
   double* h_cells = nullptr;  // pinned: n_species * n_cells
   double* h_nodal = nullptr;  // pinned: n_species * n_nodes (when asked for)
   bool done = false;
@@ -109,15 +111,24 @@ size_t nodal_bytes(const Req* q) {
 
 struct Cohort {
   int id = 0;
+  int64_t klass = 0;
   eqf_batch* b = nullptr;
   cudaStream_t stream = nullptr;
-  std::vector<Req*> reqs;
+  std::vector<Req*> reqs;  // the requests still running
+  // per trap slot: the grid it was created with (its capacity) and the request
+  // holding it (null: free since that request's last step was queued)
+  std::vector<eqf_trap_params> slot_cap;
+  std::vector<Req*> slot_owner;
+  bool filling = false;  // queue no steps until the queued ones are done, then fill slots
+  bool slots_freed = false;    // a slot was freed since the last match
+  bool was_ready = false;      // enough free slots at the last look
+  int64_t seen_submitted = -1;  // the server's submissions at the last match
   int steps_target = 0, launched = 0;
   std::deque<StepMark> inflight;
   int64_t bytes = 0;
   int remaining = 0;
   int32_t fails_seen = 0;
-  bool retired = false;  // every request done; memory kept until it is needed
+  bool retired = false;  // every request done (its memory is released right after)
 };
 
 }  // namespace
@@ -240,13 +251,15 @@ void launch_step(eqs_server* s, Cohort& c) {
   ckb(eqf_step(c.b, 1), c.b);
   const double tr = s->now();
   for (Req* q : c.reqs) {
-    if (q->r.steps != m.step) continue;
+    if (q->end_step() != m.step) continue;
     for (int k = 0; k < q->r.n_species; ++k) {
       if (q->r.n_cells > 0)
         ckb(eqf_read_cells_async(c.b, q->trap0 + k, q->r.n_cells, q->h_cells + k * q->r.n_cells),
             c.b);
       if (q->h_nodal) ckb(eqf_read_nodal_async(c.b, q->trap0 + k, q->h_nodal + k * q->n_nodes), c.b);
       ckb(eqf_set_active(c.b, q->trap0 + k, 0), c.b);
+      c.slot_owner[q->trap0 + k] = nullptr;  // reusable after these stream-ordered copies
+      c.slots_freed = true;
     }
   }
   ckb(eqf_fail_count_async(c.b, m.fail), c.b);
@@ -273,14 +286,16 @@ void retire(eqs_server* s, Cohort& c) {
     if (status != EQF_OK) {
       // the counter is per batch: every request still running at this step is suspect
       for (Req* q : c.reqs)
-        if (!q->done && q->r.steps >= m.step) q->status = status;
+        if (!q->done && q->step0 < m.step && q->end_step() >= m.step) q->status = status;
       c.fails_seen = fails;
     }
     for (Req* q : c.reqs)
-      if (q->r.steps == m.step && !q->done) {
+      if (q->end_step() == m.step && !q->done) {
         finish(s, q, q->status);
         c.remaining -= 1;
       }
+    c.reqs.erase(std::remove_if(c.reqs.begin(), c.reqs.end(), [](const Req* q) { return q->done; }),
+                 c.reqs.end());
     cudaEventDestroy(m.start);
     cudaEventDestroy(m.end);
     s->pinned.put(m.fail, sizeof(int32_t));
@@ -288,8 +303,7 @@ void retire(eqs_server* s, Cohort& c) {
   }
 }
 
-// Frees the memory of retired cohorts (cudaFree waits for the whole device, so this
-// happens only when an admission needs the memory, or at shutdown).
+// Frees the memory of retired cohorts.
 bool release_retired(eqs_server* s) {
   const double t0 = s->now();
   bool any = false;
@@ -305,6 +319,115 @@ bool release_retired(eqs_server* s) {
                    s->cohorts.end());
   s->st.release_s += s->now() - t0;
   return any;
+}
+
+// Puts request q into slots t .. t + n_species - 1 of cohort c (already holding its
+// traps' grids): cells, coupling, readout buffers; its first step is the cohort's next.
+void place(eqs_server* s, Cohort& c, Req* q, int t, double now) {
+  for (int k = 0; k < q->r.n_species; ++k) c.slot_owner[t + k] = q;
+  q->trap0 = t;
+  q->step0 = c.launched;
+  q->cohort = c.id;
+  q->t_admit = now;
+  if (q->r.n_cells > 0) {
+    ckb(eqf_set_cells(c.b, t, q->r.n_cells, q->xy.data(), q->s.data()), c.b);
+    if (q->r.n_species == 2)  // species 2 takes the same cells
+      ckb(eqf_couple_species(c.b, t, t + 1, q->sender.data(), q->r.vmax, q->r.K, q->r.uptake),
+          c.b);
+  }
+  q->h_cells = static_cast<double*>(s->pinned.get(cells_bytes(q)));
+  if (q->r.want_nodal) q->h_nodal = static_cast<double*>(s->pinned.get(nodal_bytes(q)));
+  if (!q->h_cells || (q->r.want_nodal && !q->h_nodal))
+    throw Fail{EQF_ERR_NOMEM, "page-locked host memory exhausted"};
+  c.steps_target = std::max(c.steps_target, q->end_step());
+}
+
+// Slots t .. are free and the request's grids fit them at every level
+bool fits(const Cohort& c, const Req* q, int t) {
+  if (t + q->r.n_species > (int)c.slot_cap.size()) return false;
+  for (int k = 0; k < q->r.n_species; ++k) {
+    if (c.slot_owner[t + k]) return false;
+    int32_t ok = 0;
+    if (eqf_slot_fits(c.b, t + k, &q->r.species[k], &ok) != EQF_OK || !ok) return false;
+  }
+  return true;
+}
+
+// Matches waiting requests of the cohort's class to its free slots, oldest first, each
+// into the free run of slots with the smallest capacity that fits (so large slots stay
+// for large requests).  Returns the matches as (request, first slot); with apply, also
+// marks the slots taken.
+std::vector<std::pair<Req*, int>> match_slots(eqs_server* s, Cohort& c, bool apply,
+                                              bool first_only = false) {
+  std::vector<std::pair<Req*, int>> out;
+  std::vector<int> free_at;  // first slots of the free runs
+  for (int t = 0; t < (int)c.slot_owner.size(); ++t)
+    if (!c.slot_owner[t]) free_at.push_back(t);
+  int free_slots = (int)free_at.size();
+  if (free_slots == 0) return out;
+  constexpr size_t kWindow = 1024;
+  size_t seen = 0;
+  for (Req* q : s->pending) {
+    if (++seen > kWindow || free_slots == 0 || (first_only && !out.empty())) break;
+    if (q->klass != c.klass || q->picked) continue;
+    int best = -1;
+    int64_t best_cap = 0;
+    for (int t : free_at) {
+      if (!fits(c, q, t)) continue;
+      int64_t cap = 0;
+      for (int k = 0; k < q->r.n_species; ++k)
+        cap += (int64_t)(c.slot_cap[t + k].nx + 1) * (c.slot_cap[t + k].ny + 1);
+      if (best < 0 || cap < best_cap) {
+        best = t;
+        best_cap = cap;
+      }
+    }
+    if (best < 0) continue;
+    for (int k = 0; k < q->r.n_species; ++k) c.slot_owner[best + k] = q;
+    free_slots -= q->r.n_species;
+    out.push_back({q, best});
+  }
+  if (!apply)
+    for (auto& m : out)
+      for (int k = 0; k < m.first->r.n_species; ++k) c.slot_owner[m.second + k] = nullptr;
+  return out;
+}
+
+// Admits waiting requests into the cohort's free slots: one eqf_replace_traps call for
+// all of them, then their cells.  Runs when the cohort has no step queued (the cell
+// index rebuild at its next step then waits for nothing of its own).
+bool fill_slots(eqs_server* s, Cohort& c) {
+  const double t0 = s->now();
+  std::vector<std::pair<Req*, int>> m = match_slots(s, c, true);
+  if (m.empty()) return false;
+  std::vector<int32_t> tr;
+  std::vector<eqf_trap_params> tp;
+  for (auto& e : m)
+    for (int k = 0; k < e.first->r.n_species; ++k) {
+      tr.push_back(e.second + k);
+      tp.push_back(e.first->r.species[k]);
+    }
+  const int rc = eqf_replace_traps(c.b, (int32_t)tr.size(), tr.data(), tp.data());
+  if (rc != EQF_OK) {  // nothing changed: the requests stay in the queue
+    for (auto& e : m)
+      for (int k = 0; k < e.first->r.n_species; ++k) c.slot_owner[e.second + k] = nullptr;
+    s->err = eqf_last_error(c.b);
+    return false;
+  }
+  const double now = s->now();
+  for (auto& e : m) {
+    e.first->picked = true;
+    place(s, c, e.first, e.second, now);
+    c.reqs.push_back(e.first);
+    c.remaining += 1;
+  }
+  s->pending.erase(std::remove_if(s->pending.begin(), s->pending.end(),
+                                  [](const Req* q) { return q->picked; }),
+                   s->pending.end());
+  s->st.admitted += (int64_t)m.size();
+  s->st.slot_admitted += (int64_t)m.size();
+  s->st.fill_s += s->now() - t0;
+  return true;
 }
 
 // Forms one cohort from the queue within the budget: the oldest request first, then
@@ -351,6 +474,7 @@ bool admit(eqs_server* s) {
                    s->pending.end());
   std::unique_ptr<Cohort> c(new Cohort);
   c->id = s->next_cohort++;
+  c->klass = klass;
   c->reqs = take;
   c->bytes = bytes;
   c->remaining = (int)take.size();
@@ -382,24 +506,12 @@ bool admit(eqs_server* s) {
   void* stream = nullptr;
   ckb(eqf_stream(c->b, &stream), c->b);
   c->stream = (cudaStream_t)stream;
+  c->slot_cap = tp;
+  c->slot_owner.assign(tp.size(), nullptr);
   int t = 0;
   const double now = s->now();
   for (Req* q : take) {
-    q->trap0 = t;
-    q->cohort = c->id;
-    q->t_admit = now;
-    if (q->r.n_cells > 0) {
-      ckb(eqf_set_cells(c->b, t, q->r.n_cells, q->xy.data(), q->s.data()), c->b);
-      if (q->r.n_species == 2)
-        ckb(eqf_couple_species(c->b, t, t + 1, q->sender.data(), q->r.vmax, q->r.K,
-                               q->r.uptake),
-            c->b);
-    }
-    q->h_cells = static_cast<double*>(s->pinned.get(cells_bytes(q)));
-    if (q->r.want_nodal) q->h_nodal = static_cast<double*>(s->pinned.get(nodal_bytes(q)));
-    if (!q->h_cells || (q->r.want_nodal && !q->h_nodal))
-      throw Fail{EQF_ERR_NOMEM, "page-locked host memory exhausted"};
-    c->steps_target = std::max(c->steps_target, q->r.steps);
+    place(s, *c, q, t, now);
     t += q->ntraps();
   }
   s->st.admitted += (int64_t)take.size();
@@ -414,17 +526,50 @@ void progress(eqs_server* s) {
   for (auto& c : s->cohorts) running = running || (c->b && !c->retired);
   if (running) s->st.busy_s += now - s->last_progress;
   s->last_progress = now;
-  // retire finished steps; a cohort whose requests are all done is retired (its
-  // device memory is released later, when an admission needs it)
+  // retire finished steps; a cohort whose requests are all done is retired and its
+  // device memory goes back to the memory pool at once (stream-ordered frees: no wait
+  // for the other cohorts' work)
   for (auto& c : s->cohorts) retire(s, *c);
+  // slot reuse: a cohort with free slots (a quarter of them, or all its requests done)
+  // that waiting requests of its class fit queues no further step; once its queued
+  // steps are done the requests go into the slots (one rebuild) and it resumes
+  if (s->cfg.reuse_slots)
+    for (auto& c : s->cohorts) {
+      if (!c->b || c->retired) continue;
+      if (!c->filling) {
+        int free_slots = 0;
+        for (Req* o : c->slot_owner) free_slots += o ? 0 : 1;
+        const int n = (int)c->slot_owner.size();
+        const bool ready = free_slots > 0 && (4 * free_slots >= n || c->remaining == 0);
+        // match again only when that could change the answer
+        if (ready && (!c->was_ready || c->seen_submitted != s->st.submitted || c->slots_freed)) {
+          c->seen_submitted = s->st.submitted;
+          c->slots_freed = false;
+          c->filling = !match_slots(s, *c, false, true).empty();
+        }
+        c->was_ready = ready;
+      }
+      if (c->filling && c->inflight.empty()) {
+        try {
+          fill_slots(s, *c);
+        } catch (const Fail& f) {
+          s->err = f.msg;
+          fail_cohort(s, *c, f.code);
+        }
+        c->filling = false;
+      }
+    }
+  bool retired_any = false;
   for (auto& c : s->cohorts)
-    if (c->b && !c->retired && c->remaining == 0 && c->inflight.empty()) {
+    if (c->b && !c->retired && !c->filling && c->remaining == 0 && c->inflight.empty()) {
       int idle = 0;
       const int rc = eqf_poll(c->b, &idle);  // the steps are done: reports deferred errors
       if (rc == EQF_ERR_NOT_CONVERGED)
         for (Req* q : c->reqs) q->status = rc;
       c->retired = true;
+      retired_any = true;
     }
+  if (retired_any) release_retired(s);
   int live = 0;
   for (auto& c : s->cohorts) live += c->b && !c->retired ? 1 : 0;
   // admit: an idle GPU, enough waiting requests, or a request waiting too long
@@ -441,7 +586,7 @@ void progress(eqs_server* s) {
   s->st.admit_s += tl - ta;
   // keep every cohort's queue filled
   for (auto& c : s->cohorts) {
-    if (c->retired) continue;
+    if (c->retired || c->filling) continue;
     try {
       while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight) {
         const double t1 = c->launched == 0 ? s->now() : -1.0;
@@ -484,6 +629,7 @@ int eqs_default_config(eqs_config* c) {
   c->min_batch = 16;
   c->max_wait_ms = 20.0;
   c->steps_in_flight = 4;
+  c->reuse_slots = 1;
   return EQF_OK;
 }
 

@@ -379,6 +379,26 @@ class TrapBatch:
         """Freezes (False) or resumes (True) a trap (eqf_set_active)."""
         self._ck(self._lib.eqf_set_active(self._h, int(trap), 1 if active else 0))
 
+    def replace_trap(self, trap: int, params: TrapParams):
+        """Reuses trap slot `trap` for a new trap whose grid fits it (eqf_replace_trap);
+        the new trap starts empty: set its cells afterwards."""
+        self.replace_traps([trap], [params])
+
+    def slot_fits(self, trap: int, params: TrapParams) -> bool:
+        """Whether replace_trap(trap, params) would accept the grid (eqf_slot_fits)."""
+        ok = C.c_int32()
+        self._ck(self._lib.eqf_slot_fits(self._h, int(trap), C.byref(params), C.byref(ok)))
+        return bool(ok.value)
+
+    def replace_traps(self, traps: Sequence[int], params: Sequence[TrapParams]):
+        """Several slots at once (eqf_replace_traps: one rebuild)."""
+        tr = (C.c_int32 * len(traps))(*[int(t) for t in traps])
+        pp = (TrapParams * len(params))(*params)
+        self._ck(self._lib.eqf_replace_traps(self._h, len(traps), tr, pp))
+        for t, p in zip(traps, params):
+            self._ncells[t] = 0
+            self.params[t] = p
+
     def mass_balance(self, enable: bool = True):
         """Per-step FP64 mass balance of every trap (eqf_mass_balance); enabling zeroes
         the sums."""

@@ -19,7 +19,8 @@ EXPORTS = ("eqs_default_config", "eqs_create", "eqs_destroy", "eqs_last_error", 
 class ServerConfig(C.Structure):
     _fields_ = [("opts", SolverOpts), ("hbm_budget", C.c_int64), ("max_cohorts", C.c_int32),
                 ("max_cohort_traps", C.c_int32), ("min_batch", C.c_int32),
-                ("max_wait_ms", C.c_double), ("steps_in_flight", C.c_int32)]
+                ("max_wait_ms", C.c_double), ("steps_in_flight", C.c_int32),
+                ("reuse_slots", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -43,7 +44,8 @@ class Stats(C.Structure):
                 ("step_ms_p999", C.c_double), ("step_samples", C.c_int64),
                 ("bytes_in_use", C.c_int64), ("bytes_peak", C.c_int64),
                 ("admit_s", C.c_double), ("launch_s", C.c_double), ("release_s", C.c_double),
-                ("first_step_s", C.c_double), ("readout_s", C.c_double)]
+                ("first_step_s", C.c_double), ("readout_s", C.c_double),
+                ("slot_admitted", C.c_int64), ("fill_s", C.c_double)]
 
 
 def _bind(lib):
@@ -161,6 +163,10 @@ class Server:
         nodes = (species[0].nx + 1) * (species[0].ny + 1)
         self._meta[rid.value] = (ns, len(s), nodes, want_nodal)
         return rid.value
+
+    def last_error(self) -> str:
+        msg = self._lib.eqs_last_error(self._h)
+        return msg.decode() if msg else ""
 
     def progress(self):
         self._ck(self._lib.eqs_progress(self._h))

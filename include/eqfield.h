@@ -277,6 +277,23 @@ int eqf_sync(eqf_batch* b);
  * and its field stays as it is; eqf_set_active(b, t, 1) resumes it (with a fresh
  * initial-guess history).  Frozen traps keep their device memory. */
 int eqf_poll(eqf_batch* b, int32_t* idle);
+/* Slot reuse (no reference counterpart; the serving loop admits requests into the
+ * slots of finished ones with it): trap t becomes the trap *p, whose grid must fit
+ * t's slot at every multigrid level (eqf_slot_fits tells; a smaller nx and ny is not
+ * enough, as a level halves an axis only while it has at least 4 cells), with no more
+ * levels than the batch and, if advective, in a batch that solves with BiCGSTAB.  The new trap starts from a zero field with no cells, couplings, tensor
+ * or well and with the Dirichlet walls of p->walls; it is active.  The other traps
+ * keep their state and give the same bits as without the replacement.  Operators,
+ * tile lists and the cell index are rebuilt, and the step recaptured, at the next
+ * step (stream-ordered: the call does not wait; the new geometry is in place when it
+ * returns).  A trap that carries rod cells or a
+ * flow channel cannot be replaced (EQF_ERR_INVALID). */
+int eqf_replace_trap(eqf_batch* b, int32_t trap, const eqf_trap_params* p);
+/* The same for n slots at once (one rebuild): traps[k] becomes p[k]; every entry is
+ * checked before any slot changes. */
+int eqf_replace_traps(eqf_batch* b, int32_t n, const int32_t* traps, const eqf_trap_params* p);
+/* *fits = 1 if eqf_replace_trap(b, trap, p) would accept p, else 0 (host-side check). */
+int eqf_slot_fits(const eqf_batch* b, int32_t trap, const eqf_trap_params* p, int32_t* fits);
 int eqf_read_cells_async(eqf_batch* b, int32_t trap, int64_t n, double* c);
 int eqf_read_nodal_async(eqf_batch* b, int32_t trap, double* c);
 int eqf_set_active(eqf_batch* b, int32_t trap, int32_t active);

@@ -39,6 +39,9 @@ typedef struct eqs_config {
   int32_t min_batch;        /* form a cohort once this many requests wait ... */
   double max_wait_ms;       /* ... or the oldest has waited this long, or the GPU idles */
   int32_t steps_in_flight;  /* steps queued ahead per cohort */
+  int32_t reuse_slots;      /* 1 (default): admit waiting requests into the slots of
+                               finished ones in a resident cohort (eqf_replace_traps)
+                               when their grids fit; 0: only into new cohorts */
 } eqs_config;
 
 typedef struct eqs_request {
@@ -77,6 +80,9 @@ typedef struct eqs_stats {
                                        (its one-time set-up: cell index, graph capture) */
   double readout_s;                 /* of launch_s: queueing finished requests' readouts
                                        and freezes */
+  int64_t slot_admitted;            /* of admitted: into the free slots of a resident
+                                       cohort */
+  double fill_s;                    /* host seconds spent admitting into free slots */
 } eqs_stats;
 
 int eqs_default_config(eqs_config* cfg);

@@ -130,12 +130,14 @@ def test_serving_struct_layout_matches_header():
 #include <stdio.h>
 #include "eqserve.h"
 int main(void) {
-  printf("%zu %zu %zu %zu\n", sizeof(eqs_config), offsetof(eqs_config, hbm_budget),
-         offsetof(eqs_config, max_wait_ms), offsetof(eqs_config, steps_in_flight));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(eqs_config), offsetof(eqs_config, hbm_budget),
+         offsetof(eqs_config, max_wait_ms), offsetof(eqs_config, steps_in_flight),
+         offsetof(eqs_config, reuse_slots));
   printf("%zu %zu %zu %zu\n", sizeof(eqs_request), offsetof(eqs_request, n_cells),
          offsetof(eqs_request, vmax), offsetof(eqs_request, want_nodal));
   printf("%zu %zu\n", sizeof(eqs_result_info), offsetof(eqs_result_info, cohort));
-  printf("%zu %zu\n", sizeof(eqs_stats), offsetof(eqs_stats, bytes_peak));
+  printf("%zu %zu %zu\n", sizeof(eqs_stats), offsetof(eqs_stats, bytes_peak),
+         offsetof(eqs_stats, slot_admitted));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -148,11 +150,12 @@ int main(void) {
     got = [[int(v) for v in ln.split()] for ln in lines[:4]]
     S = serve
     assert got[0] == [C.sizeof(S.ServerConfig), S.ServerConfig.hbm_budget.offset,
-                      S.ServerConfig.max_wait_ms.offset, S.ServerConfig.steps_in_flight.offset]
+                      S.ServerConfig.max_wait_ms.offset, S.ServerConfig.steps_in_flight.offset,
+                      S.ServerConfig.reuse_slots.offset]
     assert got[1] == [C.sizeof(S.Request), S.Request.n_cells.offset, S.Request.vmax.offset,
                       S.Request.want_nodal.offset]
     assert got[2] == [C.sizeof(S.ResultInfo), S.ResultInfo.cohort.offset]
-    assert got[3] == [C.sizeof(S.Stats), S.Stats.bytes_peak.offset]
+    assert got[3] == [C.sizeof(S.Stats), S.Stats.bytes_peak.offset, S.Stats.slot_admitted.offset]
 
 
 def test_serving_without_a_device_reports_no_device(lib):

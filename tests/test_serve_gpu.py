@@ -137,3 +137,34 @@ def test_arrivals_join_while_others_run(lib):
     assert rb.cohort != ra.cohort
     # b was admitted and finished while a was still running
     assert rb.t_admit < ra.t_done and rb.t_done < ra.t_done
+
+
+def test_requests_reuse_the_slots_of_finished_ones(lib):
+    """One resident cohort of four slots: the later, smaller requests run in the slots
+    of the finished ones (eqf_replace_traps), with the bits they give alone."""
+    rng = np.random.default_rng(11)
+    big = []  # slot capacities: 128 x 64, the largest grid small_traps makes
+    for _ in range(4):
+        m = 160
+        xy = np.stack([rng.uniform(0.1, 31.9, m), rng.uniform(0.1, 15.9, m)], axis=1)
+        big.append(wl.Trap(W=32.0, H=16.0, nx=128, ny=64, D=[490.0], g=[0.01], dt=0.1,
+                           steps=10, cell_xy=xy, cell_s=rng.lognormal(0.0, 0.5, m)))
+    later = small_traps(6, seed=12)
+    steps_big = [2, 3, 4, 9]
+    steps_later = [3, 5, 2, 4, 6, 3]
+    alone_big = [run_alone(t, k) for t, k in zip(big, steps_big)]
+    alone_later = [run_alone(t, k) for t, k in zip(later, steps_later)]
+    cfg = S.default_config(min_batch=4, max_wait_ms=1e6, max_cohorts=1, max_cohort_traps=4)
+    with S.Server(cfg) as srv:
+        ids = [submit(srv, t, k) for t, k in zip(big, steps_big)]
+        srv.progress()  # the cohort forms with the four large requests
+        ids += [submit(srv, t, k) for t, k in zip(later, steps_later)]
+        srv.drain()
+        st = srv.stats()
+        err = srv.last_error()
+        res = [srv.result(i) for i in ids]
+    assert st["completed"] == 10 and st["failed"] == 0
+    assert st["cohorts"] == 1 and st["slot_admitted"] == 6, (st, err, [r.cohort for r in res])
+    for r, a in zip(res, alone_big + alone_later):
+        assert r.status == 0
+        assert np.array_equal(r.cells, a)
