@@ -120,6 +120,7 @@ struct Cohort {
   std::vector<eqf_trap_params> slot_cap;
   std::vector<Req*> slot_owner;
   bool filling = false;  // queue no steps until the queued ones are done, then fill slots
+  bool closing = false;  // no more requests: runs out to make room for another cohort
   bool slots_freed = false;    // a slot was freed since the last match
   bool was_ready = false;      // enough free slots at the last look
   int64_t seen_submitted = -1;  // the server's submissions at the last match
@@ -532,10 +533,39 @@ void progress(eqs_server* s) {
   for (auto& c : s->cohorts) retire(s, *c);
   // slot reuse: a cohort with free slots (a quarter of them, or all its requests done)
   // that waiting requests of its class fit queues no further step; once its queued
-  // steps are done the requests go into the slots (one rebuild) and it resumes
-  if (s->cfg.reuse_slots)
+  // steps are done the requests go into the slots (one rebuild) and it resumes.
+  // Cohorts of fewer than half the traps a cohort may hold (formed while few requests
+  // waited) are not refilled: they run out and make room for full-size ones.  So is
+  // one cohort while the oldest waiting request has waited a second and fits no
+  // resident cohort (another class, or a grid larger than the free slots): it runs out
+  // and the request heads the next cohort.
+  if (s->cfg.reuse_slots) {
+    int live_now = 0;
+    for (auto& c : s->cohorts) live_now += c->b && !c->retired ? 1 : 0;
+    const bool starving = !s->pending.empty() && live_now >= s->cfg.max_cohorts &&
+                          now - s->pending.front()->t_submit > 1.0;
+    if (starving) {
+      Req* head = s->pending.front();
+      bool any_closing = false, fits_some = false;
+      Cohort* victim = nullptr;
+      for (auto& c : s->cohorts) {
+        if (!c->b || c->retired) continue;
+        any_closing = any_closing || c->closing;
+        if (c->closing || c->klass != head->klass) continue;
+        for (int t = 0; t + head->r.n_species <= (int)c->slot_cap.size() && !fits_some; ++t)
+          fits_some = fits(*c, head, t);
+      }
+      if (!any_closing && !fits_some)
+        for (auto& c : s->cohorts)
+          if (c->b && !c->retired && !c->filling &&
+              (!victim || c->remaining < victim->remaining))
+            victim = c.get();
+      if (victim) victim->closing = true;
+    }
     for (auto& c : s->cohorts) {
-      if (!c->b || c->retired) continue;
+      if (!c->b || c->retired || c->closing ||
+          2 * (int)c->slot_owner.size() < s->cfg.max_cohort_traps)
+        continue;
       if (!c->filling) {
         int free_slots = 0;
         for (Req* o : c->slot_owner) free_slots += o ? 0 : 1;
@@ -559,6 +589,7 @@ void progress(eqs_server* s) {
         c->filling = false;
       }
     }
+  }
   bool retired_any = false;
   for (auto& c : s->cohorts)
     if (c->b && !c->retired && !c->filling && c->remaining == 0 && c->inflight.empty()) {

@@ -149,7 +149,13 @@ def test_requests_reuse_the_slots_of_finished_ones(lib):
         xy = np.stack([rng.uniform(0.1, 31.9, m), rng.uniform(0.1, 15.9, m)], axis=1)
         big.append(wl.Trap(W=32.0, H=16.0, nx=128, ny=64, D=[490.0], g=[0.01], dt=0.1,
                            steps=10, cell_xy=xy, cell_s=rng.lognormal(0.0, 0.5, m)))
-    later = small_traps(6, seed=12)
+    later = []  # grids that fit a 128 x 64 slot at every level (eqf_slot_fits)
+    for nx, ny in ((85, 22), (87, 52), (41, 16), (96, 10), (120, 60), (64, 32)):
+        m = max(4, nx * ny // 50)
+        W, H = 0.25 * nx, 0.25 * ny
+        xy = np.stack([rng.uniform(0.1, W - 0.1, m), rng.uniform(0.1, H - 0.1, m)], axis=1)
+        later.append(wl.Trap(W=W, H=H, nx=nx, ny=ny, D=[490.0], g=[0.01], dt=0.1, steps=10,
+                             cell_xy=xy, cell_s=rng.lognormal(0.0, 0.5, m)))
     steps_big = [2, 3, 4, 9]
     steps_later = [3, 5, 2, 4, 6, 3]
     alone_big = [run_alone(t, k) for t, k in zip(big, steps_big)]
