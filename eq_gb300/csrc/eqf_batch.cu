@@ -14,6 +14,8 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <atomic>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -410,13 +412,30 @@ struct Prof {
   DevBuf<unsigned long long> work;  // one counter per record
 };
 
+// A byte range of device memory to zero (4-byte aligned, a multiple of 4 bytes).
+struct ZeroRange {
+  char* p;
+  long long bytes;
+};
+
+// Zeroes every listed range, one CTA row (blockIdx.y) per range: a reused slot's
+// vectors at every level in one launch instead of a memset each.
+__global__ void k_zero_ranges(const ZeroRange* __restrict__ r) {
+  const ZeroRange z = r[blockIdx.y];
+  const long long n4 = z.bytes >> 2;
+  unsigned* w = reinterpret_cast<unsigned*>(z.p);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+       i += (long long)gridDim.x * blockDim.x)
+    w[i] = 0u;
+}
+
 struct WorkBase {
   virtual ~WorkBase() = default;
   // one refinement sweep of `iters` preconditioned Krylov iterations
   virtual void enqueue_sweep(cudaStream_t s, bool first, int iters) = 0;
   virtual void enqueue_check(cudaStream_t s, bool update_gamma) = 0;
-  // zeroes every work vector over nodes [off, off + n) of level `lev` (a reused slot)
-  virtual void clear_slot(cudaStream_t s, int lev, long long off, long long n) = 0;
+  // the byte ranges of every work vector over nodes [off, off + n) of level `lev`
+  virtual void slot_ranges(int lev, long long off, long long n, std::vector<ZeroRange>& out) = 0;
 };
 
 class Batch;
@@ -433,12 +452,12 @@ struct Work : WorkBase {
   explicit Work(Batch& b);
   void enqueue_sweep(cudaStream_t s, bool first, int iters) override;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
-  void clear_slot(cudaStream_t s, int lev, long long off, long long n) override {
+  void slot_ranges(int lev, long long off, long long n, std::vector<ZeroRange>& out) override {
     for (DevBuf<T>* v : {&lv[lev].b, &lv[lev].x, &lv[lev].y, &lv[lev].d, &lv[lev].t})
-      EQF_CK(cudaMemsetAsync(v->p + off, 0, n * sizeof(T), s));
+      out.push_back({reinterpret_cast<char*>(v->p + off), n * (long long)sizeof(T)});
     if (lev == 0)
       for (DevBuf<T>* v : {&xs, &p0, &p1, &q, &rh})
-        if (v->p) EQF_CK(cudaMemsetAsync(v->p + off, 0, n * sizeof(T), s));
+        if (v->p) out.push_back({reinterpret_cast<char*>(v->p + off), n * (long long)sizeof(T)});
   }
   T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr);
   void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs, int max_iters);
@@ -459,6 +478,25 @@ static void retire_graph_exec(cudaGraphExec_t gx) {
     if (g_retired.size() >= kRetiredGraphs) doomed.swap(g_retired);
   }
   for (cudaGraphExec_t g : doomed) cudaGraphExecDestroy(g);
+}
+
+// f(0) .. f(n - 1) on up to 16 host threads (pure host work: no CUDA calls inside).
+template <class F>
+static void parallel_for(int n, F&& f) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min(std::min(hw, 16), (n + 3) / 4);
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next(0);
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int w = 0; w < nt; ++w)
+    th.emplace_back([&] {
+      for (int i; (i = next.fetch_add(1)) < n;) f(i);
+    });
+  for (auto& x : th) x.join();
 }
 
 class Batch {
@@ -612,8 +650,14 @@ class Batch {
     setup_walls();
     grow(dpart, 3 * std::max((size_t)L[0].ntiles(), L[0].tiles2.size()));
   }
+  void trap_levels_geom(int t, std::vector<LevelGeom>& out,
+                        std::vector<std::vector<double>>& rows) const;
   void check_replacement(int t, const eqf_trap_params& p) const;
-  void replace_trap(int t, const eqf_trap_params& p);
+  void replace_trap(int t, const eqf_trap_params& p);  // after zero_ranges(slot_ranges(t))
+  void slot_ranges(int t, std::vector<ZeroRange>& out);
+  void zero_ranges(const std::vector<ZeroRange>& r);
+  PinnedBuf<ZeroRange> zero_stage;
+  DevBuf<ZeroRange> d_zero;
   void enqueue_walls();
   void enqueue_channels();
   // anisotropic tensors (eqf_set_tensor): per trap the caller's D11, D22, D12 in grid
@@ -881,6 +925,85 @@ void Batch::level_tensor(LevelGeom& g, int level, int t) {
   g.tstride = st;
 }
 
+// Trap t's geometry at every level (sizes, spacings, constants, spectrum bounds and
+// Chebyshev tables), and for an advective trap the FP64 stencils of each level's rows
+// (rows[l]: (ny + 1) x 5 column classes x 8); no device work.  A trap with a tensor
+// gets its isotropic levels here; build_levels adds the tensor.
+void Batch::trap_levels_geom(int t, std::vector<LevelGeom>& out,
+                             std::vector<std::vector<double>>& rows) const {
+  out.assign(nlev, LevelGeom{});
+  rows.assign(nlev, {});
+  const auto& p = params[t];
+  LevelGeom g{};
+  g.nx = p.nx;
+  g.ny = p.ny;
+  g.trap = t;
+  g.walls = p.walls;
+  g.hx = g.hxl = p.width / p.nx;
+  g.hy = g.hyl = p.height / p.ny;
+  g.alpha = 1.0 + p.dt * p.decay;
+  g.beta = p.dt * p.D;
+  g.adv = (p.adv_u != 0.0 && p.adv_len > 0.0) ? p.dt * p.adv_u / p.adv_len : 0.0;
+  const eqf_boundaries& bc = bcs[t];
+  for (int w = 0; w < 4; ++w)
+    g.rob[w] = bc.wall[w].kind == EQF_BC_ROBIN ? p.dt * bc.wall[w].rate : 0.0;
+  for (int w = 0; w < 4; ++w)
+    g.dvals = g.dvals || bc.wall[w].kind == EQF_BC_CHANNEL || bc.wall[w].kind == EQF_BC_WELL ||
+              (bc.wall[w].kind == EQF_BC_DIRICHLET && bc.wall[w].value != 0.0);
+  const bool aniso = !tensor[t].empty();
+  for (int l = 0; l < nlev; ++l) {
+    if (l > 0) {
+      LevelGeom c = g;
+      c.dvals = 0;  // coarse levels carry corrections: homogeneous walls
+      c.fine_nx = g.nx;
+      c.fine_ny = g.ny;
+      c.cx = g.nx >= 4;
+      c.cy = g.ny >= 4;
+      if (c.cx) {
+        c.nx = (g.nx + 1) / 2;
+        c.hxl = (g.nx % 2 == 0) ? g.hx + g.hxl : g.hxl;
+        c.hx = 2 * g.hx;
+      }
+      if (c.cy) {
+        c.ny = (g.ny + 1) / 2;
+        c.hyl = (g.ny % 2 == 0) ? g.hy + g.hyl : g.hyl;
+        c.hy = 2 * g.hy;
+      }
+      g = c;
+    }
+    g.P = (g.nx + 1 + 3) & ~3;
+    g.inv_pitch = 1.0f / (float)g.P;
+    g.tens = g.htens = nullptr;
+    g.tensf = nullptr;
+    g.tstride = 0;
+    g.coef_f = nullptr;
+    g.coef_d = nullptr;
+    g.rowc_f = nullptr;
+    g.rowc_d = nullptr;
+    interior_constants(g);
+    if (aniso) {
+      out[l] = g;  // the tensor, its stencils and bounds come in build_levels
+      continue;
+    }
+    if (g.adv_on) {
+      // advection: the stencil depends on the row (v_y(y)) and the column class only
+      std::vector<double>& rd = rows[l];
+      rd.assign((size_t)(g.ny + 1) * 5 * 8, 0.0);
+      for (int i = 0; i <= g.ny; ++i)
+        for (int c = 0; c < 5; ++c) {
+          const int j = edge_rep(c, g.nx);
+          if (j < 0 || j > g.nx || edge_class(j, g.nx) != c) continue;  // absent class
+          const Sten<double> sd = stencil_general<double>(g, i, j);
+          const double v[8] = {sd.c, sd.e, sd.w, sd.n, sd.s, sd.ne, sd.sw, 1.0 / sd.c};
+          for (int q = 0; q < 8; ++q) rd[((size_t)i * 5 + c) * 8 + q] = v[q];
+        }
+    }
+    spectrum_bounds(g);
+    cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
+    out[l] = g;
+  }
+}
+
 void Batch::build_levels() {
   L.clear();
   int nl = 1;
@@ -895,60 +1018,48 @@ void Batch::build_levels() {
   tabd_cache.resize(ntraps);
   tabm_cache.resize(ntraps);
   auto cached = [&](int t) { return !trap_dirty[t] && (int)geom_cache[t].size() == nlev; };
+  // the levels of every changed trap without a tensor: pure host work, on all host
+  // threads (a slot replacement's traps, or a new batch's); their row tables' uploads
+  // and the tensor traps (device work per level) follow in order
+  std::vector<int> todo;
+  for (int t = 0; t < ntraps; ++t)
+    if (!cached(t) && tensor[t].empty()) todo.push_back(t);
+  std::vector<std::vector<LevelGeom>> made(todo.size());
+  std::vector<std::vector<std::vector<double>>> rows(todo.size());
+  parallel_for((int)todo.size(), [&](int k) {
+    trap_levels_geom(todo[k], made[k], rows[k]);
+  });
+  for (size_t k = 0; k < todo.size(); ++k) {
+    const int t = todo[k];
+    for (int l = 0; l < nlev; ++l) {
+      LevelGeom& g = made[k][l];
+      if (!rows[k][l].empty()) {  // advective: the rows' stencils, FP64 and rounded
+        const std::vector<double>& rd = rows[k][l];
+        const std::vector<float> rf(rd.begin(), rd.end());
+        DevBuf<float>& bf = drowc_f[{l, t}];
+        DevBuf<double>& bd = drowc_d[{l, t}];
+        bf.alloc(rf.size());
+        bf.upload(rf.data(), rf.size(), stream);
+        bd.alloc(rd.size());
+        bd.upload(rd.data(), rd.size(), stream);
+        g.rowc_f = bf.p;
+        g.rowc_d = bd.p;
+      }
+      L[l].geom[t] = g;
+    }
+  }
   for (int t = 0; t < ntraps; ++t) {
     if (cached(t)) {  // unchanged since the last build: its levels as built then
       for (int l = 0; l < nlev; ++l) L[l].geom[t] = geom_cache[t][l];
       continue;
     }
-    const auto& p = params[t];
-    LevelGeom g{};
-    g.nx = p.nx;
-    g.ny = p.ny;
-    g.trap = t;
-    g.walls = p.walls;
-    g.hx = g.hxl = p.width / p.nx;
-    g.hy = g.hyl = p.height / p.ny;
-    g.alpha = 1.0 + p.dt * p.decay;
-    g.beta = p.dt * p.D;
-    g.adv = (p.adv_u != 0.0 && p.adv_len > 0.0) ? p.dt * p.adv_u / p.adv_len : 0.0;
-    const eqf_boundaries& bc = bcs[t];
-    for (int w = 0; w < 4; ++w)
-      g.rob[w] = bc.wall[w].kind == EQF_BC_ROBIN ? p.dt * bc.wall[w].rate : 0.0;
-    for (int w = 0; w < 4; ++w)
-      g.dvals = g.dvals || bc.wall[w].kind == EQF_BC_CHANNEL || bc.wall[w].kind == EQF_BC_WELL ||
-                (bc.wall[w].kind == EQF_BC_DIRICHLET && bc.wall[w].value != 0.0);
-    for (int l = 0; l < nlev; ++l) {
-      if (l > 0) {
-        LevelGeom c = g;
-        c.dvals = 0;  // coarse levels carry corrections: homogeneous walls
-        c.fine_nx = g.nx;
-        c.fine_ny = g.ny;
-        c.cx = g.nx >= 4;
-        c.cy = g.ny >= 4;
-        if (c.cx) {
-          c.nx = (g.nx + 1) / 2;
-          c.hxl = (g.nx % 2 == 0) ? g.hx + g.hxl : g.hxl;
-          c.hx = 2 * g.hx;
-        }
-        if (c.cy) {
-          c.ny = (g.ny + 1) / 2;
-          c.hyl = (g.ny % 2 == 0) ? g.hy + g.hyl : g.hyl;
-          c.hy = 2 * g.hy;
-        }
-        g = c;
-      }
-      g.P = (g.nx + 1 + 3) & ~3;
-      g.inv_pitch = 1.0f / (float)g.P;
-      g.tens = g.htens = nullptr;
-      g.tensf = nullptr;
-      g.tstride = 0;
-      g.coef_f = nullptr;
-      g.coef_d = nullptr;
-      g.rowc_f = nullptr;
-      g.rowc_d = nullptr;
-      if (!tensor[t].empty()) level_tensor(g, l, t);
-      interior_constants(g);
-      if (g.tens) {
+    if (!tensor[t].empty()) {  // an anisotropic trap: per-node stencils built on the device
+      std::vector<LevelGeom> gl;
+      std::vector<std::vector<double>> unused;
+      trap_levels_geom(t, gl, unused);
+      for (int l = 0; l < nlev; ++l) {
+        LevelGeom& g = gl[l];
+        level_tensor(g, l, t);
         g.adv_on = 1;  // per-node stencils: every kernel takes the general path
         const long long n = (long long)g.P * (g.ny + 1);
         DevBuf<float>& cf = dcoef_f[{l, t}];
@@ -960,34 +1071,10 @@ void Batch::build_levels() {
         EQF_LAUNCH_CHECK();
         g.coef_f = cf.p;
         g.coef_d = cd.p;
-      } else if (g.adv_on) {
-        // advection: the stencil depends on the row (v_y(y)) and the column class only
-        const size_t n = (size_t)(g.ny + 1) * 5 * 8;
-        std::vector<double> rd(n, 0.0);
-        std::vector<float> rf(n, 0.0f);
-        for (int i = 0; i <= g.ny; ++i)
-          for (int c = 0; c < 5; ++c) {
-            const int j = edge_rep(c, g.nx);
-            if (j < 0 || j > g.nx || edge_class(j, g.nx) != c) continue;  // absent class
-            const Sten<double> sd = stencil_general<double>(g, i, j);
-            const double v[8] = {sd.c, sd.e, sd.w, sd.n, sd.s, sd.ne, sd.sw, 1.0 / sd.c};
-            for (int q = 0; q < 8; ++q) {
-              rd[((size_t)i * 5 + c) * 8 + q] = v[q];
-              rf[((size_t)i * 5 + c) * 8 + q] = (float)v[q];
-            }
-          }
-        DevBuf<float>& bf = drowc_f[{l, t}];
-        DevBuf<double>& bd = drowc_d[{l, t}];
-        bf.alloc(n);
-        bf.upload(rf.data(), n, stream);
-        bd.alloc(n);
-        bd.upload(rd.data(), n, stream);
-        g.rowc_f = bf.p;
-        g.rowc_d = bd.p;
+        spectrum_bounds(g);  // with the tensor: every row
+        cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
+        L[l].geom[t] = g;
       }
-      spectrum_bounds(g);
-      cheb_table(g, l == nlev - 1 ? (double)g.lam_min : (double)g.lam_max / opts.cheb_ratio);
-      L[l].geom[t] = g;
     }
     geom_cache[t].resize(nlev);
     for (int l = 0; l < nlev; ++l) geom_cache[t][l] = L[l].geom[t];
@@ -995,6 +1082,22 @@ void Batch::build_levels() {
     tabd_cache[t].clear();
     tabm_cache[t].clear();
   }
+  // the class tables of the changed traps, every level, on all host threads
+  std::vector<int> untabled;
+  for (int t = 0; t < ntraps; ++t)
+    if (tabf_cache[t].size() != (size_t)nlev * kTabPerTrap || tabm_cache[t].empty())
+      untabled.push_back(t);
+  parallel_for((int)untabled.size(), [&](int k) {  // each trap fills its own caches
+    const int t = untabled[k];
+    tabf_cache[t].assign((size_t)nlev * kTabPerTrap, 0.0f);
+    tabd_cache[t].assign((size_t)nlev * kTabPerTrap, 0.0);
+    tabm_cache[t].assign(kTabPerTrap, 0.0);
+    for (int l = 0; l < nlev; ++l) {
+      build_table<float, false>(L[l].geom[t], tabf_cache[t].data() + (size_t)l * kTabPerTrap);
+      build_table<double, false>(L[l].geom[t], tabd_cache[t].data() + (size_t)l * kTabPerTrap);
+    }
+    build_table<double, true>(L[0].geom[t], tabm_cache[t].data());
+  });
   // offsets, fine offsets and row tiles (about kTileNodes nodes each, whole rows)
   const int tsz = opts.precision == EQF_PREC_FP32_IR ? 4 : 8;
   const long long target =
@@ -1052,20 +1155,11 @@ void Batch::build_levels() {
     std::vector<float> tf((size_t)ntraps * kTabPerTrap);
     std::vector<double> td((size_t)ntraps * kTabPerTrap);
     for (int t = 0; t < ntraps; ++t) {
-      float* f = tf.data() + (size_t)t * kTabPerTrap;
-      double* d = td.data() + (size_t)t * kTabPerTrap;
-      std::vector<float>& cf = tabf_cache[t];
-      std::vector<double>& cd = tabd_cache[t];
       const size_t o = (size_t)l * kTabPerTrap;
-      if (cf.size() < o + kTabPerTrap) {  // built at this level for the first time
-        build_table<float, false>(L[l].geom[t], f);
-        build_table<double, false>(L[l].geom[t], d);
-        cf.insert(cf.end(), f, f + kTabPerTrap);
-        cd.insert(cd.end(), d, d + kTabPerTrap);
-      } else {
-        std::copy(cf.begin() + o, cf.begin() + o + kTabPerTrap, f);
-        std::copy(cd.begin() + o, cd.begin() + o + kTabPerTrap, d);
-      }
+      std::copy(tabf_cache[t].begin() + o, tabf_cache[t].begin() + o + kTabPerTrap,
+                tf.data() + (size_t)t * kTabPerTrap);
+      std::copy(tabd_cache[t].begin() + o, tabd_cache[t].begin() + o + kTabPerTrap,
+                td.data() + (size_t)t * kTabPerTrap);
     }
     L[l].tabf.alloc(tf.size());
     L[l].tabf.upload(tf.data(), tf.size(), stream);
@@ -1073,15 +1167,8 @@ void Batch::build_levels() {
     L[l].tabd.upload(td.data(), td.size(), stream);
     if (l == 0) {
       std::vector<double> tm((size_t)ntraps * kTabPerTrap);
-      for (int t = 0; t < ntraps; ++t) {
-        double* m = tm.data() + (size_t)t * kTabPerTrap;
-        if (tabm_cache[t].empty()) {
-          build_table<double, true>(L[0].geom[t], m);
-          tabm_cache[t].assign(m, m + kTabPerTrap);
-        } else {
-          std::copy(tabm_cache[t].begin(), tabm_cache[t].end(), m);
-        }
-      }
+      for (int t = 0; t < ntraps; ++t)
+        std::copy(tabm_cache[t].begin(), tabm_cache[t].end(), tm.data() + (size_t)t * kTabPerTrap);
       tabM0.alloc(tm.size());
       tabM0.upload(tm.data(), tm.size(), stream);
       // float pairs (h, l), h + l = the FP64 weight to ~2^-48; the interior class
@@ -2348,21 +2435,41 @@ void Batch::check_replacement(int t, const eqf_trap_params& p) const {
   }
 }
 
-void Batch::replace_trap(int t, const eqf_trap_params& p) {
-  // zero the slot at every level before anything reads it under the new layout (pad
-  // columns and rows must hold zeros)
-  for (int l = 0; l < nlev; ++l) work->clear_slot(stream, l, L[l].geom[t].off, slot_span[l][t]);
+// The slot's vectors at every level and its per-trap state, to zero before anything
+// reads the slot under a new layout (pad columns and rows must hold zeros).
+void Batch::slot_ranges(int t, std::vector<ZeroRange>& out) {
+  for (int l = 0; l < nlev; ++l) work->slot_ranges(l, L[l].geom[t].off, slot_span[l][t], out);
   const long long off = L[0].geom[t].off, n0 = slot_span[0][t];
+  auto add = [&](void* p, long long bytes) { out.push_back({static_cast<char*>(p), bytes}); };
   for (int q = 0; q < 2; ++q) {
-    EQF_CK(cudaMemsetAsync(U[q].p + off, 0, n0 * sizeof(double), stream));
-    EQF_CK(cudaMemsetAsync(Dd[q].p + off, 0, n0 * sizeof(float), stream));
+    add(U[q].p + off, n0 * (long long)sizeof(double));
+    add(Dd[q].p + off, n0 * (long long)sizeof(float));
   }
-  EQF_CK(cudaMemsetAsync(F.p + off, 0, n0 * sizeof(double), stream));
-  EQF_CK(cudaMemsetAsync(b64.p + off, 0, n0 * sizeof(double), stream));
-  EQF_CK(cudaMemsetAsync(dstate.p + t, 0, sizeof(CgState), stream));
-  EQF_CK(cudaMemsetAsync(d_frozen.p + t, 0, sizeof(int), stream));
-  EQF_CK(cudaMemsetAsync(d_well_c.p + t, 0, sizeof(double), stream));
-  EQF_CK(cudaMemsetAsync(d_well_under.p + t, 0, sizeof(long long), stream));
+  add(F.p + off, n0 * (long long)sizeof(double));
+  add(b64.p + off, n0 * (long long)sizeof(double));
+  add(dstate.p + t, (long long)sizeof(CgState));
+  add(d_frozen.p + t, (long long)sizeof(int));
+  add(d_well_c.p + t, (long long)sizeof(double));
+  add(d_well_under.p + t, (long long)sizeof(long long));
+}
+
+void Batch::zero_ranges(const std::vector<ZeroRange>& r) {
+  if (r.empty()) return;
+  // staged in page-locked memory: the copy does not wait for the stream; the caller
+  // syncs before the staging is reused (build_levels does)
+  zero_stage.grow(r.size());
+  std::copy(r.begin(), r.end(), zero_stage.p);
+  grow(d_zero, r.size());
+  EQF_CK(cudaMemcpyAsync(d_zero.p, zero_stage.p, r.size() * sizeof(ZeroRange),
+                         cudaMemcpyHostToDevice, stream));
+  for (size_t k = 0; k < r.size(); k += 65535) {  // grid y limit
+    const unsigned ny = (unsigned)std::min<size_t>(65535, r.size() - k);
+    k_zero_ranges<<<dim3(8, ny), 256, 0, stream>>>(d_zero.p + k);
+    EQF_LAUNCH_CHECK();
+  }
+}
+
+void Batch::replace_trap(int t, const eqf_trap_params& p) {
   params[t] = p;
   eqf_boundaries& bc = bcs[t];
   std::memset(&bc, 0, sizeof(bc));
@@ -2852,8 +2959,13 @@ int eqf_replace_traps(eqf_batch* b, int32_t n, const int32_t* traps,
       for (int32_t m = 0; m < k; ++m) EQF_REQUIRE(traps[m] != traps[k], "trap listed twice");
     }
     for (int32_t k = 0; k < n; ++k) B.check_replacement(traps[k], p[k]);  // all or none
+    if (n == 0) return;
+    std::vector<eqf::ZeroRange> z;
+    for (int32_t k = 0; k < n; ++k) B.slot_ranges(traps[k], z);
+    B.zero_ranges(z);  // one launch for every slot's vectors and state
     for (int32_t k = 0; k < n; ++k) B.replace_trap(traps[k], p[k]);
-    if (n > 0) B.ensure_ops();  // the new geometry, for readouts before the next step
+    B.ensure_ops();  // the new geometry, for readouts before the next step
+    B.sync();        // (the zeroing's page-locked staging may be reused next call)
   });
 }
 

@@ -281,13 +281,13 @@ int eqf_poll(eqf_batch* b, int32_t* idle);
  * slots of finished ones with it): trap t becomes the trap *p, whose grid must fit
  * t's slot at every multigrid level (eqf_slot_fits tells; a smaller nx and ny is not
  * enough, as a level halves an axis only while it has at least 4 cells), with no more
- * levels than the batch and, if advective, in a batch that solves with BiCGSTAB.  The new trap starts from a zero field with no cells, couplings, tensor
- * or well and with the Dirichlet walls of p->walls; it is active.  The other traps
- * keep their state and give the same bits as without the replacement.  Operators,
- * tile lists and the cell index are rebuilt, and the step recaptured, at the next
- * step (stream-ordered: the call does not wait; the new geometry is in place when it
- * returns).  A trap that carries rod cells or a
- * flow channel cannot be replaced (EQF_ERR_INVALID). */
+ * levels than the batch and, if advective, in a batch that solves with BiCGSTAB.
+ * The new trap starts from a zero field with no cells, couplings, tensor or well and
+ * with the Dirichlet walls of p->walls; it is active.  The other traps keep their
+ * state and give the same bits as without the replacement.  Operators, tile lists and
+ * the geometry are rebuilt before the call returns (it waits for the batch's own
+ * queued work), the cell index and the captured step at the next step.  A trap that
+ * carries rod cells or a flow channel cannot be replaced (EQF_ERR_INVALID). */
 int eqf_replace_trap(eqf_batch* b, int32_t trap, const eqf_trap_params* p);
 /* The same for n slots at once (one rebuild): traps[k] becomes p[k]; every entry is
  * checked before any slot changes. */
