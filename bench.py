@@ -871,8 +871,9 @@ def run_serving(args, rank, world, local_rank):
                    "of_which_release": round(st["release_s"], 2),
                    "of_which_first_steps": round(st["first_step_s"], 2),
                    "of_which_readouts": round(st["readout_s"], 2),
-                   "slot_fills": round(st["fill_s"], 2)},
-        "slot_admitted": int(st["slot_admitted"]),
+                   "slot_fills": round(st["fill_s"], 2),
+                   "of_which_launch_after_fills": round(st["refill_step_s"], 2)},
+        "slot_admitted": int(st["slot_admitted"]), "slot_fills": int(st["fills"]),
         "audit": {"sampled": len(audit), "completed": len(aud), "checked": checked,
                   "relL2_max": max(errs) if errs else None, "tolerance": 1e-6},
         "clocks": clk,

@@ -121,6 +121,7 @@ struct Cohort {
   std::vector<Req*> slot_owner;
   bool filling = false;  // queue no steps until the queued ones are done, then fill slots
   bool closing = false;  // no more requests: runs out to make room for another cohort
+  bool refilled = false;  // slots filled since the last queued step
   bool slots_freed = false;    // a slot was freed since the last match
   bool was_ready = false;      // enough free slots at the last look
   int64_t seen_submitted = -1;  // the server's submissions at the last match
@@ -427,7 +428,9 @@ bool fill_slots(eqs_server* s, Cohort& c) {
                    s->pending.end());
   s->st.admitted += (int64_t)m.size();
   s->st.slot_admitted += (int64_t)m.size();
+  s->st.fills += 1;
   s->st.fill_s += s->now() - t0;
+  c.refilled = true;
   return true;
 }
 
@@ -620,9 +623,12 @@ void progress(eqs_server* s) {
     if (c->retired || c->filling) continue;
     try {
       while (c->launched < c->steps_target && (int)c->inflight.size() < s->cfg.steps_in_flight) {
-        const double t1 = c->launched == 0 ? s->now() : -1.0;
+        const double t1 = s->now();
+        const bool first = c->launched == 0, refill = c->refilled;
+        c->refilled = false;
         launch_step(s, *c);
-        if (t1 >= 0) s->st.first_step_s += s->now() - t1;
+        if (first) s->st.first_step_s += s->now() - t1;
+        if (refill) s->st.refill_step_s += s->now() - t1;
       }
     } catch (const Fail& f) {
       s->err = f.msg;

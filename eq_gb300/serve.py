@@ -45,7 +45,8 @@ class Stats(C.Structure):
                 ("bytes_in_use", C.c_int64), ("bytes_peak", C.c_int64),
                 ("admit_s", C.c_double), ("launch_s", C.c_double), ("release_s", C.c_double),
                 ("first_step_s", C.c_double), ("readout_s", C.c_double),
-                ("slot_admitted", C.c_int64), ("fill_s", C.c_double)]
+                ("slot_admitted", C.c_int64), ("fill_s", C.c_double),
+                ("fills", C.c_int64), ("refill_step_s", C.c_double)]
 
 
 def _bind(lib):

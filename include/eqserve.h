@@ -83,6 +83,9 @@ typedef struct eqs_stats {
   int64_t slot_admitted;            /* of admitted: into the free slots of a resident
                                        cohort */
   double fill_s;                    /* host seconds spent admitting into free slots */
+  int64_t fills;                    /* slot admissions (each one eqf_replace_traps) */
+  double refill_step_s;             /* of launch_s: queueing the first step after a
+                                       fill (cell index and step graph rebuilt) */
 } eqs_stats;
 
 int eqs_default_config(eqs_config* cfg);
