@@ -771,6 +771,10 @@ def run_serving(args, rank, world, local_rank):
                               adv_u=t.adv_u, adv_len=t.adv_len) for k in range(t.n_species)]
 
     cfg = S.default_config(hbm_budget=int(args.budget_gb * (1 << 30)))
+    if args.steps_in_flight > 0:
+        cfg.steps_in_flight = args.steps_in_flight
+    if args.max_cohorts > 0:
+        cfg.max_cohorts = args.max_cohorts
     srv = S.Server(cfg)
     ids = {}
     results = {}
@@ -849,6 +853,7 @@ def run_serving(args, rank, world, local_rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-ir",
         "data": "synthetic (seeded PCG64 request stream)",
         "config": {"workload": "serving", "rate_per_s": args.rate, "duration_s": args.duration,
+                   "steps_in_flight": int(cfg.steps_in_flight), "max_cohorts": int(cfg.max_cohorts),
                    "requests": n, "budget_gb": args.budget_gb, "seed": seed,
                    "mix": "70% one species / 30% advective sender-receiver pair",
                    "sizes": "nx U{64..1024}, ny U{32..512}, h=0.25 um; steps U{1..50}"},
@@ -933,6 +938,10 @@ def main():
     ap.add_argument("--drain-limit", type=float, default=20.0,
                     help="serving: stop this long after the last arrival")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
+    ap.add_argument("--steps-in-flight", type=int, default=0,
+                    help="serving: steps queued per cohort (0: the library default)")
+    ap.add_argument("--max-cohorts", type=int, default=0,
+                    help="serving: cohorts stepping at once (0: the library default)")
     ap.add_argument("--audit-budget", type=float, default=30.0,
                     help="serving: CPU seconds for the oracle audit")
     ap.add_argument("--no-fuse", action="store_true",

@@ -517,6 +517,7 @@ class Batch {
   // the V-cycle below level bottom_lb runs in k_bottom, one CTA per trap (-1: not used)
   int bottom_lb = -1;
   size_t sm_bottom = 0;
+  DevBuf<int> bottom_order;  // k_bottom's traps by decreasing size of the first bottom level
   eqf_solver_opts opts{};
   std::vector<eqf_trap_params> params;
   std::vector<Level> L;
@@ -1304,6 +1305,17 @@ void Batch::build_levels() {
       }
     }
   }
+  if (bottom_lb >= 0) {  // largest traps first: the launch's tail is the largest CTA's
+    std::vector<int> ord(ntraps);
+    for (int t = 0; t < ntraps; ++t) ord[t] = t;
+    const Level& Lb = L[bottom_lb];
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return (long long)Lb.geom[a].P * (Lb.geom[a].ny + 1) >
+             (long long)Lb.geom[b].P * (Lb.geom[b].ny + 1);
+    });
+    bottom_order.alloc(ntraps);
+    bottom_order.upload(ord.data(), ntraps, stream);
+  }
   trap_dirty.assign(ntraps, 0);
   range.assign(ntraps, TileRange{0, 0});
   for (int i = 0; i < L[0].ntiles(); ++i) {
@@ -1499,6 +1511,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
     }
     a.deg_pre = B.opts.cheb_pre;
     a.deg_coarse = B.opts.cheb_coarse;
+    a.order = B.bottom_order.p;
     EQF_RUN(B, KC_COARSE,
             (launch_pdl(k_bottom<T>, B.ntraps, kBottomThreads, B.sm_bottom, s, a, skip, bl, cur)));
     return cur;

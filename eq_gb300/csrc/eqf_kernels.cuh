@@ -1041,6 +1041,8 @@ struct BottomArgs {
   const T* tabs[kMaxBottom];       // and its class tables
   int nlev;                        // levels lb .. lb + nlev - 1 (the last the coarsest)
   int deg_pre, deg_coarse;  // (two post-smoothing steps, as k_up)
+  const int* order;         // trap of each CTA, largest first (the tail is the largest
+                            // trap's), or null: CTA b solves trap b
 };
 // Shared-memory bytes of one level: rhs b and direction d, iterates x and y with
 // zero guards of gpad >= P + 1 nodes each side.
@@ -1078,7 +1080,7 @@ __global__ void __launch_bounds__(kBottomThreads, 1)
     k_bottom(const BottomArgs<T> a, const int* __restrict__ skip, const T* __restrict__ b0,
              T* __restrict__ x0) {
   grid_dep_sync();
-  const int trap = blockIdx.x;
+  const int trap = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
   if (skip && skip[trap]) return;
   BottomLevel<T> lv[kMaxBottom];
   Stager st(eqf_smem);
