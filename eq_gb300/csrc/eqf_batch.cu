@@ -851,6 +851,19 @@ static int trap_levels(const eqf_trap_params& p) {
 // Multigrid depth of a trap (host helper shared with the serving loop).
 int eqf_internal_trap_levels(const eqf_trap_params& p) { return eqf::trap_levels(p); }
 
+// Nodes a trap's grid spans at each of nlev levels (rows x pitch, as build_levels lays
+// them out): a trap fits a slot when it spans no more at any level.
+void eqf_internal_trap_spans(const eqf_trap_params& p, int nlev, long long* spans) {
+  int nx = p.nx, ny = p.ny;
+  for (int l = 0; l < nlev; ++l) {
+    if (l > 0) {  // build_levels' coarsening: halve an axis while it has >= 4 cells
+      if (nx >= 4) nx = (nx + 1) / 2;
+      if (ny >= 4) ny = (ny + 1) / 2;
+    }
+    spans[l] = (long long)((nx + 1 + 3) & ~3) * (ny + 1);
+  }
+}
+
 namespace eqf {
 
 // Device bytes of a batch (steady state plus the transient of the cell rebuild),
@@ -2433,18 +2446,11 @@ void Batch::check_replacement(int t, const eqf_trap_params& p) const {
       if (l == t) throw Error(EQF_ERR_INVALID, "trap carries rod cells");
   for (const auto& c : chans)
     if (c->trap == t) throw Error(EQF_ERR_INVALID, "trap carries a flow channel");
-  {  // the grid of every level must fit the slot (build_levels' coarsening)
-    int nx = p.nx, ny = p.ny;
-    for (int l = 0; l < nlev; ++l) {
-      if (l > 0) {
-        const int cx = nx >= 4, cy = ny >= 4;
-        if (cx) nx = (nx + 1) / 2;
-        if (cy) ny = (ny + 1) / 2;
-      }
-      const long long P = (nx + 1 + 3) & ~3;
-      if (P * (ny + 1) > slot_span[l][t])
-        throw Error(EQF_ERR_INVALID, "trap grid larger than its slot");
-    }
+  {  // the grid of every level must fit the slot
+    std::vector<long long> sp(nlev);
+    eqf_internal_trap_spans(p, nlev, sp.data());
+    for (int l = 0; l < nlev; ++l)
+      if (sp[l] > slot_span[l][t]) throw Error(EQF_ERR_INVALID, "trap grid larger than its slot");
   }
 }
 

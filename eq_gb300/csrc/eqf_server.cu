@@ -20,8 +20,9 @@
 #include "../../include/eqfield.h"
 #include "../../include/eqserve.h"
 
-// Multigrid depth of a trap (eqf_batch.cu).
+// Multigrid depth of a trap and the nodes its grid spans per level (eqf_batch.cu).
 int eqf_internal_trap_levels(const eqf_trap_params& p);
+void eqf_internal_trap_spans(const eqf_trap_params& p, int nlev, long long* spans);
 
 namespace {
 
@@ -44,6 +45,8 @@ struct Req {
   bool done = false;
   bool taken = false;  // result handed out (the object lives until its cohort is released)
   int64_t klass = 0;   // cohort class: multigrid depth and symmetric / advective operator
+  int levels = 0;      // the class's multigrid depth
+  std::vector<long long> spans;  // per species and level: nodes its grid spans
   bool picked = false; // taken into the cohort being formed
   int ntraps() const { return r.n_species; }
 };
@@ -118,6 +121,8 @@ struct Cohort {
   // per trap slot: the grid it was created with (its capacity) and the request
   // holding it (null: free since that request's last step was queued)
   std::vector<eqf_trap_params> slot_cap;
+  std::vector<long long> cap_spans;  // per slot and level: the nodes the slot holds
+  int levels = 0;
   std::vector<Req*> slot_owner;
   bool filling = false;  // queue no steps until the queued ones are done, then fill slots
   bool closing = false;  // no more requests: runs out to make room for another cohort
@@ -344,13 +349,17 @@ void place(eqs_server* s, Cohort& c, Req* q, int t, double now) {
   c.steps_target = std::max(c.steps_target, q->end_step());
 }
 
-// Slots t .. are free and the request's grids fit them at every level
+// Slots t .. are free and the request's grids fit them at every level (the spans
+// eqf_slot_fits compares, computed once per request and per cohort)
 bool fits(const Cohort& c, const Req* q, int t) {
-  if (t + q->r.n_species > (int)c.slot_cap.size()) return false;
+  if (t + q->r.n_species > (int)c.slot_cap.size() || q->levels != c.levels) return false;
+  const int L = c.levels;
   for (int k = 0; k < q->r.n_species; ++k) {
     if (c.slot_owner[t + k]) return false;
-    int32_t ok = 0;
-    if (eqf_slot_fits(c.b, t + k, &q->r.species[k], &ok) != EQF_OK || !ok) return false;
+    const long long* cap = c.cap_spans.data() + (size_t)(t + k) * L;
+    const long long* need = q->spans.data() + (size_t)k * L;
+    for (int l = 0; l < L; ++l)
+      if (need[l] > cap[l]) return false;
   }
   return true;
 }
@@ -511,6 +520,10 @@ bool admit(eqs_server* s) {
   ckb(eqf_stream(c->b, &stream), c->b);
   c->stream = (cudaStream_t)stream;
   c->slot_cap = tp;
+  c->levels = head->levels;
+  c->cap_spans.resize(tp.size() * (size_t)c->levels);
+  for (size_t k = 0; k < tp.size(); ++k)
+    eqf_internal_trap_spans(tp[k], c->levels, c->cap_spans.data() + k * (size_t)c->levels);
   c->slot_owner.assign(tp.size(), nullptr);
   int t = 0;
   const double now = s->now();
@@ -742,6 +755,10 @@ int eqs_submit(eqs_server* s, const eqs_request* r, int64_t* id) {
       adv = adv || (r->species[k].adv_u != 0.0 && r->species[k].adv_len > 0.0);
     }
     q->klass = 2 * (int64_t)levels + (adv ? 1 : 0);
+    q->levels = levels;
+    q->spans.resize((size_t)r->n_species * levels);
+    for (int k = 0; k < r->n_species; ++k)
+      eqf_internal_trap_spans(r->species[k], levels, q->spans.data() + (size_t)k * levels);
     if (estimate(s, {q.get()}) > s->cfg.hbm_budget)
       throw Fail{EQF_ERR_TOO_LARGE, "request larger than the server's memory budget"};
     q->id = s->next_id++;
