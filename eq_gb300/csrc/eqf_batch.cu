@@ -14,6 +14,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <exception>
 #include <atomic>
 #include <thread>
 #include <stdexcept>
@@ -481,6 +482,8 @@ static void retire_graph_exec(cudaGraphExec_t gx) {
 }
 
 // f(0) .. f(n - 1) on up to 16 host threads (pure host work: no CUDA calls inside).
+// The first exception a worker meets stops the others' remaining items and is
+// rethrown on the calling thread.
 template <class F>
 static void parallel_for(int n, F&& f) {
   const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -490,13 +493,26 @@ static void parallel_for(int n, F&& f) {
     return;
   }
   std::atomic<int> next(0);
-  std::vector<std::thread> th;
-  th.reserve(nt);
-  for (int w = 0; w < nt; ++w)
-    th.emplace_back([&] {
+  std::exception_ptr err;
+  std::mutex err_mu;
+  auto work = [&] {
+    try {
       for (int i; (i = next.fetch_add(1)) < n;) f(i);
-    });
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(err_mu);
+      if (!err) err = std::current_exception();
+      next.store(n);
+    }
+  };
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  try {
+    for (int w = 1; w < nt; ++w) th.emplace_back(work);
+  } catch (...) {  // no more threads: the ones started and this one share the items
+  }
+  work();  // the calling thread is a worker too
   for (auto& x : th) x.join();
+  if (err) std::rethrow_exception(err);
 }
 
 class Batch {

@@ -426,15 +426,26 @@ bool fill_slots(eqs_server* s, Cohort& c) {
     return false;
   }
   const double now = s->now();
-  for (auto& e : m) {
-    e.first->picked = true;
-    place(s, c, e.first, e.second, now);
-    c.reqs.push_back(e.first);
-    c.remaining += 1;
+  size_t k = 0;
+  auto take_placed = [&] {  // the placed requests leave the queue; the rest stay
+    s->pending.erase(std::remove_if(s->pending.begin(), s->pending.end(),
+                                    [](const Req* q) { return q->picked; }),
+                     s->pending.end());
+  };
+  try {
+    for (; k < m.size(); ++k) {
+      place(s, c, m[k].first, m[k].second, now);
+      m[k].first->picked = true;
+      c.reqs.push_back(m[k].first);
+      c.remaining += 1;
+    }
+  } catch (...) {
+    for (size_t j = k; j < m.size(); ++j)
+      for (int q = 0; q < m[j].first->r.n_species; ++q) c.slot_owner[m[j].second + q] = nullptr;
+    take_placed();
+    throw;
   }
-  s->pending.erase(std::remove_if(s->pending.begin(), s->pending.end(),
-                                  [](const Req* q) { return q->picked; }),
-                   s->pending.end());
+  take_placed();
   s->st.admitted += (int64_t)m.size();
   s->st.slot_admitted += (int64_t)m.size();
   s->st.fills += 1;
