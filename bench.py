@@ -775,6 +775,8 @@ def run_serving(args, rank, world, local_rank):
         cfg.steps_in_flight = args.steps_in_flight
     if args.max_cohorts > 0:
         cfg.max_cohorts = args.max_cohorts
+    if args.cohort_traps > 0:
+        cfg.max_cohort_traps = args.cohort_traps
     srv = S.Server(cfg)
     ids = {}
     results = {}
@@ -854,6 +856,7 @@ def run_serving(args, rank, world, local_rank):
         "data": "synthetic (seeded PCG64 request stream)",
         "config": {"workload": "serving", "rate_per_s": args.rate, "duration_s": args.duration,
                    "steps_in_flight": int(cfg.steps_in_flight), "max_cohorts": int(cfg.max_cohorts),
+                   "cohort_traps": int(cfg.max_cohort_traps),
                    "requests": n, "budget_gb": args.budget_gb, "seed": seed,
                    "mix": "70% one species / 30% advective sender-receiver pair",
                    "sizes": "nx U{64..1024}, ny U{32..512}, h=0.25 um; steps U{1..50}"},
@@ -942,6 +945,8 @@ def main():
                     help="serving: steps queued per cohort (0: the library default)")
     ap.add_argument("--max-cohorts", type=int, default=0,
                     help="serving: cohorts stepping at once (0: the library default)")
+    ap.add_argument("--cohort-traps", type=int, default=0,
+                    help="serving: traps per cohort (0: the library default)")
     ap.add_argument("--audit-budget", type=float, default=30.0,
                     help="serving: CPU seconds for the oracle audit")
     ap.add_argument("--no-fuse", action="store_true",
