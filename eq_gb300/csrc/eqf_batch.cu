@@ -534,6 +534,7 @@ class Batch {
   int bottom_lb = -1;
   size_t sm_bottom = 0;
   DevBuf<int> bottom_order;  // k_bottom's traps by decreasing size of the first bottom level
+  DevBuf<int> coarse_order;  // k_coarse_solve's traps by decreasing coarsest-grid size
   eqf_solver_opts opts{};
   std::vector<eqf_trap_params> params;
   std::vector<Level> L;
@@ -1338,17 +1339,20 @@ void Batch::build_levels() {
       }
     }
   }
-  if (bottom_lb >= 0) {  // largest traps first: the launch's tail is the largest CTA's
+  // one CTA per trap on the bottom and coarsest levels: largest traps first (the
+  // launch's tail is the largest CTA's)
+  auto by_size = [&](const Level& Lv, DevBuf<int>& out) {
     std::vector<int> ord(ntraps);
     for (int t = 0; t < ntraps; ++t) ord[t] = t;
-    const Level& Lb = L[bottom_lb];
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-      return (long long)Lb.geom[a].P * (Lb.geom[a].ny + 1) >
-             (long long)Lb.geom[b].P * (Lb.geom[b].ny + 1);
+      return (long long)Lv.geom[a].P * (Lv.geom[a].ny + 1) >
+             (long long)Lv.geom[b].P * (Lv.geom[b].ny + 1);
     });
-    bottom_order.alloc(ntraps);
-    bottom_order.upload(ord.data(), ntraps, stream);
-  }
+    out.alloc(ntraps);
+    out.upload(ord.data(), ntraps, stream);
+  };
+  if (bottom_lb >= 0) by_size(L[bottom_lb], bottom_order);
+  by_size(L[nlev - 1], coarse_order);
   trap_dirty.assign(ntraps, 0);
   range.assign(ntraps, TileRange{0, 0});
   for (int i = 0; i < L[0].ntiles(); ++i) {
@@ -1552,8 +1556,8 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
   if (coarsest && Lv_.sm_coarse && !dot) {
     // the whole coarsest solve in one CTA per trap
     EQF_RUN(B, KC_COARSE,
-            (launch_pdl(k_coarse_solve<T>, B.ntraps, kThreads, Lv_.sm_coarse, s, G, tab, skip, deg_pre,
-                                                                          bl, cur)));
+            (launch_pdl(k_coarse_solve<T>, B.ntraps, kCoarseThreads, Lv_.sm_coarse, s, G, tab,
+                        skip, deg_pre, bl, cur, (const int*)B.coarse_order.p)));
     return cur;
   }
   if (!coarsest && B.opts.fuse_levels && B.opts.cheb_pre == 2 && B.opts.cheb_post == 2 &&

@@ -985,13 +985,16 @@ __global__ void __launch_bounds__(kThreads)
 // Coarsest-level solve: one CTA per trap runs `deg` Chebyshev-Jacobi iterations
 // on [lmin, lmax] from zero entirely in shared memory.  Layout after the staged
 // rhs: two iterate buffers with gpad >= P+1 zero guard nodes each side, and d.
+// 512 threads, the largest traps' CTAs first (order): the launch's time is its
+// largest CTA's chain of `deg` barrier-separated sweeps.
+constexpr int kCoarseThreads = 512;
 template <class T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kCoarseThreads)
     k_coarse_solve(const LevelGeom* __restrict__ G, const T* __restrict__ tabs,
                    const int* __restrict__ skip, int deg, const T* __restrict__ b,
-                   T* __restrict__ xout) {
+                   T* __restrict__ xout, const int* __restrict__ order) {
   grid_dep_sync();
-  const LevelGeom& g = G[blockIdx.x];
+  const LevelGeom& g = G[order ? order[blockIdx.x] : (int)blockIdx.x];
   if (skip && skip[g.trap]) return;
   const int n = g.P * (g.ny + 1);
   const int na = padded_len(g);

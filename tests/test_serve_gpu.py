@@ -174,3 +174,21 @@ def test_requests_reuse_the_slots_of_finished_ones(lib):
     for r, a in zip(res, alone_big + alone_later):
         assert r.status == 0
         assert np.array_equal(r.cells, a)
+
+
+def test_without_slot_reuse_every_admission_is_a_new_cohort(lib):
+    """reuse_slots = 0: finished requests' slots stay frozen until their cohort ends,
+    new requests form new cohorts; the results are the same bits."""
+    traps = small_traps(6, seed=21)
+    steps = [2, 5, 3, 4, 6, 2]
+    alone = [run_alone(t, k) for t, k in zip(traps, steps)]
+    cfg = S.default_config(min_batch=2, max_wait_ms=1e6, max_cohorts=1, max_cohort_traps=2,
+                           reuse_slots=0)
+    with S.Server(cfg) as srv:
+        ids = [submit(srv, t, k) for t, k in zip(traps, steps)]
+        srv.drain()
+        st = srv.stats()
+        res = [srv.result(i) for i in ids]
+    assert st["completed"] == 6 and st["slot_admitted"] == 0 and st["cohorts"] == 3
+    for r, a in zip(res, alone):
+        assert r.status == 0 and np.array_equal(r.cells, a)
