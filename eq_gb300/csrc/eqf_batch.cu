@@ -1175,6 +1175,19 @@ void Batch::build_levels() {
                                (int)std::min<long long>(P, c0 + CW)});
       off = align_up(off + span[t], 32);
     }
+    if (l > 0) {
+      // coarse levels carry no per-tile partials: their tiles go largest first, so the
+      // long ones of the largest traps do not start last (level 0 keeps each trap's
+      // tiles together, in order, for the partial sums)
+      auto big1 = [](const Tile& a, const Tile& b) { return a.k1 - a.k0 > b.k1 - b.k0; };
+      auto big2 = [](const Tile2& a, const Tile2& b) {
+        return (long long)(a.r1 - a.r0) * (a.c1 - a.c0) > (long long)(b.r1 - b.r0) * (b.c1 - b.c0);
+      };
+      std::stable_sort(L[l].tiles.begin(), L[l].tiles.end(), big1);
+      std::stable_sort(gen1.begin(), gen1.end(), big1);
+      std::stable_sort(L[l].tiles2.begin(), L[l].tiles2.end(), big2);
+      std::stable_sort(gen2.begin(), gen2.end(), big2);
+    }
     L[l].ntiles_cls = (int)L[l].tiles.size();
     L[l].tiles.insert(L[l].tiles.end(), gen1.begin(), gen1.end());
     L[l].ntiles2_cls = (int)L[l].tiles2.size();
