@@ -211,7 +211,7 @@ def profiled_roofline(b, stream, prof_steps: int, workload: str):
                 "avg_launch_us": d["ms"] * 1e3 / max(d["launches"], 1),
                 "share_of_profiled_pass": round(d["ms"] / max(prof_total, 1e-9), 4)}
     roofline.update(launch_traffic(tclasses.get(dom), d))
-    if dom in ("down0", "up0"):
+    if dom in ("down0", "down0_cg", "up0"):
         roofline["note"] = ("temporally blocked level kernel: several smoothing steps per HBM "
                             "pass, bytes counted once (compute-bound by design)")
     return prof, prof_total, launches_per_step, roofline, tclasses

@@ -50,7 +50,7 @@ EQF_SIDE_BOTTOM, EQF_SIDE_TOP, EQF_SIDE_LEFT, EQF_SIDE_RIGHT = 0, 1, 2, 3
 EQF_BC_NEUMANN, EQF_BC_DIRICHLET, EQF_BC_ROBIN, EQF_BC_CHANNEL, EQF_BC_WELL = 0, 1, 2, 3, 4
 PROF_CLASSES = ("smooth0", "smooth0_first", "resid0", "restrict0", "prolong0", "coarse",
                 "cg_dir", "cg_update", "ir_resid_first", "ir_resid", "ir_update", "scalar",
-                "down0", "up0", "rod_exchange", "balance")
+                "down0", "up0", "rod_exchange", "balance", "down0_cg")
 
 # rod cells (eqf_set_rods): per cell and layer modes, and the eqf_rod record
 EQF_MAX_ROD_LAYERS = 4

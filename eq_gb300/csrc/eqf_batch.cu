@@ -381,6 +381,7 @@ enum KClass : int {
   KC_UP0,             // finest level, fused prolongation + post-smoothing
   KC_ROD,             // rod-cell exchange waves (gather, membrane exchange, deposit)
   KC_BALANCE,         // per-step FP64 mass balance (eqf_mass_balance)
+  KC_DOWN0_CG,        // finest level, fused pre-smoothing + residual + CG update
   KC_COUNT
 };
 static_assert(KC_COUNT == EQF_PROF_CLASSES, "profiler class count");
@@ -399,6 +400,8 @@ static void class_bytes(int cls, int tsize, double& per_node) {
     case KC_IR_RESID: per_node = 16.0 + tsize; break;      // b, u in; r out
     case KC_IR_UPDATE: per_node = 24.0 + tsize; break;     // x, u, d in; u, d out
     case KC_DOWN0: per_node = 3.0 * tsize; break;          // b in; x, t out
+    case KC_DOWN0_CG: per_node = 8.0 * tsize; break;       // r, q, x_cg, p in; x, t, r,
+                                                           // x_cg out
     case KC_UP0: per_node = 3.25 * tsize; break;           // x, b, 1/4 coarse in; x out
     default: per_node = 0.0;
   }
@@ -449,7 +452,14 @@ struct Work : WorkBase {
   };
   std::vector<Lv> lv;
   DevBuf<T> xs, p0, p1, q;  // fine CG: correction, directions, A p
+  DevBuf<T> r2;             // fine CG: the residual's second buffer (folded update)
   DevBuf<T> rh;             // BiCGSTAB shadow residual (only when BiCGSTAB is used)
+  // The previous CG iteration's update, for the finest level's k_down to fold in, and
+  // the inner convergence test k_s_rr runs right after it.
+  struct Fold {
+    CgFold<T> dev;
+    double tol_rel, tol_abs;
+  };
   explicit Work(Batch& b);
   void enqueue_sweep(cudaStream_t s, bool first, int iters) override;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
@@ -457,10 +467,11 @@ struct Work : WorkBase {
     for (DevBuf<T>* v : {&lv[lev].b, &lv[lev].x, &lv[lev].y, &lv[lev].d, &lv[lev].t})
       out.push_back({reinterpret_cast<char*>(v->p + off), n * (long long)sizeof(T)});
     if (lev == 0)
-      for (DevBuf<T>* v : {&xs, &p0, &p1, &q, &rh})
+      for (DevBuf<T>* v : {&xs, &p0, &p1, &q, &r2, &rh})
         if (v->p) out.push_back({reinterpret_cast<char*>(v->p + off), n * (long long)sizeof(T)});
   }
-  T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr);
+  T* vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0 = nullptr,
+            const Fold* fold = nullptr);
   void bicgstab(cudaStream_t s, T* r, double tol_rel, double tol_abs, int max_iters);
 };
 
@@ -892,11 +903,7 @@ namespace eqf {
 static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solver_opts& o,
                              long long ncells) {
   int nlev = 1;
-  bool adv = false;
-  for (int t = 0; t < n; ++t) {
-    nlev = std::max(nlev, trap_levels(traps[t]));
-    adv = adv || (traps[t].adv_u != 0.0 && traps[t].adv_len > 0.0);
-  }
+  for (int t = 0; t < n; ++t) nlev = std::max(nlev, trap_levels(traps[t]));
   const double T = o.precision == EQF_PREC_FP32_IR ? 4.0 : 8.0;
   double n0 = 0, nall = 0;
   for (int t = 0; t < n; ++t) {
@@ -911,9 +918,9 @@ static size_t estimate_bytes(int n, const eqf_trap_params* traps, const eqf_solv
       nall += nn;
     }
   }
-  const bool bicg = o.krylov == EQF_KRYLOV_BICGSTAB || (o.krylov == EQF_KRYLOV_AUTO && adv);
   double bytes = 40.0 * n0                    // U[2], Dd[2], rhs, load
-                 + T * (4 + (bicg ? 1 : 0)) * n0  // Krylov vectors
+                 + T * (4 + 1) * n0            // Krylov vectors (CG: second residual;
+                                               // BiCGSTAB: shadow residual)
                  + 5.0 * T * nall               // multigrid level vectors
                  + 12.0 * n0                    // cell rebuild transient (counts, scans)
                  + 140.0 * (double)ncells       // cell arrays, entries, segments, readout
@@ -1420,6 +1427,8 @@ static void allow_dyn_smem() {
   smem_attrs(k_irf_first, mx);
   smem_attrs(k_down<T, false>, mx);
   smem_attrs(k_down<T, true>, mx);
+  smem_attrs(k_down<T, false, true>, mx);
+  smem_attrs(k_down<T, true, true>, mx);
   smem_attrs(k_up<T, true, false>, mx);
   smem_attrs(k_up<T, false, false>, mx);
   smem_attrs(k_up<T, true, true>, mx);
@@ -1450,6 +1459,10 @@ Work<T>::Work(Batch& b) : B(b) {
   for (DevBuf<T>* v : {&xs, &p0, &p1, &q}) {
     v->alloc(n0);
     EQF_CK(cudaMemsetAsync(v->p, 0, n0 * sizeof(T), B.stream));
+  }
+  if (!B.use_bicgstab) {  // the folded CG update writes the residual here
+    r2.alloc(n0);
+    EQF_CK(cudaMemsetAsync(r2.p, 0, n0 * sizeof(T), B.stream));
   }
   if (B.use_bicgstab) {
     rh.alloc(n0);
@@ -1537,7 +1550,7 @@ const double* level_tab<double>(const Level& L) {
 // the buffer holding x.
 // With `dot`, the last smoothing step also writes partials of b.x (= r.z on level 0).
 template <class T>
-T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
+T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0, const Fold* fold) {
   const Level& Lv_ = B.L[lev];
   Lv& v = lv[lev];
   const T* bl = (lev == 0 && rhs0) ? rhs0 : v.b.p;  // this level's rhs
@@ -1582,12 +1595,30 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0) {
     const Tile2* tc2 = Lv_.dtiles2.p;
     const Tile2* tg2 = Lv_.dtiles2.p + nc2;
     const int cd = lev > 0 ? KC_COARSE : KC_DOWN0, cu = lev > 0 ? KC_COARSE : KC_UP0;
-    if (nc2 > 0)
-      EQF_RUN(B, cd, (launch_pdl(k_down<T, false>, nc2, kThreads, Lv_.sm_down, s, G, tc2, tab,
-                                 skip, bl, cur, v.t.p, W)));
-    if (ng2 > 0)
-      EQF_RUN(B, cd, (launch_pdl(k_down<T, true>, ng2, kThreads, Lv_.sm_down, s, G, tg2, tab,
-                                 skip, bl, cur, v.t.p, W)));
+    if (lev == 0 && fold) {
+      // the previous iteration's x += alpha p, r -= alpha q folded in; the partials
+      // of (r, r) go to part[the tile's index in tiles2], the test follows at once
+      CgFold<T> fc = fold->dev, fg = fold->dev;
+      fg.part += nc2;
+      if (nc2 > 0)
+        EQF_RUN(B, KC_DOWN0_CG, (launch_pdl(k_down<T, false, true>, nc2, kThreads, Lv_.sm_down,
+                                            s, G, tc2, tab, skip, bl, cur, v.t.p, fc, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, KC_DOWN0_CG, (launch_pdl(k_down<T, true, true>, ng2, kThreads, Lv_.sm_down,
+                                            s, G, tg2, tab, skip, bl, cur, v.t.p, fg, W)));
+      const int nb = (B.ntraps + 127) / 128;
+      EQF_RUN(B, KC_SCALAR,
+              (launch_pdl(k_s_rr, nb, 128, 0, s, B.ntraps, B.drange2.p, fold->dev.part,
+                          fold->tol_rel, fold->tol_abs, B.dstate.p, B.d_cg_skip.p, 1)));
+      bl = fold->dev.rout;  // the post-smoothing's right-hand side
+    } else {
+      if (nc2 > 0)
+        EQF_RUN(B, cd, (launch_pdl(k_down<T, false>, nc2, kThreads, Lv_.sm_down, s, G, tc2,
+                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, cd, (launch_pdl(k_down<T, true>, ng2, kThreads, Lv_.sm_down, s, G, tg2,
+                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, W)));
+    }
     const Level& Lc = B.L[lev + 1];
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
             (launch_pdl(k_restrict<T>, Lc.ntiles(), kThreads, Lc.sm_restrict, s,
@@ -1697,14 +1728,24 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs, iters);
     EQF_RUN(B, KC_IR_UPDATE,
-            (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out, d_out,
-                                                    W)));
+            (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out,
+                        d_out, (const CgState*)nullptr, (const T*)nullptr, W)));
     return;
   }
   T* pin = p0.p;
   T* pout = p1.p;
+  // With the fused finest level, iteration it's update x += alpha p, r -= alpha q is
+  // folded into iteration it+1's k_down (residual ping-ponged between r and r2), and
+  // the last iteration's x update into k_ir_update: no k_cg_update pass over the grid.
+  const bool fold = B.fused0 && r2.p;
+  T* rcur = r;
+  T* ralt = r2.p;
   for (int it = 0; it < iters; ++it) {
-    T* z = vcycle(s, 0, true);
+    Fold fd;
+    const bool use = fold && it > 0;
+    if (use) fd = Fold{CgFold<T>{q.p, ralt, pin, xs.p, B.dstate.p, part}, tol_rel, tol_abs};
+    T* z = vcycle(s, 0, true, rcur, use ? &fd : nullptr);
+    if (use) std::swap(rcur, ralt);
     EQF_RUN(B, KC_SCALAR,
             (launch_pdl(k_s_rz, nb, 128, 0, s, B.ntraps, B.fused0 ? B.drange2.p : B.drange.p, part,
                                        B.dstate.p, B.d_cg_skip.p)));
@@ -1732,17 +1773,23 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
       }
     }
     EQF_RUN(B, KC_SCALAR,
-            (launch_pdl(k_s_pq, nb, 128, 0, s, B.ntraps, B.drange.p, part, B.dstate.p, B.d_cg_skip.p)));
-    EQF_RUN(B, KC_CG_UPDATE,
-            (launch_pdl(k_cg_update<T>, nt, kThreads, 0, s, G, tl, B.d_cg_skip.p, B.dstate.p, pout, q.p,
-                                                    xs.p, r, part, W)));
-    EQF_RUN(B, KC_SCALAR,
-            (launch_pdl(k_s_rr, nb, 128, 0, s, B.ntraps, B.drange.p, part, tol_rel, tol_abs, B.dstate.p,
-                                       B.d_cg_skip.p)));
+            (launch_pdl(k_s_pq, nb, 128, 0, s, B.ntraps, B.drange.p, part, B.dstate.p,
+                        B.d_cg_skip.p, fold ? 1 : 0)));
+    if (!fold) {
+      EQF_RUN(B, KC_CG_UPDATE,
+              (launch_pdl(k_cg_update<T>, nt, kThreads, 0, s, G, tl, B.d_cg_skip.p, B.dstate.p,
+                          pout, q.p, xs.p, r, part, W)));
+      EQF_RUN(B, KC_SCALAR,
+              (launch_pdl(k_s_rr, nb, 128, 0, s, B.ntraps, B.drange.p, part, tol_rel, tol_abs,
+                          B.dstate.p, B.d_cg_skip.p, 0)));
+    }
     std::swap(pin, pout);
   }
+  // folded: traps still iterating at the end take their last alpha p here (pin now
+  // holds the last direction)
   EQF_RUN(B, KC_IR_UPDATE,
-          (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out, d_out, W)));
+          (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out,
+                      d_out, (const CgState*)B.dstate.p, fold ? (const T*)pin : nullptr, W)));
 }
 
 // Right-preconditioned BiCGSTAB on the correction x (xs) from residual r (the
@@ -2813,8 +2860,11 @@ int eqf_default_opts(int32_t precision, eqf_solver_opts* o) {
   if (precision == EQF_PREC_FP32_IR) {
     // 4 inner iterations a sweep and 16 coarsest-level steps: 9-10 % faster steps than
     // 6 and 12 on the 512-trap workload at the same sweeps a step (the outer FP64 test
-    // sets the accuracy either way)
-    o->rtol = 1e-8;
+    // sets the accuracy either way).  rtol 3e-8 keeps the field within ~1e-7 of the
+    // FP64 solution (relL2 about three times rtol on the uneven traps over 200 steps),
+    // a tenfold margin under the form's 1e-6 accuracy target; 1e-8 costs 8 % more per
+    // step, 1e-7 saves a further 10 % at ~3e-7
+    o->rtol = 3e-8;
     o->max_sweeps = 2;
     o->max_iters = 4;
     o->inner_tol = 1e-5;

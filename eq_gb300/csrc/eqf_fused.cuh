@@ -209,17 +209,35 @@ __device__ __forceinline__ int wl(const Win& w, int i, int j) {
   return (i - w.ra) * w.S() + (j - w.ca);
 }
 
-// Pre-smoothing (two steps from zero) and residual of one tile.
-template <class T, bool GEN>
+// The previous Krylov iteration's update, folded into the finest level's k_down
+// (UPD): r_out = r - alpha q and x_cg += alpha p, with a partial of (r_out, r_out).
+template <class T>
+struct CgFold {
+  const T* q;      // A p of the previous iteration
+  T* rout;         // the updated residual (another buffer: neighbours still stage r)
+  const T* p;      // the previous direction
+  T* xcg;          // the Krylov correction
+  const CgState* st;
+  double* part;    // (r_out, r_out) partials by 2-D tile index
+};
+
+// Pre-smoothing (two steps from zero) and residual of one tile.  UPD: b = r - alpha q
+// is formed on the window from the staged r and q (the same expression k_cg_update
+// evaluates, so the iterates do not change), stored to cf.rout on the tile, and the
+// tile's correction takes cf.xcg += alpha cf.p.
+template <class T, bool GEN, bool UPD = false>
 __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
            const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
-           T* __restrict__ x, T* __restrict__ t, unsigned long long* work) {
+           T* __restrict__ x, T* __restrict__ t, CgFold<T> cf, unsigned long long* work) {
   const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
   prefetch_l1(G + tile.geom);
   grid_dep_sync();
   const LevelGeom& g = G[tile.geom];
-  if (skip && skip[g.trap]) return;
+  if (skip && skip[g.trap]) {
+    if (UPD && threadIdx.x == 0) cf.part[blockIdx.x] = 0.0;
+    return;
+  }
   if (work && threadIdx.x == 0)
     atomicAdd(work, (unsigned long long)(tile.r1 - tile.r0) * (tile.c1 - tile.c0));
   const ChebCoef c0 = cheb_at(g, 0), c1 = cheb_at(g, 1);
@@ -234,14 +252,24 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   T* x2p = carve<T>(st, w2.count());
   const TableStage<T> tst = stage_table<T>(st, tab, ci);
   const T* stab = tst.s;
-  const RowStage<T> rs[1] = {{b + g.off, bp, w1, P, g.ny + 1}};
-  if (!stage_rows<T, 1>(st.bar, rs, tst)) return;
+  constexpr int NS = UPD ? 2 : 1;
+  RowStage<T> rs[NS];
+  rs[0] = RowStage<T>{b + g.off, bp, w1, P, g.ny + 1};
+  if constexpr (UPD) rs[1] = RowStage<T>{cf.q + g.off, x1p, w1, P, g.ny + 1};  // q into x1's room
+  if (!stage_rows<T, NS>(st.bar, rs, tst)) return;
+  const T alpha = UPD ? T(cf.st[g.trap].alpha) : T(0);
   const int S1 = w1.S(), S2 = w2.S();
-  // step 1 from zero (pointwise) on W1
+  // (UPD: b = r - alpha q, in place) step 1 from zero (pointwise) on W1
   for_quads(g, win_quads(w1), [&](int i, int cq, auto inner_) {
     constexpr bool INNER = decltype(inner_)::value;
     const int j = w1.ca + 4 * cq, kl = (i - w1.ra) * S1 + 4 * cq;
-    const Q4<T> bq = vld4<T>(bp + kl);
+    Q4<T> bq = vld4<T>(bp + kl);
+    if constexpr (UPD) {  // each quad is visited once: the in-place update is safe
+      const Q4<T> qv = vld4<T>(x1p + kl);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) bq.v[e] = fma_(-alpha, qv.v[e], bq.v[e]);
+      vst4<T>(bp + kl, bq);
+    }
     const Q4<T> id = inv_diag_quad<T, kGM<GEN>>(g, ci, stab, i, j, INNER);
     Q4<T> d;
 #pragma unroll
@@ -267,7 +295,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     });
   }
   __syncthreads();
-  // residual on the tile; store x2 and t
+  // residual on the tile; store x2 and t (UPD: and r, x_cg)
+  T acc = T(0);
   {
     const View<T> x2v{x2p, 0};
     T* xs = x + g.off;
@@ -275,6 +304,12 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
     for_quads(g, win_quads(wt), [&](int i, int cq, auto inner_) {
       constexpr bool INNER = decltype(inner_)::value;
       const int j = tile.c0 + 4 * cq;
+      const size_t k = (size_t)i * P + j;
+      [[maybe_unused]] Q4<T> pv, xv;
+      if constexpr (UPD) {  // issued before the stencil: their latency overlaps it
+        pv = vld4<T>(cf.p + g.off + k);
+        xv = vld4<T>(cf.xcg + g.off + k);
+      }
       Q4<T> xc, id;
       const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, x2v,
           wl(w2, i, j), S2, i, j, INNER, xc, id);
@@ -282,10 +317,22 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       Q4<T> r;
 #pragma unroll
       for (int e = 0; e < 4; ++e) r.v[e] = bq.v[e] - ax.v[e];
-      const size_t k = (size_t)i * P + j;
       vst4<T>(xs + k, xc);
       vst4<T>(ts + k, r);
+      if constexpr (UPD) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          xv.v[e] = fma_(alpha, pv.v[e], xv.v[e]);
+          acc += bq.v[e] * bq.v[e];
+        }
+        vst4<T>(cf.rout + g.off + k, bq);
+        vst4<T>(cf.xcg + g.off + k, xv);
+      }
     });
+  }
+  if constexpr (UPD) {
+    const double s = block_sum(acc);
+    if (threadIdx.x == 0) cf.part[blockIdx.x] = s;
   }
 }
 

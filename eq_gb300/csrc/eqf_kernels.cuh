@@ -1244,7 +1244,8 @@ struct CgState {
   double gamma;     // extrapolation factor of the initial guess
   double dn2_prev;  // |increment|^2 of the previous step
   double omega;     // BiCGSTAB: stabilisation factor (rz = rho, pq = rhat.v)
-  int iters, sweeps, it_in_sweep, pad;
+  int iters, sweeps, it_in_sweep;
+  int pend;  // alpha p of the last iteration is not yet in the correction x
 };
 
 // p_out = z (FIRST) or z + beta p_in; q = A p_out; partial dot(p_out, q).
@@ -1514,12 +1515,15 @@ __device__ __forceinline__ double to_double(float f) {
   return __longlong_as_double(e == 0u ? s : (s | (ex << 52) | m));
 }
 
-// u += x; d += x (the inner-solve correction)   (streaming, quads)
+// u += x; d += x (the inner-solve correction)   (streaming, quads).  A trap whose
+// last Krylov update is pending (CgState::pend, folded CG) takes x + alpha p_last,
+// the value k_cg_update would have left in x.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
                 const int* __restrict__ skip, const T* __restrict__ x, double* __restrict__ u,
-                float* __restrict__ d, unsigned long long* work) {
+                float* __restrict__ d, const CgState* __restrict__ st,
+                const T* __restrict__ plast, unsigned long long* work) {
   const Tile tile = tiles[blockIdx.x];  // static: read before the wait
   prefetch_l1(G + tile.geom);
   grid_dep_sync();
@@ -1527,11 +1531,18 @@ __global__ void __launch_bounds__(kThreads)
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
   const long long o = g.off;
+  const bool pend = plast && st[g.trap].pend;
+  const T alpha = pend ? T(st[g.trap].alpha) : T(0);
   const int qa = tile.k0 >> 2, qb = (tile.k1 + 3) >> 2;
   for (int qq = qa + threadIdx.x; qq < qb; qq += blockDim.x) {
     const int k = 4 * qq;
     if (k >= tile.k0 && k + 4 <= tile.k1) {
-      const Q4<T> xq = vld4<T>(x + o + k);
+      Q4<T> xq = vld4<T>(x + o + k);
+      if (pend) {
+        const Q4<T> pq = vld4<T>(plast + o + k);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) xq.v[e] = fma_(alpha, pq.v[e], xq.v[e]);
+      }
       Q4<double> uq = vld4<double>(u + o + k);
       Q4<float> dq = vld4<float>(d + o + k);
 #pragma unroll
@@ -1544,7 +1555,8 @@ __global__ void __launch_bounds__(kThreads)
     } else {
       for (int kk = k; kk < k + 4; ++kk) {
         if (kk < tile.k0 || kk >= tile.k1) continue;
-        const T v = x[o + kk];
+        T v = x[o + kk];
+        if (pend) v = fma_(alpha, plast[o + kk], v);
         u[o + kk] += to_double(v);
         d[o + kk] += float(v);
       }
@@ -1591,6 +1603,7 @@ __global__ void k_s_ir(int ntraps, const TileRange* __restrict__ range,
   s.rr0 = s.r64;
   s.rr = s.r64;
   s.it_in_sweep = 0;
+  s.pend = 0;
   if (!conv) s.sweeps += 1;
   st[t] = s;
 }
@@ -1640,10 +1653,13 @@ __global__ void k_s_rz(int ntraps, const TileRange* __restrict__ range,
   st[t] = s;
 }
 
-// After k_cg_dir: alpha = rz / pq.
+// After k_cg_dir: alpha = rz / pq.  With `folded` the update x += alpha p, r -= alpha q
+// is left to the next iteration's finest-level k_down (or, after the last iteration,
+// to k_ir_update): the trap's update is marked pending and the iteration is counted
+// here, since k_s_rr then runs one iteration later and not after the last one.
 __global__ void k_s_pq(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, CgState* __restrict__ st,
-                       const int* __restrict__ cg_skip) {
+                       const int* __restrict__ cg_skip, int folded) {
   grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || cg_skip[t]) return;
@@ -1651,20 +1667,30 @@ __global__ void k_s_pq(int ntraps, const TileRange* __restrict__ range,
   CgState s = st[t];
   s.pq = pq;
   s.alpha = pq != 0.0 ? s.rz / pq : 0.0;
+  if (folded) {
+    s.pend = 1;
+    s.it_in_sweep += 1;
+    s.iters += 1;
+  }
   st[t] = s;
 }
 
-// After k_cg_update: inner convergence test |r| <= tol_rel |r0| or |r| <= rtol |b|.
+// After the update (k_cg_update, or the finest-level k_down that folds it in: then
+// `folded`): inner convergence test |r| <= tol_rel |r0| or |r| <= rtol |b|.
 __global__ void k_s_rr(int ntraps, const TileRange* __restrict__ range,
                        const double* __restrict__ part, double tol_rel, double rtol_abs,
-                       CgState* __restrict__ st, int* __restrict__ cg_skip) {
+                       CgState* __restrict__ st, int* __restrict__ cg_skip, int folded) {
   grid_dep_sync();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntraps || cg_skip[t]) return;
   CgState s = st[t];
   s.rr = trap_sum(part, range[t]);
-  s.it_in_sweep += 1;
-  s.iters += 1;
+  if (folded) {
+    s.pend = 0;  // k_down has added alpha p to the correction
+  } else {
+    s.it_in_sweep += 1;
+    s.iters += 1;
+  }
   if (s.rr <= tol_rel * tol_rel * s.rr0 || s.rr <= rtol_abs * rtol_abs * s.bb) cg_skip[t] = 1;
   st[t] = s;
 }

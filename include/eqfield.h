@@ -540,7 +540,7 @@ int eqf_rod_relax_passes(eqf_batch* b, int32_t* passes);
  * that time the batch with their own CUDA events or order their own work. */
 int eqf_stream(eqf_batch* b, void** stream);
 
-#define EQF_PROF_CLASSES 16
+#define EQF_PROF_CLASSES 17
 int eqf_profile(eqf_batch* b, int32_t enable);
 int eqf_profile_read(eqf_batch* b, int32_t n_classes, double* ms, int64_t* launches,
                      int64_t* nodes, double* bytes);

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 TERMS = ("mass", "mass_prev", "load", "decay", "operator_loss", "wall_outflow", "drift")
 # the drift is the solver residual summed over the free rows: |sum r| <= sqrt(N) |r|_2,
 # so relative to the mass it stays below a few times the step's rtol
-DRIFT = {F.FP64: 1e-9, F.FP32_IR: 1e-7}
+DRIFT = {F.FP64: 1e-9, F.FP32_IR: 3e-7}  # FP32 form: ten times its default rtol (3e-8)
 # with wall values the Dirichlet rows' right-hand sides (the values themselves, not
 # mass-weighted) dominate |b|, and rtol |b| with them
 DRIFT_VALUES = {F.FP64: 1e-8, F.FP32_IR: 1e-6}

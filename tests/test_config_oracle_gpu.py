@@ -21,7 +21,7 @@ from eq_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 TOL = {F.FP64: 1e-9, F.FP32_IR: 1e-6}
-DRIFT = {F.FP64: 1e-9, F.FP32_IR: 1e-7}
+DRIFT = {F.FP64: 1e-9, F.FP32_IR: 3e-7}  # FP32 form: ten times its default rtol (3e-8)
 
 
 def rel(a, b):

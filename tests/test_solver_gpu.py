@@ -184,7 +184,8 @@ def test_mass_is_conserved_with_zero_flux_walls(lib, precision):
         b.step(20)
         m1 = b.total_mass(0)
     # each step conserves 1^T M u up to the solve tolerance (rtol |b| per step)
-    assert abs(m1 - m0) <= (2e-9 if precision == F.FP64 else 2e-7) * m0
+    rtol = F.default_opts(precision).rtol
+    assert abs(m1 - m0) <= (2e-9 if precision == F.FP64 else 20 * rtol) * m0
 
 
 def test_large_trap_scaled_copy_against_oracle(lib):
@@ -249,6 +250,36 @@ def test_fused_and_unfused_level_kernels_agree(lib, precision):
             out.append(u)
     assert rel(out[0], out[2]) <= TOL[precision]
     assert rel(out[1], out[2]) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [F.FP64, F.FP32_IR])
+def test_cg_update_folded_into_finest_level_kernel(lib, precision):
+    """With the fused finest level, each CG iteration's x += alpha p, r -= alpha q runs
+    inside the next iteration's k_down (and the last one inside the refinement update):
+    no k_cg_update launch, the same iteration counts, the oracle's answer.  The
+    step-by-step V-cycle keeps the separate update kernel."""
+    t = wl.scaled(wl.single_large(1), 256, 128, n_cells=2000)
+    ref = hsld.run_trap(t, steps=6)
+    prof, stats = {}, {}
+    for fuse in (1, 0):
+        with F.TrapBatch([tparams(t)], F.default_opts(precision, use_graph=0,
+                                                      fuse_levels=fuse)) as b:
+            b.set_cells(0, t.cell_xy, t.cell_s)
+            b.step(5)
+            b.profile(True)
+            b.step(1)
+            b.sync()
+            prof[fuse] = b.profile_read()
+            b.profile(False)
+            assert rel(b.read_nodal(0), ref["u"][0]) <= TOL[precision]
+            assert rel(b.read_cells(0), ref["cells"][0]) <= TOL[precision]
+            stats[fuse] = b.stats(0)
+    assert prof[1]["cg_update"]["launches"] == 0 and prof[1]["down0_cg"]["launches"] > 0
+    assert prof[0]["cg_update"]["launches"] > 0 and prof[0]["down0_cg"]["launches"] == 0
+    # one count per Krylov iteration in both: at most max_iters a sweep
+    mi = F.default_opts(precision).max_iters
+    for f in (1, 0):
+        assert 0 < stats[f]["iters"] <= mi * stats[f]["sweeps"]
 
 
 def coarse_launches(b):
