@@ -149,6 +149,25 @@ def trap_params_of(traps):
     return [F.trap_params(t.W, t.H, t.nx, t.ny, t.D[0], t.dt, t.g[0], t.walls) for t in traps]
 
 
+def tuned_schedule(table, traps, opts):
+    """The Krylov schedule and smoother degrees the batch runs with: those of the tuning
+    table's bucket that holds most of the nodes (as eqf_create_tuned picks them), else
+    the options'."""
+    out = {"max_iters": opts.max_iters, "max_sweeps": opts.max_sweeps,
+           "cheb_pre": opts.cheb_pre, "cheb_post": opts.cheb_post, "rtol": opts.rtol}
+    if table is None:
+        return out
+    mass = [0] * table.n
+    for t in traps:
+        k = next((i for i in range(table.n) if t.n_nodes <= table.b[i].max_nodes), table.n - 1)
+        mass[k] += t.n_nodes
+    b = table.b[max(range(table.n), key=lambda i: mass[i])]
+    for name in ("max_iters", "max_sweeps", "cheb_pre", "cheb_post"):
+        if getattr(b, name) > 0:
+            out[name] = getattr(b, name)
+    return out
+
+
 def sample_indices(traps, k: int):
     """k traps stratified by node count (deterministic)."""
     from eq_gb300 import workloads as wl
@@ -307,7 +326,8 @@ def run_ours(args, rank, world, local_rank):
 
     opts = F.default_opts(F.FP32_IR, use_graph=1, adaptive=1, tile_nodes=args.tile_nodes,
                           fuse_levels=0 if args.no_fuse else args.fuse_levels)
-    # the autotuner picks the row tile target and smoother degrees per size bucket
+    # the autotuner picks the tile shapes, smoother degrees and Krylov schedule per
+    # size bucket
     table = None
     if args.tune_budget > 0 and args.tile_nodes == 0:
         t_tune = time.perf_counter()
@@ -509,7 +529,8 @@ def run_ours(args, rank, world, local_rank):
                                                  f"{total_steps - 1} timed steps each",
                                        "speedup_of_batched_fp32ir": value / world / fp64_rate},
             "solver": {"sweeps_per_step": sweeps_ps, "iters_per_step": iters_ps,
-                       "sample": f"{len(probe)} traps stratified by size, timed steps"},
+                       "sample": f"{len(probe)} traps stratified by size, timed steps",
+                       "schedule": tuned_schedule(table, traps, opts)},
             "mass_balance": balance,
             "fp64_residual_variant": variant,
             "oracle_checks": checks,

@@ -82,7 +82,8 @@ class SolverOpts(C.Structure):
 class TuneBucket(C.Structure):
     _fields_ = [("max_nodes", C.c_int64), ("tile_nodes", C.c_int32), ("cheb_pre", C.c_int32),
                 ("cheb_post", C.c_int32), ("tile_cols", C.c_int32),
-                ("dof_steps_per_s", C.c_double)]
+                ("dof_steps_per_s", C.c_double), ("max_iters", C.c_int32),
+                ("max_sweeps", C.c_int32)]
 
 
 EQF_TUNE_MAX_BUCKETS = 8

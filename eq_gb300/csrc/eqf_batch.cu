@@ -2953,8 +2953,8 @@ int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_so
     o = *opts;
   else
     eqf_default_opts(EQF_PREC_FP64, &o);
-  // tile target per trap from its bucket; smoother degrees from the bucket that
-  // holds most of the batch's nodes
+  // tile target per trap from its bucket; smoother degrees and Krylov schedule from
+  // the bucket that holds most of the batch's nodes
   std::vector<int> tiles(n_traps), cols(n_traps);
   std::vector<long long> mass(table->n, 0);
   for (int t = 0; t < n_traps; ++t) {
@@ -2967,6 +2967,8 @@ int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_so
   const int kb = (int)(std::max_element(mass.begin(), mass.end()) - mass.begin());
   if (table->b[kb].cheb_pre > 0) o.cheb_pre = table->b[kb].cheb_pre;
   if (table->b[kb].cheb_post > 0) o.cheb_post = table->b[kb].cheb_post;
+  if (table->b[kb].max_iters > 0) o.max_iters = table->b[kb].max_iters;
+  if (table->b[kb].max_sweeps > 0) o.max_sweeps = table->b[kb].max_sweeps;
   return create_impl(n_traps, traps, &o, tiles.data(), cols.data(), out);
 }
 

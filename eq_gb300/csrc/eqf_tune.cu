@@ -1,6 +1,8 @@
-// Autotuner: per trap-size bucket, the finest-level row tile target and the
-// pre/post Chebyshev degrees that give the most DOF-steps/s at the solver
-// tolerance (include/eqfield.h: eqf_autotune, eqf_create_tuned).
+// Autotuner: per trap-size bucket, the finest-level row tile target, the fused
+// kernels' 2-D tile width, the pre/post Chebyshev degrees and the Krylov schedule
+// (inner iterations per refinement sweep, scheduled sweeps) that give the most
+// DOF-steps/s at the solver tolerance (include/eqfield.h: eqf_autotune,
+// eqf_create_tuned).
 //
 // Host code over the public C ABI.  Each candidate runs on a batch of the caller's
 // traps from that bucket (replicated to fill the GPU) with seeded random point
@@ -105,10 +107,13 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
   std::memset(table, 0, sizeof(*table));
   table->n = kBuckets;
   // stage 1: smoother degrees at the default tiles; stage 2: tile node targets x 2-D
-  // tile widths at the best degrees (0 = the library default)
+  // tile widths at the best degrees (0 = the library default); stage 3: Krylov
+  // schedules at the best of those (fewer inner iterations with more FP64 refinement
+  // sweeps pays on some batches: the sweeps' residuals are exact, the inner solve FP32)
   const int degs[][2] = {{0, 0}, {1, 1}, {3, 3}, {2, 1}};
   const int tiles[] = {0, 2048, 6144};
   const int widths[] = {0, 64, 256, 512};
+  const int scheds[][2] = {{2, 4}, {3, 3}};
   for (int k = 0; k < kBuckets; ++k) {
     eqf_tune_bucket& tb = table->b[k];
     tb.max_nodes = kBucketMax[k];
@@ -116,6 +121,8 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
     tb.tile_cols = 0;
     tb.cheb_pre = o.cheb_pre;
     tb.cheb_post = o.cheb_post;
+    tb.max_iters = o.max_iters;
+    tb.max_sweeps = o.max_sweeps;
     std::vector<eqf_trap_params> sel;
     for (int t = 0; t < n_traps; ++t) {
       const long long nodes = (long long)(traps[t].nx + 1) * (traps[t].ny + 1);
@@ -132,14 +139,17 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
       nodes += (long long)(p.nx + 1) * (p.ny + 1);
     }
     double best = 0.0;
-    auto trial = [&](int pre, int post, int tile, int cols) {
+    auto trial = [&](int pre, int post, int tile, int cols, int iters, int sweeps) {
       if (elapsed() > budget_s && best > 0.0) return;
       eqf_solver_opts c = o;
       c.cheb_pre = pre;
       c.cheb_post = post;
+      c.max_iters = iters;
+      c.max_sweeps = sweeps;
       const double r = measure(batch, c, tile, cols);
-      char line[160];
-      std::snprintf(line, sizeof(line), "%d %d %d %d %d %.6e\n", k, tile, cols, pre, post, r);
+      char line[192];
+      std::snprintf(line, sizeof(line), "%d %d %d %d %d %d %d %.6e\n", k, tile, cols, pre,
+                    post, iters, sweeps, r);
       text += line;
       if (r > best) {
         best = r;
@@ -147,14 +157,21 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
         tb.tile_cols = cols;
         tb.cheb_pre = pre;
         tb.cheb_post = post;
+        tb.max_iters = iters;
+        tb.max_sweeps = sweeps;
       }
     };
+    const int it0 = o.max_iters, sw0 = o.max_sweeps;
     for (const auto& d : degs)
-      trial(d[0] > 0 ? d[0] : o.cheb_pre, d[0] > 0 ? d[1] : o.cheb_post, 0, 0);
+      trial(d[0] > 0 ? d[0] : o.cheb_pre, d[0] > 0 ? d[1] : o.cheb_post, 0, 0, it0, sw0);
     const int pre = tb.cheb_pre, post = tb.cheb_post;
     for (int tile : tiles)
       for (int cols : widths)
-        if (tile != 0 || cols != 0) trial(pre, post, tile, cols);
+        if (tile != 0 || cols != 0) trial(pre, post, tile, cols, it0, sw0);
+    const int tile = tb.tile_nodes, cols = tb.tile_cols;
+    if (o.precision == EQF_PREC_FP32_IR)  // the plain form keeps its one long sweep
+      for (const auto& sc : scheds)
+        if (sc[0] != it0 || sc[1] != sw0) trial(pre, post, tile, cols, sc[0], sc[1]);
     tb.dof_steps_per_s = best;
   }
   if (log) {

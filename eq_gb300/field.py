@@ -73,9 +73,9 @@ def trap_params(W, H, nx, ny, D, dt, decay=0.0, walls=WALL_BOTTOM, adv_u=0.0,
 
 def autotune(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
              budget_s: float = 20.0) -> _lib.TuneTable:
-    """Per size bucket, the fastest tile node target, 2-D tile width and Chebyshev
-    degrees (eqf_autotune_log; runs on the GPU for about budget_s seconds at most).
-    The returned table carries every measured candidate in .log."""
+    """Per size bucket, the fastest tile node target, 2-D tile width, Chebyshev
+    degrees and Krylov schedule (eqf_autotune_log; runs on the GPU for about budget_s
+    seconds at most).  The returned table carries every measured candidate in .log."""
     lib = _lib.load()
     arr = (TrapParams * len(traps))(*traps)
     table = _lib.TuneTable()
@@ -84,7 +84,8 @@ def autotune(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
                               float(budget_s), C.byref(table), buf, len(buf))
     _check(lib, None, rc)
     table.log = [dict(zip(("bucket", "tile_nodes", "tile_cols", "cheb_pre", "cheb_post",
-                           "dof_steps_per_s"), (float(x) for x in ln.split())))
+                           "max_iters", "max_sweeps", "dof_steps_per_s"),
+                          (float(x) for x in ln.split())))
                  for ln in buf.value.decode().splitlines() if ln.strip()]
     return table
 
@@ -92,14 +93,15 @@ def autotune(traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
 def tune_table_dict(table: _lib.TuneTable) -> List[Dict[str, float]]:
     return [{"max_nodes": table.b[i].max_nodes, "tile_nodes": table.b[i].tile_nodes,
              "tile_cols": table.b[i].tile_cols, "cheb_pre": table.b[i].cheb_pre,
-             "cheb_post": table.b[i].cheb_post, "dof_steps_per_s": table.b[i].dof_steps_per_s}
+             "cheb_post": table.b[i].cheb_post, "max_iters": table.b[i].max_iters,
+             "max_sweeps": table.b[i].max_sweeps, "dof_steps_per_s": table.b[i].dof_steps_per_s}
             for i in range(table.n)]
 
 
 class TrapBatch:
     """A batch of independent traps on the GPU (C ABI handle).  With a tuning table
     (autotune) the traps take their size bucket's tile target and the batch its
-    dominant bucket's smoother degrees."""
+    dominant bucket's smoother degrees and Krylov schedule."""
 
     def __init__(self, traps: Sequence[TrapParams], opts: Optional[SolverOpts] = None,
                  tune: Optional[_lib.TuneTable] = None):

@@ -121,15 +121,18 @@ int eqf_create(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_o
  * (node count <= max_nodes, ascending; the last bucket takes the rest) to the tile
  * node target, the 2-D tile width of the fused level kernels and the pre/post
  * Chebyshev degrees that were fastest for traps of that size (DOF-steps/s at the
- * solver tolerance, measured by eqf_autotune).  eqf_create_tuned creates a batch
- * whose traps take the tile target and width of their bucket and whose smoother
- * takes the degrees of the bucket that holds most of its nodes. */
+ * solver tolerance, measured by eqf_autotune), and the Krylov schedule (inner
+ * iterations per refinement sweep, scheduled sweeps) that was fastest with them.
+ * eqf_create_tuned creates a batch whose traps take the tile target and width of
+ * their bucket and whose smoother degrees and schedule are those of the bucket that
+ * holds most of its nodes. */
 #define EQF_TUNE_MAX_BUCKETS 8
 typedef struct eqf_tune_bucket {
   int64_t max_nodes;
   int32_t tile_nodes, cheb_pre, cheb_post;
   int32_t tile_cols;      /* 2-D tile columns of the fused level kernels (0: default) */
   double dof_steps_per_s; /* measured rate of the chosen configuration */
+  int32_t max_iters, max_sweeps; /* Krylov schedule (0: the caller's eqf_solver_opts) */
 } eqf_tune_bucket;
 typedef struct eqf_tune_table {
   int32_t n;
@@ -140,13 +143,15 @@ int eqf_create_tuned(int32_t n_traps, const eqf_trap_params* traps, const eqf_so
                      const eqf_tune_table* table, eqf_batch** out);
 
 /* Measures, for each size bucket, candidate Chebyshev degrees, then tile node
- * targets x 2-D tile widths at the best degrees, on a batch of the given traps that
- * fall into the bucket (replicated up to a GPU-filling node count), with random point
- * cells, and writes the fastest into *table.  Buckets: <= 32k, <= 128k, <= 512k
- * nodes, and larger.  Takes about budget_s seconds of GPU time at most (unexplored
- * candidates keep the defaults).  When log is not NULL, one line per measured
- * candidate ("bucket tile_nodes tile_cols cheb_pre cheb_post dof_steps_per_s") is
- * written into it, at most log_size bytes including the terminating zero. */
+ * targets x 2-D tile widths at the best degrees, then Krylov schedules (inner
+ * iterations x scheduled refinement sweeps: the caller's, 2 x 4 and 3 x 3) at the best
+ * of those, on a batch of the given traps that fall into the bucket (replicated up to
+ * a GPU-filling node count), with random point cells, and writes the fastest into
+ * *table.  Buckets: <= 32k, <= 128k, <= 512k nodes, and larger.  Takes about budget_s
+ * seconds of GPU time at most (unexplored candidates keep the defaults).  When log is
+ * not NULL, one line per measured candidate ("bucket tile_nodes tile_cols cheb_pre
+ * cheb_post max_iters max_sweeps dof_steps_per_s") is written into it, at most
+ * log_size bytes including the terminating zero. */
 int eqf_autotune(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,
                  double budget_s, eqf_tune_table* table);
 int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps, const eqf_solver_opts* opts,

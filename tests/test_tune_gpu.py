@@ -30,6 +30,8 @@ def test_autotune_table_and_tuned_batch(lib):
             assert r["tile_nodes"] in (0, 2048, 6144)
             assert r["tile_cols"] in (0, 64, 256, 512)
             assert 1 <= r["cheb_pre"] <= 3 and 1 <= r["cheb_post"] <= 3
+            assert (r["max_iters"], r["max_sweeps"]) in ((opts.max_iters, opts.max_sweeps),
+                                                        (2, 4), (3, 3))
         else:
             assert r["dof_steps_per_s"] == 0
     # every measured candidate is logged, the chosen one with the bucket's best rate
