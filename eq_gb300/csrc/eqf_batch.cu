@@ -1724,7 +1724,10 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   EQF_RUN(B, KC_SCALAR,
           (launch_pdl(k_s_ir, nb, 128, 0, s, B.ntraps, B.drange.p, part, nt, first ? 1 : 0, B.opts.rtol,
                                      B.dstate.p, B.d_ir_done.p, B.d_cg_skip.p, B.d_frozen.p)));
-  EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
+  // the folded CG writes the correction at its first update (x = alpha p), so only the
+  // other Krylov paths start from a zeroed correction
+  const bool fold = !B.use_bicgstab && B.fused0 && r2.p;
+  if (!fold) EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs, iters);
     EQF_RUN(B, KC_IR_UPDATE,
@@ -1737,13 +1740,14 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   // With the fused finest level, iteration it's update x += alpha p, r -= alpha q is
   // folded into iteration it+1's k_down (residual ping-ponged between r and r2), and
   // the last iteration's x update into k_ir_update: no k_cg_update pass over the grid.
-  const bool fold = B.fused0 && r2.p;
   T* rcur = r;
   T* ralt = r2.p;
   for (int it = 0; it < iters; ++it) {
     Fold fd;
     const bool use = fold && it > 0;
-    if (use) fd = Fold{CgFold<T>{q.p, ralt, pin, xs.p, B.dstate.p, part}, tol_rel, tol_abs};
+    if (use)
+      fd = Fold{CgFold<T>{q.p, ralt, pin, xs.p, B.dstate.p, part, it == 1 ? 1 : 0}, tol_rel,
+                tol_abs};
     T* z = vcycle(s, 0, true, rcur, use ? &fd : nullptr);
     if (use) std::swap(rcur, ralt);
     EQF_RUN(B, KC_SCALAR,

@@ -219,6 +219,7 @@ struct CgFold {
   T* xcg;          // the Krylov correction
   const CgState* st;
   double* part;    // (r_out, r_out) partials by 2-D tile index
+  int first;       // the sweep's first update: x_cg = alpha p (x_cg is not read or zeroed)
 };
 
 // Pre-smoothing (two steps from zero) and residual of one tile.  UPD: b = r - alpha q
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       [[maybe_unused]] Q4<T> pv, xv;
       if constexpr (UPD) {  // issued before the stencil: their latency overlaps it
         pv = vld4<T>(cf.p + g.off + k);
-        xv = vld4<T>(cf.xcg + g.off + k);
+        if (!cf.first) xv = vld4<T>(cf.xcg + g.off + k);
       }
       Q4<T> xc, id;
       const Q4<T> ax = apply_quad<T, 0, View<T>, kGM<GEN>>(g, ci, stab, x2v,
@@ -322,7 +323,8 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
       if constexpr (UPD) {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          xv.v[e] = fma_(alpha, pv.v[e], xv.v[e]);
+          // from a zero correction fma(alpha, p, 0) is the rounded product itself
+          xv.v[e] = cf.first ? alpha * pv.v[e] : fma_(alpha, pv.v[e], xv.v[e]);
           acc += bq.v[e] * bq.v[e];
         }
         vst4<T>(cf.rout + g.off + k, bq);

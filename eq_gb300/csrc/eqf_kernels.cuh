@@ -1517,7 +1517,8 @@ __device__ __forceinline__ double to_double(float f) {
 
 // u += x; d += x (the inner-solve correction)   (streaming, quads).  A trap whose
 // last Krylov update is pending (CgState::pend, folded CG) takes x + alpha p_last,
-// the value k_cg_update would have left in x.
+// the value k_cg_update would have left in x; after a single iteration the folded
+// CG never wrote x (it is not zeroed per sweep), so x = alpha p_last.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
@@ -1532,16 +1533,24 @@ __global__ void __launch_bounds__(kThreads)
   count_work(work, tile);
   const long long o = g.off;
   const bool pend = plast && st[g.trap].pend;
+  const bool only = pend && st[g.trap].it_in_sweep == 1;  // x holds nothing of this sweep
   const T alpha = pend ? T(st[g.trap].alpha) : T(0);
   const int qa = tile.k0 >> 2, qb = (tile.k1 + 3) >> 2;
   for (int qq = qa + threadIdx.x; qq < qb; qq += blockDim.x) {
     const int k = 4 * qq;
     if (k >= tile.k0 && k + 4 <= tile.k1) {
-      Q4<T> xq = vld4<T>(x + o + k);
-      if (pend) {
+      Q4<T> xq;
+      if (only) {
         const Q4<T> pq = vld4<T>(plast + o + k);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) xq.v[e] = fma_(alpha, pq.v[e], xq.v[e]);
+        for (int e = 0; e < 4; ++e) xq.v[e] = alpha * pq.v[e];
+      } else {
+        xq = vld4<T>(x + o + k);
+        if (pend) {
+          const Q4<T> pq = vld4<T>(plast + o + k);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) xq.v[e] = fma_(alpha, pq.v[e], xq.v[e]);
+        }
       }
       Q4<double> uq = vld4<double>(u + o + k);
       Q4<float> dq = vld4<float>(d + o + k);
@@ -1555,8 +1564,8 @@ __global__ void __launch_bounds__(kThreads)
     } else {
       for (int kk = k; kk < k + 4; ++kk) {
         if (kk < tile.k0 || kk >= tile.k1) continue;
-        T v = x[o + kk];
-        if (pend) v = fma_(alpha, plast[o + kk], v);
+        T v = only ? alpha * plast[o + kk] : x[o + kk];
+        if (pend && !only) v = fma_(alpha, plast[o + kk], v);
         u[o + kk] += to_double(v);
         d[o + kk] += float(v);
       }
