@@ -924,10 +924,11 @@ def run_ncu_target(args):
         b.close()
         return
     traps = make_workload(args.workload, args.seed, args.traps)
-    b = F.TrapBatch(trap_params_of(traps), F.default_opts(prec, use_graph=0, adaptive=1,
-                                                          tile_nodes=args.tile_nodes,
-                                                          fuse_levels=0 if args.no_fuse
-                                                          else args.fuse_levels))
+    o = F.default_opts(prec, use_graph=0, adaptive=1, tile_nodes=args.tile_nodes,
+                       fuse_levels=0 if args.no_fuse else args.fuse_levels)
+    if args.schedule:  # the Krylov schedule the timed run's autotuner picked
+        o.max_iters, o.max_sweeps = (int(v) for v in args.schedule.split(","))
+    b = F.TrapBatch(trap_params_of(traps), o)
     load_traps(b, traps)
     b.mass_balance(True)  # as the timed run
     b.step(args.warmup + args.steps)
@@ -982,6 +983,9 @@ def main():
     ap.add_argument("--ncu", action="store_true",
                     help="minimal run (no graphs, no timing) as an ncu capture target")
     ap.add_argument("--fp64", action="store_true", help="with --ncu: plain FP64 form")
+    ap.add_argument("--schedule", default="",
+                    help="with --ncu: Krylov schedule 'inner_iterations,sweeps' (default: the "
+                         "library's)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
