@@ -336,6 +336,9 @@ struct Level {
 };
 
 constexpr size_t kSmemHeader = 16;              // mbarrier
+// CTAs of a listed launch over n tiles (late sweeps: a quarter of the tiles, which the
+// CTAs stride over when more are still iterating).
+static int listed_grid(int n) { return std::max(1, (n + 3) / 4); }
 // Krylov iterations of a refinement sweep added after a step missed rtol (the step's
 // own sweeps run opts.max_iters): such a sweep corrects a small residual.
 constexpr int kExtraSweepIters = 6;
@@ -435,8 +438,9 @@ __global__ void k_zero_ranges(const ZeroRange* __restrict__ r) {
 
 struct WorkBase {
   virtual ~WorkBase() = default;
-  // one refinement sweep of `iters` preconditioned Krylov iterations
-  virtual void enqueue_sweep(cudaStream_t s, bool first, int iters) = 0;
+  // one refinement sweep of `iters` preconditioned Krylov iterations; `late`: a sweep
+  // after the step's second, where few traps are still iterating
+  virtual void enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) = 0;
   virtual void enqueue_check(cudaStream_t s, bool update_gamma) = 0;
   // the byte ranges of every work vector over nodes [off, off + n) of level `lev`
   virtual void slot_ranges(int lev, long long off, long long n, std::vector<ZeroRange>& out) = 0;
@@ -461,7 +465,12 @@ struct Work : WorkBase {
     double tol_rel, tol_abs;
   };
   explicit Work(Batch& b);
-  void enqueue_sweep(cudaStream_t s, bool first, int iters) override;
+  void enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) override;
+  // Late sweeps of the folded CG: the finest level's fused kernels stride over a list
+  // of the iterating traps' 2-D tiles (class-table tiles from act_idx[0], general-path
+  // tiles from act_idx[ntiles2_cls]; counts in act_cnt[0..1]) with a quarter-size grid.
+  DevBuf<int> act_idx, act_cnt;
+  bool late_lists = false;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
   void slot_ranges(int lev, long long off, long long n, std::vector<ZeroRange>& out) override {
     for (DevBuf<T>* v : {&lv[lev].b, &lv[lev].x, &lv[lev].y, &lv[lev].d, &lv[lev].t})
@@ -1429,6 +1438,12 @@ static void allow_dyn_smem() {
   smem_attrs(k_down<T, true>, mx);
   smem_attrs(k_down<T, false, true>, mx);
   smem_attrs(k_down<T, true, true>, mx);
+  smem_attrs(k_down<T, false, false, true>, mx);
+  smem_attrs(k_down<T, true, false, true>, mx);
+  smem_attrs(k_down<T, false, true, true>, mx);
+  smem_attrs(k_down<T, true, true, true>, mx);
+  smem_attrs(k_up<T, true, false, true>, mx);
+  smem_attrs(k_up<T, true, true, true>, mx);
   smem_attrs(k_up<T, true, false>, mx);
   smem_attrs(k_up<T, false, false>, mx);
   smem_attrs(k_up<T, true, true>, mx);
@@ -1461,6 +1476,10 @@ Work<T>::Work(Batch& b) : B(b) {
     EQF_CK(cudaMemsetAsync(v->p, 0, n0 * sizeof(T), B.stream));
   }
   if (!B.use_bicgstab) {  // the folded CG update writes the residual here
+    // late sweeps' tile lists: allocated here, never in enqueue_sweep, which runs under
+    // stream capture (a stream-ordered allocation there becomes a graph memory node)
+    act_idx.alloc(std::max<size_t>(1, B.L[0].tiles2.size()));
+    act_cnt.alloc(2);
     r2.alloc(n0);
     EQF_CK(cudaMemsetAsync(r2.p, 0, n0 * sizeof(T), B.stream));
   }
@@ -1595,29 +1614,54 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0, const Fold*
     const Tile2* tc2 = Lv_.dtiles2.p;
     const Tile2* tg2 = Lv_.dtiles2.p + nc2;
     const int cd = lev > 0 ? KC_COARSE : KC_DOWN0, cu = lev > 0 ? KC_COARSE : KC_UP0;
+    const bool listed = lev == 0 && late_lists;
+    const TileList lc{act_idx.p, act_cnt.p}, lg{act_idx.p + nc2, act_cnt.p + 1};
+    const TileList none{nullptr, nullptr};
     if (lev == 0 && fold) {
       // the previous iteration's x += alpha p, r -= alpha q folded in; the partials
       // of (r, r) go to part[the tile's index in tiles2], the test follows at once
       CgFold<T> fc = fold->dev, fg = fold->dev;
-      fg.part += nc2;
-      if (nc2 > 0)
-        EQF_RUN(B, KC_DOWN0_CG, (launch_pdl(k_down<T, false, true>, nc2, kThreads, Lv_.sm_down,
-                                            s, G, tc2, tab, skip, bl, cur, v.t.p, fc, W)));
-      if (ng2 > 0)
-        EQF_RUN(B, KC_DOWN0_CG, (launch_pdl(k_down<T, true, true>, ng2, kThreads, Lv_.sm_down,
-                                            s, G, tg2, tab, skip, bl, cur, v.t.p, fg, W)));
+      if (listed) {  // absolute tile indices: both kinds index the whole array
+        if (nc2 > 0)
+          EQF_RUN(B, KC_DOWN0_CG,
+                  (launch_pdl(k_down<T, false, true, true>, listed_grid(nc2), kThreads,
+                              Lv_.sm_down, s, G, tc2, tab, skip, bl, cur, v.t.p, fc, lc, W)));
+        if (ng2 > 0)
+          EQF_RUN(B, KC_DOWN0_CG,
+                  (launch_pdl(k_down<T, true, true, true>, listed_grid(ng2), kThreads,
+                              Lv_.sm_down, s, G, tc2, tab, skip, bl, cur, v.t.p, fg, lg, W)));
+      } else {
+        fg.part += nc2;
+        if (nc2 > 0)
+          EQF_RUN(B, KC_DOWN0_CG,
+                  (launch_pdl(k_down<T, false, true>, nc2, kThreads, Lv_.sm_down, s, G, tc2, tab,
+                              skip, bl, cur, v.t.p, fc, none, W)));
+        if (ng2 > 0)
+          EQF_RUN(B, KC_DOWN0_CG,
+                  (launch_pdl(k_down<T, true, true>, ng2, kThreads, Lv_.sm_down, s, G, tg2, tab,
+                              skip, bl, cur, v.t.p, fg, none, W)));
+      }
       const int nb = (B.ntraps + 127) / 128;
       EQF_RUN(B, KC_SCALAR,
               (launch_pdl(k_s_rr, nb, 128, 0, s, B.ntraps, B.drange2.p, fold->dev.part,
                           fold->tol_rel, fold->tol_abs, B.dstate.p, B.d_cg_skip.p, 1)));
       bl = fold->dev.rout;  // the post-smoothing's right-hand side
+    } else if (listed) {
+      if (nc2 > 0)
+        EQF_RUN(B, cd, (launch_pdl(k_down<T, false, false, true>, listed_grid(nc2), kThreads,
+                                   Lv_.sm_down, s, G, tc2, tab, skip, bl, cur, v.t.p,
+                                   CgFold<T>{}, lc, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, cd, (launch_pdl(k_down<T, true, false, true>, listed_grid(ng2), kThreads,
+                                   Lv_.sm_down, s, G, tc2, tab, skip, bl, cur, v.t.p,
+                                   CgFold<T>{}, lg, W)));
     } else {
       if (nc2 > 0)
         EQF_RUN(B, cd, (launch_pdl(k_down<T, false>, nc2, kThreads, Lv_.sm_down, s, G, tc2,
-                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, W)));
+                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, none, W)));
       if (ng2 > 0)
         EQF_RUN(B, cd, (launch_pdl(k_down<T, true>, ng2, kThreads, Lv_.sm_down, s, G, tg2,
-                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, W)));
+                                   tab, skip, bl, cur, v.t.p, CgFold<T>{}, none, W)));
     }
     const Level& Lc = B.L[lev + 1];
     EQF_RUN(B, lev > 0 ? KC_COARSE : KC_RESTRICT0,
@@ -1625,20 +1669,33 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0, const Fold*
                         Lc.dgeom.p, Lc.dtiles.p, skip, v.t.p, lv[lev + 1].b.p, W)));
     T* xc = vcycle(s, lev + 1, false);
     // the dot partials of a tile go to part[its index in tiles2]
-    if (dot) {
+    if (dot && listed) {
+      if (nc2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, true, false, true>, listed_grid(nc2), kThreads,
+                                   Lv_.sm_up, s, G, Lc.dgeom.p, tc2, tab, skip, xc, bl, cur,
+                                   oth, part, lc, W)));
+      if (ng2 > 0)
+        EQF_RUN(B, cu, (launch_pdl(k_up<T, true, true, true>, listed_grid(ng2), kThreads,
+                                   Lv_.sm_up, s, G, Lc.dgeom.p, tc2, tab, skip, xc, bl, cur,
+                                   oth, part, lg, W)));
+    } else if (dot) {
       if (nc2 > 0)
         EQF_RUN(B, cu, (launch_pdl(k_up<T, true, false>, nc2, kThreads, Lv_.sm_up, s, G,
-                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, W)));
+                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, none,
+                                   W)));
       if (ng2 > 0)
         EQF_RUN(B, cu, (launch_pdl(k_up<T, true, true>, ng2, kThreads, Lv_.sm_up, s, G,
-                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2, W)));
+                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2,
+                                   none, W)));
     } else {
       if (nc2 > 0)
         EQF_RUN(B, cu, (launch_pdl(k_up<T, false, false>, nc2, kThreads, Lv_.sm_up, s, G,
-                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, W)));
+                                   Lc.dgeom.p, tc2, tab, skip, xc, bl, cur, oth, part, none,
+                                   W)));
       if (ng2 > 0)
         EQF_RUN(B, cu, (launch_pdl(k_up<T, false, true>, ng2, kThreads, Lv_.sm_up, s, G,
-                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2, W)));
+                                   Lc.dgeom.p, tg2, tab, skip, xc, bl, cur, oth, part + nc2,
+                                   none, W)));
     }
     return oth;
   }
@@ -1677,7 +1734,7 @@ T* Work<T>::vcycle(cudaStream_t s, int lev, bool dot, const T* rhs0, const Fold*
 // One refinement sweep: FP64 residual, preconditioned CG on the correction,
 // update.  The step reads U[cur] and writes U[1 - cur].
 template <class T>
-void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
+void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) {
   const Level& L0 = B.L[0];
   const int nt = L0.ntiles();
   const int nb = (B.ntraps + 127) / 128;
@@ -1728,6 +1785,16 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
   // other Krylov paths start from a zeroed correction
   const bool fold = !B.use_bicgstab && B.fused0 && r2.p;
   if (!fold) EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
+  const int n2 = (int)L0.tiles2.size();
+  // (buffers sized at construction: a batch whose tiles outgrew them runs full grids)
+  const bool listed = fold && late && act_idx.p && act_idx.n >= (size_t)n2;
+  if (listed) {  // the iterating traps' finest-level 2-D tiles
+    EQF_CK(cudaMemsetAsync(act_cnt.p, 0, 2 * sizeof(int), s));
+    EQF_RUN(B, KC_SCALAR,
+            (k_active_tiles2<<<(n2 + 255) / 256, 256, 0, s>>>(
+                G, L0.dtiles2.p, n2, L0.ntiles2_cls, B.d_cg_skip.p, act_idx.p, act_cnt.p)));
+  }
+  late_lists = listed;
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs, iters);
     EQF_RUN(B, KC_IR_UPDATE,
@@ -1789,6 +1856,7 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters) {
     }
     std::swap(pin, pout);
   }
+  late_lists = false;
   // folded: traps still iterating at the end take their last alpha p here (pin now
   // holds the last direction)
   EQF_RUN(B, KC_IR_UPDATE,
@@ -2353,7 +2421,7 @@ void Batch::run_step() {
   enqueue_coupling();
   enqueue_walls();
   for (int sw = 0; sw < opts.max_sweeps; ++sw)
-    work->enqueue_sweep(stream, sw == 0, opts.max_iters);
+    work->enqueue_sweep(stream, sw == 0, opts.max_iters, sw >= 2);
   work->enqueue_check(stream, true);
 }
 
@@ -2430,7 +2498,7 @@ void Batch::capture_step(cudaGraphExec_t& gx, bool device_loop) {
       EQF_COND_CK(cudaStreamBeginCaptureToGraph(stream, cp.conditional.phGraph_out[0], nullptr,
                                                 nullptr, 0, mode));
       capturing = true;
-      work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters));
+      work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters), true);
       work->enqueue_check(stream, false);
       k_sweep_loop<<<1, 1, 0, stream>>>(h, d_fail.p, d_loop.p, 0, kMaxExtraSweeps);
       EQF_COND_CK(cudaGetLastError());
@@ -2495,7 +2563,7 @@ void Batch::step(int n) {
         sync();
         if (f == 0) break;
         reset_fail();
-        work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters));
+        work->enqueue_sweep(stream, false, std::min(kExtraSweepIters, opts.max_iters), true);
         work->enqueue_check(stream, false);
       }
       if (f != 0) {

@@ -158,6 +158,31 @@ __device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st
   return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
+// The 2-D tiles of the traps still iterating (skip[trap] == 0): class-table tiles
+// (index < nc) into idx[0, ...), general-path tiles into idx[nc, ...), their numbers in
+// counts[0] and counts[1] (zeroed before).  The order within a list does not matter:
+// each tile's results and partial-sum slot are its own, whichever CTA computes it.
+__global__ void k_active_tiles2(const LevelGeom* __restrict__ G,
+                                const Tile2* __restrict__ tiles, int n, int nc,
+                                const int* __restrict__ skip, int* __restrict__ idx,
+                                int* __restrict__ counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || skip[G[tiles[i].geom].trap]) return;
+  const int k = i < nc ? 0 : 1;
+  idx[(k ? nc : 0) + atomicAdd(&counts[k], 1)] = i;
+}
+
+// Outcome of one tile of a fused kernel.
+constexpr int kTileSkipped = 0, kTileDone = 1, kTileFailed = -1;
+
+// Between two tiles of a listed launch: every thread is done with the windows before
+// the next tile's copies overwrite them, and a used mbarrier is invalidated before
+// stage_rows initialises it again.
+__device__ __forceinline__ void next_listed_tile(int rc) {
+  __syncthreads();
+  if (rc == kTileDone && threadIdx.x == 0) mbar_inval(reinterpret_cast<uint64_t*>(eqf_smem));
+}
+
 // Quads of a window: quad q at window row q / QW, columns 4 (q % QW) .. +3.
 struct WinQuads {
   int QW, n;
@@ -226,18 +251,18 @@ struct CgFold {
 // is formed on the window from the staged r and q (the same expression k_cg_update
 // evaluates, so the iterates do not change), stored to cf.rout on the tile, and the
 // tile's correction takes cf.xcg += alpha cf.p.
-template <class T, bool GEN, bool UPD = false>
-__global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
-    k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
-           const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
-           T* __restrict__ x, T* __restrict__ t, CgFold<T> cf, unsigned long long* work) {
-  const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
-  prefetch_l1(G + tile.geom);
-  grid_dep_sync();
+// One tile (index ti in the launch's tile array); returns kTileSkipped, kTileDone or
+// kTileFailed (a staging wait gave up).
+template <class T, bool GEN, bool UPD>
+__device__ __forceinline__ int down_tile(const LevelGeom* __restrict__ G, const Tile2& tile,
+                                         int ti, const T* __restrict__ tabs,
+                                         const int* __restrict__ skip, const T* __restrict__ b,
+                                         T* __restrict__ x, T* __restrict__ t,
+                                         const CgFold<T>& cf, unsigned long long* work) {
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
-    if (UPD && threadIdx.x == 0) cf.part[blockIdx.x] = 0.0;
-    return;
+    if (UPD && threadIdx.x == 0) cf.part[ti] = 0.0;
+    return kTileSkipped;
   }
   if (work && threadIdx.x == 0)
     atomicAdd(work, (unsigned long long)(tile.r1 - tile.r0) * (tile.c1 - tile.c0));
@@ -257,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   RowStage<T> rs[NS];
   rs[0] = RowStage<T>{b + g.off, bp, w1, P, g.ny + 1};
   if constexpr (UPD) rs[1] = RowStage<T>{cf.q + g.off, x1p, w1, P, g.ny + 1};  // q into x1's room
-  if (!stage_rows<T, NS>(st.bar, rs, tst)) return;
+  if (!stage_rows<T, NS>(st.bar, rs, tst)) return kTileFailed;
   const T alpha = UPD ? T(cf.st[g.trap].alpha) : T(0);
   const int S1 = w1.S(), S2 = w2.S();
   // (UPD: b = r - alpha q, in place) step 1 from zero (pointwise) on W1
@@ -334,7 +359,34 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   }
   if constexpr (UPD) {
     const double s = block_sum(acc);
-    if (threadIdx.x == 0) cf.part[blockIdx.x] = s;
+    if (threadIdx.x == 0) cf.part[ti] = s;
+  }
+  return kTileDone;
+}
+
+// LIST: the CTAs stride over a device-built list of the active traps' tiles (late
+// refinement sweeps, where most traps are done: a grid of all tiles would be mostly
+// CTAs that read their trap's skip flag and exit); otherwise CTA b takes tile b.
+template <class T, bool GEN, bool UPD = false, bool LIST = false>
+__global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
+    k_down(const LevelGeom* __restrict__ G, const Tile2* __restrict__ tiles,
+           const T* __restrict__ tabs, const int* __restrict__ skip, const T* __restrict__ b,
+           T* __restrict__ x, T* __restrict__ t, CgFold<T> cf, TileList tlist,
+           unsigned long long* work) {
+  if constexpr (!LIST) {
+    const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
+    prefetch_l1(G + tile.geom);
+    grid_dep_sync();
+    down_tile<T, GEN, UPD>(G, tile, (int)blockIdx.x, tabs, skip, b, x, t, cf, work);
+  } else {
+    grid_dep_sync();
+    const int n = *tlist.count;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+      const int ti = tlist.idx[w];
+      const int rc = down_tile<T, GEN, UPD>(G, tiles[ti], ti, tabs, skip, b, x, t, cf, work);
+      if (rc == kTileFailed) return;
+      next_listed_tile(rc);
+    }
   }
 }
 
@@ -342,19 +394,17 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
 // coarse correction, writes x2 to xout (another buffer: neighbouring tiles still
 // stage xin).  DOT adds a partial of b.x2 (r.z of the Krylov iteration).
 template <class T, bool DOT, bool GEN>
-__global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
-    k_up(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
-         const Tile2* __restrict__ tiles, const T* __restrict__ tabs,
-         const int* __restrict__ skip, const T* __restrict__ xc, const T* __restrict__ b,
-         const T* __restrict__ xin, T* __restrict__ xout, double* __restrict__ part,
-         unsigned long long* work) {
-  const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
-  prefetch_l1(G + tile.geom);
-  grid_dep_sync();
+__device__ __forceinline__ int up_tile(const LevelGeom* __restrict__ G,
+                                       const LevelGeom* __restrict__ Gc, const Tile2& tile,
+                                       int ti, const T* __restrict__ tabs,
+                                       const int* __restrict__ skip, const T* __restrict__ xc,
+                                       const T* __restrict__ b, const T* __restrict__ xin,
+                                       T* __restrict__ xout, double* __restrict__ part,
+                                       unsigned long long* work) {
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
-    if (DOT && threadIdx.x == 0) part[blockIdx.x] = 0.0;
-    return;
+    if (DOT && threadIdx.x == 0) part[ti] = 0.0;
+    return kTileSkipped;
   }
   if (work && threadIdx.x == 0)
     atomicAdd(work, (unsigned long long)(tile.r1 - tile.r0) * (tile.c1 - tile.c0));
@@ -376,7 +426,7 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   const RowStage<T> rs[3] = {{xin + g.off, xp, w1, P, g.ny + 1},
                              {b + g.off, bp, w2, P, g.ny + 1},
                              {xc + c.off, cp, wc, c.P, c.ny + 1}};
-  if (!stage_rows<T, 3>(st.bar, rs, tst)) return;
+  if (!stage_rows<T, 3>(st.bar, rs, tst)) return kTileFailed;
   const int S1 = w1.S(), S2 = w2.S(), SC = wc.S();
   // x0 = x + P x_c on the in-grid nodes of W1 (in place), one window quad per
   // thread.  Fine node (i, j) lies between coarse nodes (i0, j0) and (i1, j1) along
@@ -462,7 +512,35 @@ __global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
   }
   if (DOT) {
     const double s = block_sum(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (threadIdx.x == 0) part[ti] = s;
+  }
+  return kTileDone;
+}
+
+// LIST as k_down's.
+template <class T, bool DOT, bool GEN, bool LIST = false>
+__global__ void __launch_bounds__(kThreads, kFusedCtas<T>)
+    k_up(const LevelGeom* __restrict__ G, const LevelGeom* __restrict__ Gc,
+         const Tile2* __restrict__ tiles, const T* __restrict__ tabs,
+         const int* __restrict__ skip, const T* __restrict__ xc, const T* __restrict__ b,
+         const T* __restrict__ xin, T* __restrict__ xout, double* __restrict__ part,
+         TileList tlist, unsigned long long* work) {
+  if constexpr (!LIST) {
+    const Tile2 tile = tiles[blockIdx.x];  // static: read before the wait
+    prefetch_l1(G + tile.geom);
+    grid_dep_sync();
+    up_tile<T, DOT, GEN>(G, Gc, tile, (int)blockIdx.x, tabs, skip, xc, b, xin, xout, part,
+                         work);
+  } else {
+    grid_dep_sync();
+    const int n = *tlist.count;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+      const int ti = tlist.idx[w];
+      const int rc =
+          up_tile<T, DOT, GEN>(G, Gc, tiles[ti], ti, tabs, skip, xc, b, xin, xout, part, work);
+      if (rc == kTileFailed) return;
+      next_listed_tile(rc);
+    }
   }
 }
 

@@ -29,6 +29,8 @@ constexpr int kBuckets = 4;
 constexpr int64_t kBucketMax[kBuckets] = {32768, 131072, 524288, INT64_MAX};
 constexpr long long kFillNodes = 16ll << 20;  // nodes of a tuning batch (fills the GPU)
 constexpr int kMaxTraps = 1024;
+// warm-up and timed steps of the Krylov-schedule trials (the other trials: 3 and 4)
+constexpr int kSchedWarm = 10, kSchedTimed = 8;
 
 // splitmix64: a seeded stream of uniform doubles, identical on every platform
 struct Rng {
@@ -43,8 +45,9 @@ struct Rng {
 };
 
 // DOF-steps/s of one candidate (0 if it cannot run: e.g. rows too wide for the tile)
+// over `timed` steps after `warm` warm-up steps
 double measure(const std::vector<eqf_trap_params>& traps, const eqf_solver_opts& o, int tile,
-               int cols) {
+               int cols, int warm = 3, int timed = 4) {
   eqf_solver_opts c = o;
   c.tile_nodes = tile;
   c.tile_cols = cols;
@@ -70,9 +73,9 @@ double measure(const std::vector<eqf_trap_params>& traps, const eqf_solver_opts&
   }
   void* stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (ok && eqf_step(b, 3) == EQF_OK && eqf_stream(b, &stream) == EQF_OK &&
+  if (ok && eqf_step(b, warm) == EQF_OK && eqf_stream(b, &stream) == EQF_OK &&
       cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
-    const int steps = 4;
+    const int steps = timed;
     cudaEventRecord(e0, (cudaStream_t)stream);
     const int rc = eqf_step(b, steps);
     cudaEventRecord(e1, (cudaStream_t)stream);
@@ -139,14 +142,16 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
       nodes += (long long)(p.nx + 1) * (p.ny + 1);
     }
     double best = 0.0;
-    auto trial = [&](int pre, int post, int tile, int cols, int iters, int sweeps) {
+    auto trial = [&](int pre, int post, int tile, int cols, int iters, int sweeps,
+                     bool longer = false) {
       if (elapsed() > budget_s && best > 0.0) return;
       eqf_solver_opts c = o;
       c.cheb_pre = pre;
       c.cheb_post = post;
       c.max_iters = iters;
       c.max_sweeps = sweeps;
-      const double r = measure(batch, c, tile, cols);
+      const double r = longer ? measure(batch, c, tile, cols, kSchedWarm, kSchedTimed)
+                              : measure(batch, c, tile, cols);
       char line[192];
       std::snprintf(line, sizeof(line), "%d %d %d %d %d %d %d %.6e\n", k, tile, cols, pre,
                     post, iters, sweeps, r);
@@ -169,9 +174,17 @@ extern "C" int eqf_autotune_log(int32_t n_traps, const eqf_trap_params* traps,
       for (int cols : widths)
         if (tile != 0 || cols != 0) trial(pre, post, tile, cols, it0, sw0);
     const int tile = tb.tile_nodes, cols = tb.tile_cols;
-    if (o.precision == EQF_PREC_FP32_IR)  // the plain form keeps its one long sweep
+    if (o.precision == EQF_PREC_FP32_IR) {  // the plain form keeps its one long sweep
+      // schedules differ by a few percent once the fields have settled, which the
+      // short trials above do not resolve: the incumbent is measured again the same
+      // longer way and the schedules compete among themselves
+      const double short_best = best;
+      best = 0.0;
+      trial(pre, post, tile, cols, it0, sw0, true);
       for (const auto& sc : scheds)
-        if (sc[0] != it0 || sc[1] != sw0) trial(pre, post, tile, cols, sc[0], sc[1]);
+        if (sc[0] != it0 || sc[1] != sw0) trial(pre, post, tile, cols, sc[0], sc[1], true);
+      if (best == 0.0) best = short_best;  // out of budget before the longer trials
+    }
     tb.dof_steps_per_s = best;
   }
   if (log) {
