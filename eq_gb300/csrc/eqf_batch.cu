@@ -468,8 +468,10 @@ struct Work : WorkBase {
   void enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) override;
   // Late sweeps of the folded CG: the finest level's fused kernels stride over a list
   // of the iterating traps' 2-D tiles (class-table tiles from act_idx[0], general-path
-  // tiles from act_idx[ntiles2_cls]; counts in act_cnt[0..1]) with a quarter-size grid.
-  DevBuf<int> act_idx, act_cnt;
+  // tiles from act_idx[ntiles2_cls]; counts in act_cnt[0..1]) with a quarter-size grid,
+  // the CG direction and refinement update over one of their row tiles (act_ridx from
+  // 0 and ntiles_cls, counts in act_cnt[2..3]).
+  DevBuf<int> act_idx, act_cnt, act_ridx;
   bool late_lists = false;
   void enqueue_check(cudaStream_t s, bool update_gamma) override;
   void slot_ranges(int lev, long long off, long long n, std::vector<ZeroRange>& out) override {
@@ -1430,6 +1432,10 @@ static void allow_dyn_smem() {
   smem_attrs(k_cg_dir<T, false, false>, mx);
   smem_attrs(k_cg_dir<T, true, true>, mx);
   smem_attrs(k_cg_dir<T, false, true>, mx);
+  smem_attrs(k_cg_dir<T, true, false, true>, mx);
+  smem_attrs(k_cg_dir<T, false, false, true>, mx);
+  smem_attrs(k_cg_dir<T, true, true, true>, mx);
+  smem_attrs(k_cg_dir<T, false, true, true>, mx);
   smem_attrs(k_ir_first<T>, mx);
   smem_attrs(k_ir_residual<T, true>, mx);
   smem_attrs(k_ir_residual<T, false>, mx);
@@ -1479,7 +1485,8 @@ Work<T>::Work(Batch& b) : B(b) {
     // late sweeps' tile lists: allocated here, never in enqueue_sweep, which runs under
     // stream capture (a stream-ordered allocation there becomes a graph memory node)
     act_idx.alloc(std::max<size_t>(1, B.L[0].tiles2.size()));
-    act_cnt.alloc(2);
+    act_ridx.alloc(std::max<size_t>(1, (size_t)B.L[0].ntiles()));
+    act_cnt.alloc(4);
     r2.alloc(n0);
     EQF_CK(cudaMemsetAsync(r2.p, 0, n0 * sizeof(T), B.stream));
   }
@@ -1787,19 +1794,24 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) {
   if (!fold) EQF_CK(cudaMemsetAsync(xs.p, 0, B.L[0].nodes * sizeof(T), s));
   const int n2 = (int)L0.tiles2.size();
   // (buffers sized at construction: a batch whose tiles outgrew them runs full grids)
-  const bool listed = fold && late && act_idx.p && act_idx.n >= (size_t)n2;
-  if (listed) {  // the iterating traps' finest-level 2-D tiles
-    EQF_CK(cudaMemsetAsync(act_cnt.p, 0, 2 * sizeof(int), s));
+  const bool listed = fold && late && act_idx.p && act_idx.n >= (size_t)n2 &&
+                      act_ridx.n >= (size_t)nt;
+  if (listed) {  // the iterating traps' finest-level 2-D tiles and row tiles
+    EQF_CK(cudaMemsetAsync(act_cnt.p, 0, 4 * sizeof(int), s));
     EQF_RUN(B, KC_SCALAR,
-            (k_active_tiles2<<<(n2 + 255) / 256, 256, 0, s>>>(
+            (k_active_tiles<Tile2><<<(n2 + 255) / 256, 256, 0, s>>>(
                 G, L0.dtiles2.p, n2, L0.ntiles2_cls, B.d_cg_skip.p, act_idx.p, act_cnt.p)));
+    EQF_RUN(B, KC_SCALAR,
+            (k_active_tiles<Tile><<<(nt + 255) / 256, 256, 0, s>>>(
+                G, tl, nt, L0.ntiles_cls, B.d_cg_skip.p, act_ridx.p, act_cnt.p + 2)));
   }
   late_lists = listed;
   if (B.use_bicgstab) {
     bicgstab(s, r, tol_rel, tol_abs, iters);
     EQF_RUN(B, KC_IR_UPDATE,
             (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out,
-                        d_out, (const CgState*)nullptr, (const T*)nullptr, W)));
+                        d_out, (const CgState*)nullptr, (const T*)nullptr,
+                        TileList{nullptr, nullptr}, W)));
     return;
   }
   T* pin = p0.p;
@@ -1824,23 +1836,50 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) {
       const int nc = L0.ntiles_cls, ng = nt - nc;
       int* sk = B.d_cg_skip.p;
       CgState* cs = B.dstate.p;
-      if (it == 0) {
+      const TileList none{nullptr, nullptr};
+      if (listed) {  // absolute tile indices into the whole row-tile array
+        const TileList rc{act_ridx.p, act_cnt.p + 2}, rg{act_ridx.p + nc, act_cnt.p + 3};
+        if (it == 0) {
+          if (nc > 0)
+            EQF_RUN(B, KC_CG_DIR,
+                    (launch_pdl(k_cg_dir<T, true, false, true>, listed_grid(nc), kThreads,
+                                L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, rc,
+                                W)));
+          if (ng > 0)
+            EQF_RUN(B, KC_CG_DIR,
+                    (launch_pdl(k_cg_dir<T, true, true, true>, listed_grid(ng), kThreads,
+                                L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, rg,
+                                W)));
+        } else {
+          if (nc > 0)
+            EQF_RUN(B, KC_CG_DIR,
+                    (launch_pdl(k_cg_dir<T, false, false, true>, listed_grid(nc), kThreads,
+                                L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, rc,
+                                W)));
+          if (ng > 0)
+            EQF_RUN(B, KC_CG_DIR,
+                    (launch_pdl(k_cg_dir<T, false, true, true>, listed_grid(ng), kThreads,
+                                L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, rg,
+                                W)));
+        }
+      } else if (it == 0) {
         if (nc > 0)
           EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, true, false>, nc, kThreads, L0.sm_cgdir,
-                                            s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, W)));
+                                            s, G, tl, tab, sk, cs, z, pin, pout, q.p, part, none,
+                                            W)));
         if (ng > 0)
           EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, true, true>, ng, kThreads, L0.sm_cgdir, s,
                                             G, tl + nc, tab, sk, cs, z, pin, pout, q.p,
-                                            part + nc, W)));
+                                            part + nc, none, W)));
       } else {
         if (nc > 0)
           EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, false, false>, nc, kThreads,
                                             L0.sm_cgdir, s, G, tl, tab, sk, cs, z, pin, pout,
-                                            q.p, part, W)));
+                                            q.p, part, none, W)));
         if (ng > 0)
           EQF_RUN(B, KC_CG_DIR, (launch_pdl(k_cg_dir<T, false, true>, ng, kThreads,
                                             L0.sm_cgdir, s, G, tl + nc, tab, sk, cs, z, pin,
-                                            pout, q.p, part + nc, W)));
+                                            pout, q.p, part + nc, none, W)));
       }
     }
     EQF_RUN(B, KC_SCALAR,
@@ -1859,9 +1898,25 @@ void Work<T>::enqueue_sweep(cudaStream_t s, bool first, int iters, bool late) {
   late_lists = false;
   // folded: traps still iterating at the end take their last alpha p here (pin now
   // holds the last direction)
-  EQF_RUN(B, KC_IR_UPDATE,
-          (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out,
-                      d_out, (const CgState*)B.dstate.p, fold ? (const T*)pin : nullptr, W)));
+  const T* plast = fold ? (const T*)pin : nullptr;
+  if (listed) {  // the sweep's iterating traps are the ones not done (ir_done == cg_skip)
+    const int nc = L0.ntiles_cls, ng = nt - nc;
+    if (nc > 0)
+      EQF_RUN(B, KC_IR_UPDATE,
+              (launch_pdl(k_ir_update<T, true>, listed_grid(nc), kThreads, 0, s, G, tl,
+                          B.d_ir_done.p, xs.p, u_out, d_out, (const CgState*)B.dstate.p, plast,
+                          TileList{act_ridx.p, act_cnt.p + 2}, W)));
+    if (ng > 0)
+      EQF_RUN(B, KC_IR_UPDATE,
+              (launch_pdl(k_ir_update<T, true>, listed_grid(ng), kThreads, 0, s, G, tl,
+                          B.d_ir_done.p, xs.p, u_out, d_out, (const CgState*)B.dstate.p, plast,
+                          TileList{act_ridx.p + nc, act_cnt.p + 3}, W)));
+  } else {
+    EQF_RUN(B, KC_IR_UPDATE,
+            (launch_pdl(k_ir_update<T>, nt, kThreads, 0, s, G, tl, B.d_ir_done.p, xs.p, u_out,
+                        d_out, (const CgState*)B.dstate.p, plast, TileList{nullptr, nullptr},
+                        W)));
+  }
 }
 
 // Right-preconditioned BiCGSTAB on the correction x (xs) from residual r (the

@@ -158,29 +158,19 @@ __device__ __forceinline__ bool stage_rows(uint64_t* bar, const RowStage<T> (&st
   return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
-// The 2-D tiles of the traps still iterating (skip[trap] == 0): class-table tiles
-// (index < nc) into idx[0, ...), general-path tiles into idx[nc, ...), their numbers in
-// counts[0] and counts[1] (zeroed before).  The order within a list does not matter:
-// each tile's results and partial-sum slot are its own, whichever CTA computes it.
-__global__ void k_active_tiles2(const LevelGeom* __restrict__ G,
-                                const Tile2* __restrict__ tiles, int n, int nc,
-                                const int* __restrict__ skip, int* __restrict__ idx,
-                                int* __restrict__ counts) {
+// The tiles (row tiles or 2-D tiles) of the traps still iterating (skip[trap] == 0):
+// class-table tiles (index < nc) into idx[0, ...), general-path tiles into idx[nc, ...),
+// their numbers in counts[0] and counts[1] (zeroed before).  The order within a list
+// does not matter: each tile's results and partial-sum slot are its own, whichever CTA
+// computes it.
+template <class TT>
+__global__ void k_active_tiles(const LevelGeom* __restrict__ G, const TT* __restrict__ tiles,
+                               int n, int nc, const int* __restrict__ skip,
+                               int* __restrict__ idx, int* __restrict__ counts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || skip[G[tiles[i].geom].trap]) return;
   const int k = i < nc ? 0 : 1;
   idx[(k ? nc : 0) + atomicAdd(&counts[k], 1)] = i;
-}
-
-// Outcome of one tile of a fused kernel.
-constexpr int kTileSkipped = 0, kTileDone = 1, kTileFailed = -1;
-
-// Between two tiles of a listed launch: every thread is done with the windows before
-// the next tile's copies overwrite them, and a used mbarrier is invalidated before
-// stage_rows initialises it again.
-__device__ __forceinline__ void next_listed_tile(int rc) {
-  __syncthreads();
-  if (rc == kTileDone && threadIdx.x == 0) mbar_inval(reinterpret_cast<uint64_t*>(eqf_smem));
 }
 
 // Quads of a window: quad q at window row q / QW, columns 4 (q % QW) .. +3.

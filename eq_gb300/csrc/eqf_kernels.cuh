@@ -77,6 +77,17 @@ struct TileList {
   const int* idx;
   const int* count;
 };
+
+// Outcome of one tile of a staged kernel.
+constexpr int kTileSkipped = 0, kTileDone = 1, kTileFailed = -1;
+
+// Between two tiles of a listed launch: every thread is done with the staged windows
+// before the next tile's copies overwrite them, and a used mbarrier (at the start of
+// the dynamic shared memory) is invalidated before it is initialised again.
+__device__ __forceinline__ void next_listed_tile(int rc) {
+  __syncthreads();
+  if (rc == kTileDone && threadIdx.x == 0) mbar_inval(reinterpret_cast<uint64_t*>(eqf_smem));
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
                "r"(bytes)
@@ -1289,20 +1300,20 @@ struct PNew {  // p_out = z + beta p_in evaluated on the fly from the staged z, 
 
 // GEN: launched on the tiles of general-path traps (inline stencil fetch), else on
 // the tiles of class-table traps only (see apply_quad).
+// One row tile (index ti of the launch's tile array); returns kTileSkipped, kTileDone
+// or kTileFailed.
 template <class T, bool FIRST, bool GEN>
-__global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
-    k_cg_dir(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
-             const T* __restrict__ tabs, const int* __restrict__ skip,
-             const CgState* __restrict__ st, const T* __restrict__ z, const T* __restrict__ pin,
-             T* __restrict__ pout, T* __restrict__ q, double* __restrict__ part,
-             unsigned long long* work) {
-  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
-  prefetch_l1(G + tile.geom);
-  grid_dep_sync();
+__device__ __forceinline__ int cgdir_tile(const LevelGeom* __restrict__ G, const Tile& tile,
+                                          int ti, const T* __restrict__ tabs,
+                                          const int* __restrict__ skip,
+                                          const CgState* __restrict__ st, const T* __restrict__ z,
+                                          const T* __restrict__ pin, T* __restrict__ pout,
+                                          T* __restrict__ q, double* __restrict__ part,
+                                          unsigned long long* work) {
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) {
-    if (threadIdx.x == 0) part[blockIdx.x] = 0.0;
-    return;
+    if (threadIdx.x == 0) part[ti] = 0.0;
+    return kTileSkipped;
   }
   count_work(work, tile);
   const T beta = FIRST ? T(0) : T(st[g.trap].beta);
@@ -1316,7 +1327,7 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
   const Interior<T> ci = interior<T>(g);
   const TableStage<T> tst = stage_table<T>(sg, tab, ci);
   const T* stab = tst.s;
-  if (!sg.run(tst)) return;
+  if (!sg.run(tst)) return kTileFailed;
   const PNew<T, FIRST> pnew{zv, pv, beta};
   T* po = pout + g.off;
   T* qs = q + g.off;
@@ -1335,7 +1346,36 @@ __global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
     vst4<T>(qs + k, a);
   });
   const double t = block_sum(acc);
-  if (threadIdx.x == 0) part[blockIdx.x] = t;
+  if (threadIdx.x == 0) part[ti] = t;
+  return kTileDone;
+}
+
+// LIST: the CTAs stride over a device-built list of the iterating traps' row tiles
+// (late refinement sweeps); otherwise CTA b takes tile b.
+template <class T, bool FIRST, bool GEN, bool LIST = false>
+__global__ void __launch_bounds__(kThreads, kStencilCtas<T>)
+    k_cg_dir(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+             const T* __restrict__ tabs, const int* __restrict__ skip,
+             const CgState* __restrict__ st, const T* __restrict__ z, const T* __restrict__ pin,
+             T* __restrict__ pout, T* __restrict__ q, double* __restrict__ part,
+             TileList tlist, unsigned long long* work) {
+  if constexpr (!LIST) {
+    const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+    prefetch_l1(G + tile.geom);
+    grid_dep_sync();
+    cgdir_tile<T, FIRST, GEN>(G, tile, (int)blockIdx.x, tabs, skip, st, z, pin, pout, q, part,
+                              work);
+  } else {
+    grid_dep_sync();
+    const int n = *tlist.count;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+      const int ti = tlist.idx[w];
+      const int rc = cgdir_tile<T, FIRST, GEN>(G, tiles[ti], ti, tabs, skip, st, z, pin, pout,
+                                               q, part, work);
+      if (rc == kTileFailed) return;
+      next_listed_tile(rc);
+    }
+  }
 }
 
 // x += alpha p; r -= alpha q; partial dot(r, r)   (streaming, quads)
@@ -1529,14 +1569,13 @@ __device__ __forceinline__ double to_double(float f) {
 // the value k_cg_update would have left in x; after a single iteration the folded
 // CG never wrote x (it is not zeroed per sweep), so x = alpha p_last.
 template <class T>
-__global__ void __launch_bounds__(kThreads)
-    k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
-                const int* __restrict__ skip, const T* __restrict__ x, double* __restrict__ u,
-                float* __restrict__ d, const CgState* __restrict__ st,
-                const T* __restrict__ plast, unsigned long long* work) {
-  const Tile tile = tiles[blockIdx.x];  // static: read before the wait
-  prefetch_l1(G + tile.geom);
-  grid_dep_sync();
+__device__ __forceinline__ void irupd_tile(const LevelGeom* __restrict__ G, const Tile& tile,
+                                           const int* __restrict__ skip,
+                                           const T* __restrict__ x, double* __restrict__ u,
+                                           float* __restrict__ d,
+                                           const CgState* __restrict__ st,
+                                           const T* __restrict__ plast,
+                                           unsigned long long* work) {
   const LevelGeom& g = G[tile.geom];
   if (skip && skip[g.trap]) return;
   count_work(work, tile);
@@ -1579,6 +1618,26 @@ __global__ void __launch_bounds__(kThreads)
         d[o + kk] += float(v);
       }
     }
+  }
+}
+
+// LIST as k_cg_dir's (no shared memory: nothing to hand over between tiles).
+template <class T, bool LIST = false>
+__global__ void __launch_bounds__(kThreads)
+    k_ir_update(const LevelGeom* __restrict__ G, const Tile* __restrict__ tiles,
+                const int* __restrict__ skip, const T* __restrict__ x, double* __restrict__ u,
+                float* __restrict__ d, const CgState* __restrict__ st,
+                const T* __restrict__ plast, TileList tlist, unsigned long long* work) {
+  if constexpr (!LIST) {
+    const Tile tile = tiles[blockIdx.x];  // static: read before the wait
+    prefetch_l1(G + tile.geom);
+    grid_dep_sync();
+    irupd_tile<T>(G, tile, skip, x, u, d, st, plast, work);
+  } else {
+    grid_dep_sync();
+    const int n = *tlist.count;
+    for (int w = blockIdx.x; w < n; w += gridDim.x)
+      irupd_tile<T>(G, tiles[tlist.idx[w]], skip, x, u, d, st, plast, work);
   }
 }
 
