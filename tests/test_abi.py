@@ -48,6 +48,8 @@ int main(void) {
          offsetof(eqf_trap_params, adv_len), offsetof(eqf_trap_params, dt));
   printf("%zu %zu %zu %zu\n", sizeof(eqf_solver_opts), offsetof(eqf_solver_opts, adaptive),
          offsetof(eqf_solver_opts, cheb_ratio), offsetof(eqf_solver_opts, inner_tol));
+  printf("%zu %zu %zu %zu\n", sizeof(eqf_tune_bucket), offsetof(eqf_tune_bucket, tile_cols),
+         offsetof(eqf_tune_bucket, dof_steps_per_s), offsetof(eqf_tune_bucket, max_sweeps));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -59,9 +61,12 @@ int main(void) {
         lines = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
     tp = [int(v) for v in lines[0].split()]
     so = [int(v) for v in lines[1].split()]
+    tb = [int(v) for v in lines[2].split()]
     T, S = _lib.TrapParams, _lib.SolverOpts
     assert tp == [C.sizeof(T), T.walls.offset, T.adv_len.offset, T.dt.offset]
     assert so == [C.sizeof(S), S.adaptive.offset, S.cheb_ratio.offset, S.inner_tol.offset]
+    B = _lib.TuneBucket
+    assert tb == [C.sizeof(B), B.tile_cols.offset, B.dof_steps_per_s.offset, B.max_sweeps.offset]
 
 
 def test_default_opts_without_gpu(lib):
